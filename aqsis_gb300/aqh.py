@@ -1,0 +1,313 @@
+"""ctypes front end of libaqh (include/aqh.h), the GB300 hider.
+
+This mirrors the reference's hider boundary for Python callers and tests:
+``Hider.frame_begin`` takes the RI frame options, ``submit_grid`` /
+``submit_scene`` stand in for CqImageBuffer::AddMPG, ``render`` for
+CqImageBuffer::RenderImage, and ``read_channels`` / ``read_bucket`` /
+``read_quantized`` hand back what CqDDManager::DisplayBucket receives.
+
+The library must be built (``aqsis_gb300.build.build()``); there is no
+fallback -- loading fails loudly when the shared object is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build
+from .scene import FILTERS, Scene
+
+_f32p = C.POINTER(C.c_float)
+_i32p = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+_u32p = C.POINTER(C.c_uint32)
+_u8p = C.POINTER(C.c_uint8)
+
+AQH_OK = 0
+STATUS = {0: "AQH_OK", 1: "AQH_EINVAL", 2: "AQH_ENOMEM", 3: "AQH_EDEVICE", 4: "AQH_ETIMEDOUT",
+          5: "AQH_EREJECTED", 6: "AQH_ENOTREADY", 7: "AQH_ELIMIT"}
+
+
+class AqhError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+class FrameDesc(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int),
+                ("crop_xmin", C.c_int), ("crop_xmax", C.c_int), ("crop_ymin", C.c_int), ("crop_ymax", C.c_int),
+                ("bucket_x", C.c_int), ("bucket_y", C.c_int),
+                ("xsamples", C.c_int), ("ysamples", C.c_int),
+                ("xfilter", C.c_float), ("yfilter", C.c_float), ("filter", C.c_int),
+                ("gain", C.c_float), ("gamma", C.c_float),
+                ("q_one", C.c_float), ("q_min", C.c_float), ("q_max", C.c_float), ("q_dither", C.c_float),
+                ("shutter_open", C.c_float), ("shutter_close", C.c_float),
+                ("fstop", C.c_float), ("focal_length", C.c_float), ("focal_distance", C.c_float),
+                ("dof_scale_x", C.c_float), ("dof_scale_y", C.c_float),
+                ("depth_filter", C.c_int), ("zthreshold", C.c_float * 3), ("display_z", C.c_int)]
+
+
+class Grid(C.Structure):
+    _fields_ = [("cu", C.c_int), ("cv", C.c_int), ("nkeys", C.c_int), ("key_times", _f32p),
+                ("P", _f32p), ("Ci", _f32p), ("Oi", _f32p), ("culled", _u8p), ("flags", C.c_int)]
+
+
+class Samples(C.Structure):
+    _fields_ = [("npatterns", C.c_int), ("pos", _f32p), ("time", _f32p), ("dof", _f32p), ("shuffle", _i32p),
+                ("lod", _f32p), ("pos_index", _u32p), ("dof_index", _u32p), ("time_index", _u32p),
+                ("shuffle_index", _u32p), ("lod_index", _u32p), ("dither", _f32p)]
+
+
+class FrameStats(C.Structure):
+    _fields_ = [("micropolygons", C.c_int64), ("samples", C.c_int64), ("grids", C.c_int64),
+                ("tile_grid_pairs", C.c_int64), ("fragments", C.c_int64),
+                ("ms_bin", C.c_float), ("ms_sample", C.c_float), ("ms_filter", C.c_float), ("ms_total", C.c_float)]
+
+
+class DeviceOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("vertex_capacity", C.c_size_t), ("grid_capacity", C.c_size_t)]
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load libaqh.so.  Raises if it is missing (no fallback path exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise RuntimeError("libaqh.so is not built (%s); run aqsis_gb300.build.build()" % path)
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.aqh_create.argtypes = [C.POINTER(DeviceOpts), C.POINTER(vp)]
+    L.aqh_destroy.argtypes = [vp]
+    L.aqh_destroy.restype = None
+    L.aqh_last_error.argtypes = [vp]
+    L.aqh_last_error.restype = C.c_char_p
+    L.aqh_status_string.argtypes = [C.c_int]
+    L.aqh_status_string.restype = C.c_char_p
+    L.aqh_frame_desc_defaults.argtypes = [C.POINTER(FrameDesc)]
+    L.aqh_frame_desc_defaults.restype = None
+    L.aqh_frame_begin.argtypes = [vp, C.POINTER(FrameDesc)]
+    L.aqh_set_samples.argtypes = [vp, C.POINTER(Samples)]
+    L.aqh_submit_grid.argtypes = [vp, C.POINTER(Grid)]
+    L.aqh_submit_grids_device.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int64]
+    L.aqh_render.argtypes = [vp, C.c_int]
+    L.aqh_synchronize.argtypes = [vp]
+    L.aqh_read_channels.argtypes = [vp, _f32p, C.c_size_t]
+    L.aqh_read_bucket.argtypes = [vp, C.c_int, C.c_int, _f32p, C.c_size_t, _i32p, _i32p]
+    L.aqh_read_quantized_u8.argtypes = [vp, _i32p, C.c_int, _u8p, C.c_size_t]
+    L.aqh_read_samples.argtypes = [vp, _i32p, _f32p, _i32p, _u8p, _f32p, C.c_size_t]
+    L.aqh_get_stats.argtypes = [vp, C.POINTER(FrameStats)]
+    L.aqh_filter_table.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, C.c_int, _f32p, C.c_int]
+    L.aqh_filter_table.restype = C.c_int
+    L.aqh_test_invbilinear.argtypes = [_f32p, _f32p, C.c_int, _f32p]
+    for name in ("aqh_create", "aqh_frame_begin", "aqh_set_samples", "aqh_submit_grid", "aqh_submit_grids_device",
+                 "aqh_render", "aqh_synchronize", "aqh_read_channels", "aqh_read_bucket", "aqh_read_quantized_u8",
+                 "aqh_read_samples", "aqh_get_stats", "aqh_test_invbilinear"):
+        getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def frame_desc(fr) -> FrameDesc:
+    """aqh_frame_desc from an aqsis_gb300.scene.Frame."""
+    d = FrameDesc()
+    load().aqh_frame_desc_defaults(C.byref(d))
+    d.width, d.height = fr.width, fr.height
+    if fr.crop is not None:
+        d.crop_xmin, d.crop_xmax, d.crop_ymin, d.crop_ymax = fr.crop
+    d.bucket_x, d.bucket_y = fr.bucket
+    d.xsamples, d.ysamples = fr.xsamples, fr.ysamples
+    d.xfilter, d.yfilter = fr.xfilter, fr.yfilter
+    d.filter = FILTERS[fr.filter]
+    d.gain, d.gamma = fr.gain, fr.gamma
+    d.q_one, d.q_min, d.q_max, d.q_dither = fr.q_one, fr.q_min, fr.q_max, fr.q_dither
+    d.shutter_open, d.shutter_close = fr.shutter
+    d.fstop, d.focal_length, d.focal_distance = fr.fstop, fr.focal_length, fr.focal_distance
+    d.dof_scale_x, d.dof_scale_y = fr.dof_scale
+    d.depth_filter = fr.depth_filter
+    d.zthreshold = (C.c_float * 3)(*fr.zthreshold)
+    d.display_z = fr.display_z
+    return d
+
+
+def filter_table(filter_id: int, xw: float, yw: float, xs: int, ys: int) -> np.ndarray:
+    L = load()
+    n = -L.aqh_filter_table(filter_id, xw, yw, xs, ys, None, 0)
+    out = np.zeros(max(n, 1), np.float32)
+    L.aqh_filter_table(filter_id, xw, yw, xs, ys, _p(out, _f32p), n)
+    return out[:n]
+
+
+def invbilinear(quad, pts) -> np.ndarray:
+    """Device CqInvBilinear lookups (test hook)."""
+    q = np.ascontiguousarray(quad, np.float32).reshape(8)
+    P = np.ascontiguousarray(pts, np.float32).reshape(-1, 2)
+    uv = np.zeros_like(P)
+    rc = load().aqh_test_invbilinear(_p(q, _f32p), _p(P, _f32p), P.shape[0], _p(uv, _f32p))
+    if rc != AQH_OK:
+        raise AqhError(rc, "aqh_test_invbilinear failed")
+    return uv
+
+
+class Hider:
+    """One hider context (aqh_ctx) on one CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self.L = load()
+        self.ctx = C.c_void_p()
+        opts = DeviceOpts(device, 0, 0)
+        self._check(self.L.aqh_create(C.byref(opts), C.byref(self.ctx)), "aqh_create")
+        self._keep = []
+        self.frame = None
+
+    def close(self):
+        if self.ctx:
+            self.L.aqh_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, what: str):
+        if rc != AQH_OK:
+            msg = self.L.aqh_last_error(self.ctx).decode() if self.ctx else what
+            raise AqhError(rc, "%s: %s" % (what, msg))
+
+    # ---- frame --------------------------------------------------------------
+    def frame_begin(self, fr):
+        self.frame = fr
+        self._keep = []
+        self._check(self.L.aqh_frame_begin(self.ctx, C.byref(frame_desc(fr))), "aqh_frame_begin")
+
+    def set_samples(self, s):
+        keep = []
+
+        def a(x, dt):
+            if x is None:
+                return None
+            x = np.ascontiguousarray(x, dt)
+            keep.append(x)
+            return x
+        cs = Samples(int(s.npatterns), _p(a(s.pos, np.float32), _f32p), _p(a(s.time, np.float32), _f32p),
+                     _p(a(s.dof, np.float32), _f32p), _p(a(s.shuffle, np.int32), _i32p),
+                     _p(a(s.lod, np.float32), _f32p), _p(a(s.pos_index, np.uint32), _u32p),
+                     _p(a(s.dof_index, np.uint32), _u32p), _p(a(s.time_index, np.uint32), _u32p),
+                     _p(a(s.shuffle_index, np.uint32), _u32p), _p(a(s.lod_index, np.uint32), _u32p),
+                     _p(a(s.dither, np.float32), _f32p))
+        self._check(self.L.aqh_set_samples(self.ctx, C.byref(cs)), "aqh_set_samples")
+        self._check(self.L.aqh_synchronize(self.ctx), "aqh_synchronize")
+
+    def submit_grid(self, cu, cv, P, Ci=None, Oi=None, flags=1, key_times=None, culled=None):
+        P = np.ascontiguousarray(P, np.float32)
+        nkeys = 1 if key_times is None else len(key_times)
+        kt = None if key_times is None else np.ascontiguousarray(key_times, np.float32)
+        Ci = None if Ci is None else np.ascontiguousarray(Ci, np.float32)
+        Oi = None if Oi is None else np.ascontiguousarray(Oi, np.float32)
+        cl = None if culled is None else np.ascontiguousarray(culled, np.uint8)
+        g = Grid(cu, cv, nkeys, _p(kt, _f32p), _p(P, _f32p), _p(Ci, _f32p), _p(Oi, _f32p), _p(cl, _u8p), flags)
+        self._check(self.L.aqh_submit_grid(self.ctx, C.byref(g)), "aqh_submit_grid")
+
+    def submit_scene_grids(self, g):
+        """Submit every grid of a scene.Grids through aqh_submit_grid, in order."""
+        mpbase = 0
+        for i in range(g.ngrids):
+            cu, cv, nk = int(g.cu[i]), int(g.cv[i]), int(g.nkeys[i])
+            nv = (cu + 1) * (cv + 1)
+            pb, cb = int(g.pbase[i]), int(g.cbase[i])
+            kt = None
+            if nk > 1:
+                kt = g.times[int(g.tbase[i]):int(g.tbase[i]) + nk]
+            cl = None
+            if g.culled is not None:
+                cl = g.culled[mpbase:mpbase + cu * cv]
+            self.submit_grid(cu, cv, g.P[pb:pb + nv * nk], g.Ci[cb:cb + nv], g.Oi[cb:cb + nv], int(g.flags[i]),
+                             kt, cl)
+            mpbase += cu * cv
+
+    def submit_grids_device(self, ngrids, d_cu, d_cv, d_nkeys, d_flags, d_pbase, d_cbase, d_tbase, d_times,
+                            d_P, d_Ci, d_Oi, total_mps):
+        """Device-resident grids: every argument is a device pointer (int)."""
+        self._check(self.L.aqh_submit_grids_device(self.ctx, ngrids, d_cu, d_cv, d_nkeys, d_flags, d_pbase,
+                                                   d_cbase, d_tbase, d_times, d_P, d_Ci, d_Oi, total_mps),
+                    "aqh_submit_grids_device")
+
+    def render(self, sync: bool = True):
+        self._check(self.L.aqh_render(self.ctx, 1 if sync else 0), "aqh_render")
+
+    def synchronize(self):
+        self._check(self.L.aqh_synchronize(self.ctx), "aqh_synchronize")
+
+    # ---- results ------------------------------------------------------------
+    def _dims(self):
+        cx0, cx1, cy0, cy1 = self.frame.crop_window
+        return cx1 - cx0, cy1 - cy0
+
+    def read_channels(self) -> np.ndarray:
+        w, h = self._dims()
+        out = np.zeros((h, w, 9), np.float32)
+        self._check(self.L.aqh_read_channels(self.ctx, _p(out, _f32p), out.size), "aqh_read_channels")
+        return out
+
+    def read_bucket(self, bx: int, by: int) -> np.ndarray:
+        bw, bh = C.c_int32(), C.c_int32()
+        out = np.zeros(self.frame.bucket[0] * self.frame.bucket[1] * 9, np.float32)
+        self._check(self.L.aqh_read_bucket(self.ctx, bx, by, _p(out, _f32p), out.size, C.byref(bw), C.byref(bh)),
+                    "aqh_read_bucket")
+        return out[:bw.value * bh.value * 9].reshape(bh.value, bw.value, 9)
+
+    def read_quantized(self, channels=(0, 1, 2, 6)) -> np.ndarray:
+        w, h = self._dims()
+        ch = np.array(channels, np.int32)
+        out = np.zeros((h, w, len(ch)), np.uint8)
+        self._check(self.L.aqh_read_quantized_u8(self.ctx, _p(ch, _i32p), len(ch), _p(out, _u8p), out.size),
+                    "aqh_read_quantized_u8")
+        return out
+
+    def read_samples(self) -> dict:
+        x0, y0, w, h = self.frame.sample_region
+        n = w * h * self.frame.spp
+        r = {"winner": np.zeros(n, np.int32), "occlz": np.zeros(n, np.float32), "nfrag": np.zeros(n, np.int32),
+             "valid": np.zeros(n, np.uint8), "sdata": np.zeros((n, 7), np.float32)}
+        self._check(self.L.aqh_read_samples(self.ctx, _p(r["winner"], _i32p), _p(r["occlz"], _f32p),
+                                            _p(r["nfrag"], _i32p), _p(r["valid"], _u8p), _p(r["sdata"], _f32p), n),
+                    "aqh_read_samples")
+        return r
+
+    def stats(self) -> dict:
+        st = FrameStats()
+        self._check(self.L.aqh_get_stats(self.ctx, C.byref(st)), "aqh_get_stats")
+        return {k: getattr(st, k) for k, _ in FrameStats._fields_}
+
+    # ---- convenience ----------------------------------------------------------
+    def render_scene(self, scene: Scene, qchannels=(0, 1, 2, 6), samples: bool = True) -> dict:
+        self.frame_begin(scene.frame)
+        self.set_samples(scene.samples)
+        self.submit_scene_grids(scene.grids)
+        self.render(sync=True)
+        res = {"channels": self.read_channels(), "quantized": self.read_quantized(qchannels)}
+        if samples:
+            res.update(self.read_samples())
+        res["stats"] = self.stats()
+        return res

@@ -1,0 +1,975 @@
+// api.cu -- host runtime behind include/aqh.h.
+//
+// Owns the device buffers of a frame, stages host-submitted grids in pinned
+// memory, resolves the frame options the way SqOptionCache/CqRenderer do, and
+// runs the stages on the context's stream:
+//   bin      grid rectangles -> ordered super-tile grid lists   (bin.cu)
+//   sample   hit tests, early-z, store, Combine                 (sample.cu)
+//   filter   reconstruction filter, exposure (+ quantize)       (filter.cu)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/aqh.h"
+#include "aqh_internal.h"
+
+using namespace aqh;
+
+namespace {
+
+struct DevBuf {
+	void* p = nullptr;
+	size_t cap = 0;
+	~DevBuf() { release(); }
+	void release() {
+		if (p) cudaFree(p);
+		p = nullptr;
+		cap = 0;
+	}
+	cudaError_t ensure(size_t bytes) {
+		if (bytes <= cap) return cudaSuccess;
+		release();
+		size_t want = std::max<size_t>(bytes, 256);
+		cudaError_t e = cudaMalloc(&p, want);
+		if (e != cudaSuccess) {
+			p = nullptr;
+			cap = 0;
+			return e;
+		}
+		cap = want;
+		return cudaSuccess;
+	}
+	template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct PinnedBuf {
+	void* p = nullptr;
+	size_t cap = 0, used = 0;
+	~PinnedBuf() { if (p) cudaFreeHost(p); }
+	cudaError_t reserve(size_t bytes) {
+		if (bytes <= cap) return cudaSuccess;
+		size_t want = std::max(bytes, cap * 2 + (1u << 20));
+		void* q = nullptr;
+		cudaError_t e = cudaMallocHost(&q, want);
+		if (e != cudaSuccess) return e;
+		if (p) {
+			std::memcpy(q, p, used);
+			cudaFreeHost(p);
+		}
+		p = q;
+		cap = want;
+		return cudaSuccess;
+	}
+	cudaError_t append(const void* src, size_t bytes) {
+		cudaError_t e = reserve(used + bytes);
+		if (e != cudaSuccess) return e;
+		std::memcpy(static_cast<char*>(p) + used, src, bytes);
+		used += bytes;
+		return cudaSuccess;
+	}
+};
+
+// Host copies of the RI filter functions (libs/core/filters.cpp), restated from
+// the RenderMan Interface 3.2 forms the reference implements.
+float filter_eval(int filter, float x, float y, float xwidth, float ywidth) {
+	auto fmin_ = [](float a, float b) { return a < b ? a : b; };
+	switch (filter) {
+	case AQH_FILTER_GAUSSIAN:
+		x /= xwidth;
+		y /= ywidth;
+		return std::exp(-8.0 * (x * x + y * y));
+	case AQH_FILTER_BOX:
+		return fmin_((std::fabs(x) <= xwidth / 2.0 ? 1.0f : 0.0f), (std::fabs(y) <= ywidth / 2.0 ? 1.0f : 0.0f));
+	case AQH_FILTER_TRIANGLE: {
+		float hx = xwidth / 2.0, hy = ywidth / 2.0;
+		float ax = std::fabs(x), ay = std::fabs(y);
+		return fmin_((ax <= hx ? (hx - ax) / hx : 0.0f), (ay <= hy ? (hy - ay) / hy : 0.0f));
+	}
+	case AQH_FILTER_CATMULLROM: {
+		float r2 = (x * x + y * y);
+		float r = std::sqrt(r2);
+		return (r >= 2.0) ? 0.0 : (r < 1.0) ? (3.0 * r * r2 - 5.0 * r2 + 2.0) : (-r * r2 + 5.0 * r2 - 8.0 * r + 4.0);
+	}
+	case AQH_FILTER_SINC: {
+		const double pi = 3.14159265358979323846;
+		if (x != 0.0) { x *= pi; x = std::cos(0.5 * x / xwidth) * std::sin(x) / x; } else x = 1.0;
+		if (y != 0.0) { y *= pi; y = std::cos(0.5 * y / ywidth) * std::sin(y) / y; } else y = 1.0;
+		return x * y;
+	}
+	case AQH_FILTER_DISK: {
+		double xx = x * x, yy = y * y;
+		xwidth *= 0.5; ywidth *= 0.5;
+		double d = xx / (xwidth * xwidth) + yy / (ywidth * ywidth);
+		return d < 1.0 ? 1.0f : 0.0f;
+	}
+	case AQH_FILTER_BESSEL: {
+		const double pi = 3.14159265358979323846;
+		double xx = x * x, yy = y * y;
+		xwidth *= 0.5; ywidth *= 0.5;
+		double w = xx / (xwidth * xwidth) + yy / (ywidth * ywidth);
+		if (w < 1.0) {
+			double d = std::sqrt(xx + yy);
+			if (d != 0.0) {
+				w = std::cos(0.5 * pi * std::sqrt(w));
+				return w * 2 * j1(pi * d) / d;
+			}
+			return pi;
+		}
+		return 0.0f;
+	}
+	case AQH_FILTER_MITCHELL: {
+		const float B = 1 / 3.0f, C = 1 / 3.0f;
+		const float ixw = 1.0f / xwidth, iyw = 1.0f / ywidth;
+		auto ev = [&](float t) {
+			t = std::fabs(2.f * t);
+			if (t > 1.f)
+				return ((-B - 6 * C) * t * t * t + (6 * B + 30 * C) * t * t + (-12 * B - 48 * C) * t + (8 * B + 24 * C)) *
+				       (1.f / 6.f);
+			return ((12 - 9 * B - 6 * C) * t * t * t + (-18 + 12 * B + 6 * C) * t * t + (6 - 2 * B)) * (1.f / 6.f);
+		};
+		return ev(x * ixw) * ev(y * iyw);
+	}
+	}
+	return 0.0f;
+}
+
+int lfloor_h(float x) { int i = (int)x; return i - ((x < 0 && x != (float)i) ? 1 : 0); }
+
+// Tile shape: `spt` samples per thread, kBlock threads, near-square tiles.
+void set_tiling(FrameParams& fp, int spt) {
+	fp.tpp = (fp.spp + spt - 1) / spt;
+	const int tpix = kBlock / fp.tpp;
+	int tw = 1;
+	while ((tw + 1) * (tw + 1) <= tpix) ++tw;
+	const int th = tpix / tw;
+	fp.tile_w = tw;
+	fp.tile_h = th;
+	fp.ntx = (fp.sw + tw - 1) / tw;
+	fp.nty = (fp.sh + th - 1) / th;
+	fp.st_tiles = std::max(1, 128 / std::max(tw, th));
+	fp.nstx = (fp.ntx + fp.st_tiles - 1) / fp.st_tiles;
+	fp.nsty = (fp.nty + fp.st_tiles - 1) / fp.st_tiles;
+}
+
+// CqImagePixel::projectToCircle (imagepixel.h:429-436)
+void project_to_circle_h(float x, float y, float& ox, float& oy) {
+	float r;
+	if (y == 0.0f) r = std::fabs(x);
+	else if (x == 0.0f) r = std::fabs(y);
+	else r = std::sqrt((x * x) + (y * y));
+	if (r == 0.0f) { ox = 0.0f; oy = 0.0f; return; }
+	const float ax = std::fabs(x), ay = std::fabs(y);
+	const float adj = (ax < ay ? ay : ax) / r;
+	ox = adj * x;
+	oy = adj * y;
+}
+
+// CqBucketProcessor::CalculateDofBounds (bucketprocessor.cpp:858-913): the
+// region of the lens each sub-pixel stratum's offsets fall in, as
+// {min.x, min.y, max.x, max.y}.
+void dof_bounds_h(int xs, int ys, std::vector<float4>& out) {
+	out.resize((size_t)xs * ys);
+	const float dx = 2.0 / xs, dy = 2.0 / ys;
+	float minX = -1.0, minY = -1.0;
+	int which = 0;
+	for (int j = 0; j < ys; ++j) {
+		for (int i = 0; i < xs; ++i) {
+			float tlx, tly, trx, try_, blx, bly, brx, bry;
+			project_to_circle_h(minX, minY, tlx, tly);
+			project_to_circle_h(minX + dx, minY, trx, try_);
+			project_to_circle_h(minX, minY + dy, blx, bly);
+			project_to_circle_h(minX + dx, minY + dy, brx, bry);
+			if ((tly > 0.0 && bly < 0.0) || (tly < 0.0 && bly > 0.0)) {
+				tlx = minX; blx = minX; trx = minX + dx; brx = minX + dx;
+			}
+			if ((tlx > 0.0 && trx < 0.0) || (tlx < 0.0 && trx > 0.0)) {
+				tly = minY; bly = minY + dy; try_ = minY; bry = minY + dy;
+			}
+			float mnx = tlx, mny = tly, mxx = tlx, mxy = tly;
+			auto enc = [&](float x, float y) {
+				mnx = x < mnx ? x : mnx; mny = y < mny ? y : mny;
+				mxx = mxx < x ? x : mxx; mxy = mxy < y ? y : mxy;
+			};
+			enc(trx, try_);
+			enc(blx, bly);
+			enc(brx, bry);
+			out[which++] = make_float4(mnx, mny, mxx, mxy);
+			minX += dx;
+		}
+		minX = -1.0;
+		minY += dy;
+	}
+}
+
+}  // namespace
+
+struct aqh_ctx {
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	cudaEvent_t ev[6] = {};
+	std::string err;
+	bool frame_open = false;
+	aqh_frame_desc desc{};
+	FrameParams fp{};
+	std::vector<float> ftab;
+
+	// host-submitted grids
+	std::vector<int32_t> h_cu, h_cv, h_nkeys, h_flags, h_tbase;
+	std::vector<int64_t> h_pbase, h_cbase, h_mpbase;
+	std::vector<float> h_times;
+	std::vector<uint8_t> h_culled;
+	bool any_culled = false;
+	PinnedBuf hP, hCi, hOi;
+	int64_t h_verts_p = 0, h_verts_c = 0, h_mps = 0;
+	bool h_has_ci = true, h_has_oi = true;
+	bool any_transparent = false;
+
+	// host-submitted packed arrays (caller-owned, uploaded at render)
+	bool host_packed = false;
+	struct {
+		int ngrids;
+		const int32_t *cu, *cv, *nkeys, *flags, *tbase;
+		const int64_t *pbase, *cbase;
+		const float *times, *P, *Ci, *Oi;
+		size_t ntimes, nP, nC;
+	} hp{};
+	cudaStream_t own_stream = nullptr;
+	// device-submitted grids (caller-owned)
+	bool dev_grids = false;
+	GridsDev dg{};
+	int64_t dev_mps = 0;
+
+	// device buffers
+	DevBuf d_cu, d_cv, d_nkeys, d_flags, d_tbase, d_pbase, d_cbase, d_mpbase, d_times, d_culled, d_P, d_Ci, d_Oi;
+	DevBuf d_mpcount;
+	DevBuf d_rect, d_stcount, d_stoffset, d_stlist;
+	DevBuf d_sa, d_sb, d_win, d_oz, d_nf;
+	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err;
+	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb;
+	bool dev_motion = false;
+	// sampler
+	DevBuf s_pos, s_time, s_dof, s_shuffle, s_lod, s_ipos, s_idof, s_itime, s_ishuf, s_ilod, s_dither;
+	SamplerDev smp{};
+	bool samples_set = false;
+	int64_t frag_capacity = 0;
+	bool debug_samples = true;
+	aqh_frame_stats stats{};
+	int64_t st_list_cap = 0;
+
+	aqh_status fail(aqh_status s, const char* fmt, ...) {
+		char buf[512];
+		va_list ap;
+		va_start(ap, fmt);
+		vsnprintf(buf, sizeof buf, fmt, ap);
+		va_end(ap);
+		err = buf;
+		return s;
+	}
+	aqh_status cuda_fail(cudaError_t e, const char* what) {
+		return fail(e == cudaErrorMemoryAllocation ? AQH_ENOMEM : AQH_EDEVICE, "%s: %s", what, cudaGetErrorString(e));
+	}
+};
+
+#define AQH_TRY(expr, what)                                   \
+	do {                                                      \
+		cudaError_t e_ = (expr);                              \
+		if (e_ != cudaSuccess) return ctx->cuda_fail(e_, what); \
+	} while (0)
+
+extern "C" {
+
+const char* aqh_status_string(aqh_status s) {
+	switch (s) {
+	case AQH_OK: return "ok";
+	case AQH_EINVAL: return "invalid argument";
+	case AQH_ENOMEM: return "out of memory";
+	case AQH_EDEVICE: return "device error";
+	case AQH_ETIMEDOUT: return "timed out";
+	case AQH_EREJECTED: return "rejected";
+	case AQH_ENOTREADY: return "not ready";
+	case AQH_ELIMIT: return "limit exceeded";
+	}
+	return "unknown";
+}
+
+void aqh_frame_desc_defaults(aqh_frame_desc* d) {
+	std::memset(d, 0, sizeof *d);
+	d->width = 640;
+	d->height = 480;
+	d->bucket_x = d->bucket_y = 16;
+	d->xsamples = d->ysamples = 2;
+	d->xfilter = d->yfilter = 2.0f;
+	d->filter = AQH_FILTER_GAUSSIAN;
+	d->gain = d->gamma = 1.0f;
+	d->q_one = 255.0f;
+	d->q_min = 0.0f;
+	d->q_max = 255.0f;
+	d->q_dither = 0.5f;
+	d->fstop = FLT_MAX;
+	d->dof_scale_x = d->dof_scale_y = 1.0f;
+	d->zthreshold[0] = d->zthreshold[1] = d->zthreshold[2] = 1.0f;
+}
+
+aqh_status aqh_create(const aqh_device_opts* opts, aqh_ctx** out) {
+	if (!out) return AQH_EINVAL;
+	*out = nullptr;
+	aqh_ctx* ctx = new aqh_ctx();
+	ctx->device = opts ? opts->device : 0;
+	cudaError_t e = cudaSetDevice(ctx->device);
+	if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+	ctx->own_stream = ctx->stream;
+	for (int i = 0; e == cudaSuccess && i < 6; ++i) e = cudaEventCreate(&ctx->ev[i]);
+	if (e != cudaSuccess) {
+		delete ctx;
+		return e == cudaErrorMemoryAllocation ? AQH_ENOMEM : AQH_EDEVICE;
+	}
+	*out = ctx;
+	return AQH_OK;
+}
+
+void aqh_destroy(aqh_ctx* ctx) {
+	if (!ctx) return;
+	cudaSetDevice(ctx->device);
+	if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+	if (ctx->own_stream && ctx->own_stream != ctx->stream) cudaStreamSynchronize(ctx->own_stream);
+	for (auto& ev : ctx->ev)
+		if (ev) cudaEventDestroy(ev);
+	if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+	delete ctx;
+}
+
+const char* aqh_last_error(const aqh_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int aqh_filter_table(int filter, float xw, float yw, int xs, int ys, float* out, int max_out) {
+	// CqBucketProcessor::InitialiseFilterValues (bucketprocessor.cpp:811-856)
+	const int nsub = xs * ys;
+	const int xmax = lfloor_h(xw / 2.0f), ymax = lfloor_h(yw / 2.0f);
+	const int n = (2 * xmax + 1) * (2 * ymax + 1) * nsub;
+	if (!out || n > max_out) return -n;
+	const float xfwo2 = std::ceil(xw) * 0.5f, yfwo2 = std::ceil(yw) * 0.5f;
+	for (int py = -ymax; py <= ymax; py++)
+		for (int px = -xmax; px <= xmax; px++) {
+			int idx = ((py + ymax) * (2 * xmax + 1) + px + xmax) * nsub;
+			for (int sy = 0; sy < ys; sy++)
+				for (int sx = 0; sx < xs; sx++, ++idx) {
+					float fx = (sx + 0.5f) / xs + px - 0.5f;
+					float fy = (sy + 0.5f) / ys + py - 0.5f;
+					float w = 0;
+					if (fx >= -xfwo2 && fy >= -yfwo2 && fx <= xfwo2 && fy <= yfwo2)
+						w = filter_eval(filter, fx, fy, std::ceil(xw), std::ceil(yw));
+					out[idx] = w;
+				}
+		}
+	return n;
+}
+
+aqh_status aqh_frame_begin(aqh_ctx* ctx, const aqh_frame_desc* d) {
+	if (!ctx || !d) return AQH_EINVAL;
+	if (d->width <= 0 || d->height <= 0) return ctx->fail(AQH_EINVAL, "bad resolution %dx%d", d->width, d->height);
+	if (d->xsamples <= 0 || d->ysamples <= 0 || d->xsamples * d->ysamples > AQH_MAX_SPP)
+		return ctx->fail(AQH_ELIMIT, "PixelSamples %d %d outside 1..%d samples", d->xsamples, d->ysamples, AQH_MAX_SPP);
+	if (!(d->xfilter > 0) || !(d->yfilter > 0) || d->xfilter > 64 || d->yfilter > 64)
+		return ctx->fail(AQH_EINVAL, "bad filter width");
+	if (d->display_z && d->depth_filter == AQH_DEPTH_MIDPOINT)
+		return ctx->fail(AQH_EINVAL, "midpoint depth filter with a z display is not supported");
+	ctx->desc = *d;
+	FrameParams& fp = ctx->fp;
+	std::memset(&fp, 0, sizeof fp);
+	int cx0 = d->crop_xmin, cx1 = d->crop_xmax, cy0 = d->crop_ymin, cy1 = d->crop_ymax;
+	if (cx0 == 0 && cx1 == 0 && cy0 == 0 && cy1 == 0) { cx1 = d->width; cy1 = d->height; }
+	if (cx0 < 0 || cy0 < 0 || cx1 > d->width || cy1 > d->height || cx0 >= cx1 || cy0 >= cy1)
+		return ctx->fail(AQH_EINVAL, "bad crop window");
+	fp.crop_x0 = cx0; fp.crop_x1 = cx1; fp.crop_y0 = cy0; fp.crop_y1 = cy1;
+	fp.xs = d->xsamples; fp.ys = d->ysamples; fp.spp = fp.xs * fp.ys;
+	fp.shiftX = lfloor_h(d->xfilter / 2.0f);
+	fp.shiftY = lfloor_h(d->yfilter / 2.0f);
+	fp.xfwo2 = std::ceil(d->xfilter) * 0.5f;
+	fp.yfwo2 = std::ceil(d->yfilter) * 0.5f;
+	fp.sx0 = cx0 - fp.shiftX; fp.sy0 = cy0 - fp.shiftY;
+	fp.sw = (cx1 - cx0) + 2 * fp.shiftX; fp.sh = (cy1 - cy0) + 2 * fp.shiftY;
+	fp.cull_x0 = cx0 - d->xfilter / 2.0f; fp.cull_x1 = cx1 + d->xfilter / 2.0f;
+	fp.cull_y0 = cy0 - d->yfilter / 2.0f; fp.cull_y1 = cy1 + d->yfilter / 2.0f;
+	fp.use_dof = (d->fstop > 0.0f && d->fstop < FLT_MAX) ? 1 : 0;
+	if (fp.use_dof) {
+		// CqRenderer::SetDepthOfFieldData (renderer.h:368-377)
+		float lensDiameter = d->focal_length / d->fstop;
+		fp.dof_mult = 0.5 * lensDiameter * d->focal_distance / (d->focal_distance + lensDiameter);
+		fp.dof_inv_fd = 1.0 / d->focal_distance;
+		fp.dof_scale_x = d->dof_scale_x;
+		fp.dof_scale_y = d->dof_scale_y;
+	}
+	fp.shutter_open = d->shutter_open;
+	fp.shutter_close = d->shutter_close;
+	fp.depth_filter = d->depth_filter;
+	fp.cullable = !(d->display_z && (d->depth_filter == AQH_DEPTH_MAX || d->depth_filter == AQH_DEPTH_AVERAGE));
+	fp.midpoint_store = 0;
+	for (int k = 0; k < 3; ++k) fp.zthr[k] = d->zthreshold[k];
+	fp.gain = d->gain; fp.gamma = d->gamma;
+	fp.q_one = d->q_one; fp.q_min = d->q_min; fp.q_max = d->q_max; fp.q_dither = d->q_dither;
+	set_tiling(fp, kSamplesPerThread);
+	// filter table
+	int n = aqh_filter_table(d->filter, d->xfilter, d->yfilter, fp.xs, fp.ys, nullptr, 0);
+	ctx->ftab.assign(-n, 0.0f);
+	aqh_filter_table(d->filter, d->xfilter, d->yfilter, fp.xs, fp.ys, ctx->ftab.data(), -n);
+	fp.ftab_n = -n;
+	// reset grid stream
+	ctx->h_cu.clear(); ctx->h_cv.clear(); ctx->h_nkeys.clear(); ctx->h_flags.clear(); ctx->h_tbase.clear();
+	ctx->h_pbase.clear(); ctx->h_cbase.clear(); ctx->h_mpbase.clear(); ctx->h_times.clear(); ctx->h_culled.clear();
+	ctx->any_culled = false;
+	ctx->hP.used = ctx->hCi.used = ctx->hOi.used = 0;
+	ctx->h_verts_p = ctx->h_verts_c = ctx->h_mps = 0;
+	ctx->h_has_ci = ctx->h_has_oi = true;
+	ctx->any_transparent = false;
+	ctx->dev_grids = false;
+	ctx->dev_motion = false;
+	ctx->host_packed = false;
+	ctx->dev_mps = 0;
+	ctx->samples_set = false;
+	ctx->frame_open = true;
+	return AQH_OK;
+}
+
+aqh_status aqh_set_samples(aqh_ctx* ctx, const aqh_samples* s) {
+	if (!ctx || !s || !s->pos || s->npatterns <= 0) return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	cudaSetDevice(ctx->device);
+	const FrameParams& fp = ctx->fp;
+	const size_t np = (size_t)s->npatterns * fp.spp;
+	const size_t npix = (size_t)fp.sw * fp.sh;
+	const size_t ndisp = (size_t)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
+	if (!s->pos_index && (size_t)s->npatterns < npix)
+		return ctx->fail(AQH_EINVAL, "explicit samples need one pattern per pixel of the %dx%d sample region", fp.sw, fp.sh);
+	SamplerDev& m = ctx->smp;
+	std::memset(&m, 0, sizeof m);
+	m.npatterns = s->npatterns;
+	auto up = [&](DevBuf& b, const void* src, size_t bytes) -> cudaError_t {
+		if (!src) return cudaSuccess;
+		cudaError_t e = b.ensure(bytes);
+		if (e != cudaSuccess) return e;
+		return cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+	};
+	AQH_TRY(up(ctx->s_pos, s->pos, np * sizeof(float2)), "upload sample positions");
+	AQH_TRY(up(ctx->s_time, s->time, np * sizeof(float)), "upload sample times");
+	AQH_TRY(up(ctx->s_dof, s->dof, np * sizeof(float2)), "upload lens samples");
+	AQH_TRY(up(ctx->s_shuffle, s->shuffle, np * sizeof(int32_t)), "upload lens shuffles");
+	AQH_TRY(up(ctx->s_lod, s->lod, np * sizeof(float)), "upload lod samples");
+	AQH_TRY(up(ctx->s_ipos, s->pos_index, npix * sizeof(uint32_t)), "upload pattern choices");
+	AQH_TRY(up(ctx->s_idof, s->dof_index, npix * sizeof(uint32_t)), "upload pattern choices");
+	AQH_TRY(up(ctx->s_itime, s->time_index, npix * sizeof(uint32_t)), "upload pattern choices");
+	AQH_TRY(up(ctx->s_ishuf, s->shuffle_index, npix * sizeof(uint32_t)), "upload pattern choices");
+	AQH_TRY(up(ctx->s_ilod, s->lod_index, npix * sizeof(uint32_t)), "upload pattern choices");
+	AQH_TRY(up(ctx->s_dither, s->dither, ndisp * sizeof(float)), "upload dither");
+	m.pos = ctx->s_pos.as<float2>();
+	m.time = s->time ? ctx->s_time.as<float>() : nullptr;
+	m.dof = s->dof ? ctx->s_dof.as<float2>() : nullptr;
+	m.shuffle = s->shuffle ? ctx->s_shuffle.as<int32_t>() : nullptr;
+	m.lod = s->lod ? ctx->s_lod.as<float>() : nullptr;
+	m.pos_index = s->pos_index ? ctx->s_ipos.as<uint32_t>() : nullptr;
+	m.dof_index = s->dof_index ? ctx->s_idof.as<uint32_t>() : nullptr;
+	m.time_index = s->time_index ? ctx->s_itime.as<uint32_t>() : nullptr;
+	m.shuffle_index = s->shuffle_index ? ctx->s_ishuf.as<uint32_t>() : nullptr;
+	m.lod_index = s->lod_index ? ctx->s_ilod.as<uint32_t>() : nullptr;
+	m.dither = s->dither ? ctx->s_dither.as<float>() : nullptr;
+	ctx->samples_set = true;
+	return AQH_OK;
+}
+
+aqh_status aqh_submit_grid(aqh_ctx* ctx, const aqh_grid* gr) {
+	if (!ctx || !gr || !gr->P) return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	if (ctx->dev_grids || ctx->host_packed) return ctx->fail(AQH_EINVAL, "frame already holds packed grids");
+	if (gr->cu <= 0 || gr->cv <= 0) return ctx->fail(AQH_EINVAL, "empty grid %dx%d", gr->cu, gr->cv);
+	if (gr->nkeys < 1 || gr->nkeys > AQH_MAX_KEYS)
+		return ctx->fail(AQH_ELIMIT, "grid has %d motion keys; 1..%d supported", gr->nkeys, AQH_MAX_KEYS);
+	if (gr->nkeys > 1 && !gr->key_times) return ctx->fail(AQH_EINVAL, "motion grid without key times");
+	const int64_t nv = (int64_t)(gr->cu + 1) * (gr->cv + 1);
+	const int64_t nmp = (int64_t)gr->cu * gr->cv;
+	if (ctx->h_mps + nmp > INT32_MAX) return ctx->fail(AQH_ELIMIT, "more than 2^31 micropolygons in one frame");
+	ctx->h_cu.push_back(gr->cu);
+	ctx->h_cv.push_back(gr->cv);
+	ctx->h_nkeys.push_back(gr->nkeys);
+	int flags = gr->flags;
+	ctx->h_pbase.push_back(ctx->h_verts_p);
+	ctx->h_cbase.push_back(ctx->h_verts_c);
+	ctx->h_mpbase.push_back(ctx->h_mps);
+	ctx->h_tbase.push_back((int32_t)ctx->h_times.size());
+	if (gr->nkeys > 1)
+		ctx->h_times.insert(ctx->h_times.end(), gr->key_times, gr->key_times + gr->nkeys);
+	else
+		ctx->h_times.push_back(0.0f);
+	cudaError_t e = ctx->hP.append(gr->P, (size_t)nv * gr->nkeys * 16);
+	if (e == cudaSuccess) {
+		if (gr->Ci) e = ctx->hCi.append(gr->Ci, (size_t)nv * 16);
+		else {
+			std::vector<float> w((size_t)nv * 4, 1.0f);
+			e = ctx->hCi.append(w.data(), w.size() * 4);
+		}
+	}
+	if (e == cudaSuccess) {
+		if (gr->Oi) {
+			e = ctx->hOi.append(gr->Oi, (size_t)nv * 16);
+			if (!(flags & AQH_GRID_OPAQUE)) ctx->any_transparent = true;
+		} else {
+			std::vector<float> w((size_t)nv * 4, 1.0f);
+			e = ctx->hOi.append(w.data(), w.size() * 4);
+			flags |= AQH_GRID_OPAQUE;
+		}
+	}
+	if (e != cudaSuccess) return ctx->cuda_fail(e, "stage grid");
+	ctx->h_flags.push_back(flags);
+	if (gr->culled) {
+		if (!ctx->any_culled) {
+			ctx->h_culled.assign((size_t)ctx->h_mps, 0);
+			ctx->any_culled = true;
+		}
+		ctx->h_culled.insert(ctx->h_culled.end(), gr->culled, gr->culled + nmp);
+	} else if (ctx->any_culled) {
+		ctx->h_culled.insert(ctx->h_culled.end(), (size_t)nmp, 0);
+	}
+	ctx->h_verts_p += nv * gr->nkeys;
+	ctx->h_verts_c += nv;
+	ctx->h_mps += nmp;
+	return AQH_OK;
+}
+
+namespace {
+__global__ void mpcount_kernel(int n, const int32_t* cu, const int32_t* cv, int32_t* out) {
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) out[i] = cu[i] * cv[i];
+}
+__global__ void widen_kernel(int n, const int32_t* in, int64_t* out) {
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i <= n) out[i] = in[i];
+}
+__global__ void any_transparent_kernel(int n, const int32_t* flags, const int32_t* nkeys, int32_t* out) {
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n && !(flags[i] & AQH_GRID_OPAQUE)) out[0] = 1;
+	if (i < n && nkeys[i] > 1) out[1] = 1;
+}
+}  // namespace
+
+aqh_status aqh_set_stream(aqh_ctx* ctx, void* stream) {
+	if (!ctx) return AQH_EINVAL;
+	cudaSetDevice(ctx->device);
+	AQH_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
+	ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+	return AQH_OK;
+}
+
+void* aqh_host_alloc(size_t bytes) {
+	void* p = nullptr;
+	if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+	return p;
+}
+
+void aqh_host_free(void* p) {
+	if (p) cudaFreeHost(p);
+}
+
+aqh_status aqh_submit_grids_host(aqh_ctx* ctx, int ngrids, const int32_t* cu, const int32_t* cv,
+                                 const int32_t* nkeys, const int32_t* flags, const int64_t* pbase,
+                                 const int64_t* cbase, const int32_t* tbase, const float* times, size_t ntimes,
+                                 const float* P, size_t nP, const float* Ci, const float* Oi, size_t nC,
+                                 int64_t total_mps) {
+	if (!ctx || ngrids < 0 || !cu || !cv || !nkeys || !flags || !pbase || !cbase || !tbase || !P) return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	if (!ctx->h_cu.empty() || ctx->dev_grids || ctx->host_packed) return ctx->fail(AQH_EINVAL, "frame already holds grids");
+	if (total_mps > INT32_MAX) return ctx->fail(AQH_ELIMIT, "more than 2^31 micropolygons in one frame");
+	int64_t mps = 0;
+	bool transp = false;
+	for (int i = 0; i < ngrids; ++i) {
+		if (cu[i] <= 0 || cv[i] <= 0 || nkeys[i] < 1 || nkeys[i] > AQH_MAX_KEYS)
+			return ctx->fail(AQH_EINVAL, "grid %d: bad size or key count", i);
+		const int64_t nv = (int64_t)(cu[i] + 1) * (cv[i] + 1);
+		if (pbase[i] < 0 || (size_t)(pbase[i] + nv * nkeys[i]) > nP || cbase[i] < 0 || (size_t)(cbase[i] + nv) > nC)
+			return ctx->fail(AQH_EINVAL, "grid %d: vertices out of range", i);
+		if (nkeys[i] > 1 && (tbase[i] < 0 || (size_t)(tbase[i] + nkeys[i]) > ntimes))
+			return ctx->fail(AQH_EINVAL, "grid %d: key times out of range", i);
+		mps += (int64_t)cu[i] * cv[i];
+		if (!(flags[i] & AQH_GRID_OPAQUE)) transp = true;
+	}
+	if (mps != total_mps) return ctx->fail(AQH_EINVAL, "total_micropolygons %lld != %lld", (long long)total_mps, (long long)mps);
+	ctx->hp.ngrids = ngrids;
+	ctx->hp.cu = cu; ctx->hp.cv = cv; ctx->hp.nkeys = nkeys; ctx->hp.flags = flags; ctx->hp.tbase = tbase;
+	ctx->hp.pbase = pbase; ctx->hp.cbase = cbase; ctx->hp.times = times; ctx->hp.ntimes = ntimes;
+	ctx->hp.P = P; ctx->hp.nP = nP; ctx->hp.Ci = Ci; ctx->hp.Oi = Oi; ctx->hp.nC = nC;
+	ctx->h_mpbase.resize(ngrids);
+	int64_t acc = 0;
+	for (int i = 0; i < ngrids; ++i) { ctx->h_mpbase[i] = acc; acc += (int64_t)cu[i] * cv[i]; }
+	ctx->h_mps = mps;
+	ctx->any_transparent = transp && Oi;
+	ctx->host_packed = true;
+	return AQH_OK;
+}
+
+aqh_status aqh_submit_grids_device(aqh_ctx* ctx, int ngrids, const int32_t* d_cu, const int32_t* d_cv,
+                                   const int32_t* d_nkeys, const int32_t* d_flags, const int64_t* d_pbase,
+                                   const int64_t* d_cbase, const int32_t* d_tbase, const float* d_times,
+                                   const float* d_P, const float* d_Ci, const float* d_Oi, int64_t total_mps) {
+	if (!ctx || ngrids < 0 || !d_cu || !d_cv || !d_nkeys || !d_flags || !d_pbase || !d_cbase || !d_P)
+		return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	if (!ctx->h_cu.empty() || ctx->dev_grids || ctx->host_packed) return ctx->fail(AQH_EINVAL, "frame already holds grids");
+	if (total_mps > INT32_MAX) return ctx->fail(AQH_ELIMIT, "more than 2^31 micropolygons in one frame");
+	cudaSetDevice(ctx->device);
+	GridsDev& g = ctx->dg;
+	g.ngrids = ngrids;
+	g.cu = d_cu; g.cv = d_cv; g.nkeys = d_nkeys; g.flags = d_flags;
+	g.pbase = d_pbase; g.cbase = d_cbase; g.tbase = d_tbase; g.times = d_times;
+	g.P = reinterpret_cast<const float4*>(d_P);
+	g.Ci = reinterpret_cast<const float4*>(d_Ci);
+	g.Oi = reinterpret_cast<const float4*>(d_Oi);
+	g.culled = nullptr;
+	// first micropolygon id of every grid
+	AQH_TRY(ctx->d_mpcount.ensure(sizeof(int32_t) * (ngrids + 1) * 2 + 64), "alloc");
+	AQH_TRY(ctx->d_mpbase.ensure(sizeof(int64_t) * (ngrids + 1)), "alloc");
+	int32_t* cnt = ctx->d_mpcount.as<int32_t>();
+	int32_t* off = cnt + (ngrids + 1);
+	if (ngrids > 0) mpcount_kernel<<<(ngrids + 255) / 256, 256, 0, ctx->stream>>>(ngrids, d_cu, d_cv, cnt);
+	launch_scan_i32(cnt, off, ngrids, nullptr, ctx->stream);
+	widen_kernel<<<(ngrids + 256) / 256, 256, 0, ctx->stream>>>(ngrids, off, ctx->d_mpbase.as<int64_t>());
+	g.mpbase = ctx->d_mpbase.as<int64_t>();
+	// does any grid need the transparency path?
+	AQH_TRY(ctx->d_err.ensure(64), "alloc");
+	AQH_TRY(cudaMemsetAsync(ctx->d_err.p, 0, 64, ctx->stream), "memset");
+	if (ngrids > 0)
+		any_transparent_kernel<<<(ngrids + 255) / 256, 256, 0, ctx->stream>>>(ngrids, d_flags, d_nkeys,
+		                                                                    ctx->d_err.as<int32_t>() + 8);
+	int32_t anyt[2] = {0, 0};
+	AQH_TRY(cudaMemcpyAsync(anyt, ctx->d_err.as<int32_t>() + 8, 8, cudaMemcpyDeviceToHost, ctx->stream), "readback");
+	AQH_TRY(cudaStreamSynchronize(ctx->stream), "sync");
+	ctx->any_transparent = anyt[0] != 0;
+	ctx->dev_motion = anyt[1] != 0;
+	ctx->dev_grids = true;
+	ctx->dev_mps = total_mps;
+	return AQH_OK;
+}
+
+static aqh_status upload_packed_grids(aqh_ctx* ctx) {
+	auto& hp = ctx->hp;
+	const int G = hp.ngrids;
+	auto up = [&](DevBuf& b, const void* src, size_t bytes) -> cudaError_t {
+		cudaError_t e = b.ensure(bytes);
+		if (e != cudaSuccess || bytes == 0 || !src) return e;
+		return cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+	};
+	AQH_TRY(up(ctx->d_cu, hp.cu, G * 4), "upload grids");
+	AQH_TRY(up(ctx->d_cv, hp.cv, G * 4), "upload grids");
+	AQH_TRY(up(ctx->d_nkeys, hp.nkeys, G * 4), "upload grids");
+	AQH_TRY(up(ctx->d_flags, hp.flags, G * 4), "upload grids");
+	AQH_TRY(up(ctx->d_tbase, hp.tbase, G * 4), "upload grids");
+	AQH_TRY(up(ctx->d_pbase, hp.pbase, G * 8), "upload grids");
+	AQH_TRY(up(ctx->d_cbase, hp.cbase, G * 8), "upload grids");
+	AQH_TRY(up(ctx->d_mpbase, ctx->h_mpbase.data(), G * 8), "upload grids");
+	AQH_TRY(up(ctx->d_times, hp.times, std::max<size_t>(hp.ntimes, 1) * 4), "upload grids");
+	AQH_TRY(up(ctx->d_P, hp.P, hp.nP * 16), "upload P");
+	AQH_TRY(up(ctx->d_Ci, hp.Ci, hp.nC * 16), "upload Ci");
+	AQH_TRY(up(ctx->d_Oi, hp.Oi, hp.nC * 16), "upload Oi");
+	GridsDev& g = ctx->dg;
+	g.ngrids = G;
+	g.cu = ctx->d_cu.as<int32_t>(); g.cv = ctx->d_cv.as<int32_t>(); g.nkeys = ctx->d_nkeys.as<int32_t>();
+	g.flags = ctx->d_flags.as<int32_t>(); g.tbase = ctx->d_tbase.as<int32_t>();
+	g.pbase = ctx->d_pbase.as<int64_t>(); g.cbase = ctx->d_cbase.as<int64_t>(); g.mpbase = ctx->d_mpbase.as<int64_t>();
+	g.times = hp.times ? ctx->d_times.as<float>() : nullptr;
+	g.P = ctx->d_P.as<float4>();
+	g.Ci = hp.Ci ? ctx->d_Ci.as<float4>() : nullptr;
+	g.Oi = hp.Oi ? ctx->d_Oi.as<float4>() : nullptr;
+	g.culled = nullptr;
+	return AQH_OK;
+}
+
+static aqh_status upload_host_grids(aqh_ctx* ctx) {
+	const int G = (int)ctx->h_cu.size();
+	auto up = [&](DevBuf& b, const void* src, size_t bytes) -> cudaError_t {
+		cudaError_t e = b.ensure(bytes);
+		if (e != cudaSuccess || bytes == 0) return e;
+		return cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+	};
+	AQH_TRY(up(ctx->d_cu, ctx->h_cu.data(), G * 4), "upload grids");
+	AQH_TRY(up(ctx->d_cv, ctx->h_cv.data(), G * 4), "upload grids");
+	AQH_TRY(up(ctx->d_nkeys, ctx->h_nkeys.data(), G * 4), "upload grids");
+	AQH_TRY(up(ctx->d_flags, ctx->h_flags.data(), G * 4), "upload grids");
+	AQH_TRY(up(ctx->d_tbase, ctx->h_tbase.data(), G * 4), "upload grids");
+	AQH_TRY(up(ctx->d_pbase, ctx->h_pbase.data(), G * 8), "upload grids");
+	AQH_TRY(up(ctx->d_cbase, ctx->h_cbase.data(), G * 8), "upload grids");
+	AQH_TRY(up(ctx->d_mpbase, ctx->h_mpbase.data(), G * 8), "upload grids");
+	AQH_TRY(up(ctx->d_times, ctx->h_times.data(), ctx->h_times.size() * 4), "upload grids");
+	AQH_TRY(up(ctx->d_P, ctx->hP.p, ctx->hP.used), "upload P");
+	AQH_TRY(up(ctx->d_Ci, ctx->hCi.p, ctx->hCi.used), "upload Ci");
+	AQH_TRY(up(ctx->d_Oi, ctx->hOi.p, ctx->hOi.used), "upload Oi");
+	if (ctx->any_culled) AQH_TRY(up(ctx->d_culled, ctx->h_culled.data(), ctx->h_culled.size()), "upload culled");
+	GridsDev& g = ctx->dg;
+	g.ngrids = G;
+	g.cu = ctx->d_cu.as<int32_t>(); g.cv = ctx->d_cv.as<int32_t>(); g.nkeys = ctx->d_nkeys.as<int32_t>();
+	g.flags = ctx->d_flags.as<int32_t>(); g.tbase = ctx->d_tbase.as<int32_t>();
+	g.pbase = ctx->d_pbase.as<int64_t>(); g.cbase = ctx->d_cbase.as<int64_t>(); g.mpbase = ctx->d_mpbase.as<int64_t>();
+	g.times = ctx->d_times.as<float>();
+	g.P = ctx->d_P.as<float4>(); g.Ci = ctx->d_Ci.as<float4>(); g.Oi = ctx->d_Oi.as<float4>();
+	g.culled = ctx->any_culled ? ctx->d_culled.as<uint8_t>() : nullptr;
+	return AQH_OK;
+}
+
+aqh_status aqh_render(aqh_ctx* ctx, int sync) {
+	if (!ctx) return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	if (!ctx->samples_set) return ctx->fail(AQH_EINVAL, "aqh_set_samples was not called");
+	cudaSetDevice(ctx->device);
+	FrameParams& fp = ctx->fp;
+	cudaStream_t s = ctx->stream;
+	aqh_status st = AQH_OK;
+	if (ctx->host_packed) {
+		st = upload_packed_grids(ctx);
+		if (st != AQH_OK) return st;
+	} else if (!ctx->dev_grids) {
+		st = upload_host_grids(ctx);
+		if (st != AQH_OK) return st;
+	}
+	const GridsDev& g = ctx->dg;
+	const int64_t nmps = ctx->dev_grids ? ctx->dev_mps : ctx->h_mps;
+	bool motion = false;
+	if (ctx->host_packed) {
+		for (int i = 0; i < ctx->hp.ngrids; ++i) motion = motion || ctx->hp.nkeys[i] > 1;
+	} else if (!ctx->dev_grids) {
+		for (int k : ctx->h_nkeys) motion = motion || k > 1;
+	}
+	if (ctx->dev_grids) motion = ctx->dev_motion;
+	fp.any_motion = motion ? 1 : 0;
+	const bool mbdof = fp.use_dof || fp.any_motion;
+	set_tiling(fp, mbdof ? mb_samples_per_thread() : kSamplesPerThread);
+	if (mbdof) {
+		std::vector<float4> db;
+		dof_bounds_h(fp.xs, fp.ys, db);
+		AQH_TRY(ctx->d_dofb.ensure(db.size() * sizeof(float4)), "alloc");
+		AQH_TRY(cudaMemcpyAsync(ctx->d_dofb.p, db.data(), db.size() * sizeof(float4), cudaMemcpyHostToDevice, s),
+		        "upload lens bounds");
+	}
+	const int G = g.ngrids;
+	const size_t nsamp = (size_t)fp.sw * fp.sh * fp.spp;
+	const int nst = fp.nstx * fp.nsty;
+	BinBuffers bb{};
+	bb.range_size = 4096;
+	bb.nranges = std::max(1, (G + bb.range_size - 1) / bb.range_size);
+	AQH_TRY(ctx->d_rect.ensure(sizeof(int4) * std::max(G, 1)), "alloc rects");
+	AQH_TRY(ctx->d_stcount.ensure(sizeof(int32_t) * ((size_t)nst * bb.nranges + 1)), "alloc bins");
+	AQH_TRY(ctx->d_stoffset.ensure(sizeof(int32_t) * ((size_t)nst * bb.nranges + 1)), "alloc bins");
+	bb.grid_rect = ctx->d_rect.as<int4>();
+	bb.st_count = ctx->d_stcount.as<int32_t>();
+	bb.st_offset = ctx->d_stoffset.as<int32_t>();
+	// sample store
+	AQH_TRY(ctx->d_sa.ensure(nsamp * sizeof(float4)), "alloc sample store");
+	AQH_TRY(ctx->d_sb.ensure(nsamp * sizeof(float4)), "alloc sample store");
+	SampleStore store{};
+	store.a = ctx->d_sa.as<float4>();
+	store.b = ctx->d_sb.as<float4>();
+	if (ctx->debug_samples) {
+		AQH_TRY(ctx->d_win.ensure(nsamp * 4), "alloc");
+		AQH_TRY(ctx->d_oz.ensure(nsamp * 4), "alloc");
+		AQH_TRY(ctx->d_nf.ensure(nsamp * 4), "alloc");
+		store.winner = ctx->d_win.as<int32_t>();
+		store.occlz = ctx->d_oz.as<float>();
+		store.nfrag = ctx->d_nf.as<int32_t>();
+	}
+	AQH_TRY(ctx->d_ftab.ensure(ctx->ftab.size() * 4), "alloc");
+	AQH_TRY(cudaMemcpyAsync(ctx->d_ftab.p, ctx->ftab.data(), ctx->ftab.size() * 4, cudaMemcpyHostToDevice, s), "ftab");
+	const size_t ndisp = (size_t)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
+	AQH_TRY(ctx->d_chan.ensure(ndisp * 9 * 4), "alloc channels");
+	AQH_TRY(ctx->d_err.ensure(64), "alloc");
+
+	cudaEventRecord(ctx->ev[0], s);
+	launch_grid_rects(fp, g, bb.grid_rect, s);
+	launch_st_count(fp, g, bb, s);
+	launch_scan_i32(bb.st_count, bb.st_offset, nst * bb.nranges, nullptr, s);
+	int32_t total = 0;
+	AQH_TRY(cudaMemcpyAsync(&total, bb.st_offset + (size_t)nst * bb.nranges, 4, cudaMemcpyDeviceToHost, s), "readback");
+	AQH_TRY(cudaStreamSynchronize(s), "bin");
+	AQH_TRY(ctx->d_stlist.ensure(sizeof(int32_t) * std::max(total, 1)), "alloc tile lists");
+	bb.st_list = ctx->d_stlist.as<int32_t>();
+	bb.list_capacity = total;
+	launch_st_write(fp, g, bb, s);
+	cudaEventRecord(ctx->ev[1], s);
+
+	FragPool pool{};
+	if (ctx->any_transparent || !fp.cullable) {
+		if (ctx->frag_capacity == 0) ctx->frag_capacity = std::max<int64_t>(1 << 20, (int64_t)nsamp * 2);
+		AQH_TRY(ctx->d_frag.ensure(ctx->frag_capacity * sizeof(float4)), "alloc fragments");
+		AQH_TRY(ctx->d_next.ensure(ctx->frag_capacity * sizeof(int32_t)), "alloc fragments");
+		AQH_TRY(ctx->d_fcount.ensure(16), "alloc");
+		AQH_TRY(ctx->d_foverflow.ensure(16), "alloc");
+		pool.frag = ctx->d_frag.as<float4>();
+		pool.next = ctx->d_next.as<int32_t>();
+		pool.count = ctx->d_fcount.as<unsigned long long>();
+		pool.overflow = ctx->d_foverflow.as<int32_t>();
+		pool.capacity = ctx->frag_capacity;
+	}
+	for (int attempt = 0; attempt < 4; ++attempt) {
+		if (pool.capacity > 0) {
+			AQH_TRY(cudaMemsetAsync(pool.count, 0, 8, s), "memset");
+			AQH_TRY(cudaMemsetAsync(pool.overflow, 0, 4, s), "memset");
+		}
+		cudaEventRecord(ctx->ev[1], s);
+		if (mbdof)
+			launch_sample_mb(fp, g, ctx->smp, bb, store, pool, ctx->d_dofb.as<float4>(), s);
+		else
+			launch_sample_tiles(fp, g, ctx->smp, bb, store, pool, ctx->d_err.as<int32_t>(), s);
+		AQH_TRY(cudaGetLastError(), "sample kernel launch");
+		if (pool.capacity == 0) break;
+		int32_t ovf = 0;
+		unsigned long long used = 0;
+		AQH_TRY(cudaMemcpyAsync(&ovf, pool.overflow, 4, cudaMemcpyDeviceToHost, s), "readback");
+		AQH_TRY(cudaMemcpyAsync(&used, pool.count, 8, cudaMemcpyDeviceToHost, s), "readback");
+		AQH_TRY(cudaStreamSynchronize(s), "sample");
+		ctx->stats.fragments = (int64_t)used;
+		if (!ovf) break;
+		// grow the fragment pool to what this frame needed and sample again
+		ctx->frag_capacity = (int64_t)used + (int64_t)used / 4 + 1024;
+		AQH_TRY(ctx->d_frag.ensure(ctx->frag_capacity * sizeof(float4)), "alloc fragments");
+		AQH_TRY(ctx->d_next.ensure(ctx->frag_capacity * sizeof(int32_t)), "alloc fragments");
+		pool.frag = ctx->d_frag.as<float4>();
+		pool.next = ctx->d_next.as<int32_t>();
+		pool.capacity = ctx->frag_capacity;
+	}
+	cudaEventRecord(ctx->ev[2], s);
+	launch_filter(fp, ctx->smp, store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(), s);
+	AQH_TRY(cudaGetLastError(), "filter kernel launch");
+	cudaEventRecord(ctx->ev[3], s);
+	ctx->stats.micropolygons = nmps;
+	ctx->stats.samples = (int64_t)nsamp;
+	ctx->stats.grids = G;
+	ctx->stats.tile_grid_pairs = total;
+	if (sync) {
+		AQH_TRY(cudaStreamSynchronize(s), "render");
+		float a = 0, b = 0, c = 0;
+		cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
+		cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
+		cudaEventElapsedTime(&c, ctx->ev[2], ctx->ev[3]);
+		ctx->stats.ms_bin = a;
+		ctx->stats.ms_sample = b;
+		ctx->stats.ms_filter = c;
+		ctx->stats.ms_total = a + b + c;
+	}
+	return AQH_OK;
+}
+
+aqh_status aqh_synchronize(aqh_ctx* ctx) {
+	if (!ctx) return AQH_EINVAL;
+	cudaSetDevice(ctx->device);
+	AQH_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
+	return AQH_OK;
+}
+
+aqh_status aqh_read_channels(aqh_ctx* ctx, float* out, size_t out_floats) {
+	if (!ctx || !out) return AQH_EINVAL;
+	const FrameParams& fp = ctx->fp;
+	const size_t n = (size_t)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0) * 9;
+	if (out_floats < n) return ctx->fail(AQH_EINVAL, "output holds %zu floats, %zu needed", out_floats, n);
+	cudaSetDevice(ctx->device);
+	AQH_TRY(cudaMemcpyAsync(out, ctx->d_chan.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "read channels");
+	AQH_TRY(cudaStreamSynchronize(ctx->stream), "read channels");
+	return AQH_OK;
+}
+
+aqh_status aqh_read_bucket(aqh_ctx* ctx, int bx, int by, float* out, size_t out_floats, int* bw, int* bh) {
+	if (!ctx || !out) return AQH_EINVAL;
+	const FrameParams& fp = ctx->fp;
+	const int bsx = ctx->desc.bucket_x > 0 ? ctx->desc.bucket_x : 16;
+	const int bsy = ctx->desc.bucket_y > 0 ? ctx->desc.bucket_y : 16;
+	const int cw = fp.crop_x1 - fp.crop_x0, ch = fp.crop_y1 - fp.crop_y0;
+	const int x0 = bx * bsx, y0 = by * bsy;
+	if (bx < 0 || by < 0 || x0 >= cw || y0 >= ch) return ctx->fail(AQH_EINVAL, "bucket (%d,%d) outside the image", bx, by);
+	const int w = std::min(bsx, cw - x0), h = std::min(bsy, ch - y0);
+	if (out_floats < (size_t)w * h * 9) return ctx->fail(AQH_EINVAL, "bucket buffer too small");
+	cudaSetDevice(ctx->device);
+	AQH_TRY(cudaMemcpy2DAsync(out, (size_t)w * 9 * 4, ctx->d_chan.as<float>() + ((size_t)y0 * cw + x0) * 9,
+	                          (size_t)cw * 9 * 4, (size_t)w * 9 * 4, h, cudaMemcpyDeviceToHost, ctx->stream),
+	        "read bucket");
+	AQH_TRY(cudaStreamSynchronize(ctx->stream), "read bucket");
+	if (bw) *bw = w;
+	if (bh) *bh = h;
+	return AQH_OK;
+}
+
+aqh_status aqh_read_quantized_u8(aqh_ctx* ctx, const int* channels, int nchan, uint8_t* out, size_t out_bytes) {
+	if (!ctx || !channels || nchan <= 0 || nchan > 16 || !out) return AQH_EINVAL;
+	const FrameParams& fp = ctx->fp;
+	if (fp.q_one != 0.0f && (fp.q_min < 0.0f || fp.q_max > 255.0f))
+		return ctx->fail(AQH_EINVAL, "quantize range [%g,%g] does not fit 8 bits", fp.q_min, fp.q_max);
+	const size_t npix = (size_t)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
+	if (out_bytes < npix * nchan) return ctx->fail(AQH_EINVAL, "output too small");
+	for (int c = 0; c < nchan; ++c)
+		if (channels[c] < 0 || channels[c] >= AQH_NCHANNELS) return ctx->fail(AQH_EINVAL, "bad channel %d", channels[c]);
+	cudaSetDevice(ctx->device);
+	AQH_TRY(ctx->d_qchan.ensure(64), "alloc");
+	AQH_TRY(ctx->d_q8.ensure(npix * nchan), "alloc");
+	AQH_TRY(cudaMemcpyAsync(ctx->d_qchan.p, channels, nchan * 4, cudaMemcpyHostToDevice, ctx->stream), "upload");
+	launch_quantize_u8(fp, ctx->smp, ctx->d_chan.as<float>(), ctx->d_qchan.as<int>(), nchan, ctx->d_q8.as<uint8_t>(),
+	                   ctx->stream);
+	AQH_TRY(cudaGetLastError(), "quantize launch");
+	AQH_TRY(cudaMemcpyAsync(out, ctx->d_q8.p, npix * nchan, cudaMemcpyDeviceToHost, ctx->stream), "read quantized");
+	AQH_TRY(cudaStreamSynchronize(ctx->stream), "read quantized");
+	return AQH_OK;
+}
+
+aqh_status aqh_read_samples(aqh_ctx* ctx, int32_t* winner, float* occlz, int32_t* nfrag, uint8_t* valid,
+                            float* sdata, size_t nsamples) {
+	if (!ctx) return AQH_EINVAL;
+	const FrameParams& fp = ctx->fp;
+	const size_t n = (size_t)fp.sw * fp.sh * fp.spp;
+	if (nsamples < n) return ctx->fail(AQH_EINVAL, "buffers hold %zu samples, %zu needed", nsamples, n);
+	if (!ctx->debug_samples && (winner || occlz || nfrag)) return ctx->fail(AQH_EINVAL, "debug sample outputs are off");
+	cudaSetDevice(ctx->device);
+	cudaStream_t s = ctx->stream;
+	if (winner) AQH_TRY(cudaMemcpyAsync(winner, ctx->d_win.p, n * 4, cudaMemcpyDeviceToHost, s), "read");
+	if (occlz) AQH_TRY(cudaMemcpyAsync(occlz, ctx->d_oz.p, n * 4, cudaMemcpyDeviceToHost, s), "read");
+	if (nfrag) AQH_TRY(cudaMemcpyAsync(nfrag, ctx->d_nf.p, n * 4, cudaMemcpyDeviceToHost, s), "read");
+	if (valid || sdata) {
+		std::vector<float4> a(n), b(n);
+		AQH_TRY(cudaMemcpyAsync(a.data(), ctx->d_sa.p, n * 16, cudaMemcpyDeviceToHost, s), "read");
+		AQH_TRY(cudaMemcpyAsync(b.data(), ctx->d_sb.p, n * 16, cudaMemcpyDeviceToHost, s), "read");
+		AQH_TRY(cudaStreamSynchronize(s), "read");
+		for (size_t i = 0; i < n; ++i) {
+			if (valid) valid[i] = b[i].w != 0.0f ? 1 : 0;
+			if (sdata) {
+				float* d = sdata + 7 * i;
+				d[0] = a[i].x; d[1] = a[i].y; d[2] = a[i].z;
+				d[3] = b[i].x; d[4] = b[i].y; d[5] = b[i].z; d[6] = a[i].w;
+			}
+		}
+	}
+	AQH_TRY(cudaStreamSynchronize(s), "read");
+	return AQH_OK;
+}
+
+aqh_status aqh_get_stats(aqh_ctx* ctx, aqh_frame_stats* st) {
+	if (!ctx || !st) return AQH_EINVAL;
+	*st = ctx->stats;
+	return AQH_OK;
+}
+
+aqh_status aqh_test_invbilinear(const float* quad8, const float* P, int n, float* uv) {
+	if (!quad8 || !P || !uv || n < 0) return AQH_EINVAL;
+	float* dq = nullptr;
+	float2 *dp = nullptr, *du = nullptr;
+	cudaError_t e = cudaMalloc(&dq, 8 * 4);
+	if (e == cudaSuccess) e = cudaMalloc(&dp, sizeof(float2) * std::max(n, 1));
+	if (e == cudaSuccess) e = cudaMalloc(&du, sizeof(float2) * std::max(n, 1));
+	if (e == cudaSuccess) e = cudaMemcpy(dq, quad8, 32, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemcpy(dp, P, sizeof(float2) * n, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) {
+		launch_test_invbilinear(dq, dp, n, du, 0);
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess) e = cudaMemcpy(uv, du, sizeof(float2) * n, cudaMemcpyDeviceToHost);
+	cudaFree(dq);
+	cudaFree(dp);
+	cudaFree(du);
+	return e == cudaSuccess ? AQH_OK : AQH_EDEVICE;
+}
+
+}  // extern "C"

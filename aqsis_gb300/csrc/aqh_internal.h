@@ -1,0 +1,126 @@
+// aqh_internal.h -- device-side frame layout shared by the host runtime and
+// the CUDA kernels of the hider.  Not part of the public C-ABI.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace aqh {
+
+// Samples a thread owns.  A pixel with spp samples is split over
+// ceil(spp / kSamplesPerThread) threads; per-sample depth and position live in
+// that thread's registers while it walks the pixel's candidate micropolygons.
+constexpr int kSamplesPerThread = 16;
+// Micropolygon records staged in shared memory per sampling pass.
+constexpr int kSlots = 256;
+constexpr int kSlotWords = kSlots / 32;
+constexpr int kMaxKeys = 4;
+constexpr int kBlock = 256;
+#define AQH_MAX_SPP_DEV 256
+
+// Frame options resolved for the device (SqOptionCache + CqRenderer state).
+struct FrameParams {
+	int crop_x0, crop_x1, crop_y0, crop_y1;  // display region (crop window)
+	int sx0, sy0, sw, sh;                    // sample region = crop grown by the shift
+	int xs, ys, spp;                         // PixelSamples
+	int tpp;                                 // threads per pixel
+	int shiftX, shiftY;                      // lfloor(filterwidth / 2)
+	float xfwo2, yfwo2;                      // ceil(filterwidth) * 0.5f
+	float cull_x0, cull_x1, cull_y0, cull_y1;  // AddMPG crop cull window (crop -/+ filterwidth / 2)
+	int use_dof;
+	float dof_mult, dof_inv_fd, dof_scale_x, dof_scale_y;
+	float shutter_open, shutter_close;
+	int cullable;                            // samples are occlusion cullable (depth filter min/midpoint)
+	int depth_filter;
+	int midpoint_store;                      // display_z && depth_filter == midpoint
+	float zthr[3];
+	float gain, gamma;
+	float q_one, q_min, q_max, q_dither;
+	// tiling of the sample region
+	int tile_w, tile_h, ntx, nty;
+	int st_tiles;                            // tiles per super-tile side
+	int nstx, nsty;
+	int any_motion;
+	int ftab_n;                              // floats in the filter table
+};
+
+// Grid stream in device memory (aqh_submit_grids_device layout).
+struct GridsDev {
+	int ngrids;
+	const int32_t* cu;
+	const int32_t* cv;
+	const int32_t* nkeys;
+	const int32_t* flags;
+	const int64_t* pbase;
+	const int64_t* cbase;
+	const int32_t* tbase;
+	const int64_t* mpbase;   // first global micropolygon id of each grid
+	const float* times;
+	const float4* P;
+	const float4* Ci;
+	const float4* Oi;
+	const uint8_t* culled;   // per global micropolygon id, may be null
+};
+
+// Sample pattern caches (aqh_samples) in device memory.
+struct SamplerDev {
+	int npatterns;
+	const float2* pos;
+	const float* time;
+	const float2* dof;       // raw lens samples in [0,1)^2
+	const int32_t* shuffle;
+	const float* lod;
+	const uint32_t* pos_index;
+	const uint32_t* dof_index;
+	const uint32_t* time_index;
+	const uint32_t* shuffle_index;
+	const uint32_t* lod_index;
+	const float* dither;
+};
+
+// Per-sample resolved store (after Combine): R G B depth / OR OG OB flags.
+struct SampleStore {
+	float4* a;        // r, g, b, depth
+	float4* b;        // or, og, ob, valid (1.0f / 0.0f)
+	int32_t* winner;  // debug: occluding hit id before Combine (or null)
+	float* occlz;     // debug: occlZ (or null)
+	int32_t* nfrag;   // debug: transparent fragment count (or null)
+};
+
+// Transparent fragment pool: {depth, micropolygon id bits, u, v} + next link.
+struct FragPool {
+	float4* frag;
+	int32_t* next;
+	unsigned long long* count;
+	int64_t capacity;
+	int32_t* overflow;
+};
+
+struct BinBuffers {
+	int4* grid_rect;       // pixel rectangle [x0,x1) x [y0,y1) touched by each grid (empty: x0 >= x1)
+	int32_t* st_count;     // [nst][nranges]
+	int32_t* st_offset;    // exclusive scan of st_count, plus total at the end
+	int32_t* st_list;      // grid ids per super-tile, in grid order
+	int nranges;
+	int range_size;
+	int64_t list_capacity;
+};
+
+// Kernel launchers (implemented in the .cu files).
+void launch_grid_rects(const FrameParams& fp, const GridsDev& g, int4* rect, cudaStream_t s);
+void launch_st_count(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);
+void launch_scan_i32(const int32_t* in, int32_t* out, int n, int32_t* scratch, cudaStream_t s);
+void launch_st_write(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);
+void launch_sample_tiles(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
+                         SampleStore st, FragPool fp_pool, int32_t* err, cudaStream_t s);
+void launch_sample_mb(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
+                      SampleStore st, FragPool pool, const float4* dof_bounds, cudaStream_t s);
+int mb_samples_per_thread();
+void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStore& st, const float* ftab,
+                   float* channels, cudaStream_t s);
+void launch_quantize_u8(const FrameParams& fp, const SamplerDev& sm, const float* channels, const int* chans,
+                        int nchan, uint8_t* out, cudaStream_t s);
+void launch_test_invbilinear(const float* quad8, const float2* P, int n, float2* uv, cudaStream_t s);
+
+}  // namespace aqh

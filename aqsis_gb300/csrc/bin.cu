@@ -1,0 +1,189 @@
+// bin.cu -- bound-and-bin stage: per-grid raster rectangles and ordered
+// per-super-tile grid lists.
+//
+// Replaces CqImageBuffer::AddMPG's bucket assignment (libs/core/imagebuffer.cpp:
+// 514-591) at grid granularity.  A grid is listed for every super-tile (a
+// square of sampling tiles) its pixel rectangle touches, and each list keeps
+// grid submission order, so a tile that walks its super-tile's list sees its
+// micropolygons in the reference's insertion order (grid order, then iv, iu).
+// The exact per-micropolygon tests (bound, AddMPG crop cull) run in the
+// sampling kernel; this stage only needs conservative rectangles.
+#include "aqh_internal.h"
+#include "hider_device.cuh"
+
+namespace aqh {
+
+// One warp per grid: min/max of x, y, z over every vertex of every key, grown
+// by the largest circle of confusion in the grid's depth range when depth of
+// field is on, turned into the pixel rectangle [floor(min), ceil(max)] + 1
+// clipped to the sample region.
+__global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect) {
+	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const int lane = threadIdx.x & 31;
+	if (warp >= g.ngrids) return;
+	const int cu = g.cu[warp], cv = g.cv[warp];
+	const int nk = g.nkeys[warp];
+	const long long nv = (long long)(cu + 1) * (cv + 1) * nk;
+	const float4* P = g.P + g.pbase[warp];
+	float mnx = FLT_MAX, mny = FLT_MAX, mnz = FLT_MAX, mxx = -FLT_MAX, mxy = -FLT_MAX, mxz = -FLT_MAX;
+	for (long long i = lane; i < nv; i += 32) {
+		float4 p = __ldg(P + i);
+		mnx = fminf(mnx, p.x); mxx = fmaxf(mxx, p.x);
+		mny = fminf(mny, p.y); mxy = fmaxf(mxy, p.y);
+		mnz = fminf(mnz, p.z); mxz = fmaxf(mxz, p.z);
+	}
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+		mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+		mnz = fminf(mnz, __shfl_xor_sync(0xffffffffu, mnz, o));
+		mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+		mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+		mxz = fmaxf(mxz, __shfl_xor_sync(0xffffffffu, mxz, o));
+	}
+	if (lane != 0) return;
+	if (fp.use_dof) {
+		float2 c1 = coc(mnz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+		float2 c2 = coc(mxz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+		float cx = fmaxf(c1.x, c2.x), cy = fmaxf(c1.y, c2.y);
+		// a grid straddling the focal plane has its largest blur at an end of
+		// its depth range as well, so the two ends bound it
+		mnx -= cx; mxx += cx; mny -= cy; mxy += cy;
+	}
+	int4 r;
+	// one pixel of slack on every side keeps the rectangle conservative
+	// against rounding in the per-micropolygon ranges
+	float fx0 = floorf(mnx) - 1.0f, fy0 = floorf(mny) - 1.0f;
+	float fx1 = ceilf(mxx) + 2.0f, fy1 = ceilf(mxy) + 2.0f;
+	const float rx0 = (float)fp.sx0, ry0 = (float)fp.sy0;
+	const float rx1 = (float)(fp.sx0 + fp.sw), ry1 = (float)(fp.sy0 + fp.sh);
+	fx0 = fmaxf(fx0, rx0); fy0 = fmaxf(fy0, ry0);
+	fx1 = fminf(fx1, rx1); fy1 = fminf(fy1, ry1);
+	if (!(fx0 < fx1 && fy0 < fy1) || !(mnx <= mxx)) {
+		r = make_int4(0, 0, 0, 0);  // empty (also catches NaN)
+	} else {
+		r = make_int4((int)fx0, (int)fx1, (int)fy0, (int)fy1);
+	}
+	rect[warp] = r;
+}
+
+__device__ __forceinline__ void st_rect(const FrameParams& fp, int st, int& x0, int& x1, int& y0, int& y1) {
+	const int stx = st % fp.nstx, sty = st / fp.nstx;
+	x0 = fp.sx0 + stx * fp.st_tiles * fp.tile_w;
+	y0 = fp.sy0 + sty * fp.st_tiles * fp.tile_h;
+	x1 = x0 + fp.st_tiles * fp.tile_w;
+	y1 = y0 + fp.st_tiles * fp.tile_h;
+}
+
+__device__ __forceinline__ bool rect_hits(int4 r, int x0, int x1, int y0, int y1) {
+	return r.x < r.y && r.x < x1 && r.y > x0 && r.z < y1 && r.w > y0;
+}
+
+// grid (blockIdx.x = super-tile, blockIdx.y = grid range): count the range's
+// grids that touch the super-tile.
+__global__ void st_count_kernel(FrameParams fp, int ngrids, const int4* rect, int nranges, int range_size,
+                                int32_t* count) {
+	const int st = blockIdx.x, r = blockIdx.y;
+	int x0, x1, y0, y1;
+	st_rect(fp, st, x0, x1, y0, y1);
+	const int g0 = r * range_size, g1 = min(ngrids, g0 + range_size);
+	int c = 0;
+	for (int gi = g0 + threadIdx.x; gi < g1; gi += blockDim.x) c += rect_hits(rect[gi], x0, x1, y0, y1) ? 1 : 0;
+	__shared__ int red[32];
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+	if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+	__syncthreads();
+	if (threadIdx.x < 32) {
+		int v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0;
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+		if (threadIdx.x == 0) count[st * nranges + r] = v;
+	}
+}
+
+// Ordered compaction: write the range's touching grids at the super-tile's
+// offset, in grid order.
+__global__ void st_write_kernel(FrameParams fp, int ngrids, const int4* rect, int nranges, int range_size,
+                                const int32_t* offset, int32_t* list) {
+	const int st = blockIdx.x, r = blockIdx.y;
+	int x0, x1, y0, y1;
+	st_rect(fp, st, x0, x1, y0, y1);
+	const int g0 = r * range_size, g1 = min(ngrids, g0 + range_size);
+	__shared__ int warp_tot[32];
+	__shared__ int base;
+	if (threadIdx.x == 0) base = offset[st * nranges + r];
+	__syncthreads();
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	for (int c0 = g0; c0 < g1; c0 += blockDim.x) {
+		const int gi = c0 + threadIdx.x;
+		const bool f = gi < g1 && rect_hits(rect[gi], x0, x1, y0, y1);
+		const unsigned bal = __ballot_sync(0xffffffffu, f);
+		if (lane == 0) warp_tot[wid] = __popc(bal);
+		__syncthreads();
+		int pre = 0, tot = 0;
+		for (int w = 0; w < nw; ++w) {
+			int t = warp_tot[w];
+			pre += (w < wid) ? t : 0;
+			tot += t;
+		}
+		if (f) list[base + pre + __popc(bal & ((1u << lane) - 1u))] = gi;
+		__syncthreads();
+		if (threadIdx.x == 0) base += tot;
+		__syncthreads();
+	}
+}
+
+// Single-block exclusive scan with the grand total appended at out[n].
+__global__ void scan_i32_kernel(const int32_t* in, int32_t* out, int n) {
+	__shared__ int warp_sum[32];
+	__shared__ int carry;
+	if (threadIdx.x == 0) carry = 0;
+	__syncthreads();
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	for (int c0 = 0; c0 < n; c0 += blockDim.x) {
+		const int i = c0 + threadIdx.x;
+		int v = i < n ? in[i] : 0;
+		int x = v;
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			int y = __shfl_up_sync(0xffffffffu, x, o);
+			if (lane >= o) x += y;
+		}
+		if (lane == 31) warp_sum[wid] = x;
+		__syncthreads();
+		int pre = 0, tot = 0;
+		for (int w = 0; w < nw; ++w) {
+			pre += (w < wid) ? warp_sum[w] : 0;
+			tot += warp_sum[w];
+		}
+		if (i < n) out[i] = carry + pre + x - v;
+		__syncthreads();
+		if (threadIdx.x == 0) carry += tot;
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) out[n] = carry;
+}
+
+void launch_grid_rects(const FrameParams& fp, const GridsDev& g, int4* rect, cudaStream_t s) {
+	if (g.ngrids == 0) return;
+	const int wpb = kBlock / 32;
+	grid_rects_kernel<<<(g.ngrids + wpb - 1) / wpb, kBlock, 0, s>>>(fp, g, rect);
+}
+
+void launch_st_count(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s) {
+	dim3 grid(fp.nstx * fp.nsty, b.nranges);
+	st_count_kernel<<<grid, kBlock, 0, s>>>(fp, g.ngrids, b.grid_rect, b.nranges, b.range_size, b.st_count);
+}
+
+void launch_scan_i32(const int32_t* in, int32_t* out, int n, int32_t*, cudaStream_t s) {
+	scan_i32_kernel<<<1, 1024, 0, s>>>(in, out, n);
+}
+
+void launch_st_write(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s) {
+	dim3 grid(fp.nstx * fp.nsty, b.nranges);
+	st_write_kernel<<<grid, kBlock, 0, s>>>(fp, g.ngrids, b.grid_rect, b.nranges, b.range_size, b.st_offset,
+	                                        b.st_list);
+}
+
+}  // namespace aqh

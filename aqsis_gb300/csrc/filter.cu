@@ -1,0 +1,148 @@
+// filter.cu -- pixel reconstruction filter, exposure and quantize.
+//
+// Replaces CqBucketProcessor::FilterBucket (non-separable path,
+// libs/core/bucketprocessor.cpp:584-664, 686-707), ExposeBucket (766-806) and
+// the quantize of CqDisplayRequest::FormatBucketForDisplay
+// (ddmanager/ddmanager.cpp:1022-1119).  One thread per display pixel walks
+// the (2*shift+1)^2 neighbouring pixels and their samples in the reference's
+// loop order (fy, fx, sy, sx), so the float sums round identically.
+#include "aqh_internal.h"
+#include "hider_device.cuh"
+
+namespace aqh {
+
+namespace {
+
+__global__ void __launch_bounds__(256)
+filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __restrict__ ftab,
+              float* __restrict__ chan) {
+	const int x = fp.crop_x0 + blockIdx.x * 16 + (threadIdx.x & 15);
+	const int y = fp.crop_y0 + blockIdx.y * 16 + (threadIdx.x >> 4);
+	if (x >= fp.crop_x1 || y >= fp.crop_y1) return;
+	const float xcent = x + 0.5f, ycent = y + 0.5f;
+	const int xmax = fp.shiftX, ymax = fp.shiftY;
+	const int spp = fp.spp;
+	float gTot = 0.0f;
+	int count = 0;
+	float acc[7] = {0, 0, 0, 0, 0, 0, 0};
+	for (int fy = -ymax; fy <= ymax; fy++) {
+		const int py = y + fy;
+		for (int fx = -xmax; fx <= xmax; fx++) {
+			const int px = x + fx;
+			const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
+			const long long pat = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
+			const int index = ((fy + ymax) * (2 * xmax + 1) + fx + xmax) * spp;
+			const float fpx = (float)px, fpy = (float)py;
+			for (int i = 0; i < spp; ++i) {
+				const float2 o = __ldg(smp.pos + pat * spp + i);
+				const float vx = (fpx + o.x) - xcent;
+				const float vy = (fpy + o.y) - ycent;
+				if (vx >= -fp.xfwo2 && vy >= -fp.yfwo2 && vx <= fp.xfwo2 && vy <= fp.yfwo2) {
+					const float gw = __ldg(ftab + index + i);
+					gTot += gw;
+					const float4 b = st.b[pix * spp + i];
+					if (b.w != 0.0f) {
+						const float4 a = st.a[pix * spp + i];
+						acc[0] += a.x * gw;
+						acc[1] += a.y * gw;
+						acc[2] += a.z * gw;
+						acc[3] += b.x * gw;
+						acc[4] += b.y * gw;
+						acc[5] += b.z * gw;
+						acc[6] += a.w * gw;
+						count++;
+					}
+				}
+			}
+		}
+	}
+	float c[9];
+	float coverage;
+	if (count == 0) {
+#pragma unroll
+		for (int k = 0; k < 9; ++k) c[k] = 0.0f;
+		c[7] = FLT_MAX;
+		coverage = 0.0f;
+	} else {
+		const float inv = (float)(1.0 / (double)gTot);
+		c[0] = acc[0] * inv; c[1] = acc[1] * inv; c[2] = acc[2] * inv;
+		c[3] = acc[3] * inv; c[4] = acc[4] * inv; c[5] = acc[5] * inv;
+		c[7] = acc[6] * inv;
+		coverage = (count >= spp) ? 1.0f : (float)count / (float)spp;
+	}
+	const float a = (c[3] + c[4] + c[5]) / 3.0f;
+	c[6] = a * coverage;
+	c[8] = coverage;
+	// ExposeBucket: color = (color * gain) ^ (1 / gamma)
+	if (!(fp.gain == 1.0f && fp.gamma == 1.0f)) {
+		const float oneovergamma = 1.0f / fp.gamma;
+		if (fp.gain != 1.0f) { c[0] *= fp.gain; c[1] *= fp.gain; c[2] *= fp.gain; }
+		if (fp.gamma != 1.0f) {
+			c[0] = (float)pow((double)c[0], (double)oneovergamma);
+			c[1] = (float)pow((double)c[1], (double)oneovergamma);
+			c[2] = (float)pow((double)c[2], (double)oneovergamma);
+		}
+	}
+	float* out = chan + ((long long)(y - fp.crop_y0) * (fp.crop_x1 - fp.crop_x0) + (x - fp.crop_x0)) * 9;
+#pragma unroll
+	for (int k = 0; k < 9; ++k) out[k] = c[k];
+}
+
+// aqsis lround (math.h:67-70) in double: lfloor(x - 0.5) + 1
+__device__ __forceinline__ double lround_d(double x) {
+	const double y = x - 0.5;
+	long long i = (long long)y;
+	i -= (y < 0.0 && y != (double)i) ? 1 : 0;
+	return (double)(i + 1);
+}
+
+__global__ void quantize_u8_kernel(FrameParams fp, SamplerDev smp, const float* __restrict__ chan,
+                                   const int* __restrict__ chans, int nchan, uint8_t* __restrict__ out) {
+	const long long npix = (long long)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
+	const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (p >= npix) return;
+	const double s = smp.dither ? (double)__ldg(smp.dither + p) : 0.0;
+	for (int c = 0; c < nchan; ++c) {
+		double value = chan[p * 9 + chans[c]];
+		if (fp.q_one != 0.0f) {
+			value = lround_d(0.0 + value * (double)(fp.q_one - 0.0f) + ((double)fp.q_dither * s));
+			value = value < (double)fp.q_min ? (double)fp.q_min : (value > (double)fp.q_max ? (double)fp.q_max : value);
+		}
+		out[p * nchan + c] = (uint8_t)(int)value;
+	}
+}
+
+__global__ void test_invbilinear_kernel(const float* q, const float2* P, int n, float2* uv) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	V3f v[4] = {V3f{q[0], q[1], 0.0f}, V3f{q[2], q[3], 0.0f}, V3f{q[4], q[5], 0.0f}, V3f{q[6], q[7], 0.0f}};
+	HitCoeffs h;
+	hit_setup(v, 0, h);
+	float u, w;
+	inv_bilinear(h.ax, h.ay, h.e_x, h.e_y, h.f_x, h.f_y, h.g_x, h.g_y, h.linear, P[i].x, P[i].y, u, w);
+	uv[i] = make_float2(u, w);
+}
+
+}  // namespace
+
+void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStore& st, const float* ftab,
+                   float* channels, cudaStream_t s) {
+	const int w = fp.crop_x1 - fp.crop_x0, h = fp.crop_y1 - fp.crop_y0;
+	if (w <= 0 || h <= 0) return;
+	dim3 grid((w + 15) / 16, (h + 15) / 16);
+	filter_kernel<<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels);
+}
+
+void launch_quantize_u8(const FrameParams& fp, const SamplerDev& sm, const float* channels, const int* chans,
+                        int nchan, uint8_t* out, cudaStream_t s) {
+	const long long npix = (long long)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
+	if (npix <= 0) return;
+	quantize_u8_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(fp, sm, channels, chans, nchan, out);
+}
+
+void launch_test_invbilinear(const float* quad8, const float2* P, int n, float2* uv, cudaStream_t s) {
+	if (n <= 0) return;
+	test_invbilinear_kernel<<<(n + 127) / 128, 128, 0, s>>>(quad8, P, n, uv);
+}
+
+}  // namespace aqh

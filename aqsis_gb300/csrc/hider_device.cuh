@@ -1,0 +1,191 @@
+// hider_device.cuh -- per-micropolygon and per-sample arithmetic of the hider.
+//
+// Every expression keeps the reference's operation order and single-precision
+// rounding; the translation units that include this file are compiled with
+// -fmad=false so no multiply-add is contracted into an FMA, and with the
+// default IEEE division and square root.  References are to aqsis libs/core.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+namespace aqh {
+
+// math.h:47-62
+__device__ __forceinline__ int lfloor_f(float x) {
+	int i = static_cast<int>(x);
+	return i - ((x < 0.0f && x != static_cast<float>(i)) ? 1 : 0);
+}
+__device__ __forceinline__ int lceil_f(float x) {
+	int i = static_cast<int>(x);
+	return i + ((x > 0.0f && x != static_cast<float>(i)) ? 1 : 0);
+}
+// Aqsis::min / Aqsis::max (math.h:112-126): a < b ? a : b, a < b ? b : a.
+__device__ __forceinline__ float amin(float a, float b) { return a < b ? a : b; }
+__device__ __forceinline__ float amax(float a, float b) { return a < b ? b : a; }
+
+struct V3f { float x, y, z; };
+
+__device__ __forceinline__ V3f ld3(const float4* P, long long i) {
+	float4 v = __ldg(P + i);
+	return V3f{v.x, v.y, v.z};
+}
+
+// CqVector3D::Magnitude2 of a difference (vector3d.h:345-348)
+__device__ __forceinline__ float mag2diff(V3f a, V3f b) {
+	float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+	return dx * dx + dy * dy + dz * dz;
+}
+
+constexpr int kDegeneracyMask = 0x8000000;  // micropolygon.h:791
+
+// CqMicroPolygon::ComputeVertexOrder (micropolygon.cpp:1207-1284).  v[0..3] are
+// the grid points at index, index+1, index+cu+1, index+cu+2.
+__device__ __forceinline__ int vertex_order(const V3f v[4]) {
+	// natural slots: A = v[0], B = v[1], C = v[3] (index+cu+2), D = v[2] (index+cu+1)
+	V3f pa = v[0], pb = v[1], pc = v[3], pd = v[2];
+	int codeA = 0, codeB = 1, codeC = 3, codeD = 2;
+	V3f vA = pa, vB = pb, vC = pc;
+	bool degenerate = false;
+	if (mag2diff(pa, pb) < 1e-8) {
+		// A--B degenerate: B <- C, C <- D
+		vB = pc; codeB = codeC; vC = pd; codeC = codeD; degenerate = true;
+	} else if (mag2diff(pb, pc) < 1e-8) {
+		vB = pc; codeB = codeC; vC = pd; codeC = codeD; degenerate = true;
+	} else if (mag2diff(pc, pd) < 1e-8) {
+		vC = pd; codeC = codeD; degenerate = true;
+	} else if (mag2diff(pd, pa) < 1e-8) {
+		degenerate = true;  // the reference only drops D here
+	}
+	bool flip = ((vA.x - vB.x) * (vB.y - vC.y)) >= ((vA.y - vB.y) * (vB.x - vC.x));
+	int code;
+	if (!flip) {
+		code = degenerate ? ((codeA & 3) | ((codeC & 3) << 2) | ((codeB & 3) << 4) | kDegeneracyMask)
+		                  : ((codeA & 3) | ((codeD & 3) << 2) | ((codeC & 3) << 4) | ((codeB & 3) << 6));
+	} else {
+		code = degenerate ? ((codeA & 3) | ((codeB & 3) << 2) | ((codeC & 3) << 4) | kDegeneracyMask)
+		                  : ((codeA & 3) | ((codeB & 3) << 2) | ((codeC & 3) << 4) | ((codeD & 3) << 6));
+	}
+	return code;
+}
+
+// Point-in-polygon coefficients and inverse-bilinear setup: CqHitTestCache as
+// filled by CqMicroPolygon::cachePointInPolyTest (micropolygon.cpp:1346-1392)
+// and CqInvBilinear::setVertices (bilinear.h:260-275).
+struct HitCoeffs {
+	float ym[4], xm[4], ex[4], ey[4];
+	float ax, ay, e_x, e_y, f_x, f_y, g_x, g_y;
+	float z[4];
+	bool linear;
+};
+
+__device__ __forceinline__ void hit_setup(const V3f p[4], int code, HitCoeffs& h) {
+	h.z[0] = p[0].z; h.z[1] = p[1].z; h.z[2] = p[2].z; h.z[3] = p[3].z;
+	// setVertices(A, B, C, D) with A=p0, B=p1, C=p2, D=p3
+	h.ax = p[0].x; h.ay = p[0].y;
+	h.e_x = p[1].x - p[0].x; h.e_y = p[1].y - p[0].y;
+	h.f_x = p[2].x - p[0].x; h.f_y = p[2].y - p[0].y;
+	// G = -E - C + D
+	h.g_x = ((-h.e_x) - p[2].x) + p[3].x;
+	h.g_y = ((-h.e_y) - p[2].y) + p[3].y;
+	float patch = amax(amax(fabsf(h.f_x), fabsf(h.f_y)), amax(fabsf(h.e_x), fabsf(h.e_y)));
+	float irr = amax(fabsf(h.g_x), fabsf(h.g_y));
+	h.linear = static_cast<double>(irr) < 1e-2 * static_cast<double>(patch);
+	// reorder by the vertex code (selects keep the points in registers)
+	auto pick = [&](int k) -> V3f { return k == 0 ? p[0] : (k == 1 ? p[1] : (k == 2 ? p[2] : p[3])); };
+	V3f q[4] = {pick((code >> 2) & 3), pick((code >> 4) & 3), pick((code >> 6) & 3), pick(code & 3)};
+	int j = 3;
+#pragma unroll
+	for (int i = 0; i < 4; ++i) {
+		h.ym[i] = q[i].x - q[j].x;
+		h.xm[i] = q[i].y - q[j].y;
+		h.ex[i] = q[j].x;
+		h.ey[i] = q[j].y;
+		j = i;
+	}
+	if (code & kDegeneracyMask) {
+#pragma unroll
+		for (int i = 2; i < 4; ++i) {
+			h.ym[i] = q[3].x - q[1].x;
+			h.xm[i] = q[3].y - q[1].y;
+			h.ex[i] = q[1].x;
+			h.ey[i] = q[1].y;
+		}
+	}
+}
+
+// The four edge tests of CqMicroPolygon::fContains (micropolygon.cpp:1295-1332):
+// edges 0 and 1 reject on <= 0, edges 2 and 3 on < 0.  The reference's
+// starting edge only changes which test fails first, not the answer.
+__device__ __forceinline__ bool edges_inside(const float ym[4], const float xm[4], const float ex[4],
+                                             const float ey[4], float x, float y) {
+	float v0 = ((y - ey[0]) * ym[0]) - ((x - ex[0]) * xm[0]);
+	float v1 = ((y - ey[1]) * ym[1]) - ((x - ex[1]) * xm[1]);
+	float v2 = ((y - ey[2]) * ym[2]) - ((x - ex[2]) * xm[2]);
+	float v3 = ((y - ey[3]) * ym[3]) - ((x - ex[3]) * xm[3]);
+	// written as negated rejections so NaN behaves as in the reference
+	return !(v0 <= 0.0f) & !(v1 <= 0.0f) & !(v2 < 0.0f) & !(v3 < 0.0f);
+}
+
+// CqInvBilinear::operator() (bilinear.h:277-305): one Newton step from the
+// centre, a second one unless the micropolygon is almost rectangular.
+__device__ __forceinline__ void inv_bilinear(float ax, float ay, float ex, float ey, float fx, float fy, float gx,
+                                             float gy, bool linear, float px, float py, float& u, float& v) {
+	u = 0.5f;
+	v = 0.5f;
+#pragma unroll
+	for (int it = 0; it < 2; ++it) {
+		if (it == 1 && linear) break;
+		// M1 = E + G*v, M2 = F + G*u
+		float m1x = ex + gx * v, m1y = ey + gy * v;
+		float m2x = fx + gx * u, m2y = fy + gy * u;
+		// bilinEval(uv) - P = A + E*u + F*v + G*u*v - P
+		float bx = (((ax + ex * u) + fx * v) + (gx * u) * v) - px;
+		float by = (((ay + ey * u) + fy * v) + (gy * u) * v) - py;
+		float det = m1x * m2y - m1y * m2x;
+		if (it == 0 || det != 0.0f) det = 1.0f / det;
+		float cb2 = bx * m2y - by * m2x;   // cross(b, M2)
+		float cb1 = bx * m1y - by * m1x;   // cross(b, M1)
+		float du = det * cb2;
+		float dv = det * (-cb1);
+		u = u - du;
+		v = v - dv;
+	}
+}
+
+// bilerp (bilinear.h:228-236)
+__device__ __forceinline__ float bilerp1(float a, float b, float c, float d, float u, float v) {
+	float w0 = (1.0f - v) * (1.0f - u);
+	float w1 = (1.0f - v) * u;
+	float w2 = v * (1.0f - u);
+	float w3 = v * u;
+	return ((w0 * a + w1 * b) + w2 * c) + w3 * d;
+}
+
+// CqMicroPolygon::InterpolateOutputs smooth weights (micropolygon.cpp:1449-1455)
+__device__ __forceinline__ void smooth_weights(float u, float v, float w[4]) {
+	w[0] = (1.0f - u) * (1.0f - v);
+	w[1] = u * (1.0f - v);
+	w[2] = (1.0f - u) * v;
+	w[3] = u * v;
+}
+
+// CqRenderer::GetCircleOfConfusion (renderer.h:401-406)
+__device__ __forceinline__ float2 coc(float depth, float mult, float inv_fd, float sx, float sy) {
+	float c = mult * fabsf(1.0f / depth - inv_fd);
+	return make_float2(sx * c, sy * c);
+}
+
+// CqImagePixel::projectToCircle (imagepixel.h:429-436) with CqVector2D::Magnitude
+// (vector2d.h:141-147).
+__device__ __forceinline__ float2 project_to_circle(float x, float y) {
+	float r;
+	if (y == 0.0f) r = fabsf(x);
+	else if (x == 0.0f) r = fabsf(y);
+	else r = sqrtf((x * x) + (y * y));
+	if (r == 0.0f) return make_float2(0.0f, 0.0f);
+	float adj = amax(fabsf(x), fabsf(y)) / r;
+	return make_float2(adj * x, adj * y);
+}
+
+}  // namespace aqh

@@ -1,0 +1,221 @@
+// sample_common.cuh -- pieces shared by the sampling kernels: block scan,
+// sub-sample ranges, output interpolation and CqImagePixel::Combine.
+#pragma once
+
+#include "aqh_internal.h"
+#include "hider_device.cuh"
+
+namespace aqh {
+
+// Exclusive prefix count of `f` over the block (blockDim.x a multiple of 32,
+// at most 1024 threads); `warp_tot` is shared scratch of 32 ints.
+__device__ __forceinline__ int block_excl_scan(int* warp_tot, bool f, int& total) {
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	const unsigned bal = __ballot_sync(0xffffffffu, f);
+	if (lane == 0) warp_tot[wid] = __popc(bal);
+	__syncthreads();
+	int pre = 0, tot = 0;
+	for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+		int t = warp_tot[w];
+		pre += (w < wid) ? t : 0;
+		tot += t;
+	}
+	total = tot;
+	return pre + __popc(bal & ((1u << lane) - 1u));
+}
+
+// Sub-sample index range of pixel `p` inside [s, e) of a bound edge
+// (bucketprocessor.cpp:1119-1138, 1149-1153), for one axis.
+__device__ __forceinline__ void sub_range(int p, float bmin, float bmax, int ns, int& lo, int& hi) {
+	const int s = (int)floorf(bmin);
+	const int e = lceil_f(bmax);
+	const int im = (int)floorf((bmin - (float)s) * (float)ns);
+	const int em = lceil_f((bmax - (float)(e - 1)) * (float)ns);
+	lo = (p == s) ? im : 0;
+	hi = (p == e - 1) ? em : ns;
+}
+
+// Colour and opacity of micropolygon `m` of grid `gi` at (u,v):
+// CqMicroPolygon::InterpolateOutputs (micropolygon.cpp:1443-1462) over the
+// cached SqMpgSampleInfo (1464-1529).  Also returns the hit flags
+// (Flag_Matte = 1, Flag_MatteAlpha = 2).
+__device__ __forceinline__ void hit_colour(const GridsDev& g, int gi, int m, float u, float v, float dat[7],
+                                           int& flg) {
+	const int cu = __ldg(g.cu + gi);
+	const int iv = m / cu, iu = m - iv * cu;
+	const int index = iv * (cu + 1) + iu;
+	const long long cb = __ldg(g.cbase + gi);
+	const int gflags = __ldg(g.flags + gi);
+	if (gflags & 1) {
+		const int vi[4] = {index, index + 1, index + cu + 1, index + cu + 2};
+		float wt[4];
+		smooth_weights(u, v, wt);
+		float4 c[4], o[4];
+#pragma unroll
+		for (int q = 0; q < 4; ++q) {
+			c[q] = g.Ci ? __ldg(g.Ci + cb + vi[q]) : make_float4(1, 1, 1, 0);
+			o[q] = g.Oi ? __ldg(g.Oi + cb + vi[q]) : make_float4(1, 1, 1, 0);
+		}
+		dat[0] = ((wt[0] * c[0].x + wt[1] * c[1].x) + wt[2] * c[2].x) + wt[3] * c[3].x;
+		dat[1] = ((wt[0] * c[0].y + wt[1] * c[1].y) + wt[2] * c[2].y) + wt[3] * c[3].y;
+		dat[2] = ((wt[0] * c[0].z + wt[1] * c[1].z) + wt[2] * c[2].z) + wt[3] * c[3].z;
+		dat[3] = ((wt[0] * o[0].x + wt[1] * o[1].x) + wt[2] * o[2].x) + wt[3] * o[3].x;
+		dat[4] = ((wt[0] * o[0].y + wt[1] * o[1].y) + wt[2] * o[2].y) + wt[3] * o[3].y;
+		dat[5] = ((wt[0] * o[0].z + wt[1] * o[1].z) + wt[2] * o[2].z) + wt[3] * o[3].z;
+	} else {
+		const float4 c = g.Ci ? __ldg(g.Ci + cb + index) : make_float4(1, 1, 1, 0);
+		const float4 o = g.Oi ? __ldg(g.Oi + cb + index) : make_float4(1, 1, 1, 0);
+		dat[0] = c.x; dat[1] = c.y; dat[2] = c.z;
+		dat[3] = o.x; dat[4] = o.y; dat[5] = o.z;
+	}
+	flg = ((gflags & 2) ? 1 : 0) | ((gflags & 4) ? 2 : 0);
+}
+
+// Grid owning a global micropolygon id (binary search over first ids).
+__device__ __forceinline__ int grid_of(const GridsDev& g, int id) {
+	int lo = 0, hi = g.ngrids - 1;
+	while (lo < hi) {
+		const int mid = (lo + hi + 1) >> 1;
+		if (__ldg(g.mpbase + mid) <= id) lo = mid; else hi = mid - 1;
+	}
+	return lo;
+}
+
+// Entry k of a sample's fragment set in Combine's sort order.  The set is the
+// transparent fragments in insertion order followed by the occluding hit
+// (imagepixel.cpp:155-161), sorted by ascending depth; exact depth ties keep
+// that order.  The list is newest-first, so list position p has sequence
+// n-1-p.  Selection by (depth, sequence) keys needs no per-sample storage.
+struct FragKey { float d; int seq; int idx; };
+
+__device__ __forceinline__ FragKey next_key(const FragPool& pool, int head, int n, bool has_occl, float occl_d,
+                                            FragKey prev, bool first, bool descending) {
+	FragKey best{descending ? -FLT_MAX : FLT_MAX, descending ? -1 : 0x7fffffff, -2};
+	int seq = n - 1;
+	bool any = false;
+	for (int f = head; f >= 0; f = pool.next[f], --seq) {
+		const float d = pool.frag[f].x;
+		bool beyond, better;
+		if (descending) {
+			beyond = first || d < prev.d || (d == prev.d && seq < prev.seq);
+			better = !any || d > best.d || (d == best.d && seq > best.seq);
+		} else {
+			beyond = first || d > prev.d || (d == prev.d && seq > prev.seq);
+			better = !any || d < best.d || (d == best.d && seq < best.seq);
+		}
+		if (beyond && better) { best = FragKey{d, seq, f}; any = true; }
+	}
+	if (has_occl) {
+		const float d = occl_d;
+		const int sq = n;
+		bool beyond, better;
+		if (descending) {
+			beyond = first || d < prev.d || (d == prev.d && sq < prev.seq);
+			better = !any || d > best.d || (d == best.d && sq > best.seq);
+		} else {
+			beyond = first || d > prev.d || (d == prev.d && sq > prev.seq);
+			better = !any || d < best.d || (d == best.d && sq < best.seq);
+		}
+		if (beyond && better) best = FragKey{d, sq, -1};
+	}
+	return best;
+}
+
+__device__ __forceinline__ void key_data(const GridsDev& g, const FragPool& pool, const FragKey& k,
+                                         const float occl[7], int occl_flags, float dat[7], int& flg) {
+	if (k.idx == -1) {
+#pragma unroll
+		for (int q = 0; q < 7; ++q) dat[q] = occl[q];
+		flg = occl_flags;
+	} else {
+		const float4 fr = pool.frag[k.idx];
+		const int id = __float_as_int(fr.y);
+		const int gi = grid_of(g, id);
+		hit_colour(g, gi, id - (int)__ldg(g.mpbase + gi), fr.z, fr.w, dat, flg);
+		dat[6] = fr.x;
+	}
+}
+
+// CqImagePixel::Combine for a sample with transparent fragments
+// (imagepixel.cpp:155-301).  Returns the fragment count; writes the collapsed
+// sample into occl / occl_flags.
+__device__ inline int combine_fragments(const FrameParams& fp, const GridsDev& g, const FragPool& pool, int head,
+                                 bool has_occl, float occlZ, float occl[7], int& occl_flags) {
+	int n = 0;
+	for (int f = head; f >= 0; f = pool.next[f]) ++n;
+	const int ntot = n + (has_occl ? 1 : 0);
+	float sc[3] = {0, 0, 0}, so[3] = {0, 0, 0};
+	float opaque0 = occlZ, opaque1 = FLT_MAX, maxOpaque = FLT_MAX;
+	float top[7] = {0, 0, 0, 0, 0, 0, 0};
+	int top_flags = 0;
+	FragKey prev{0, 0, -2};
+	for (int k = 0; k < ntot; ++k) {
+		const FragKey key = next_key(pool, head, n, has_occl, occl[6], prev, k == 0, true);
+		prev = key;
+		float dat[7];
+		int flg;
+		key_data(g, pool, key, occl, occl_flags, dat, flg);
+		if (flg & 1) {
+			float nc[3], no[3];
+#pragma unroll
+			for (int q = 0; q < 3; ++q) nc[q] = (1.0f - dat[3 + q]) * sc[q] + dat[3 + q] * 0.0f;
+#pragma unroll
+			for (int q = 0; q < 3; ++q) no[q] = (1.0f - dat[q]) * so[q] + dat[q] * 0.0f;
+#pragma unroll
+			for (int q = 0; q < 3; ++q) { sc[q] = nc[q]; so[q] = no[q]; }
+		} else {
+#pragma unroll
+			for (int q = 0; q < 3; ++q) {
+				const float o = dat[3 + q];
+				const float cl = o < 0.0f ? 0.0f : (o > 1.0f ? 1.0f : o);
+				sc[q] = (sc[q] * (1.0f - cl)) + dat[q];
+			}
+#pragma unroll
+			for (int q = 0; q < 3; ++q) so[q] = ((1.0f - so[q]) * dat[3 + q]) + so[q];
+		}
+		if (dat[3] >= fp.zthr[0] && dat[4] >= fp.zthr[1] && dat[5] >= fp.zthr[2]) {
+			opaque1 = opaque0;
+			opaque0 = dat[6];
+			if (!(maxOpaque < FLT_MAX)) maxOpaque = dat[6];
+		}
+		if (k == ntot - 1) {
+#pragma unroll
+			for (int q = 0; q < 7; ++q) top[q] = dat[q];
+			top_flags = flg;
+		}
+	}
+	float depth = top[6];
+	if (fp.depth_filter == 0) {
+		depth = opaque0;
+	} else if (fp.depth_filter == 1) {
+		depth = (ntot > 1) ? ((opaque0 + opaque1) * 0.5f) : FLT_MAX;
+	} else if (fp.depth_filter == 2) {
+		depth = maxOpaque;
+	} else {
+		// average over entries with any opacity channel at the threshold, in
+		// ascending order (imagepixel.cpp:279-296)
+		float tot = 0.0f;
+		int cnt = 0;
+		FragKey pk{0, 0, -2};
+		for (int k = 0; k < ntot; ++k) {
+			const FragKey key = next_key(pool, head, n, has_occl, occl[6], pk, k == 0, false);
+			pk = key;
+			float dat[7];
+			int flg;
+			key_data(g, pool, key, occl, occl_flags, dat, flg);
+			if (dat[3] >= fp.zthr[0] || dat[4] >= fp.zthr[1] || dat[5] >= fp.zthr[2]) {
+				tot += dat[6];
+				cnt++;
+			}
+		}
+		depth = tot / (float)cnt;
+	}
+	occl[0] = sc[0]; occl[1] = sc[1]; occl[2] = sc[2];
+	occl[3] = so[0]; occl[4] = so[1]; occl[5] = so[2];
+	occl[6] = depth;
+	occl_flags = top_flags;
+	return n;
+}
+
+
+}  // namespace aqh

@@ -1,0 +1,357 @@
+"""Seeded micropolygon streams, frame options and sample patterns.
+
+A ``Scene`` holds exactly what the hider consumes, in the layouts of
+``include/aqh.h``: shaded grids (raster-space P plus Ci/Oi, float4 SoA), the
+frame options that SqOptionCache / CqRenderer supply (libs/core/optioncache.cpp,
+renderer.h), and the sample pattern caches an IqSampler hands to
+CqImagePixel::setSamples (libs/core/isampler.h, imagepixel.cpp:334-359).
+
+The generators make the workloads the benchmark configurations name:
+
+* ``opaque_stream`` -- 16x16-quad grids in raster space, origins uniform over
+  the image, vertex spacing 1 px with +-0.3 px jitter, z = z0 + s*(x - x0),
+  Ci ~ U[0,1]^3, Oi = 1 (gaussian 2x2, PixelSamples 4 4 at full size).
+* ``transparent_stream`` -- the same generator with Oi ~ U[0.1,0.9]^3 and grid
+  origins concentrated in a centre window.
+* ``motion_dof_stream`` -- two motion keys per vertex with a per-grid
+  displacement, plus depth-of-field lens samples.
+
+Inputs are synthetic stand-ins with the configured shapes, sizes and value
+distributions; nothing here reads a dataset.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import Optional
+
+import numpy as np
+
+FILTERS = {"box": 0, "triangle": 1, "gaussian": 2, "catmull-rom": 3, "sinc": 4,
+           "disk": 5, "bessel": 6, "mitchell": 7}
+GRID_SMOOTH, GRID_MATTE, GRID_MATTEALPHA, GRID_OPAQUE = 1, 2, 4, 8
+FLT_MAX = float(np.finfo(np.float32).max)
+
+
+@dataclasses.dataclass
+class Frame:
+    """Frame options (aqh_frame_desc).  Defaults are the reference's
+    (libs/core/options.cpp:273-310)."""
+    width: int = 640
+    height: int = 480
+    crop: Optional[tuple] = None          # (xmin, xmax, ymin, ymax) in pixels
+    bucket: tuple = (16, 16)
+    xsamples: int = 2
+    ysamples: int = 2
+    xfilter: float = 2.0
+    yfilter: float = 2.0
+    filter: str = "gaussian"
+    gain: float = 1.0
+    gamma: float = 1.0
+    q_one: float = 255.0
+    q_min: float = 0.0
+    q_max: float = 255.0
+    q_dither: float = 0.5
+    shutter: tuple = (0.0, 0.0)
+    fstop: float = FLT_MAX
+    focal_length: float = 0.0
+    focal_distance: float = 0.0
+    dof_scale: tuple = (1.0, 1.0)
+    depth_filter: int = 0
+    zthreshold: tuple = (1.0, 1.0, 1.0)
+    display_z: int = 0
+
+    @property
+    def spp(self) -> int:
+        return self.xsamples * self.ysamples
+
+    @property
+    def crop_window(self) -> tuple:
+        return self.crop if self.crop is not None else (0, self.width, 0, self.height)
+
+    @property
+    def shift(self) -> tuple:
+        # CqBucketProcessor::m_DiscreteShiftX/Y = lfloor(filterwidth/2)
+        return (int(math.floor(np.float32(self.xfilter) / np.float32(2.0))),
+                int(math.floor(np.float32(self.yfilter) / np.float32(2.0))))
+
+    @property
+    def sample_region(self) -> tuple:
+        """(x0, y0, w, h) of the sample region: crop window grown by the shift."""
+        cx0, cx1, cy0, cy1 = self.crop_window
+        sx, sy = self.shift
+        return (cx0 - sx, cy0 - sy, (cx1 - cx0) + 2 * sx, (cy1 - cy0) + 2 * sy)
+
+    @property
+    def use_dof(self) -> bool:
+        return 0.0 < self.fstop < FLT_MAX
+
+    def dof_terms(self) -> tuple:
+        """(m_DofMultiplier, m_OneOverFocalDistance) as CqRenderer::SetDepthOfFieldData
+        computes them (renderer.h:368-377): double arithmetic stored to float."""
+        if not self.use_dof:
+            return (0.0, 0.0)
+        lens = np.float32(np.float32(self.focal_length) / np.float32(self.fstop))
+        fd = np.float32(self.focal_distance)
+        mult = np.float32(0.5 * float(lens) * float(fd) / float(np.float32(fd + lens)))
+        inv = np.float32(1.0 / float(fd))
+        return (float(mult), float(inv))
+
+
+@dataclasses.dataclass
+class Grids:
+    """Packed shaded grids (aqh_submit_grids_device layout)."""
+    cu: np.ndarray        # int32[G]
+    cv: np.ndarray        # int32[G]
+    nkeys: np.ndarray     # int32[G]
+    flags: np.ndarray     # int32[G]
+    pbase: np.ndarray     # int64[G] first vertex of key 0 in P
+    cbase: np.ndarray     # int64[G] first vertex in Ci/Oi
+    tbase: np.ndarray     # int32[G] first key time
+    times: np.ndarray     # float32[T]
+    P: np.ndarray         # float32[NP, 4]
+    Ci: np.ndarray        # float32[NC, 4]
+    Oi: np.ndarray        # float32[NC, 4]
+    culled: Optional[np.ndarray] = None  # uint8[total micropolygons]
+
+    @property
+    def ngrids(self) -> int:
+        return int(self.cu.shape[0])
+
+    @property
+    def micropolygons(self) -> int:
+        return int(np.sum(self.cu.astype(np.int64) * self.cv.astype(np.int64)))
+
+    def nbytes_algorithmic(self) -> int:
+        """P per key plus Ci and Oi per vertex, float4 each, read once."""
+        nv = (self.cu.astype(np.int64) + 1) * (self.cv.astype(np.int64) + 1)
+        return int(np.sum(nv * (16 * self.nkeys.astype(np.int64) + 32)))
+
+
+@dataclasses.dataclass
+class Samples:
+    """Sample pattern caches plus per-pixel choices (aqh_samples)."""
+    npatterns: int
+    pos: np.ndarray                      # float32[npat, spp, 2]
+    time: Optional[np.ndarray] = None    # float32[npat, spp]
+    dof: Optional[np.ndarray] = None     # float32[npat, spp, 2]
+    shuffle: Optional[np.ndarray] = None  # int32[npat, spp]
+    lod: Optional[np.ndarray] = None
+    pos_index: Optional[np.ndarray] = None   # uint32[npix]
+    dof_index: Optional[np.ndarray] = None
+    time_index: Optional[np.ndarray] = None
+    shuffle_index: Optional[np.ndarray] = None
+    lod_index: Optional[np.ndarray] = None
+    dither: Optional[np.ndarray] = None      # float32[crop h * crop w]
+
+
+@dataclasses.dataclass
+class Scene:
+    frame: Frame
+    grids: Grids
+    samples: Samples
+
+
+# ---------------------------------------------------------------------------
+# Sample patterns
+
+def stratified_patterns(xs: int, ys: int, npatterns: int, rng: np.random.Generator,
+                        with_time: bool = False, with_dof: bool = False) -> dict:
+    """The build's own stratified-jittered pattern cache: sample (ix, iy) lies in
+    sub-pixel cell (ix, iy); times are stratified over the spp strata with one
+    random offset per pattern (multijitter.cpp:176-190 style); lens positions are
+    stratified over the xs*ys lens cells; the lens-shuffle table is a random
+    permutation per pattern (multijitter.cpp:192-201 style)."""
+    spp = xs * ys
+    ix = np.tile(np.arange(xs), ys).astype(np.float32)
+    iy = np.repeat(np.arange(ys), xs).astype(np.float32)
+    jx = rng.random((npatterns, spp), dtype=np.float32)
+    jy = rng.random((npatterns, spp), dtype=np.float32)
+    pos = np.empty((npatterns, spp, 2), np.float32)
+    pos[..., 0] = (ix + jx) * np.float32(1.0 / xs)
+    pos[..., 1] = (iy + jy) * np.float32(1.0 / ys)
+    np.clip(pos, 0.0, np.nextafter(np.float32(1.0), np.float32(0.0)), out=pos)
+    out = {"pos": pos}
+    if with_time:
+        delta = np.float32(1.0 / spp)
+        r = rng.random((npatterns, 1), dtype=np.float32) * delta
+        out["time"] = (np.arange(spp, dtype=np.float32)[None, :] * delta + r).astype(np.float32)
+    if with_dof:
+        lx = rng.random((npatterns, spp), dtype=np.float32)
+        ly = rng.random((npatterns, spp), dtype=np.float32)
+        dof = np.empty((npatterns, spp, 2), np.float32)
+        dof[..., 0] = (ix + lx) * np.float32(1.0 / xs)
+        dof[..., 1] = (iy + ly) * np.float32(1.0 / ys)
+        np.clip(dof, 0.0, np.nextafter(np.float32(1.0), np.float32(0.0)), out=dof)
+        out["dof"] = dof
+        out["shuffle"] = np.argsort(rng.random((npatterns, spp)), axis=1).astype(np.int32)
+    return out
+
+
+def make_samples(frame: Frame, rng: np.random.Generator, npatterns: int = 250,
+                 explicit: bool = False, dither: bool = False) -> Samples:
+    """Pattern caches of `npatterns` entries picked per pixel at random (as the
+    reference's sampler does), or one explicit pattern per pixel."""
+    x0, y0, w, h = frame.sample_region
+    npix = w * h
+    mb = frame.shutter[1] != frame.shutter[0]
+    pats = stratified_patterns(frame.xsamples, frame.ysamples, npix if explicit else npatterns, rng,
+                               with_time=mb, with_dof=frame.use_dof)
+    n = npix if explicit else npatterns
+
+    def idx():
+        if explicit:
+            return None
+        return rng.integers(0, n, npix, dtype=np.uint32)
+
+    cx0, cx1, cy0, cy1 = frame.crop_window
+    dith = rng.random((cy1 - cy0) * (cx1 - cx0), dtype=np.float32) if dither else None
+    return Samples(npatterns=n, pos=pats["pos"], time=pats.get("time"), dof=pats.get("dof"),
+                   shuffle=pats.get("shuffle"), pos_index=idx(), time_index=idx() if mb else None,
+                   dof_index=idx() if frame.use_dof else None,
+                   shuffle_index=idx() if frame.use_dof else None, dither=dith)
+
+
+# ---------------------------------------------------------------------------
+# Grid streams
+
+def _pack(cu, cv, nkeys, flags, P_list_or_arr, Ci, Oi, times=None, tbase=None) -> Grids:
+    G = len(cu)
+    nv = (cu.astype(np.int64) + 1) * (cv.astype(np.int64) + 1)
+    pbase = np.zeros(G, np.int64)
+    pbase[1:] = np.cumsum(nv * nkeys)[:-1]
+    cbase = np.zeros(G, np.int64)
+    cbase[1:] = np.cumsum(nv)[:-1]
+    if times is None:
+        times = np.zeros(1, np.float32)
+        tbase = np.zeros(G, np.int32)
+    return Grids(cu=cu.astype(np.int32), cv=cv.astype(np.int32), nkeys=nkeys.astype(np.int32),
+                 flags=flags.astype(np.int32), pbase=pbase, cbase=cbase, tbase=tbase.astype(np.int32),
+                 times=times.astype(np.float32), P=P_list_or_arr, Ci=Ci, Oi=Oi)
+
+
+def regular_grids(ngrids: int, width: int, height: int, rng: np.random.Generator, n: int = 16,
+                  jitter: float = 0.3, zrange=(1.0, 1000.0), slope: float = 0.01,
+                  window: Optional[tuple] = None, opacity=None, motion: Optional[float] = None,
+                  smooth: bool = True, origin_margin: float = 0.0) -> Grids:
+    """n x n-quad grids in raster space.  Grid origin uniform over `window`
+    (default the image); vertex (i, j) = origin + (i, j) + U[-jitter, jitter]^2;
+    z = z0 + s*(x - x0), z0 ~ U[zrange], s ~ U[-slope, slope]; Ci ~ U[0,1]^3;
+    Oi = 1, or U[opacity]^3 when `opacity` = (lo, hi).  With `motion` = M a
+    second key displaces every vertex of a grid by one vector of length U[0, M]
+    in a uniform direction (key times 0 and 1)."""
+    nv1 = n + 1
+    nvert = nv1 * nv1
+    wx0, wx1, wy0, wy1 = window if window is not None else (0.0, float(width), 0.0, float(height))
+    ox = rng.uniform(wx0 - origin_margin, wx1, ngrids).astype(np.float32)
+    oy = rng.uniform(wy0 - origin_margin, wy1, ngrids).astype(np.float32)
+    z0 = rng.uniform(zrange[0], zrange[1], ngrids).astype(np.float32)
+    s = rng.uniform(-slope, slope, ngrids).astype(np.float32)
+    gi = np.tile(np.arange(nv1, dtype=np.float32), nv1)
+    gj = np.repeat(np.arange(nv1, dtype=np.float32), nv1)
+    nkeys = 2 if motion is not None else 1
+    P = np.empty((ngrids, nkeys, nvert, 4), np.float32)
+    jx = rng.uniform(-jitter, jitter, (ngrids, nvert)).astype(np.float32)
+    jy = rng.uniform(-jitter, jitter, (ngrids, nvert)).astype(np.float32)
+    x = ox[:, None] + gi[None, :] + jx
+    y = oy[:, None] + gj[None, :] + jy
+    P[:, 0, :, 0] = x
+    P[:, 0, :, 1] = y
+    P[:, 0, :, 2] = z0[:, None] + s[:, None] * (x - ox[:, None])
+    P[:, 0, :, 3] = 0.0
+    if motion is not None:
+        mag = rng.uniform(0.0, motion, ngrids).astype(np.float32)
+        ang = rng.uniform(0.0, 2 * np.pi, ngrids)
+        dx = (mag * np.cos(ang)).astype(np.float32)
+        dy = (mag * np.sin(ang)).astype(np.float32)
+        P[:, 1] = P[:, 0]
+        P[:, 1, :, 0] += dx[:, None]
+        P[:, 1, :, 1] += dy[:, None]
+    Ci = np.empty((ngrids, nvert, 4), np.float32)
+    Ci[..., :3] = rng.random((ngrids, nvert, 3), dtype=np.float32)
+    Ci[..., 3] = 0.0
+    Oi = np.ones((ngrids, nvert, 4), np.float32)
+    Oi[..., 3] = 0.0
+    flags = np.full(ngrids, GRID_SMOOTH if smooth else 0, np.int32)
+    if opacity is not None:
+        Oi[..., :3] = rng.uniform(opacity[0], opacity[1], (ngrids, nvert, 3)).astype(np.float32)
+    else:
+        flags |= GRID_OPAQUE
+    cu = np.full(ngrids, n, np.int32)
+    cv = np.full(ngrids, n, np.int32)
+    times = None
+    tbase = None
+    if motion is not None:
+        times = np.tile(np.array([0.0, 1.0], np.float32), ngrids)
+        tbase = np.arange(ngrids, dtype=np.int32) * 2
+    return _pack(cu, cv, np.full(ngrids, nkeys, np.int32), flags, P.reshape(-1, 4),
+                 Ci.reshape(-1, 4), Oi.reshape(-1, 4), times, tbase)
+
+
+def concat_grids(parts: list) -> Grids:
+    """Concatenate grid streams in order."""
+    cu = np.concatenate([g.cu for g in parts])
+    cv = np.concatenate([g.cv for g in parts])
+    nkeys = np.concatenate([g.nkeys for g in parts])
+    flags = np.concatenate([g.flags for g in parts])
+    P = np.concatenate([g.P for g in parts])
+    Ci = np.concatenate([g.Ci for g in parts])
+    Oi = np.concatenate([g.Oi for g in parts])
+    times = np.concatenate([g.times for g in parts])
+    tb, off = [], 0
+    for g in parts:
+        tb.append(g.tbase + off)
+        off += len(g.times)
+    return _pack(cu, cv, nkeys, flags, P, Ci, Oi, times, np.concatenate(tb))
+
+
+def opaque_stream(width=1920, height=1080, ngrids=200_000, xs=4, ys=4, seed=0xC1,
+                  npatterns=250, explicit_samples=False, filt=("gaussian", 2.0, 2.0)) -> Scene:
+    """Opaque synthetic stream: 16x16-quad raster grids, Oi = 1, PixelSamples xs ys."""
+    rng = np.random.default_rng(seed)
+    fr = Frame(width=width, height=height, xsamples=xs, ysamples=ys, filter=filt[0],
+               xfilter=filt[1], yfilter=filt[2], q_dither=0.0)
+    g = regular_grids(ngrids, width, height, rng)
+    return Scene(fr, g, make_samples(fr, rng, npatterns, explicit_samples))
+
+
+def transparent_stream(width=1920, height=1080, ngrids=16_200, xs=8, ys=8, seed=0xC2,
+                       npatterns=250, explicit_samples=False, window_frac=0.5) -> Scene:
+    """Transparent stream: grid origins in a centre window (window_frac of each
+    image dimension), Oi ~ U[0.1,0.9]^3, catmull-rom 3x3."""
+    rng = np.random.default_rng(seed)
+    fr = Frame(width=width, height=height, xsamples=xs, ysamples=ys, filter="catmull-rom",
+               xfilter=3.0, yfilter=3.0, q_dither=0.0)
+    ww, wh = width * window_frac, height * window_frac
+    win = ((width - ww) / 2, (width + ww) / 2, (height - wh) / 2, (height + wh) / 2)
+    g = regular_grids(ngrids, width, height, rng, window=win, opacity=(0.1, 0.9))
+    return Scene(fr, g, make_samples(fr, rng, npatterns, explicit_samples))
+
+
+def motion_dof_stream(width=1920, height=1080, ngrids=100_000, xs=6, ys=6, seed=0xC3,
+                      npatterns=250, explicit_samples=False, motion=20.0, dof=True,
+                      fstop=2.8, focal_length=0.05, focal_distance=50.0,
+                      dof_scale=(540.0, 540.0)) -> Scene:
+    """Motion blur + depth of field: two keys per vertex with a per-grid
+    displacement of length U[0, motion] px; Shutter 0 1; DepthOfField fstop,
+    focal length, focal distance; box 1x1 filter."""
+    rng = np.random.default_rng(seed)
+    fr = Frame(width=width, height=height, xsamples=xs, ysamples=ys, filter="box",
+               xfilter=1.0, yfilter=1.0, q_dither=0.0, shutter=(0.0, 1.0) if motion else (0.0, 0.0))
+    if dof:
+        fr.fstop, fr.focal_length, fr.focal_distance = fstop, focal_length, focal_distance
+        fr.dof_scale = dof_scale
+    g = regular_grids(ngrids, width, height, rng, motion=motion)
+    return Scene(fr, g, make_samples(fr, rng, npatterns, explicit_samples))
+
+
+def scaled(scene_fn, scale: float, **kw) -> Scene:
+    """A smaller copy of a benchmark stream: image and grid count scaled so the
+    depth complexity stays the same."""
+    w = max(16, int(round(kw.pop("width", 1920) * scale)))
+    h = max(16, int(round(kw.pop("height", 1080) * scale)))
+    n = kw.pop("ngrids", None)
+    if n is None:
+        n = {"opaque_stream": 200_000, "transparent_stream": 16_200, "motion_dof_stream": 100_000}[scene_fn.__name__]
+    n = max(1, int(round(n * scale * scale)))
+    return scene_fn(width=w, height=h, ngrids=n, **kw)

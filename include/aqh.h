@@ -1,0 +1,252 @@
+/*
+ * aqh.h -- C-ABI of the GB300-native REYES hider ("aqh").
+ *
+ * This is the drop-in boundary for the aqsis hider path: the part of
+ * aqsis libs/core that runs after shading (bin micropolygons into buckets,
+ * sample them with depth/opacity compositing into the pixel sample store,
+ * reconstruct pixels with the pixel filter, expose and quantize).  The
+ * reference's RI front end, CPU dicer and shading VM keep producing shaded
+ * grids; its CqImageBuffer hands them to this library instead of splitting
+ * them into CqMicroPolygon objects, and its display manager reads finished
+ * buckets back through an IqChannelBuffer view of aqh_read_bucket().
+ *
+ * Plain C types only; no exceptions cross this boundary.  Every call returns
+ * an aqh_status; aqh_last_error() gives the message of the last failure on
+ * a context.  One host thread per context.
+ *
+ * Insertion order: micropolygons are ordered by grid submission order, then
+ * by row (iv), then column (iu), exactly the order in which
+ * CqMicroPolyGrid::Split feeds CqImageBuffer::AddMPG
+ * (libs/core/micropolygon.cpp:770-880).  Opaque sample ties are resolved by
+ * that order, as in the reference.
+ */
+#ifndef AQH_H
+#define AQH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AQH_VERSION_MAJOR 0
+#define AQH_VERSION_MINOR 1
+
+typedef enum {
+	AQH_OK = 0,
+	AQH_EINVAL = 1,      /* bad argument or state */
+	AQH_ENOMEM = 2,      /* device or host allocation failed */
+	AQH_EDEVICE = 3,     /* CUDA error */
+	AQH_ETIMEDOUT = 4,   /* a bounded device wait ran out */
+	AQH_EREJECTED = 5,   /* admission refused (serving) */
+	AQH_ENOTREADY = 6,   /* job still running (serving) */
+	AQH_ELIMIT = 7       /* a documented size limit was exceeded */
+} aqh_status;
+
+/* RiPixelFilter filter functions (libs/core/filters.cpp). */
+typedef enum {
+	AQH_FILTER_BOX = 0,
+	AQH_FILTER_TRIANGLE = 1,
+	AQH_FILTER_GAUSSIAN = 2,
+	AQH_FILTER_CATMULLROM = 3,
+	AQH_FILTER_SINC = 4,
+	AQH_FILTER_DISK = 5,
+	AQH_FILTER_BESSEL = 6,
+	AQH_FILTER_MITCHELL = 7
+} aqh_filter;
+
+/* Hider "depthfilter" (libs/core/optioncache.h:34). */
+typedef enum { AQH_DEPTH_MIN = 0, AQH_DEPTH_MIDPOINT = 1, AQH_DEPTH_MAX = 2, AQH_DEPTH_AVERAGE = 3 } aqh_depth_filter;
+
+/* Per-grid flags (SqGridInfo, libs/core/micropolygon.h:57-63). */
+enum {
+	AQH_GRID_SMOOTH = 1,      /* ShadingInterpolation "smooth": bilinear Ci/Oi across the micropolygon */
+	AQH_GRID_MATTE = 2,       /* Matte 1 (SqImageSample::Flag_Matte) */
+	AQH_GRID_MATTEALPHA = 4,  /* aqsis "matte alpha" (Flag_MatteAlpha) */
+	AQH_GRID_OPAQUE = 8       /* caller guarantees Oi >= 1 on every vertex (skips reading Oi while sampling) */
+};
+
+typedef struct aqh_ctx aqh_ctx;
+
+typedef struct {
+	int device;                 /* CUDA device ordinal */
+	size_t vertex_capacity;     /* initial device capacity in vertices (0 = grow on demand) */
+	size_t grid_capacity;       /* initial device capacity in grids (0 = grow on demand) */
+} aqh_device_opts;
+
+/*
+ * Frame options.  Replaces the hider's reads of SqOptionCache::cacheOptions
+ * (libs/core/optioncache.cpp:48-118) and CqRenderer state set by the RI
+ * option calls RiFormat / RiCropWindow / RiPixelSamples (api/ri.cpp:852-858) /
+ * RiPixelFilter (:862-867) / RiExposure (:873-877) / RiQuantize (:902-930) /
+ * RiShutter (:832-836) / RiDepthOfField (:821-826) / RiHider (:1014-1038) and
+ * Option "limits" "bucketsize" / "zthreshold".
+ */
+typedef struct {
+	int width, height;                 /* Format */
+	int crop_xmin, crop_xmax;          /* raster crop window in pixels (CqRenderer::initialiseCropWindow); */
+	int crop_ymin, crop_ymax;          /*   all zero = whole image */
+	int bucket_x, bucket_y;            /* Option "limits" "bucketsize" (0 = 16) */
+	int xsamples, ysamples;            /* PixelSamples */
+	float xfilter, yfilter;            /* PixelFilter widths */
+	int filter;                        /* aqh_filter */
+	float gain, gamma;                 /* Exposure */
+	float q_one, q_min, q_max, q_dither; /* Quantize "rgba" one min max dither */
+	float shutter_open, shutter_close; /* Shutter */
+	float fstop, focal_length, focal_distance; /* DepthOfField (fstop >= FLT_MAX or 0 = off) */
+	float dof_scale_x, dof_scale_y;    /* raster size of a unit camera-space vector at z=-1 (options.cpp:162-171) */
+	int depth_filter;                  /* aqh_depth_filter */
+	float zthreshold[3];               /* Option "limits" "zthreshold" (default 1 1 1) */
+	int display_z;                     /* nonzero when a display asks for z (DMode_Z) */
+} aqh_frame_desc;
+
+/* Fill `d` with the reference defaults (libs/core/options.cpp:273-310):
+ * 640x480, PixelSamples 2 2, gaussian 2x2, Exposure 1 1, Quantize 255 0 255 0.5. */
+void aqh_frame_desc_defaults(aqh_frame_desc* d);
+
+/*
+ * One shaded grid.  Replaces the per-micropolygon CqImageBuffer::AddMPG()
+ * calls made by CqMicroPolyGrid::Split / CqMotionMicroPolyGrid::Split
+ * (libs/core/micropolygon.cpp:641-892, 946-1156; imagebuffer.cpp:514-591).
+ * P is already in the hybrid raster space Split produces: raster x, raster y,
+ * camera-space z.  The library copies the arrays before returning.
+ */
+typedef struct {
+	int cu, cv;                  /* micropolygons along u and v; (cu+1)*(cv+1) vertices */
+	int nkeys;                   /* motion keys (1 = static, at most AQH_MAX_KEYS) */
+	const float* key_times;      /* nkeys shutter times, ascending (NULL when nkeys == 1) */
+	const float* P;              /* float4[nkeys][(cu+1)*(cv+1)]: x, y, z, unused */
+	const float* Ci;             /* float4[(cu+1)*(cv+1)]: r, g, b, unused; NULL = white */
+	const float* Oi;             /* float4[(cu+1)*(cv+1)]: r, g, b, unused; NULL = opaque */
+	const uint8_t* culled;       /* cu*cv bytes, nonzero = culled micropolygon (m_CulledPolys); may be NULL */
+	int flags;                   /* AQH_GRID_* */
+} aqh_grid;
+
+#define AQH_MAX_KEYS 4
+#define AQH_MAX_SPP 256
+
+/*
+ * Sample patterns.  Mirrors IqSampler (libs/core/isampler.h:42-78) and
+ * CqImagePixel::setSamples (imagepixel.cpp:334-359): each pixel picks a
+ * position pattern, a lens pattern, a time pattern and a lens-shuffle table
+ * out of pattern caches.  Explicit per-pixel samples are the special case of
+ * one pattern per pixel with NULL index arrays.
+ *
+ * The sample region is the crop window grown by floor(filterwidth/2) pixels
+ * on every side (bucketprocessor.cpp:112-125); pixel indices are row-major
+ * over that region.
+ */
+typedef struct {
+	int npatterns;                /* patterns in each table */
+	const float* pos;             /* float2[npatterns][spp]: offsets inside the pixel (added to x, y) */
+	const float* time;            /* float[npatterns][spp] in [0,1): scaled to the shutter; NULL = 0 */
+	const float* dof;             /* float2[npatterns][spp]: lens positions in [0,1)^2 (projected to the
+	                                 unit disc by the library); NULL = no lens offsets */
+	const int32_t* shuffle;       /* int[npatterns][spp] lens-shuffle tables; NULL = identity */
+	const float* lod;             /* float[npatterns][spp] detail levels; NULL = 0 */
+	/* per-pixel pattern choices over the sample region; NULL = pattern index == pixel index */
+	const uint32_t* pos_index;
+	const uint32_t* dof_index;
+	const uint32_t* time_index;
+	const uint32_t* shuffle_index;
+	const uint32_t* lod_index;
+	/* per display pixel (crop window, row-major) dither value s in [0,1); NULL = 0 */
+	const float* dither;
+} aqh_samples;
+
+/* ---- context ------------------------------------------------------------ */
+aqh_status aqh_create(const aqh_device_opts* opts, aqh_ctx** out);
+void aqh_destroy(aqh_ctx* ctx);
+const char* aqh_last_error(const aqh_ctx* ctx);
+const char* aqh_status_string(aqh_status s);
+
+/* ---- frame (RiWorldBegin ... RiWorldEnd) --------------------------------- */
+/* Validate options and reset the frame's grid stream.  RiWorldBegin's
+ * CqImageBuffer::SetImage (imagebuffer.cpp:174-228). */
+aqh_status aqh_frame_begin(aqh_ctx* ctx, const aqh_frame_desc* desc);
+/* Upload sample patterns; required before aqh_render.  Copies the arrays. */
+aqh_status aqh_set_samples(aqh_ctx* ctx, const aqh_samples* samples);
+/* Append one grid (host arrays) in insertion order: CqImageBuffer::AddMPG. */
+aqh_status aqh_submit_grid(aqh_ctx* ctx, const aqh_grid* grid);
+/* Append many grids whose arrays already live in device memory, packed:
+ *   cu, cv, nkeys, flags: per grid;  vbase: first vertex of each grid in P/Ci/Oi
+ *   (key k of grid g starts at vbase[g] + k*(cu+1)*(cv+1) in P; Ci/Oi are indexed
+ *   by cbase[g]); times: key times at tbase[g].  All pointers are device pointers
+ *   that must stay valid until aqh_render returns.  Used by callers that dice
+ *   and shade on the device or that keep a scene resident between frames. */
+aqh_status aqh_submit_grids_device(aqh_ctx* ctx, int ngrids,
+                                   const int32_t* d_cu, const int32_t* d_cv, const int32_t* d_nkeys,
+                                   const int32_t* d_flags, const int64_t* d_pbase, const int64_t* d_cbase,
+                                   const int32_t* d_tbase, const float* d_times,
+                                   const float* d_P, const float* d_Ci, const float* d_Oi,
+                                   int64_t total_micropolygons);
+/* Append many grids from packed HOST arrays (same layout as
+ * aqh_submit_grids_device).  Nothing is copied until aqh_render, which
+ * uploads them in one transfer per array; the arrays must stay valid until
+ * then.  Page-locked memory (aqh_host_alloc) transfers fastest. */
+aqh_status aqh_submit_grids_host(aqh_ctx* ctx, int ngrids,
+                                 const int32_t* cu, const int32_t* cv, const int32_t* nkeys,
+                                 const int32_t* flags, const int64_t* pbase, const int64_t* cbase,
+                                 const int32_t* tbase, const float* times, size_t ntimes,
+                                 const float* P, size_t nP, const float* Ci, const float* Oi, size_t nC,
+                                 int64_t total_micropolygons);
+/* Page-locked host memory for grid arrays. */
+void* aqh_host_alloc(size_t bytes);
+void aqh_host_free(void* p);
+/* Issue the context's work on a caller-owned CUDA stream (cudaStream_t passed
+ * as void*; NULL restores the context's own stream). */
+aqh_status aqh_set_stream(aqh_ctx* ctx, void* stream);
+/* Run the hider over every submitted grid: CqImageBuffer::RenderImage
+ * (imagebuffer.cpp:605-772) with the per-bucket preProcess/process/postProcess
+ * (bucketprocessor.cpp:95-359) done on the device.  Asynchronous on the
+ * context's stream unless `sync` is nonzero. */
+aqh_status aqh_render(aqh_ctx* ctx, int sync);
+aqh_status aqh_synchronize(aqh_ctx* ctx);
+
+/* ---- results ------------------------------------------------------------- */
+/* Channel-buffer layout of one display pixel, CqBucketProcessor::FilterBucket
+ * (bucketprocessor.cpp:385-398): Ci r g b, Oi r g b, a, z, coverage. */
+#define AQH_NCHANNELS 9
+/* Copy the whole crop window's channel buffer (float[h][w][9]) to host memory. */
+aqh_status aqh_read_channels(aqh_ctx* ctx, float* out, size_t out_floats);
+/* One bucket as CqDDManager::DisplayBucket receives it (iddmanager.h:99):
+ * float[bh][bw][9] for bucket (bx, by) of the crop window, bucket size from
+ * the frame.  Returns the bucket's width and height. */
+aqh_status aqh_read_bucket(aqh_ctx* ctx, int bx, int by, float* out, size_t out_floats, int* bw, int* bh);
+/* Quantized display data, CqDisplayRequest::FormatBucketForDisplay
+ * (ddmanager.cpp:1022-1119): for each pixel of the crop window and each of
+ * `nchan` channel-buffer indices in `channels` (e.g. {6,0,1,2} for the
+ * reference's a,r,g,b), lround(v*one + dither*s) clamped to [min,max], stored
+ * as uint8 when the range fits (selectDataFormat, ddmanager.cpp:249-285). */
+aqh_status aqh_read_quantized_u8(aqh_ctx* ctx, const int* channels, int nchan, uint8_t* out, size_t out_bytes);
+/* Per-sample results for parity checks, over the sample region (pixel-major,
+ * sample-minor): occluding-hit micropolygon id before Combine (-1 none), occlZ,
+ * transparent fragment count, valid flag after Combine, and the combined
+ * 7-float sample (R G B OR OG OB depth).  Any pointer may be NULL. */
+aqh_status aqh_read_samples(aqh_ctx* ctx, int32_t* winner, float* occlz, int32_t* nfrag,
+                            uint8_t* valid, float* sdata, size_t nsamples);
+
+/* ---- statistics and timing ------------------------------------------------ */
+typedef struct {
+	int64_t micropolygons;        /* micropolygons submitted this frame */
+	int64_t samples;              /* samples in the sample region */
+	int64_t grids;
+	int64_t tile_grid_pairs;      /* grid references the tile lists hold */
+	int64_t fragments;            /* transparent fragments stored */
+	float ms_bin, ms_sample, ms_filter, ms_total;  /* device time per stage of the last render */
+} aqh_frame_stats;
+aqh_status aqh_get_stats(aqh_ctx* ctx, aqh_frame_stats* st);
+
+/* ---- weight table and test hooks ----------------------------------------- */
+/* Host-side filter weight table [(2*sy+1)*(2*sx+1)][spp] evaluated at sub-pixel
+ * centres (CqBucketProcessor::InitialiseFilterValues, bucketprocessor.cpp:811-856).
+ * Returns the number of floats written, or -needed when max_out is too small. */
+int aqh_filter_table(int filter, float xw, float yw, int xs, int ys, float* out, int max_out);
+/* Device CqInvBilinear (libs/core/bilinear.h:260-305) for n points against one quad. */
+aqh_status aqh_test_invbilinear(const float* quad8, const float* P, int n, float* uv);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AQH_H */

@@ -1,0 +1,134 @@
+/*
+ * aqh_oracle.h -- C interface of the CPU oracle for the aqsis REYES hider.
+ *
+ * TEST INFRASTRUCTURE ONLY.  The oracle is a plain C++17 restatement of the
+ * reference hider (aqsis libs/core) used by tests/, __graft_entry__.smoke()
+ * and the cpu_baseline leg of bench.py as the checker.  No product code path
+ * may call it.
+ *
+ * All arrays are plain host memory.  Layouts match the ones the product's
+ * C-ABI (include/aqh.h) consumes, so a test can hand the same buffers to both.
+ */
+#ifndef AQH_ORACLE_H
+#define AQH_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+	ORC_FILTER_BOX = 0,
+	ORC_FILTER_TRIANGLE = 1,
+	ORC_FILTER_GAUSSIAN = 2,
+	ORC_FILTER_CATMULLROM = 3,
+	ORC_FILTER_SINC = 4,
+	ORC_FILTER_DISK = 5,
+	ORC_FILTER_BESSEL = 6,
+	ORC_FILTER_MITCHELL = 7
+};
+
+enum { ORC_DEPTH_MIN = 0, ORC_DEPTH_MIDPOINT = 1, ORC_DEPTH_MAX = 2, ORC_DEPTH_AVERAGE = 3 };
+
+/* Grid flags (SqGridInfo, micropolygon.h:57-63). */
+enum {
+	ORC_GRID_SMOOTH = 1,      /* ShadingInterpolation "smooth" */
+	ORC_GRID_MATTE = 2,       /* SqImageSample::Flag_Matte */
+	ORC_GRID_MATTEALPHA = 4   /* SqImageSample::Flag_MatteAlpha */
+};
+
+typedef struct {
+	int32_t width, height;                  /* Format */
+	int32_t crop_xmin, crop_xmax;           /* raster crop window, CqRenderer::initialiseCropWindow */
+	int32_t crop_ymin, crop_ymax;
+	int32_t xsamples, ysamples;             /* PixelSamples */
+	float xfilter, yfilter;                 /* PixelFilter widths */
+	float gain, gamma;                      /* Exposure */
+	float q_zero, q_one, q_min, q_max, q_dither; /* Quantize (ddmanager.cpp:428-457) */
+	float shutter_open, shutter_close;      /* Shutter */
+	int32_t use_dof;                        /* CqRenderer::UsingDepthOfField */
+	float dof_mult, dof_inv_fd;             /* m_DofMultiplier, m_OneOverFocalDistance (renderer.h:368-377) */
+	float dof_scale_x, dof_scale_y;         /* SetDepthOfFieldScale (options.cpp:162-171) */
+	int32_t depth_filter;                   /* Hider "depthfilter" */
+	float zthreshold[3];                    /* Option "limits" "zthreshold" */
+	int32_t display_z;                      /* DisplayMode includes DMode_Z */
+} OrcFrame;
+
+typedef struct {
+	int32_t ngrids;
+	const int32_t* cu;        /* micropolygons along u, per grid */
+	const int32_t* cv;        /* micropolygons along v, per grid */
+	const int32_t* nkeys;     /* motion keys per grid (1 = static) */
+	const int64_t* pbase;     /* first vertex of key 0 in P (float4 units); key k at pbase + k*(cu+1)*(cv+1) */
+	const int64_t* cbase;     /* first vertex in Ci/Oi (float4 units) */
+	const int64_t* tbase;     /* first key time in `times` */
+	const float* times;       /* motion key times */
+	const float* P;           /* float4: raster x, raster y, camera z, unused */
+	const float* Ci;          /* float4: r g b unused (NULL = white) */
+	const float* Oi;          /* float4: r g b unused (NULL = opaque white) */
+	const int32_t* flags;     /* ORC_GRID_* */
+	const uint8_t* culled;    /* per micropolygon (global mp id) 1 = culled, or NULL */
+} OrcGrids;
+
+typedef struct {
+	int32_t x0, y0, w, h;     /* sample region in pixels: [x0,x0+w) x [y0,y0+h) */
+	/* Pattern caches and per-pixel choices, as IqSampler / CqImagePixel::setSamples
+	 * use them (isampler.h:42-78, imagepixel.cpp:334-359).  NULL index = pixel index. */
+	int32_t npatterns;
+	const float* pos;         /* float2[npatterns][spp] offsets within the pixel */
+	const float* time;        /* float[npatterns][spp] in [0,1) (NULL = 0) */
+	const float* dof;         /* float2[npatterns][spp] lens samples in [0,1)^2 (NULL = none) */
+	const int32_t* shuffle;   /* int[npatterns][spp] (NULL = identity) */
+	const float* lod;         /* float[npatterns][spp] (NULL = 0) */
+	const uint32_t* pos_index;
+	const uint32_t* dof_index;
+	const uint32_t* time_index;
+	const uint32_t* shuffle_index;
+	const uint32_t* lod_index;
+	const float* dither;      /* per display pixel (crop window, row-major) random float s */
+} OrcSamples;
+
+typedef struct {
+	/* per sample of the sample region (pixel-major, sample-minor) */
+	int32_t* winner;          /* occluding hit micropolygon id before Combine, -1 if none */
+	float* occlz;             /* occlZ after sampling */
+	int32_t* nfrag;           /* transparent fragments stored */
+	uint8_t* valid;           /* occludingHit valid after Combine */
+	float* sdata;             /* 7 floats after Combine: R G B OR OG OB depth */
+	/* per display pixel of the crop window: Ci(3) Oi(3) a z coverage (channelbuffer order) */
+	float* channels;
+	/* per display pixel: quantized value of each requested channel, as double */
+	double* quantized;
+	const int32_t* qchannels; /* channel-buffer indices to quantize, in display order */
+	int32_t nqchannels;
+	/* statistics */
+	int64_t spl_count, spl_bound_hits, spl_hits;
+} OrcOut;
+
+/* Weight table [(2*shiftY+1)*(2*shiftX+1)][spp] (bucketprocessor.cpp:811-856). */
+int orc_filter_table(int filter, float xw, float yw, int xs, int ys, float* out, int max_out);
+/* Evaluate one RI filter function (filters.cpp). */
+float orc_filter_eval(int filter, float x, float y, float xw, float yw);
+
+/* CqInvBilinear lookup (bilinear.h:260-305) for n points against one quad A B C D. */
+void orc_invbilinear(const float* quad8, const float* P, int n, float* uv);
+/* bilerp (bilinear.h:228-236) of 2D vertices at n (u,v). */
+void orc_bilerp2(const float* quad8, const float* uv, int n, float* P);
+
+/* Whole-frame hider: sample, combine, filter, expose, quantize. */
+int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples* s,
+               const float* filter_table, OrcOut* out);
+
+/* The reference's global MT19937 (libs/math/random.cpp) and its multi-jittered
+ * sample tables, for regenerating aqsis' own sample patterns. */
+void orc_mt_seed(uint32_t s);
+uint32_t orc_mt_int32(void);
+float orc_mt_float(void);
+/* Fill the 250-pattern caches of CqMultiJitteredSampler (multijitter.cpp:130-202).
+ * pos: [250*spp*2], t1d: [250*spp], shuffle: [250*spp]. Consumes the global MT. */
+void orc_multijitter_tables(int xs, int ys, float* pos, float* t1d, int32_t* shuffle);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

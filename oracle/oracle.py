@@ -1,0 +1,191 @@
+"""ctypes front end of the CPU oracle (oracle/aqh_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's
+cpu_baseline leg use it as the checker.  Product code never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libaqh_oracle.so")
+
+_f32p = C.POINTER(C.c_float)
+_i32p = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+_u32p = C.POINTER(C.c_uint32)
+_u8p = C.POINTER(C.c_uint8)
+_f64p = C.POINTER(C.c_double)
+
+
+class OrcFrame(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32),
+                ("crop_xmin", C.c_int32), ("crop_xmax", C.c_int32),
+                ("crop_ymin", C.c_int32), ("crop_ymax", C.c_int32),
+                ("xsamples", C.c_int32), ("ysamples", C.c_int32),
+                ("xfilter", C.c_float), ("yfilter", C.c_float),
+                ("gain", C.c_float), ("gamma", C.c_float),
+                ("q_zero", C.c_float), ("q_one", C.c_float), ("q_min", C.c_float),
+                ("q_max", C.c_float), ("q_dither", C.c_float),
+                ("shutter_open", C.c_float), ("shutter_close", C.c_float),
+                ("use_dof", C.c_int32), ("dof_mult", C.c_float), ("dof_inv_fd", C.c_float),
+                ("dof_scale_x", C.c_float), ("dof_scale_y", C.c_float),
+                ("depth_filter", C.c_int32), ("zthreshold", C.c_float * 3),
+                ("display_z", C.c_int32)]
+
+
+class OrcGrids(C.Structure):
+    _fields_ = [("ngrids", C.c_int32), ("cu", _i32p), ("cv", _i32p), ("nkeys", _i32p),
+                ("pbase", _i64p), ("cbase", _i64p), ("tbase", _i64p), ("times", _f32p),
+                ("P", _f32p), ("Ci", _f32p), ("Oi", _f32p), ("flags", _i32p), ("culled", _u8p)]
+
+
+class OrcSamples(C.Structure):
+    _fields_ = [("x0", C.c_int32), ("y0", C.c_int32), ("w", C.c_int32), ("h", C.c_int32),
+                ("npatterns", C.c_int32), ("pos", _f32p), ("time", _f32p), ("dof", _f32p),
+                ("shuffle", _i32p), ("lod", _f32p), ("pos_index", _u32p), ("dof_index", _u32p),
+                ("time_index", _u32p), ("shuffle_index", _u32p), ("lod_index", _u32p),
+                ("dither", _f32p)]
+
+
+class OrcOut(C.Structure):
+    _fields_ = [("winner", _i32p), ("occlz", _f32p), ("nfrag", _i32p), ("valid", _u8p),
+                ("sdata", _f32p), ("channels", _f32p), ("quantized", _f64p),
+                ("qchannels", _i32p), ("nqchannels", C.c_int32),
+                ("spl_count", C.c_int64), ("spl_bound_hits", C.c_int64), ("spl_hits", C.c_int64)]
+
+
+def build(quiet: bool = True) -> str:
+    """Compile the oracle with its Makefile (gcc only)."""
+    out = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        L.orc_render.argtypes = [C.POINTER(OrcFrame), C.POINTER(OrcGrids), C.POINTER(OrcSamples), _f32p,
+                                 C.POINTER(OrcOut)]
+        L.orc_render.restype = C.c_int
+        L.orc_filter_table.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, C.c_int, _f32p, C.c_int]
+        L.orc_filter_table.restype = C.c_int
+        L.orc_filter_eval.argtypes = [C.c_int, C.c_float, C.c_float, C.c_float, C.c_float]
+        L.orc_filter_eval.restype = C.c_float
+        L.orc_invbilinear.argtypes = [_f32p, _f32p, C.c_int, _f32p]
+        L.orc_bilerp2.argtypes = [_f32p, _f32p, C.c_int, _f32p]
+        L.orc_mt_seed.argtypes = [C.c_uint32]
+        L.orc_mt_int32.restype = C.c_uint32
+        L.orc_mt_float.restype = C.c_float
+        L.orc_multijitter_tables.argtypes = [C.c_int, C.c_int, _f32p, _f32p, _i32p]
+        _lib = L
+    return _lib
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def filter_table(filter_id: int, xw: float, yw: float, xs: int, ys: int) -> np.ndarray:
+    buf = np.zeros(1 << 16, np.float32)
+    n = lib().orc_filter_table(filter_id, xw, yw, xs, ys, _p(buf, _f32p), buf.size)
+    if n < 0:
+        raise ValueError("filter table too large")
+    return buf[:n].copy()
+
+
+def invbilinear(quad, pts) -> np.ndarray:
+    q = np.ascontiguousarray(quad, np.float32).reshape(8)
+    P = np.ascontiguousarray(pts, np.float32).reshape(-1, 2)
+    uv = np.zeros_like(P)
+    lib().orc_invbilinear(_p(q, _f32p), _p(P, _f32p), P.shape[0], _p(uv, _f32p))
+    return uv
+
+
+def bilerp2(quad, uv) -> np.ndarray:
+    q = np.ascontiguousarray(quad, np.float32).reshape(8)
+    U = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    P = np.zeros_like(U)
+    lib().orc_bilerp2(_p(q, _f32p), _p(U, _f32p), U.shape[0], _p(P, _f32p))
+    return P
+
+
+def multijitter_tables(xs: int, ys: int, seed: int = 545):
+    """The reference's 250-entry multi-jitter caches after Reseed(seed)."""
+    spp = xs * ys
+    pos = np.zeros((250, spp, 2), np.float32)
+    t = np.zeros((250, spp), np.float32)
+    sh = np.zeros((250, spp), np.int32)
+    L = lib()
+    L.orc_mt_seed(seed)
+    L.orc_multijitter_tables(xs, ys, _p(pos, _f32p), _p(t, _f32p), _p(sh, _i32p))
+    return pos, t, sh
+
+
+def render(scene, qchannels=(0, 1, 2, 6), want_samples: bool = True) -> dict:
+    """Run the oracle on a Scene (aqsis_gb300.scene).  Returns numpy arrays."""
+    from aqsis_gb300.scene import FILTERS
+    fr, g, s = scene.frame, scene.grids, scene.samples
+    cx0, cx1, cy0, cy1 = fr.crop_window
+    x0, y0, w, h = fr.sample_region
+    spp = fr.spp
+    mult, inv = fr.dof_terms()
+    of = OrcFrame(fr.width, fr.height, cx0, cx1, cy0, cy1, fr.xsamples, fr.ysamples,
+                  fr.xfilter, fr.yfilter, fr.gain, fr.gamma, 0.0, fr.q_one, fr.q_min, fr.q_max,
+                  fr.q_dither, fr.shutter[0], fr.shutter[1], 1 if fr.use_dof else 0, mult, inv,
+                  fr.dof_scale[0], fr.dof_scale[1], fr.depth_filter,
+                  (C.c_float * 3)(*fr.zthreshold), fr.display_z)
+    keep = []
+
+    def arr(a, dt):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dt)
+        keep.append(a)
+        return a
+
+    tb = arr(g.tbase.astype(np.int64), np.int64)
+    og = OrcGrids(g.ngrids, _p(arr(g.cu, np.int32), _i32p), _p(arr(g.cv, np.int32), _i32p),
+                  _p(arr(g.nkeys, np.int32), _i32p), _p(arr(g.pbase, np.int64), _i64p),
+                  _p(arr(g.cbase, np.int64), _i64p), _p(tb, _i64p), _p(arr(g.times, np.float32), _f32p),
+                  _p(arr(g.P, np.float32), _f32p), _p(arr(g.Ci, np.float32), _f32p),
+                  _p(arr(g.Oi, np.float32), _f32p), _p(arr(g.flags, np.int32), _i32p),
+                  _p(arr(g.culled, np.uint8), _u8p))
+    os_ = OrcSamples(x0, y0, w, h, s.npatterns, _p(arr(s.pos, np.float32), _f32p),
+                     _p(arr(s.time, np.float32), _f32p), _p(arr(s.dof, np.float32), _f32p),
+                     _p(arr(s.shuffle, np.int32), _i32p), _p(arr(s.lod, np.float32), _f32p),
+                     _p(arr(s.pos_index, np.uint32), _u32p), _p(arr(s.dof_index, np.uint32), _u32p),
+                     _p(arr(s.time_index, np.uint32), _u32p), _p(arr(s.shuffle_index, np.uint32), _u32p),
+                     _p(arr(s.lod_index, np.uint32), _u32p), _p(arr(s.dither, np.float32), _f32p))
+    ftab = filter_table(FILTERS[fr.filter], fr.xfilter, fr.yfilter, fr.xsamples, fr.ysamples)
+    ns = w * h * spp
+    dw, dh = cx1 - cx0, cy1 - cy0
+    res = {}
+    if want_samples:
+        res["winner"] = np.zeros(ns, np.int32)
+        res["occlz"] = np.zeros(ns, np.float32)
+        res["nfrag"] = np.zeros(ns, np.int32)
+        res["valid"] = np.zeros(ns, np.uint8)
+        res["sdata"] = np.zeros((ns, 7), np.float32)
+    res["channels"] = np.zeros((dh, dw, 9), np.float32)
+    qc = np.array(qchannels, np.int32)
+    res["quantized"] = np.zeros((dh, dw, len(qc)), np.float64)
+    oo = OrcOut(_p(res.get("winner"), _i32p), _p(res.get("occlz"), _f32p), _p(res.get("nfrag"), _i32p),
+                _p(res.get("valid"), _u8p), _p(res.get("sdata"), _f32p), _p(res["channels"], _f32p),
+                _p(res["quantized"], _f64p), _p(qc, _i32p), len(qc), 0, 0, 0)
+    rc = lib().orc_render(C.byref(of), C.byref(og), C.byref(os_), _p(ftab, _f32p), C.byref(oo))
+    if rc != 0:
+        raise RuntimeError("oracle render failed: %d" % rc)
+    res["spl_count"], res["spl_bound_hits"], res["spl_hits"] = oo.spl_count, oo.spl_bound_hits, oo.spl_hits
+    return res

@@ -1,0 +1,157 @@
+"""GPU hider vs the CPU oracle on the same seeded inputs.
+
+Bit-exact: per-sample winning micropolygon ids (the occluding hit before
+Combine), occlZ, transparent fragment counts and valid masks.  Composited
+samples and filtered pixels: within 1e-5 relative (absolute 1e-6 near zero);
+8-bit quantized values: within 1 LSB.  In practice both are exact because
+the device follows the reference's operation order without FMA contraction.
+"""
+import numpy as np
+import pytest
+
+from tests import scenes_small as SS
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-5
+ABS = 1e-6
+
+
+def close_or_same(a, b):
+    """Within REL/ABS, or the same non-finite value (the reference's own z
+    channel overflows to inf/NaN where FLT_MAX depths meet negative filter
+    lobes)."""
+    with np.errstate(invalid="ignore", over="ignore"):
+        d = np.abs(a - b)
+        ok = (d <= REL * np.abs(b)) | (d <= ABS)
+    ok |= (np.isnan(a) & np.isnan(b)) | (np.isinf(a) & (a == b))
+    return ok
+
+
+def compare(res, ref, exact_pixels=False):
+    assert np.array_equal(res["winner"], ref["winner"]), \
+        "winner mismatch at %d samples" % int((res["winner"] != ref["winner"]).sum())
+    assert np.array_equal(res["occlz"].view(np.uint32), ref["occlz"].view(np.uint32))
+    assert np.array_equal(res["nfrag"], ref["nfrag"])
+    assert np.array_equal(res["valid"], ref["valid"])
+    ok = close_or_same(res["sdata"], ref["sdata"])
+    assert ok.all(), "sample data differs at %d entries" % int((~ok).sum())
+    ca, cb = res["channels"], ref["channels"]
+    ok = close_or_same(ca, cb)
+    assert ok.all(), "channels differ at %d entries" % int((~ok).sum())
+    q = np.abs(res["quantized"].astype(np.int32) - ref["quantized"].astype(np.int32))
+    assert q.max() <= 1
+    if exact_pixels:
+        assert np.array_equal(ca.view(np.uint32), cb.view(np.uint32))
+        assert q.max() == 0
+
+
+def run_both(hider, oracle, scene, qch=(0, 1, 2, 6)):
+    res = hider.render_scene(scene, qch)
+    ref = oracle.render(scene, qch)
+    return res, ref
+
+
+def test_opaque_stream_small(hider, oracle):
+    res, ref = run_both(hider, oracle, SS.opaque_small(seed=11))
+    compare(res, ref, exact_pixels=True)
+    assert res["valid"].mean() > 0.5
+
+
+def test_opaque_stream_explicit_samples(hider, oracle):
+    res, ref = run_both(hider, oracle, SS.opaque_small(seed=12, explicit=True))
+    compare(res, ref, exact_pixels=True)
+
+
+@pytest.mark.parametrize("xs,ys", [(1, 1), (2, 2), (3, 3), (4, 4), (5, 3), (8, 8)])
+def test_edge_cases_sample_counts(hider, oracle, xs, ys):
+    res, ref = run_both(hider, oracle, SS.edge_cases(seed=20 + xs, xs=xs, ys=ys))
+    compare(res, ref, exact_pixels=True)
+
+
+@pytest.mark.parametrize("filt", [("box", 1.0, 1.0), ("catmull-rom", 3.0, 3.0), ("sinc", 4.0, 4.0),
+                                  ("triangle", 2.5, 1.5), ("mitchell", 4.0, 4.0), ("disk", 3.0, 3.0)])
+def test_edge_cases_filters(hider, oracle, filt):
+    res, ref = run_both(hider, oracle, SS.edge_cases(seed=31, filt=filt))
+    compare(res, ref, exact_pixels=True)
+
+
+def test_transparent_small(hider, oracle):
+    res, ref = run_both(hider, oracle, SS.transparent_small(seed=41))
+    compare(res, ref)
+    assert res["nfrag"].max() > 1
+
+
+@pytest.mark.parametrize("xs,ys", [(3, 3), (8, 8)])
+def test_transparent_edge_cases(hider, oracle, xs, ys):
+    res, ref = run_both(hider, oracle, SS.transparent_edge(seed=42, xs=xs, ys=ys))
+    compare(res, ref)
+
+
+def test_crop_window_and_exposure(hider, oracle):
+    sc = SS.edge_cases(seed=51)
+    sc.frame.crop = (7, 50, 5, 40)
+    sc.frame.gain, sc.frame.gamma = 1.7, 2.2
+    from aqsis_gb300 import scene as S
+    sc.samples = S.make_samples(sc.frame, np.random.default_rng(3), 32, dither=True)
+    sc.frame.q_dither = 0.5
+    res, ref = run_both(hider, oracle, sc)
+    compare(res, ref)
+
+
+def test_quantized_channel_orders(hider, oracle):
+    sc = SS.edge_cases(seed=61)
+    for qch in [(6, 0, 1, 2), (0, 1, 2), (7,), (8, 6)]:
+        res, ref = run_both(hider, oracle, sc, qch)
+        q = np.abs(res["quantized"].astype(np.int32) - ref["quantized"].astype(np.int32))
+        assert q.max() <= 1, qch
+
+
+def test_empty_frame(hider, oracle):
+    from aqsis_gb300 import scene as S
+    fr = S.Frame(width=33, height=17, xsamples=2, ysamples=2, q_dither=0.0)
+    g = SS.plane(200, 200, 2, 2, 5.0)  # entirely outside
+    sc = SS.custom(fr, g)
+    res, ref = run_both(hider, oracle, sc)
+    compare(res, ref, exact_pixels=True)
+    assert not res["valid"].any()
+
+
+def test_bucket_readback_matches_channels(hider, oracle):
+    sc = SS.edge_cases(seed=71)
+    res = hider.render_scene(sc)
+    ch = res["channels"]
+    b = hider.read_bucket(1, 2)
+    assert np.array_equal(b, ch[32:48, 16:32])
+    b = hider.read_bucket(3, 2)  # partial bucket at the right edge (64 = 4*16, so full)
+    assert b.shape[1] == 16
+
+
+def test_device_invbilinear_matches_oracle(aqh_lib, oracle):
+    from tests.test_oracle_bilinear import CASES, fixture_uv, quad_array
+    for name, quad, ex, rel, ab in CASES:
+        q = quad_array(quad)
+        P = oracle.bilerp2(q, fixture_uv(*ex))
+        a = aqh_lib.invbilinear(q, P)
+        b = oracle.invbilinear(q, P)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), name
+
+
+def test_motion_blur_and_dof(hider, oracle):
+    res, ref = run_both(hider, oracle, SS.motion_dof_small(seed=81))
+    compare(res, ref, exact_pixels=True)
+
+
+def test_motion_blur_only(hider, oracle):
+    res, ref = run_both(hider, oracle, SS.motion_dof_small(seed=82, dof=False, xs=4, ys=4))
+    compare(res, ref, exact_pixels=True)
+
+
+def test_dof_only(hider, oracle):
+    res, ref = run_both(hider, oracle, SS.dof_only_small(seed=83))
+    compare(res, ref, exact_pixels=True)
+
+
+def test_motion_blur_transparent(hider, oracle):
+    res, ref = run_both(hider, oracle, SS.motion_dof_small(seed=84, dof=False, xs=3, ys=3, transparent=True))
+    compare(res, ref)
