@@ -142,15 +142,24 @@ float filter_eval(int filter, float x, float y, float xwidth, float ywidth) {
 
 int lfloor_h(float x) { int i = (int)x; return i - ((x < 0 && x != (float)i) ? 1 : 0); }
 
-// Tile shape: `spt` samples per thread, kBlock threads, near-square tiles.
+}  // namespace
+
+namespace aqh {
+
+// Tile shape.  spt == 0: the static kernel's shape; else `spt` samples per
+// thread with kBlock threads in near-square tiles (motion blur / DoF kernel).
 void set_tiling(FrameParams& fp, int spt) {
-	fp.tpp = (fp.spp + spt - 1) / spt;
-	const int tpix = kBlock / fp.tpp;
-	int tw = 1;
-	while ((tw + 1) * (tw + 1) <= tpix) ++tw;
-	const int th = tpix / tw;
-	fp.tile_w = tw;
-	fp.tile_h = th;
+	if (spt == 0) {
+		static_tiling(fp);
+	} else {
+		fp.tpp = (fp.spp + spt - 1) / spt;
+		const int tpix = kBlock / fp.tpp;
+		int tw = 1;
+		while ((tw + 1) * (tw + 1) <= tpix) ++tw;
+		fp.tile_w = tw;
+		fp.tile_h = tpix / tw;
+	}
+	const int tw = fp.tile_w, th = fp.tile_h;
 	fp.ntx = (fp.sw + tw - 1) / tw;
 	fp.nty = (fp.sh + th - 1) / th;
 	fp.st_tiles = std::max(1, 128 / std::max(tw, th));
@@ -208,7 +217,74 @@ void dof_bounds_h(int xs, int ys, std::vector<float4>& out) {
 	}
 }
 
-}  // namespace
+
+// Frame options resolved the way SqOptionCache / CqRenderer / CqBucketProcessor
+// derive them (optioncache.cpp:48-118, renderer.h:368-377,
+// bucketprocessor.cpp:36-37, 811-856, imagebuffer.cpp:533-539).
+aqh_status resolve_frame(const aqh_frame_desc& dd, FrameParams& fp, std::vector<float>& ftab, std::string& err) {
+	const aqh_frame_desc* d = &dd;
+	char buf[256];
+	if (d->width <= 0 || d->height <= 0) {
+		snprintf(buf, sizeof buf, "bad resolution %dx%d", d->width, d->height);
+		err = buf;
+		return AQH_EINVAL;
+	}
+	if (d->xsamples <= 0 || d->ysamples <= 0 || d->xsamples * d->ysamples > AQH_MAX_SPP) {
+		snprintf(buf, sizeof buf, "PixelSamples %d %d outside 1..%d samples", d->xsamples, d->ysamples, AQH_MAX_SPP);
+		err = buf;
+		return AQH_ELIMIT;
+	}
+	if (!(d->xfilter > 0) || !(d->yfilter > 0) || d->xfilter > 64 || d->yfilter > 64) {
+		err = "bad filter width";
+		return AQH_EINVAL;
+	}
+	if (d->display_z && d->depth_filter == AQH_DEPTH_MIDPOINT) {
+		err = "midpoint depth filter with a z display is not supported";
+		return AQH_EINVAL;
+	}
+	std::memset(&fp, 0, sizeof fp);
+	int cx0 = d->crop_xmin, cx1 = d->crop_xmax, cy0 = d->crop_ymin, cy1 = d->crop_ymax;
+	if (cx0 == 0 && cx1 == 0 && cy0 == 0 && cy1 == 0) { cx1 = d->width; cy1 = d->height; }
+	if (cx0 < 0 || cy0 < 0 || cx1 > d->width || cy1 > d->height || cx0 >= cx1 || cy0 >= cy1) {
+		err = "bad crop window";
+		return AQH_EINVAL;
+	}
+	fp.crop_x0 = cx0; fp.crop_x1 = cx1; fp.crop_y0 = cy0; fp.crop_y1 = cy1;
+	fp.xs = d->xsamples; fp.ys = d->ysamples; fp.spp = fp.xs * fp.ys;
+	fp.shiftX = lfloor_h(d->xfilter / 2.0f);
+	fp.shiftY = lfloor_h(d->yfilter / 2.0f);
+	fp.xfwo2 = std::ceil(d->xfilter) * 0.5f;
+	fp.yfwo2 = std::ceil(d->yfilter) * 0.5f;
+	fp.sx0 = cx0 - fp.shiftX; fp.sy0 = cy0 - fp.shiftY;
+	fp.sw = (cx1 - cx0) + 2 * fp.shiftX; fp.sh = (cy1 - cy0) + 2 * fp.shiftY;
+	fp.cull_x0 = cx0 - d->xfilter / 2.0f; fp.cull_x1 = cx1 + d->xfilter / 2.0f;
+	fp.cull_y0 = cy0 - d->yfilter / 2.0f; fp.cull_y1 = cy1 + d->yfilter / 2.0f;
+	fp.use_dof = (d->fstop > 0.0f && d->fstop < FLT_MAX) ? 1 : 0;
+	if (fp.use_dof) {
+		// CqRenderer::SetDepthOfFieldData (renderer.h:368-377)
+		float lensDiameter = d->focal_length / d->fstop;
+		fp.dof_mult = 0.5 * lensDiameter * d->focal_distance / (d->focal_distance + lensDiameter);
+		fp.dof_inv_fd = 1.0 / d->focal_distance;
+		fp.dof_scale_x = d->dof_scale_x;
+		fp.dof_scale_y = d->dof_scale_y;
+	}
+	fp.shutter_open = d->shutter_open;
+	fp.shutter_close = d->shutter_close;
+	fp.depth_filter = d->depth_filter;
+	fp.cullable = !(d->display_z && (d->depth_filter == AQH_DEPTH_MAX || d->depth_filter == AQH_DEPTH_AVERAGE));
+	fp.midpoint_store = 0;
+	for (int k = 0; k < 3; ++k) fp.zthr[k] = d->zthreshold[k];
+	fp.gain = d->gain; fp.gamma = d->gamma;
+	fp.q_one = d->q_one; fp.q_min = d->q_min; fp.q_max = d->q_max; fp.q_dither = d->q_dither;
+	set_tiling(fp, 0);
+	const int n = aqh_filter_table(d->filter, d->xfilter, d->yfilter, fp.xs, fp.ys, nullptr, 0);
+	ftab.assign(-n, 0.0f);
+	aqh_filter_table(d->filter, d->xfilter, d->yfilter, fp.xs, fp.ys, ftab.data(), -n);
+	fp.ftab_n = -n;
+	return AQH_OK;
+}
+
+}  // namespace aqh
 
 struct aqh_ctx {
 	int device = 0;
@@ -372,53 +448,12 @@ int aqh_filter_table(int filter, float xw, float yw, int xs, int ys, float* out,
 
 aqh_status aqh_frame_begin(aqh_ctx* ctx, const aqh_frame_desc* d) {
 	if (!ctx || !d) return AQH_EINVAL;
-	if (d->width <= 0 || d->height <= 0) return ctx->fail(AQH_EINVAL, "bad resolution %dx%d", d->width, d->height);
-	if (d->xsamples <= 0 || d->ysamples <= 0 || d->xsamples * d->ysamples > AQH_MAX_SPP)
-		return ctx->fail(AQH_ELIMIT, "PixelSamples %d %d outside 1..%d samples", d->xsamples, d->ysamples, AQH_MAX_SPP);
-	if (!(d->xfilter > 0) || !(d->yfilter > 0) || d->xfilter > 64 || d->yfilter > 64)
-		return ctx->fail(AQH_EINVAL, "bad filter width");
-	if (d->display_z && d->depth_filter == AQH_DEPTH_MIDPOINT)
-		return ctx->fail(AQH_EINVAL, "midpoint depth filter with a z display is not supported");
+	FrameParams fp;
+	std::string err;
+	const aqh_status st = aqh::resolve_frame(*d, fp, ctx->ftab, err);
+	if (st != AQH_OK) return ctx->fail(st, "%s", err.c_str());
 	ctx->desc = *d;
-	FrameParams& fp = ctx->fp;
-	std::memset(&fp, 0, sizeof fp);
-	int cx0 = d->crop_xmin, cx1 = d->crop_xmax, cy0 = d->crop_ymin, cy1 = d->crop_ymax;
-	if (cx0 == 0 && cx1 == 0 && cy0 == 0 && cy1 == 0) { cx1 = d->width; cy1 = d->height; }
-	if (cx0 < 0 || cy0 < 0 || cx1 > d->width || cy1 > d->height || cx0 >= cx1 || cy0 >= cy1)
-		return ctx->fail(AQH_EINVAL, "bad crop window");
-	fp.crop_x0 = cx0; fp.crop_x1 = cx1; fp.crop_y0 = cy0; fp.crop_y1 = cy1;
-	fp.xs = d->xsamples; fp.ys = d->ysamples; fp.spp = fp.xs * fp.ys;
-	fp.shiftX = lfloor_h(d->xfilter / 2.0f);
-	fp.shiftY = lfloor_h(d->yfilter / 2.0f);
-	fp.xfwo2 = std::ceil(d->xfilter) * 0.5f;
-	fp.yfwo2 = std::ceil(d->yfilter) * 0.5f;
-	fp.sx0 = cx0 - fp.shiftX; fp.sy0 = cy0 - fp.shiftY;
-	fp.sw = (cx1 - cx0) + 2 * fp.shiftX; fp.sh = (cy1 - cy0) + 2 * fp.shiftY;
-	fp.cull_x0 = cx0 - d->xfilter / 2.0f; fp.cull_x1 = cx1 + d->xfilter / 2.0f;
-	fp.cull_y0 = cy0 - d->yfilter / 2.0f; fp.cull_y1 = cy1 + d->yfilter / 2.0f;
-	fp.use_dof = (d->fstop > 0.0f && d->fstop < FLT_MAX) ? 1 : 0;
-	if (fp.use_dof) {
-		// CqRenderer::SetDepthOfFieldData (renderer.h:368-377)
-		float lensDiameter = d->focal_length / d->fstop;
-		fp.dof_mult = 0.5 * lensDiameter * d->focal_distance / (d->focal_distance + lensDiameter);
-		fp.dof_inv_fd = 1.0 / d->focal_distance;
-		fp.dof_scale_x = d->dof_scale_x;
-		fp.dof_scale_y = d->dof_scale_y;
-	}
-	fp.shutter_open = d->shutter_open;
-	fp.shutter_close = d->shutter_close;
-	fp.depth_filter = d->depth_filter;
-	fp.cullable = !(d->display_z && (d->depth_filter == AQH_DEPTH_MAX || d->depth_filter == AQH_DEPTH_AVERAGE));
-	fp.midpoint_store = 0;
-	for (int k = 0; k < 3; ++k) fp.zthr[k] = d->zthreshold[k];
-	fp.gain = d->gain; fp.gamma = d->gamma;
-	fp.q_one = d->q_one; fp.q_min = d->q_min; fp.q_max = d->q_max; fp.q_dither = d->q_dither;
-	set_tiling(fp, kSamplesPerThread);
-	// filter table
-	int n = aqh_filter_table(d->filter, d->xfilter, d->yfilter, fp.xs, fp.ys, nullptr, 0);
-	ctx->ftab.assign(-n, 0.0f);
-	aqh_filter_table(d->filter, d->xfilter, d->yfilter, fp.xs, fp.ys, ctx->ftab.data(), -n);
-	fp.ftab_n = -n;
+	ctx->fp = fp;
 	// reset grid stream
 	ctx->h_cu.clear(); ctx->h_cv.clear(); ctx->h_nkeys.clear(); ctx->h_flags.clear(); ctx->h_tbase.clear();
 	ctx->h_pbase.clear(); ctx->h_cbase.clear(); ctx->h_mpbase.clear(); ctx->h_times.clear(); ctx->h_culled.clear();
@@ -742,7 +777,7 @@ aqh_status aqh_render(aqh_ctx* ctx, int sync) {
 	if (ctx->dev_grids) motion = ctx->dev_motion;
 	fp.any_motion = motion ? 1 : 0;
 	const bool mbdof = fp.use_dof || fp.any_motion;
-	set_tiling(fp, mbdof ? mb_samples_per_thread() : kSamplesPerThread);
+	set_tiling(fp, mbdof ? mb_samples_per_thread() : 0);
 	if (mbdof) {
 		std::vector<float4> db;
 		dof_bounds_h(fp.xs, fp.ys, db);

@@ -6,6 +6,11 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <string>
+#include <vector>
+
+#include "../../include/aqh.h"
+
 namespace aqh {
 
 // Samples a thread owns.  A pixel with spp samples is split over
@@ -113,10 +118,16 @@ void launch_st_count(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cu
 void launch_scan_i32(const int32_t* in, int32_t* out, int n, int32_t* scratch, cudaStream_t s);
 void launch_st_write(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);
 void launch_sample_tiles(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
-                         SampleStore st, FragPool fp_pool, int32_t* err, cudaStream_t s);
+                         SampleStore st, FragPool pool, int32_t* err, cudaStream_t s);
 void launch_sample_mb(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
                       SampleStore st, FragPool pool, const float4* dof_bounds, cudaStream_t s);
 int mb_samples_per_thread();
+void static_tiling(FrameParams& fp);
+// Frame options resolved from an aqh_frame_desc (plus the host filter table).
+aqh_status resolve_frame(const aqh_frame_desc& d, FrameParams& fp, std::vector<float>& ftab, std::string& err);
+// Tile grid, super-tiles and the MB/DoF lens-stratum bounds (api.cu).
+void set_tiling(FrameParams& fp, int spt);
+void dof_bounds_h(int xs, int ys, std::vector<float4>& out);
 void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStore& st, const float* ftab,
                    float* channels, cudaStream_t s);
 void launch_quantize_u8(const FrameParams& fp, const SamplerDev& sm, const float* channels, const int* chans,

@@ -6,21 +6,25 @@
 // CqMicroPolygon::Sample / fContains (micropolygon.cpp:1295-1660, 1768-1914)
 // and CqImagePixel::Combine (imagepixel.cpp:144-332).
 //
-// Layout.  One CTA owns a tile of tile_w x tile_h pixels of the sample region;
-// each pixel's samples are split over `tpp` threads, a thread holding up to
-// kSamplesPerThread samples (position and occluding depth in registers).
-// The CTA walks its super-tile's grid list in submission order and expands
-// the grids touching the tile into micropolygons, kSlots at a time:
-//   phase A (one thread per micropolygon): bound, vertex order, edge and
-//     inverse-bilinear coefficients into a shared-memory record, and a bit
-//     per covered pixel in that pixel's candidate mask;
-//   phase B (pixel-owner threads): each thread walks its pixel's mask in
-//     ascending slot order -- the insertion order -- and runs the reference's
+// Layout.  One CTA (16 warps) owns a tile of the sample region holding at
+// most 4096 samples (16x16 pixels at 16 samples per pixel).  It walks its
+// super-tile's grid list in submission order and expands the grids touching
+// the tile into micropolygons, kSlotsS at a time:
+//   phase A: one micropolygon per thread tests bound, crop cull and a
+//     tile-wide early-z; survivors are compacted in insertion order, then
+//     every thread builds one shared-memory record (vertex order, edge and
+//     inverse-bilinear coefficients, pixel and sub-sample ranges) and sets a
+//     bit per covered pixel in that pixel's candidate mask;
+//   phase B: a warp takes 32 consecutive samples of the tile, one per lane,
+//     and walks the union of their pixels' masks in ascending slot order --
+//     the insertion order -- with warp-uniform control flow: records are
+//     shared-memory broadcasts, a candidate behind all 32 samples' occluding
+//     depths is skipped by the whole warp, and each lane runs the reference's
 //     per-sample sequence (sub-sample range, inclusive bound test, early-z,
 //     edge tests, inverse bilinear, depth, store).
-// Because one thread owns each sample and visits its candidates in insertion
-// order, the reference's order-dependent early-z and its "first of equal
-// depths wins" rule hold exactly.  Colours are resolved once per sample at the
+// Because each sample is owned by one lane that visits its candidates in
+// insertion order, the reference's order-dependent early-z and its "first of
+// equal depths wins" rule hold exactly.  Colours are resolved once per sample at the
 // end (the reference interpolates them at store time; the values are the
 // same because they depend only on the winning micropolygon and (u,v)).
 #include "aqh_internal.h"
@@ -31,41 +35,119 @@ namespace aqh {
 
 namespace {
 
-// Shared-memory micropolygon record for the static path.
-struct MpRec {
+constexpr int kThreadsS = 512;                   // 16 warps
+constexpr int kWarpsS = kThreadsS / 32;
+constexpr int kSlotsS = 256;                     // records per pass
+constexpr int kWordsS = kSlotsS / 32;
+constexpr int kTilePixMax = 256;
+constexpr int kTileSampMax = 4096;
+
+// Shared-memory record of one candidate micropolygon (static path).
+struct RecS {
 	float bminx, bmaxx, bminy, bmaxy, bminz;
+	int px0, px1, py0, py1;        // pixels RenderMPG_Static visits: [floor(bmin), lceil(bmax))
+	int im, em, in_, en;           // sub-sample starts / ends on the first / last pixel
 	float ym[4], xm[4], ex[4], ey[4];
 	float ax, ay, e_x, e_y, f_x, f_y, g_x, g_y;
 	float z[4];
-	int id;       // global micropolygon id
-	int grid;
-	int bits;     // 1 linear, 2 occluding store (opaque or matte alpha), 4 smooth, 8 matte, 16 matte alpha
-	float pad;    // odd word stride keeps records of different slots on different banks
-};
+	int id;                        // global micropolygon id
+	int bits;                      // 1 linear, 2 occluding store
+};  // 43 words: an odd stride spreads neighbouring records over the banks
 
-constexpr int kRecLinear = 1, kRecOccluding = 2, kRecSmooth = 4, kRecMatte = 8, kRecMatteAlpha = 16;
+constexpr int kRecLinear = 1, kRecOccluding = 2;
 
-struct Smem {
-	MpRec rec[kSlots];
-	uint32_t mask[kBlock][kSlotWords];  // per tile pixel (tile pixels <= kBlock)
-	int qgrid[kBlock];                  // grids of the current list chunk touching the tile
-	int warp_tot[kBlock / 32];
-	int qn;
-	int nslots;
-	int consumed;
+struct SmemS {
+	RecS rec[kSlotsS];
+	uint32_t mask[kTilePixMax][kWordsS];  // candidate bits per tile pixel
+	int2 pend[kSlotsS];                   // (grid, micropolygon) of the staged candidates
+	int qgrid[kThreadsS];                 // grids of the current list chunk that touch the tile
+	int qcum[kThreadsS + 1];              // running micropolygon counts of those grids
+	int warp_tot[32];
+	float warp_max[32];
 	int first_reject;
+	int qn;
+	float tile_ozmax;                     // largest occluding depth over the tile's samples
+	float soz[kTileSampMax];              // occlZ per tile sample
+	int swin[kTileSampMax];               // occluding micropolygon per tile sample (-1 none)
 };
+
+__device__ __forceinline__ float warp_max_f(float v) {
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+	return v;
+}
+
+// Record of micropolygon m of grid gi: bound (CalculateBound), vertex order
+// (ComputeVertexOrder), point-in-polygon and inverse-bilinear coefficients
+// (cachePointInPolyTest), opacity (CacheOutputInterpCoeffs*), and the pixel
+// and sub-sample ranges RenderMPG_Static walks.
+__device__ __forceinline__ void build_record(const FrameParams& fp, const GridsDev& g, int gi, int m, RecS& rec) {
+	const int cu = __ldg(g.cu + gi);
+	const long long pb = __ldg(g.pbase + gi);
+	const int gflags = __ldg(g.flags + gi);
+	const int iv = m / cu, iu = m - iv * cu;
+	const int index = iv * (cu + 1) + iu;
+	V3f v[4];
+	v[0] = ld3(g.P, pb + index);
+	v[1] = ld3(g.P, pb + index + 1);
+	v[2] = ld3(g.P, pb + index + cu + 1);
+	v[3] = ld3(g.P, pb + index + cu + 2);
+	const float bminx = amin(amin(amin(v[0].x, v[1].x), v[3].x), v[2].x);
+	const float bminy = amin(amin(amin(v[0].y, v[1].y), v[3].y), v[2].y);
+	const float bminz = amin(amin(amin(v[0].z, v[1].z), v[3].z), v[2].z);
+	const float bmaxx = amax(amax(amax(v[0].x, v[1].x), v[3].x), v[2].x);
+	const float bmaxy = amax(amax(amax(v[0].y, v[1].y), v[3].y), v[2].y);
+	HitCoeffs h;
+	hit_setup(v, vertex_order(v), h);
+	rec.bminx = bminx; rec.bmaxx = bmaxx; rec.bminy = bminy; rec.bmaxy = bmaxy; rec.bminz = bminz;
+	// bucketprocessor.cpp:1119-1138 (the clip to the sample region does not
+	// change the range of any pixel inside it)
+	const int sX = (int)floorf(bminx), eX = lceil_f(bmaxx);
+	const int sY = (int)floorf(bminy), eY = lceil_f(bmaxy);
+	rec.px0 = sX; rec.px1 = eX; rec.py0 = sY; rec.py1 = eY;
+	rec.im = (int)floorf((bminx - (float)sX) * (float)fp.xs);
+	rec.in_ = (int)floorf((bminy - (float)sY) * (float)fp.ys);
+	rec.em = lceil_f((bmaxx - (float)(eX - 1)) * (float)fp.xs);
+	rec.en = lceil_f((bmaxy - (float)(eY - 1)) * (float)fp.ys);
+#pragma unroll
+	for (int k = 0; k < 4; ++k) {
+		rec.ym[k] = h.ym[k]; rec.xm[k] = h.xm[k]; rec.ex[k] = h.ex[k]; rec.ey[k] = h.ey[k];
+		rec.z[k] = h.z[k];
+	}
+	rec.ax = h.ax; rec.ay = h.ay; rec.e_x = h.e_x; rec.e_y = h.e_y;
+	rec.f_x = h.f_x; rec.f_y = h.f_y; rec.g_x = h.g_x; rec.g_y = h.g_y;
+	rec.id = (int)(__ldg(g.mpbase + gi) + m);
+	// SqMpgSampleInfo::isOpaque (micropolygon.cpp:1477-1529)
+	bool opaque = true;
+	const bool smooth = (gflags & 1) != 0;
+	if (!(gflags & 8) && g.Oi) {
+		const long long cb = __ldg(g.cbase + gi);
+		const float4 o0 = __ldg(g.Oi + cb + index);
+		opaque = o0.x >= 1.0f && o0.y >= 1.0f && o0.z >= 1.0f;
+		if (smooth) {
+			const float4 o1 = __ldg(g.Oi + cb + index + 1);
+			const float4 o2 = __ldg(g.Oi + cb + index + cu + 1);
+			const float4 o3 = __ldg(g.Oi + cb + index + cu + 2);
+			opaque = opaque && (o1.x >= 1.0f && o1.y >= 1.0f && o1.z >= 1.0f) &&
+			         (o2.x >= 1.0f && o2.y >= 1.0f && o2.z >= 1.0f) && (o3.x >= 1.0f && o3.y >= 1.0f && o3.z >= 1.0f);
+		}
+	}
+	int bits = h.linear ? kRecLinear : 0;
+	if (opaque || (gflags & 4)) bits |= kRecOccluding;
+	rec.bits = bits;
+}
 
 // Final value of one sample: the occluding hit's colour at its (u,v), or the
 // Combine of its transparent fragments; written to the sample store.
 template <bool TRANSP>
 __device__ __forceinline__ void resolve_sample(const FrameParams& fp, const GridsDev& g, const FragPool& pool,
-                                            const SampleStore& st, long long sidx, float x, float y, float oz,
-                                            int w, int wg, int head) {
+                                               const SampleStore& st, long long sidx, float x, float y, float oz,
+                                               int w, int head) {
 	float occl[7] = {0, 0, 0, 0, 0, 0, 0};
 	int occl_flags = 0;
 	if (w >= 0) {
 		// recompute (u,v) of the winner exactly as when it was stored
+		const int wg = grid_of(g, w);
 		const int cu = __ldg(g.cu + wg);
 		const int m = w - (int)__ldg(g.mpbase + wg);
 		const int iv = m / cu, iu = m - iv * cu;
@@ -101,271 +183,274 @@ __device__ __forceinline__ void resolve_sample(const FrameParams& fp, const Grid
 }
 
 template <bool TRANSP>
-__global__ void __launch_bounds__(kBlock, 2)
-sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, SampleStore st, FragPool pool,
-                     int32_t* err) {
+__global__ void __launch_bounds__(kThreadsS, 2)
+sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, SampleStore st, FragPool pool) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
-	int32_t* win = reinterpret_cast<int32_t*>(smem_raw + sizeof(Smem));  // [kBlock * kSamplesPerThread]
-	int32_t* wgrid = win + kBlock * kSamplesPerThread;                    // grid of the winner
-	int32_t* fhead = wgrid + kBlock * kSamplesPerThread;                  // TRANSP: fragment list heads
+	SmemS& sm = *reinterpret_cast<SmemS*>(smem_raw);
+	int32_t* fhead = reinterpret_cast<int32_t*>(smem_raw + sizeof(SmemS));  // TRANSP: fragment lists
 
 	const int tile = blockIdx.x;
 	const int tx = tile % fp.ntx, ty = tile / fp.ntx;
 	const int tpx0 = fp.sx0 + tx * fp.tile_w, tpy0 = fp.sy0 + ty * fp.tile_h;
 	const int tpx1 = min(tpx0 + fp.tile_w, fp.sx0 + fp.sw), tpy1 = min(tpy0 + fp.tile_h, fp.sy0 + fp.sh);
 	const int st_idx = (ty / fp.st_tiles) * fp.nstx + (tx / fp.st_tiles);
-	const int t = threadIdx.x;
+	const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+	const int spp = fp.spp;
+	const int tpix = fp.tile_w * fp.tile_h;
+	const int tsamp = tpix * spp;
+	const int ngroups = (tsamp + 31) >> 5;
+	const int cullable = fp.cullable;
 
-	// thread -> (pixel, sample group)
-	const int pl = t / fp.tpp;
-	const int sg = t - pl * fp.tpp;
-	const int lx = pl % fp.tile_w, ly = pl / fp.tile_w;
-	const int mypx = tpx0 + lx, mypy = tpy0 + ly;
-	const bool own = (pl < fp.tile_w * fp.tile_h) && mypx < tpx1 && mypy < tpy1;
-	const int s0 = sg * kSamplesPerThread;
-	const int nmine = own ? min(kSamplesPerThread, fp.spp - s0) : 0;
-	const long long pix = own ? (long long)(mypy - fp.sy0) * fp.sw + (mypx - fp.sx0) : 0;
-	const int n0 = s0 / fp.xs, m0 = s0 - n0 * fp.xs;
-
-	float sx[kSamplesPerThread], sy[kSamplesPerThread], oz[kSamplesPerThread];
-	{
-		const long long pat = own ? (smp.pos_index ? (long long)smp.pos_index[pix] : pix) : 0;
-		const float fx = (float)mypx, fy = (float)mypy;
-#pragma unroll
-		for (int i = 0; i < kSamplesPerThread; ++i) {
-			float2 o = make_float2(0.0f, 0.0f);
-			if (i < nmine) o = __ldg(smp.pos + pat * fp.spp + s0 + i);
-			sx[i] = fx + o.x;  // CqImagePixel::setSamples: offset + positions[i]
-			sy[i] = fy + o.y;
-			oz[i] = FLT_MAX;
-		}
+	for (int i = t; i < tsamp; i += kThreadsS) {
+		sm.soz[i] = FLT_MAX;
+		sm.swin[i] = -1;
+		if (TRANSP) fhead[i] = -1;
 	}
-#pragma unroll
-	for (int i = 0; i < kSamplesPerThread; ++i) {
-		win[t * kSamplesPerThread + i] = -1;
-		if (TRANSP) fhead[t * kSamplesPerThread + i] = -1;
+	for (int i = t; i < kTilePixMax * kWordsS; i += kThreadsS) (&sm.mask[0][0])[i] = 0u;
+	if (t == 0) {
+		sm.tile_ozmax = FLT_MAX;
+		sm.qn = 0;
+		sm.qcum[0] = 0;
 	}
-	for (int i = t; i < kBlock * kSlotWords; i += kBlock) (&sm.mask[0][0])[i] = 0u;
 	__syncthreads();
 
 	const int lbeg = bb.st_offset[st_idx * bb.nranges];
 	const int lend = bb.st_offset[(st_idx + 1) * bb.nranges];
-	const int cullable = fp.cullable;
 
-	// Stream cursor (uniform over the block): list position of the next chunk,
-	// grid index inside the current chunk, next micropolygon of that grid.
-	int lp = lbeg, qi = 0, qn = 0, r0 = 0;
-	int nslots = 0;
+	// Stream cursor (uniform over the block): next list chunk, position in
+	// the micropolygon stream of the queued grids.
+	int lp = lbeg, r0 = 0, qtotal = 0;
+	int npend = 0;
 	for (;;) {
-		// ---- phase A: fill up to kSlots records in insertion order ----
+		// ---- phase A: stage up to kSlotsS candidates, in insertion order ----
 		bool exhausted = false;
-		while (nslots < kSlots) {
-			if (qi >= qn) {
+		while (npend < kSlotsS) {
+			if (r0 >= qtotal) {
 				if (lp >= lend) { exhausted = true; break; }
-				// which grids of this chunk of the super-tile list touch the tile?
+				// grids of the next list chunk that touch the tile, in order
 				const int li = lp + t;
-				int gid = -1;
+				int gid = -1, nmp = 0;
 				bool f = false;
 				if (li < lend) {
 					gid = bb.st_list[li];
 					const int4 rc = bb.grid_rect[gid];
 					f = rc.x < rc.y && rc.x < tpx1 && rc.y > tpx0 && rc.z < tpy1 && rc.w > tpy0;
+					if (f) nmp = __ldg(g.cu + gid) * __ldg(g.cv + gid);
 				}
 				int total;
 				const int pos = block_excl_scan(sm.warp_tot, f, total);
 				if (f) sm.qgrid[pos] = gid;
 				__syncthreads();
-				qn = total;
-				qi = 0;
+				// running micropolygon counts of the queued grids
+				if (t == 0) {
+					int acc = 0;
+					for (int k = 0; k < total; ++k) {
+						sm.qcum[k] = acc;
+						const int q = sm.qgrid[k];
+						acc += __ldg(g.cu + q) * __ldg(g.cv + q);
+					}
+					sm.qcum[total] = acc;
+					sm.qn = total;
+				}
+				(void)nmp;
+				__syncthreads();
+				qtotal = sm.qcum[sm.qn];
 				r0 = 0;
-				lp += kBlock;
+				lp += kThreadsS;
 				continue;
 			}
-			const int gi = sm.qgrid[qi];
-			const int cu = __ldg(g.cu + gi), cv = __ldg(g.cv + gi);
-			const int nmp = cu * cv;
-			if (r0 >= nmp) { ++qi; r0 = 0; continue; }
-			const int gflags = __ldg(g.flags + gi);
-			const long long pb = __ldg(g.pbase + gi);
-			const long long cb = __ldg(g.cbase + gi);
-			const long long mpb = __ldg(g.mpbase + gi);
-			// one micropolygon per thread
-			const int m = r0 + t;
+			// one micropolygon of the stream per thread: is it a candidate of this tile?
+			const int p = r0 + t;
 			bool active = false;
-			V3f v[4];
-			float bminx = 0, bmaxx = 0, bminy = 0, bmaxy = 0, bminz = 0;
-			int index = 0;
-			if (m < nmp) {
+			int gid = 0, m = 0;
+			if (p < qtotal) {
+				int lo = 0, hi = sm.qn - 1;
+				while (lo < hi) {
+					const int mid = (lo + hi + 1) >> 1;
+					if (sm.qcum[mid] <= p) lo = mid; else hi = mid - 1;
+				}
+				gid = sm.qgrid[lo];
+				m = p - sm.qcum[lo];
+				const int cu = __ldg(g.cu + gid);
+				const long long pb = __ldg(g.pbase + gid);
 				const int iv = m / cu, iu = m - iv * cu;
-				index = iv * (cu + 1) + iu;
-				const bool culled = g.culled && g.culled[mpb + m];
-				v[0] = ld3(g.P, pb + index);
-				v[1] = ld3(g.P, pb + index + 1);
-				v[2] = ld3(g.P, pb + index + cu + 1);
-				v[3] = ld3(g.P, pb + index + cu + 2);
-				// CalculateBound: min(min(min(A,B),C),D), C = index+cu+2, D = index+cu+1
-				bminx = amin(amin(amin(v[0].x, v[1].x), v[3].x), v[2].x);
-				bminy = amin(amin(amin(v[0].y, v[1].y), v[3].y), v[2].y);
-				bminz = amin(amin(amin(v[0].z, v[1].z), v[3].z), v[2].z);
-				bmaxx = amax(amax(amax(v[0].x, v[1].x), v[3].x), v[2].x);
-				bmaxy = amax(amax(amax(v[0].y, v[1].y), v[3].y), v[2].y);
+				const int index = iv * (cu + 1) + iu;
+				const V3f a = ld3(g.P, pb + index), b = ld3(g.P, pb + index + 1);
+				const V3f c = ld3(g.P, pb + index + cu + 1), d = ld3(g.P, pb + index + cu + 2);
+				const float bminx = amin(amin(amin(a.x, b.x), d.x), c.x);
+				const float bminy = amin(amin(amin(a.y, b.y), d.y), c.y);
+				const float bminz = amin(amin(amin(a.z, b.z), d.z), c.z);
+				const float bmaxx = amax(amax(amax(a.x, b.x), d.x), c.x);
+				const float bmaxy = amax(amax(amax(a.y, b.y), d.y), c.y);
+				const bool culled = g.culled && g.culled[__ldg(g.mpbase + gid) + m];
 				// AddMPG crop cull (imagebuffer.cpp:533-539)
 				const bool cropped =
 				    bmaxx < fp.cull_x0 || bmaxy < fp.cull_y0 || bminx > fp.cull_x1 || bminy > fp.cull_y1;
-				// pixels RenderMPG_Static visits: [floor(bmin), lceil(bmax)) clipped to the tile
+				// early-z for the whole tile: behind every sample's occluding depth
+				const bool hidden = cullable && bminz > sm.tile_ozmax;
 				const int sX = max((int)floorf(bminx), tpx0), eX = min(lceil_f(bmaxx), tpx1);
 				const int sY = max((int)floorf(bminy), tpy0), eY = min(lceil_f(bmaxy), tpy1);
-				active = !culled && !cropped && sX < eX && sY < eY;
+				active = !culled && !cropped && !hidden && sX < eX && sY < eY;
 			}
 			int total;
 			const int rank = block_excl_scan(sm.warp_tot, active, total);
-			const int navail = kSlots - nslots;
-			if (t == 0) sm.first_reject = kBlock;
+			const int navail = kSlotsS - npend;
+			if (t == 0) sm.first_reject = kThreadsS;
 			__syncthreads();
 			if (active && rank == navail) sm.first_reject = t;
-			if (active && rank < navail) {
-				const int slot = nslots + rank;
-				MpRec& rec = sm.rec[slot];
-				HitCoeffs h;
-				const int code = vertex_order(v);
-				hit_setup(v, code, h);
-				rec.bminx = bminx; rec.bmaxx = bmaxx; rec.bminy = bminy; rec.bmaxy = bmaxy; rec.bminz = bminz;
-#pragma unroll
-				for (int k = 0; k < 4; ++k) {
-					rec.ym[k] = h.ym[k]; rec.xm[k] = h.xm[k]; rec.ex[k] = h.ex[k]; rec.ey[k] = h.ey[k];
-					rec.z[k] = h.z[k];
-				}
-				rec.ax = h.ax; rec.ay = h.ay; rec.e_x = h.e_x; rec.e_y = h.e_y;
-				rec.f_x = h.f_x; rec.f_y = h.f_y; rec.g_x = h.g_x; rec.g_y = h.g_y;
-				rec.id = (int)(mpb + m);
-				rec.grid = gi;
-				// SqMpgSampleInfo::isOpaque (micropolygon.cpp:1477-1529)
-				bool opaque = true;
-				const bool smooth = (gflags & 1) != 0;
-				if (!(gflags & 8) && g.Oi) {
-					const float4 o0 = __ldg(g.Oi + cb + index);
-					opaque = o0.x >= 1.0f && o0.y >= 1.0f && o0.z >= 1.0f;
-					if (smooth) {
-						const float4 o1 = __ldg(g.Oi + cb + index + 1);
-						const float4 o2 = __ldg(g.Oi + cb + index + cu + 1);
-						const float4 o3 = __ldg(g.Oi + cb + index + cu + 2);
-						opaque = opaque && (o1.x >= 1.0f && o1.y >= 1.0f && o1.z >= 1.0f) &&
-						         (o2.x >= 1.0f && o2.y >= 1.0f && o2.z >= 1.0f) &&
-						         (o3.x >= 1.0f && o3.y >= 1.0f && o3.z >= 1.0f);
-					}
-				}
-				int bits = h.linear ? kRecLinear : 0;
-				if (opaque || (gflags & 4)) bits |= kRecOccluding;
-				if (smooth) bits |= kRecSmooth;
-				if (gflags & 2) bits |= kRecMatte;
-				if (gflags & 4) bits |= kRecMatteAlpha;
-				rec.bits = bits;
-				// candidate bit for every tile pixel of the visited range
-				const int sX = max((int)floorf(bminx), tpx0), eX = min(lceil_f(bmaxx), tpx1);
-				const int sY = max((int)floorf(bminy), tpy0), eY = min(lceil_f(bmaxy), tpy1);
-				const uint32_t bit = 1u << (slot & 31);
-				const int wd = slot >> 5;
-				for (int yy = sY; yy < eY; ++yy)
-					for (int xx = sX; xx < eX; ++xx)
-						atomicOr(&sm.mask[(yy - tpy0) * fp.tile_w + (xx - tpx0)][wd], bit);
-			}
+			if (active && rank < navail) sm.pend[npend + rank] = make_int2(gid, m);
 			__syncthreads();
-			const int consumed = (total > navail) ? sm.first_reject : min(kBlock, nmp - r0);
-			nslots += min(total, navail);
+			const int consumed = (total > navail) ? sm.first_reject : min(kThreadsS, qtotal - r0);
+			npend += min(total, navail);
 			r0 += consumed;
 		}
-		if (nslots == 0) break;
+		if (npend == 0) break;
 
-		// ---- phase B: walk this pixel's candidates in insertion order ----
-		if (own) {
+		// ---- build the staged records with every thread busy ----
+		for (int slot = t; slot < npend; slot += kThreadsS) {
+			const int2 e = sm.pend[slot];
+			RecS& rec = sm.rec[slot];
+			build_record(fp, g, e.x, e.y, rec);
+			const int sX = max(rec.px0, tpx0), eX = min(rec.px1, tpx1);
+			const int sY = max(rec.py0, tpy0), eY = min(rec.py1, tpy1);
+			const uint32_t bit = 1u << (slot & 31);
+			const int wd = slot >> 5;
+			for (int yy = sY; yy < eY; ++yy)
+				for (int xx = sX; xx < eX; ++xx)
+					atomicOr(&sm.mask[(yy - tpy0) * fp.tile_w + (xx - tpx0)][wd], bit);
+		}
+		__syncthreads();
+
+		// ---- phase B: a warp walks 32 samples' candidates in insertion order ----
+		float wmax = -FLT_MAX;
+		for (int gq = warp; gq < ngroups; gq += kWarpsS) {
+			const int s = gq * 32 + lane;
+			const int pl = s / spp;
+			const int si = s - pl * spp;
+			const int lx = pl % fp.tile_w, ly = pl / fp.tile_w;
+			const int px = tpx0 + lx, py = tpy0 + ly;
+			const bool valid = s < tsamp && px < tpx1 && py < tpy1;
+			const int sn = si / fp.xs, smm = si - sn * fp.xs;
+			float x = 0.0f, y = 0.0f, oz = -FLT_MAX;
+			int w = -1, fh = -1;
+			if (valid) {
+				const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
+				const long long pat = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
+				const float2 o = __ldg(smp.pos + pat * spp + si);
+				x = (float)px + o.x;  // CqImagePixel::setSamples: offset + positions[i]
+				y = (float)py + o.y;
+				oz = sm.soz[s];
+				w = sm.swin[s];
+				if (TRANSP) fh = fhead[s];
+			}
+			float gmax = warp_max_f(oz);
 #pragma unroll 1
-			for (int wd = 0; wd < kSlotWords; ++wd) {
-				uint32_t bits = sm.mask[pl][wd];
+			for (int wd = 0; wd < kWordsS; ++wd) {
+				const uint32_t mine = sm.mask[valid ? pl : 0][wd];  // index stays in bounds for idle lanes
+				uint32_t bits = __reduce_or_sync(0xffffffffu, valid ? mine : 0u);
 				while (bits) {
 					const int b = __ffs(bits) - 1;
 					bits &= bits - 1u;
-					const MpRec& r = sm.rec[wd * 32 + b];
-					int m_lo, m_hi, n_lo, n_hi;
-					sub_range(mypx, r.bminx, r.bmaxx, fp.xs, m_lo, m_hi);
-					sub_range(mypy, r.bminy, r.bmaxy, fp.ys, n_lo, n_hi);
-					int m = m0, n = n0;  // sub-pixel column and row of sample s0 + i
-#pragma unroll
-					for (int i = 0; i < kSamplesPerThread; ++i) {
-						const int mi = m, ni = n;
-						if (++m == fp.xs) { m = 0; ++n; }
-						if (i >= nmine || mi < m_lo || mi >= m_hi || ni < n_lo || ni >= n_hi) continue;
-						const float x = sx[i], y = sy[i];
-						// CqBound::Contains2D (bound.h:144-151)
-						if ((x < r.bminx || x > r.bmaxx) || (y < r.bminy || y > r.bmaxy)) continue;
-						// early-z (bucketprocessor.cpp:1179)
-						if (cullable && r.bminz > oz[i]) continue;
-						if (!edges_inside(r.ym, r.xm, r.ex, r.ey, x, y)) continue;
+					const RecS& r = sm.rec[wd * 32 + b];
+					if (cullable && r.bminz > gmax) continue;  // hidden from all 32 samples
+					bool ok = valid && px >= r.px0 && px < r.px1 && py >= r.py0 && py < r.py1;
+					if (ok) {
+						const int m_lo = (px == r.px0) ? r.im : 0;
+						const int m_hi = (px == r.px1 - 1) ? r.em : fp.xs;
+						const int n_lo = (py == r.py0) ? r.in_ : 0;
+						const int n_hi = (py == r.py1 - 1) ? r.en : fp.ys;
+						ok = smm >= m_lo && smm < m_hi && sn >= n_lo && sn < n_hi;
+					}
+					// CqBound::Contains2D (bound.h:144-151) and early-z (bucketprocessor.cpp:1179)
+					ok = ok && !((x < r.bminx || x > r.bmaxx) || (y < r.bminy || y > r.bmaxy));
+					ok = ok && !(cullable && r.bminz > oz);
+					ok = ok && edges_inside(r.ym, r.xm, r.ex, r.ey, x, y);
+					bool stored = false;
+					if (ok) {
 						float u, v;
-						inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y, (r.bits & kRecLinear) != 0,
-						             x, y, u, v);
+						inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y,
+						             (r.bits & kRecLinear) != 0, x, y, u, v);
 						const float D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
 						// StoreSample (bucketprocessor.cpp:1471-1569)
-						if (cullable && oz[i] <= D) continue;
-						if ((r.bits & kRecOccluding) && cullable) {
-							oz[i] = D;
-							win[t * kSamplesPerThread + i] = r.id;
-							wgrid[t * kSamplesPerThread + i] = r.grid;
-						} else if (TRANSP) {
-							// append a fragment {depth, id, u, v}; list head is newest-first
-							const unsigned act = __activemask();
-							const int leader = __ffs(act) - 1;
-							const int rank = __popc(act & ((1u << (threadIdx.x & 31)) - 1u));
-							unsigned long long base = 0;
-							if ((threadIdx.x & 31) == leader)
-								base = atomicAdd(pool.count, (unsigned long long)__popc(act));
-							base = __shfl_sync(act, base, leader);
-							const long long idx = (long long)base + rank;
-							if (idx < pool.capacity) {
-								pool.frag[idx] = make_float4(D, __int_as_float(r.id), u, v);
-								pool.next[idx] = fhead[t * kSamplesPerThread + i];
-								fhead[t * kSamplesPerThread + i] = (int)idx;
-							} else {
-								atomicOr(pool.overflow, 1);
+						if (!(cullable && oz <= D)) {
+							if ((r.bits & kRecOccluding) && cullable) {
+								oz = D;
+								w = r.id;
+								stored = true;
+							} else if (TRANSP) {
+								// append a fragment {depth, id, u, v}; lists are newest-first
+								const unsigned act = __activemask();
+								const int leader = __ffs(act) - 1;
+								const int rank = __popc(act & ((1u << lane) - 1u));
+								unsigned long long base = 0;
+								if (lane == leader) base = atomicAdd(pool.count, (unsigned long long)__popc(act));
+								base = __shfl_sync(act, base, leader);
+								const long long idx = (long long)base + rank;
+								if (idx < pool.capacity) {
+									pool.frag[idx] = make_float4(D, __int_as_float(r.id), u, v);
+									pool.next[idx] = fh;
+									fh = (int)idx;
+								} else {
+									atomicOr(pool.overflow, 1);
+								}
 							}
 						}
 					}
+					if (__any_sync(0xffffffffu, stored)) gmax = warp_max_f(oz);
 				}
 			}
+			if (valid) {
+				sm.soz[s] = oz;
+				sm.swin[s] = w;
+				if (TRANSP) fhead[s] = fh;
+			}
+			wmax = fmaxf(wmax, gmax);
 		}
+		// tile-wide largest occluding depth, then clear the masks
+		if (lane == 0) sm.warp_max[warp] = wmax;
 		__syncthreads();
-		for (int i = t; i < kBlock * kSlotWords; i += kBlock) (&sm.mask[0][0])[i] = 0u;
+		if (t == 0) {
+			float mx = -FLT_MAX;
+			for (int k = 0; k < kWarpsS; ++k) mx = fmaxf(mx, sm.warp_max[k]);
+			sm.tile_ozmax = mx;
+		}
+		for (int i = t; i < kTilePixMax * kWordsS; i += kThreadsS) (&sm.mask[0][0])[i] = 0u;
 		__syncthreads();
-		nslots = 0;
+		npend = 0;
 		if (exhausted) break;
 	}
 
-	// Resolve: colours of the occluding hits, Combine of transparent lists.
-	// The record area is free now; park the occluding depths there so the
-	// per-sample loop below can index them dynamically without pulling the
-	// register arrays into local memory.  Positions are recomputed from the
-	// pattern tables, which gives the same values.
-	__syncthreads();
-	if (!own) return;
-	float* ozs = reinterpret_cast<float*>(sm.rec);
-#pragma unroll
-	for (int i = 0; i < kSamplesPerThread; ++i) ozs[t * kSamplesPerThread + i] = oz[i];
-	const long long pat = smp.pos_index ? (long long)smp.pos_index[pix] : pix;
-	for (int i = 0; i < nmine; ++i) {
-		const float2 o = __ldg(smp.pos + pat * fp.spp + s0 + i);
-		resolve_sample<TRANSP>(fp, g, pool, st, pix * fp.spp + s0 + i, (float)mypx + o.x, (float)mypy + o.y,
-		                       ozs[t * kSamplesPerThread + i], win[t * kSamplesPerThread + i],
-		                       wgrid[t * kSamplesPerThread + i], TRANSP ? fhead[t * kSamplesPerThread + i] : -1);
+	// ---- resolve: colours of the occluding hits, Combine of fragment lists ----
+	for (int s = t; s < tsamp; s += kThreadsS) {
+		const int pl = s / spp;
+		const int si = s - pl * spp;
+		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
+		if (px >= tpx1 || py >= tpy1) continue;
+		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
+		const long long pat = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
+		const float2 o = __ldg(smp.pos + pat * spp + si);
+		resolve_sample<TRANSP>(fp, g, pool, st, pix * spp + si, (float)px + o.x, (float)py + o.y, sm.soz[s],
+		                       sm.swin[s], TRANSP ? fhead[s] : -1);
 	}
 }
 
 }  // namespace
 
+void static_tiling(FrameParams& fp) {
+	const int tpix = min(kTilePixMax, max(1, kTileSampMax / fp.spp));
+	int tw = 1;
+	while ((tw + 1) * (tw + 1) <= tpix) ++tw;
+	fp.tile_w = tw;
+	fp.tile_h = tpix / tw;
+	fp.tpp = 1;
+}
+
 void launch_sample_tiles(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
                          SampleStore st, FragPool pool, int32_t* err, cudaStream_t s) {
+	(void)err;
 	const int ntiles = fp.ntx * fp.nty;
-	const size_t smem_opaque = sizeof(Smem) + 2 * sizeof(int32_t) * kBlock * kSamplesPerThread;
-	const size_t smem_transp = smem_opaque + sizeof(int32_t) * kBlock * kSamplesPerThread;
+	const size_t smem_opaque = sizeof(SmemS);
+	const size_t smem_transp = smem_opaque + sizeof(int32_t) * kTileSampMax;
 	static bool configured = false;
 	if (!configured) {
 		cudaFuncSetAttribute(sample_static_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_opaque);
@@ -373,9 +458,9 @@ void launch_sample_tiles(const FrameParams& fp, const GridsDev& g, const Sampler
 		configured = true;
 	}
 	if (pool.capacity > 0)
-		sample_static_kernel<true><<<ntiles, kBlock, smem_transp, s>>>(fp, g, sm, b, st, pool, err);
+		sample_static_kernel<true><<<ntiles, kThreadsS, smem_transp, s>>>(fp, g, sm, b, st, pool);
 	else
-		sample_static_kernel<false><<<ntiles, kBlock, smem_opaque, s>>>(fp, g, sm, b, st, pool, err);
+		sample_static_kernel<false><<<ntiles, kThreadsS, smem_opaque, s>>>(fp, g, sm, b, st, pool);
 }
 
 }  // namespace aqh
