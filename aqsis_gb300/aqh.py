@@ -104,8 +104,10 @@ def load(build_if_missing: bool = False):
     L.aqh_frame_begin.argtypes = [vp, C.POINTER(FrameDesc)]
     L.aqh_set_samples.argtypes = [vp, C.POINTER(Samples)]
     L.aqh_submit_grid.argtypes = [vp, C.POINTER(Grid)]
-    L.aqh_submit_grids_device.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int64]
+    L.aqh_submit_grids_device.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int64]
     L.aqh_render.argtypes = [vp, C.c_int]
+    L.aqh_set_mode.argtypes = [vp, C.c_int]
+    L.aqh_set_stream.argtypes = [vp, vp]
     L.aqh_synchronize.argtypes = [vp]
     L.aqh_read_channels.argtypes = [vp, _f32p, C.c_size_t]
     L.aqh_read_bucket.argtypes = [vp, C.c_int, C.c_int, _f32p, C.c_size_t, _i32p, _i32p]
@@ -115,7 +117,7 @@ def load(build_if_missing: bool = False):
     L.aqh_filter_table.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, C.c_int, _f32p, C.c_int]
     L.aqh_filter_table.restype = C.c_int
     L.aqh_test_invbilinear.argtypes = [_f32p, _f32p, C.c_int, _f32p]
-    for name in ("aqh_create", "aqh_frame_begin", "aqh_set_samples", "aqh_submit_grid", "aqh_submit_grids_device",
+    for name in ("aqh_create", "aqh_set_mode", "aqh_set_stream", "aqh_frame_begin", "aqh_set_samples", "aqh_submit_grid", "aqh_submit_grids_device",
                  "aqh_render", "aqh_synchronize", "aqh_read_channels", "aqh_read_bucket", "aqh_read_quantized_u8",
                  "aqh_read_samples", "aqh_get_stats", "aqh_test_invbilinear"):
         getattr(L, name).restype = C.c_int
@@ -247,11 +249,18 @@ class Hider:
             mpbase += cu * cv
 
     def submit_grids_device(self, ngrids, d_cu, d_cv, d_nkeys, d_flags, d_pbase, d_cbase, d_tbase, d_times,
-                            d_P, d_Ci, d_Oi, total_mps):
+                            d_P, d_Ci, d_Oi, total_mps, d_culled=None):
         """Device-resident grids: every argument is a device pointer (int)."""
         self._check(self.L.aqh_submit_grids_device(self.ctx, ngrids, d_cu, d_cv, d_nkeys, d_flags, d_pbase,
-                                                   d_cbase, d_tbase, d_times, d_P, d_Ci, d_Oi, total_mps),
+                                                   d_cbase, d_tbase, d_times, d_P, d_Ci, d_Oi, d_culled, total_mps),
                     "aqh_submit_grids_device")
+
+    def set_mode(self, batched: bool):
+        """AQH_MODE_BATCHED (persistent work queue + CUDA graph) or AQH_MODE_PLAIN."""
+        self._check(self.L.aqh_set_mode(self.ctx, 1 if batched else 0), "aqh_set_mode")
+
+    def set_stream(self, stream_handle: int):
+        self._check(self.L.aqh_set_stream(self.ctx, stream_handle or None), "aqh_set_stream")
 
     def render(self, sync: bool = True):
         self._check(self.L.aqh_render(self.ctx, 1 if sync else 0), "aqh_render")
@@ -311,3 +320,161 @@ class Hider:
             res.update(self.read_samples())
         res["stats"] = self.stats()
         return res
+
+
+# ---------------------------------------------------------------------------
+# Serving (aqh_server_*)
+
+class Job(C.Structure):
+    _fields_ = [("frame", FrameDesc), ("samples", Samples), ("ngrids", C.c_int),
+                ("cu", C.c_void_p), ("cv", C.c_void_p), ("nkeys", C.c_void_p), ("flags", C.c_void_p),
+                ("pbase", C.c_void_p), ("cbase", C.c_void_p), ("tbase", C.c_void_p), ("times", C.c_void_p),
+                ("ntimes", C.c_size_t), ("P", C.c_void_p), ("nP", C.c_size_t), ("Ci", C.c_void_p),
+                ("Oi", C.c_void_p), ("nC", C.c_size_t), ("culled", C.c_void_p), ("micropolygons", C.c_int64),
+                ("rgba", C.c_void_p), ("channels", C.c_void_p)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int), ("state", C.c_int), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_done", C.c_double), ("footprint", C.c_size_t),
+                ("ms_device", C.c_float), ("slot", C.c_int)]
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("hbm_budget", C.c_size_t), ("slots", C.c_int), ("mode", C.c_int)]
+
+
+class ServerInfo(C.Structure):
+    _fields_ = [("budget", C.c_size_t), ("in_use", C.c_size_t), ("peak_in_use", C.c_size_t),
+                ("pending", C.c_int64), ("completed", C.c_int64), ("running", C.c_int), ("peak_running", C.c_int)]
+
+
+def _bind_server(L):
+    if getattr(L, "_server_bound", False):
+        return
+    vp = C.c_void_p
+    L.aqh_server_create.argtypes = [C.POINTER(ServerOpts), C.POINTER(vp)]
+    L.aqh_server_destroy.argtypes = [vp]
+    L.aqh_server_destroy.restype = None
+    L.aqh_server_submit.argtypes = [vp, C.POINTER(Job), C.POINTER(C.c_int64)]
+    L.aqh_server_poll.argtypes = [vp, C.c_int64, C.POINTER(JobInfo)]
+    L.aqh_server_wait.argtypes = [vp, C.c_int64, C.c_int, C.POINTER(JobInfo)]
+    L.aqh_server_cancel.argtypes = [vp, C.c_int64]
+    L.aqh_server_job_error.argtypes = [vp, C.c_int64]
+    L.aqh_server_job_error.restype = C.c_char_p
+    L.aqh_server_stats.argtypes = [vp, C.POINTER(ServerInfo)]
+    L.aqh_job_footprint.argtypes = [C.POINTER(Job)]
+    L.aqh_job_footprint.restype = C.c_size_t
+    for n in ("aqh_server_create", "aqh_server_submit", "aqh_server_poll", "aqh_server_wait", "aqh_server_cancel",
+              "aqh_server_stats"):
+        getattr(L, n).restype = C.c_int
+    L._server_bound = True
+
+
+def make_job(scene: Scene, keep: list, want_channels: bool = False):
+    """aqh_job for a scene; arrays it points to are appended to `keep`."""
+    fr, g, s = scene.frame, scene.grids, scene.samples
+
+    def a(x, dt):
+        if x is None:
+            return None
+        x = np.ascontiguousarray(x, dt)
+        keep.append(x)
+        return x
+    j = Job()
+    j.frame = frame_desc(fr)
+    j.samples = Samples(int(s.npatterns), _p(a(s.pos, np.float32), _f32p), _p(a(s.time, np.float32), _f32p),
+                        _p(a(s.dof, np.float32), _f32p), _p(a(s.shuffle, np.int32), _i32p),
+                        _p(a(s.lod, np.float32), _f32p), _p(a(s.pos_index, np.uint32), _u32p),
+                        _p(a(s.dof_index, np.uint32), _u32p), _p(a(s.time_index, np.uint32), _u32p),
+                        _p(a(s.shuffle_index, np.uint32), _u32p), _p(a(s.lod_index, np.uint32), _u32p),
+                        _p(a(s.dither, np.float32), _f32p))
+    j.ngrids = g.ngrids
+    for k, dt in (("cu", np.int32), ("cv", np.int32), ("nkeys", np.int32), ("flags", np.int32),
+                  ("pbase", np.int64), ("cbase", np.int64), ("tbase", np.int32), ("times", np.float32),
+                  ("P", np.float32), ("Ci", np.float32), ("Oi", np.float32)):
+        setattr(j, k, a(getattr(g, k), dt).ctypes.data)
+    j.ntimes = int(g.times.size)
+    j.nP = int(g.P.shape[0])
+    j.nC = int(g.Ci.shape[0])
+    if g.culled is not None:
+        j.culled = a(g.culled, np.uint8).ctypes.data
+    j.micropolygons = g.micropolygons
+    cx0, cx1, cy0, cy1 = fr.crop_window
+    rgba = np.zeros((cy1 - cy0, cx1 - cx0, 4), np.uint8)
+    keep.append(rgba)
+    j.rgba = rgba.ctypes.data
+    chans = None
+    if want_channels:
+        chans = np.zeros((cy1 - cy0, cx1 - cx0, 9), np.float32)
+        keep.append(chans)
+        j.channels = chans.ctypes.data
+    return j, rgba, chans
+
+
+class Server:
+    """aqh_server: jobs admitted by HBM footprint onto `slots` resident contexts."""
+
+    def __init__(self, device: int = 0, budget: int = 0, slots: int = 4, batched: bool = True):
+        self.L = load()
+        _bind_server(self.L)
+        self.sv = C.c_void_p()
+        rc = self.L.aqh_server_create(C.byref(ServerOpts(device, budget, slots, 1 if batched else 0)),
+                                      C.byref(self.sv))
+        if rc != AQH_OK:
+            raise AqhError(rc, "aqh_server_create")
+        self._jobs = {}
+
+    def close(self):
+        if self.sv:
+            self.L.aqh_server_destroy(self.sv)
+            self.sv = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def footprint(self, scene: Scene) -> int:
+        keep = []
+        j, _, _ = make_job(scene, keep)
+        return int(self.L.aqh_job_footprint(C.byref(j)))
+
+    def submit(self, scene: Scene, want_channels: bool = False) -> int:
+        keep = []
+        j, rgba, chans = make_job(scene, keep, want_channels)
+        jid = C.c_int64()
+        rc = self.L.aqh_server_submit(self.sv, C.byref(j), C.byref(jid))
+        if rc != AQH_OK:
+            raise AqhError(rc, "aqh_server_submit")
+        self._jobs[jid.value] = (j, keep, rgba, chans)
+        return jid.value
+
+    def wait(self, jid: int, timeout_ms: int = 600000):
+        info = JobInfo()
+        rc = self.L.aqh_server_wait(self.sv, jid, timeout_ms, C.byref(info))
+        return rc, info
+
+    def poll(self, jid: int):
+        info = JobInfo()
+        rc = self.L.aqh_server_poll(self.sv, jid, C.byref(info))
+        return rc, info
+
+    def cancel(self, jid: int) -> int:
+        return self.L.aqh_server_cancel(self.sv, jid)
+
+    def error(self, jid: int) -> str:
+        return self.L.aqh_server_job_error(self.sv, jid).decode()
+
+    def result(self, jid: int):
+        _, _, rgba, chans = self._jobs[jid]
+        return rgba, chans
+
+    def release(self, jid: int):
+        self._jobs.pop(jid, None)
+
+    def stats(self) -> dict:
+        si = ServerInfo()
+        self.L.aqh_server_stats(self.sv, C.byref(si))
+        return {k: getattr(si, k) for k, _ in ServerInfo._fields_}

@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libaqh.so")
-SOURCES = ["api.cu", "bin.cu", "sample.cu", "sample_mb.cu", "filter.cu"]
+SOURCES = ["api.cu", "bin.cu", "sample.cu", "sample_mb.cu", "filter.cu", "server.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
               "-Xptxas", "-v"]
@@ -54,7 +54,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     with open(os.path.join(OUT, "ptxas.log"), "w") as f:
         f.write("\n".join(logs))
     objs = [r[1] for r in results]
-    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)

@@ -180,6 +180,23 @@ void project_to_circle_h(float x, float y, float& ox, float& oy) {
 	oy = adj * y;
 }
 
+// Accumulated slice end times of CqMicroPolygonMotion::BuildBoundList
+// (micropolygon.cpp:1714-1752) for every slice count d in 1..max(4, spp):
+// dt = (close - open) / d, time = open + dt, then time += dt per slice.
+void slice_times_h(float open, float close, int spp, std::vector<float>& out) {
+	const int maxd = std::max(4, spp);
+	out.assign((size_t)maxd * (maxd + 1) / 2, 0.0f);
+	for (int d = 1; d <= maxd; ++d) {
+		const float dt = (close - open) / d;
+		float time = open + dt;
+		float* T = out.data() + (size_t)d * (d - 1) / 2;
+		for (int b = 0; b < d; ++b) {
+			T[b] = time;
+			time += dt;
+		}
+	}
+}
+
 // CqBucketProcessor::CalculateDofBounds (bucketprocessor.cpp:858-913): the
 // region of the lens each sub-pixel stratum's offsets fall in, as
 // {min.x, min.y, max.x, max.y}.
@@ -314,6 +331,7 @@ struct aqh_ctx {
 		const int32_t *cu, *cv, *nkeys, *flags, *tbase;
 		const int64_t *pbase, *cbase;
 		const float *times, *P, *Ci, *Oi;
+		const uint8_t* culled;
 		size_t ntimes, nP, nC;
 	} hp{};
 	cudaStream_t own_stream = nullptr;
@@ -325,11 +343,21 @@ struct aqh_ctx {
 	// device buffers
 	DevBuf d_cu, d_cv, d_nkeys, d_flags, d_tbase, d_pbase, d_cbase, d_mpbase, d_times, d_culled, d_P, d_Ci, d_Oi;
 	DevBuf d_mpcount;
-	DevBuf d_rect, d_stcount, d_stoffset, d_stlist;
+	DevBuf d_rect, d_minz, d_stcount, d_stoffset, d_stlist;
 	DevBuf d_sa, d_sb, d_win, d_oz, d_nf;
 	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err;
 	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb;
 	bool dev_motion = false;
+	DevBuf d_queue, d_slices;
+	std::vector<float4> h_dofb;
+	std::vector<float> h_slices;
+	int mode = AQH_MODE_PLAIN;
+	cudaGraphExec_t graph_exec = nullptr;
+	bool graph_valid = false;
+	std::vector<unsigned char> graph_key;
+	int64_t graphs_built = 0, overflow_rerenders = 0;
+	bool pending_check = false;
+	aqh::RenderPlan pending_plan{};
 	// sampler
 	DevBuf s_pos, s_time, s_dof, s_shuffle, s_lod, s_ipos, s_idof, s_itime, s_ishuf, s_ilod, s_dither;
 	SamplerDev smp{};
@@ -401,6 +429,7 @@ aqh_status aqh_create(const aqh_device_opts* opts, aqh_ctx** out) {
 	cudaError_t e = cudaSetDevice(ctx->device);
 	if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
 	ctx->own_stream = ctx->stream;
+	if (e == cudaSuccess) aqh::configure_sample_kernels();
 	for (int i = 0; e == cudaSuccess && i < 6; ++i) e = cudaEventCreate(&ctx->ev[i]);
 	if (e != cudaSuccess) {
 		delete ctx;
@@ -417,6 +446,7 @@ void aqh_destroy(aqh_ctx* ctx) {
 	if (ctx->own_stream && ctx->own_stream != ctx->stream) cudaStreamSynchronize(ctx->own_stream);
 	for (auto& ev : ctx->ev)
 		if (ev) cudaEventDestroy(ev);
+	if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
 	if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
 	delete ctx;
 }
@@ -612,7 +642,7 @@ aqh_status aqh_submit_grids_host(aqh_ctx* ctx, int ngrids, const int32_t* cu, co
                                  const int32_t* nkeys, const int32_t* flags, const int64_t* pbase,
                                  const int64_t* cbase, const int32_t* tbase, const float* times, size_t ntimes,
                                  const float* P, size_t nP, const float* Ci, const float* Oi, size_t nC,
-                                 int64_t total_mps) {
+                                 const uint8_t* culled, int64_t total_mps) {
 	if (!ctx || ngrids < 0 || !cu || !cv || !nkeys || !flags || !pbase || !cbase || !tbase || !P) return AQH_EINVAL;
 	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
 	if (!ctx->h_cu.empty() || ctx->dev_grids || ctx->host_packed) return ctx->fail(AQH_EINVAL, "frame already holds grids");
@@ -635,6 +665,7 @@ aqh_status aqh_submit_grids_host(aqh_ctx* ctx, int ngrids, const int32_t* cu, co
 	ctx->hp.cu = cu; ctx->hp.cv = cv; ctx->hp.nkeys = nkeys; ctx->hp.flags = flags; ctx->hp.tbase = tbase;
 	ctx->hp.pbase = pbase; ctx->hp.cbase = cbase; ctx->hp.times = times; ctx->hp.ntimes = ntimes;
 	ctx->hp.P = P; ctx->hp.nP = nP; ctx->hp.Ci = Ci; ctx->hp.Oi = Oi; ctx->hp.nC = nC;
+	ctx->hp.culled = culled;
 	ctx->h_mpbase.resize(ngrids);
 	int64_t acc = 0;
 	for (int i = 0; i < ngrids; ++i) { ctx->h_mpbase[i] = acc; acc += (int64_t)cu[i] * cv[i]; }
@@ -647,7 +678,8 @@ aqh_status aqh_submit_grids_host(aqh_ctx* ctx, int ngrids, const int32_t* cu, co
 aqh_status aqh_submit_grids_device(aqh_ctx* ctx, int ngrids, const int32_t* d_cu, const int32_t* d_cv,
                                    const int32_t* d_nkeys, const int32_t* d_flags, const int64_t* d_pbase,
                                    const int64_t* d_cbase, const int32_t* d_tbase, const float* d_times,
-                                   const float* d_P, const float* d_Ci, const float* d_Oi, int64_t total_mps) {
+                                   const float* d_P, const float* d_Ci, const float* d_Oi, const uint8_t* d_culled,
+                                   int64_t total_mps) {
 	if (!ctx || ngrids < 0 || !d_cu || !d_cv || !d_nkeys || !d_flags || !d_pbase || !d_cbase || !d_P)
 		return AQH_EINVAL;
 	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
@@ -661,7 +693,7 @@ aqh_status aqh_submit_grids_device(aqh_ctx* ctx, int ngrids, const int32_t* d_cu
 	g.P = reinterpret_cast<const float4*>(d_P);
 	g.Ci = reinterpret_cast<const float4*>(d_Ci);
 	g.Oi = reinterpret_cast<const float4*>(d_Oi);
-	g.culled = nullptr;
+	g.culled = d_culled;
 	// first micropolygon id of every grid
 	AQH_TRY(ctx->d_mpcount.ensure(sizeof(int32_t) * (ngrids + 1) * 2 + 64), "alloc");
 	AQH_TRY(ctx->d_mpbase.ensure(sizeof(int64_t) * (ngrids + 1)), "alloc");
@@ -707,6 +739,7 @@ static aqh_status upload_packed_grids(aqh_ctx* ctx) {
 	AQH_TRY(up(ctx->d_P, hp.P, hp.nP * 16), "upload P");
 	AQH_TRY(up(ctx->d_Ci, hp.Ci, hp.nC * 16), "upload Ci");
 	AQH_TRY(up(ctx->d_Oi, hp.Oi, hp.nC * 16), "upload Oi");
+	if (hp.culled) AQH_TRY(up(ctx->d_culled, hp.culled, (size_t)ctx->h_mps), "upload culled");
 	GridsDev& g = ctx->dg;
 	g.ngrids = G;
 	g.cu = ctx->d_cu.as<int32_t>(); g.cv = ctx->d_cv.as<int32_t>(); g.nkeys = ctx->d_nkeys.as<int32_t>();
@@ -716,7 +749,7 @@ static aqh_status upload_packed_grids(aqh_ctx* ctx) {
 	g.P = ctx->d_P.as<float4>();
 	g.Ci = hp.Ci ? ctx->d_Ci.as<float4>() : nullptr;
 	g.Oi = hp.Oi ? ctx->d_Oi.as<float4>() : nullptr;
-	g.culled = nullptr;
+	g.culled = hp.culled ? ctx->d_culled.as<uint8_t>() : nullptr;
 	return AQH_OK;
 }
 
@@ -751,11 +784,8 @@ static aqh_status upload_host_grids(aqh_ctx* ctx) {
 	return AQH_OK;
 }
 
-aqh_status aqh_render(aqh_ctx* ctx, int sync) {
-	if (!ctx) return AQH_EINVAL;
-	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
-	if (!ctx->samples_set) return ctx->fail(AQH_EINVAL, "aqh_set_samples was not called");
-	cudaSetDevice(ctx->device);
+
+static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	FrameParams& fp = ctx->fp;
 	cudaStream_t s = ctx->stream;
 	aqh_status st = AQH_OK;
@@ -767,7 +797,7 @@ aqh_status aqh_render(aqh_ctx* ctx, int sync) {
 		if (st != AQH_OK) return st;
 	}
 	const GridsDev& g = ctx->dg;
-	const int64_t nmps = ctx->dev_grids ? ctx->dev_mps : ctx->h_mps;
+	P.nmps = ctx->dev_grids ? ctx->dev_mps : ctx->h_mps;
 	bool motion = false;
 	if (ctx->host_packed) {
 		for (int i = 0; i < ctx->hp.ngrids; ++i) motion = motion || ctx->hp.nkeys[i] > 1;
@@ -776,37 +806,46 @@ aqh_status aqh_render(aqh_ctx* ctx, int sync) {
 	}
 	if (ctx->dev_grids) motion = ctx->dev_motion;
 	fp.any_motion = motion ? 1 : 0;
-	const bool mbdof = fp.use_dof || fp.any_motion;
-	set_tiling(fp, mbdof ? mb_samples_per_thread() : 0);
-	if (mbdof) {
-		std::vector<float4> db;
-		dof_bounds_h(fp.xs, fp.ys, db);
-		AQH_TRY(ctx->d_dofb.ensure(db.size() * sizeof(float4)), "alloc");
-		AQH_TRY(cudaMemcpyAsync(ctx->d_dofb.p, db.data(), db.size() * sizeof(float4), cudaMemcpyHostToDevice, s),
+	P.mbdof = fp.use_dof || fp.any_motion;
+	set_tiling(fp, 0);
+	if (P.mbdof) {
+		ctx->h_dofb.clear();
+		dof_bounds_h(fp.xs, fp.ys, ctx->h_dofb);
+		AQH_TRY(ctx->d_dofb.ensure(ctx->h_dofb.size() * sizeof(float4)), "alloc");
+		AQH_TRY(cudaMemcpyAsync(ctx->d_dofb.p, ctx->h_dofb.data(), ctx->h_dofb.size() * sizeof(float4),
+		                        cudaMemcpyHostToDevice, s),
 		        "upload lens bounds");
+		slice_times_h(fp.shutter_open, fp.shutter_close, fp.spp, ctx->h_slices);
+		AQH_TRY(ctx->d_slices.ensure(ctx->h_slices.size() * sizeof(float)), "alloc");
+		AQH_TRY(cudaMemcpyAsync(ctx->d_slices.p, ctx->h_slices.data(), ctx->h_slices.size() * sizeof(float),
+		                        cudaMemcpyHostToDevice, s),
+		        "upload slice times");
 	}
 	const int G = g.ngrids;
-	const size_t nsamp = (size_t)fp.sw * fp.sh * fp.spp;
-	const int nst = fp.nstx * fp.nsty;
-	BinBuffers bb{};
+	P.nsamp = (size_t)fp.sw * fp.sh * fp.spp;
+	P.nst = fp.nstx * fp.nsty;
+	BinBuffers& bb = P.bb;
+	bb = BinBuffers{};
 	bb.range_size = 4096;
 	bb.nranges = std::max(1, (G + bb.range_size - 1) / bb.range_size);
 	AQH_TRY(ctx->d_rect.ensure(sizeof(int4) * std::max(G, 1)), "alloc rects");
-	AQH_TRY(ctx->d_stcount.ensure(sizeof(int32_t) * ((size_t)nst * bb.nranges + 1)), "alloc bins");
-	AQH_TRY(ctx->d_stoffset.ensure(sizeof(int32_t) * ((size_t)nst * bb.nranges + 1)), "alloc bins");
+	AQH_TRY(ctx->d_minz.ensure(sizeof(float) * std::max(G, 1)), "alloc rects");
+	AQH_TRY(ctx->d_stcount.ensure(sizeof(int32_t) * ((size_t)P.nst * bb.nranges + 1)), "alloc bins");
+	AQH_TRY(ctx->d_stoffset.ensure(sizeof(int32_t) * ((size_t)P.nst * bb.nranges + 1)), "alloc bins");
 	bb.grid_rect = ctx->d_rect.as<int4>();
+	bb.grid_minz = ctx->d_minz.as<float>();
 	bb.st_count = ctx->d_stcount.as<int32_t>();
 	bb.st_offset = ctx->d_stoffset.as<int32_t>();
-	// sample store
-	AQH_TRY(ctx->d_sa.ensure(nsamp * sizeof(float4)), "alloc sample store");
-	AQH_TRY(ctx->d_sb.ensure(nsamp * sizeof(float4)), "alloc sample store");
-	SampleStore store{};
+	AQH_TRY(ctx->d_sa.ensure(P.nsamp * sizeof(float4)), "alloc sample store");
+	AQH_TRY(ctx->d_sb.ensure(P.nsamp * sizeof(float4)), "alloc sample store");
+	SampleStore& store = P.store;
+	store = SampleStore{};
 	store.a = ctx->d_sa.as<float4>();
 	store.b = ctx->d_sb.as<float4>();
 	if (ctx->debug_samples) {
-		AQH_TRY(ctx->d_win.ensure(nsamp * 4), "alloc");
-		AQH_TRY(ctx->d_oz.ensure(nsamp * 4), "alloc");
-		AQH_TRY(ctx->d_nf.ensure(nsamp * 4), "alloc");
+		AQH_TRY(ctx->d_win.ensure(P.nsamp * 4), "alloc");
+		AQH_TRY(ctx->d_oz.ensure(P.nsamp * 4), "alloc");
+		AQH_TRY(ctx->d_nf.ensure(P.nsamp * 4), "alloc");
 		store.winner = ctx->d_win.as<int32_t>();
 		store.occlz = ctx->d_oz.as<float>();
 		store.nfrag = ctx->d_nf.as<int32_t>();
@@ -815,24 +854,14 @@ aqh_status aqh_render(aqh_ctx* ctx, int sync) {
 	AQH_TRY(cudaMemcpyAsync(ctx->d_ftab.p, ctx->ftab.data(), ctx->ftab.size() * 4, cudaMemcpyHostToDevice, s), "ftab");
 	const size_t ndisp = (size_t)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
 	AQH_TRY(ctx->d_chan.ensure(ndisp * 9 * 4), "alloc channels");
+	AQH_TRY(ctx->d_q8.ensure(ndisp * 4), "alloc quantized");
+	AQH_TRY(ctx->d_qchan.ensure(64), "alloc");
 	AQH_TRY(ctx->d_err.ensure(64), "alloc");
-
-	cudaEventRecord(ctx->ev[0], s);
-	launch_grid_rects(fp, g, bb.grid_rect, s);
-	launch_st_count(fp, g, bb, s);
-	launch_scan_i32(bb.st_count, bb.st_offset, nst * bb.nranges, nullptr, s);
-	int32_t total = 0;
-	AQH_TRY(cudaMemcpyAsync(&total, bb.st_offset + (size_t)nst * bb.nranges, 4, cudaMemcpyDeviceToHost, s), "readback");
-	AQH_TRY(cudaStreamSynchronize(s), "bin");
-	AQH_TRY(ctx->d_stlist.ensure(sizeof(int32_t) * std::max(total, 1)), "alloc tile lists");
-	bb.st_list = ctx->d_stlist.as<int32_t>();
-	bb.list_capacity = total;
-	launch_st_write(fp, g, bb, s);
-	cudaEventRecord(ctx->ev[1], s);
-
-	FragPool pool{};
+	AQH_TRY(ctx->d_queue.ensure(64), "alloc");
+	FragPool& pool = P.pool;
+	pool = FragPool{};
 	if (ctx->any_transparent || !fp.cullable) {
-		if (ctx->frag_capacity == 0) ctx->frag_capacity = std::max<int64_t>(1 << 20, (int64_t)nsamp * 2);
+		if (ctx->frag_capacity == 0) ctx->frag_capacity = std::max<int64_t>(1 << 20, (int64_t)P.nsamp * 2);
 		AQH_TRY(ctx->d_frag.ensure(ctx->frag_capacity * sizeof(float4)), "alloc fragments");
 		AQH_TRY(ctx->d_next.ensure(ctx->frag_capacity * sizeof(int32_t)), "alloc fragments");
 		AQH_TRY(ctx->d_fcount.ensure(16), "alloc");
@@ -843,22 +872,112 @@ aqh_status aqh_render(aqh_ctx* ctx, int sync) {
 		pool.overflow = ctx->d_foverflow.as<int32_t>();
 		pool.capacity = ctx->frag_capacity;
 	}
+	int nsm = 0;
+	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+	P.nctas = std::max(1, std::min(fp.ntx * fp.nty, nsm * sample_static_ctas_per_sm(pool.capacity > 0)));
+	P.fp = fp;
+	P.g = g;
+	return AQH_OK;
+}
+
+static const int kDefaultDisplay[4] = {0, 1, 2, 6};  // r, g, b, a
+
+// The device work of one frame after binning's list capacity is known.
+// `batched`: persistent sampling kernel fed from a work queue; no host
+// synchronization anywhere, so the sequence can be captured in a CUDA graph.
+static aqh_status enqueue_frame(aqh_ctx* ctx, RenderPlan& P, bool batched, bool timing) {
+	cudaStream_t s = ctx->stream;
+	FrameParams& fp = P.fp;
+	// inside a graph capture the stage events must be external record nodes to
+	// be usable for timing after the graph runs
+	auto mark = [&](cudaEvent_t e) {
+		if (batched) cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+		else cudaEventRecord(e, s);
+	};
+	if (timing) mark(ctx->ev[0]);
+	if (P.g.ngrids > 0) {
+		launch_grid_rects(fp, P.g, P.bb.grid_rect, P.bb.grid_minz, s);
+		launch_st_count(fp, P.g, P.bb, s);
+		launch_scan_i32(P.bb.st_count, P.bb.st_offset, P.nst * P.bb.nranges, nullptr, s);
+		launch_st_write(fp, P.g, P.bb, s);
+	} else {
+		AQH_TRY(cudaMemsetAsync(P.bb.st_offset, 0, sizeof(int32_t) * ((size_t)P.nst * P.bb.nranges + 1), s), "memset");
+	}
+	if (P.pool.capacity > 0) {
+		AQH_TRY(cudaMemsetAsync(P.pool.count, 0, 8, s), "memset");
+		AQH_TRY(cudaMemsetAsync(P.pool.overflow, 0, 4, s), "memset");
+	}
+	if (timing) mark(ctx->ev[1]);
+	if (P.mbdof) {
+		launch_sample_mb(fp, P.g, ctx->smp, P.bb, P.store, P.pool, ctx->d_dofb.as<float4>(), ctx->d_slices.as<float>(), s);
+	} else if (batched) {
+		AQH_TRY(cudaMemsetAsync(ctx->d_queue.p, 0, 4, s), "memset");
+		launch_sample_tiles_q(fp, P.g, ctx->smp, P.bb, P.store, P.pool, ctx->d_queue.as<int>(), nullptr, P.nctas, s);
+	} else {
+		launch_sample_tiles(fp, P.g, ctx->smp, P.bb, P.store, P.pool, ctx->d_err.as<int32_t>(), s);
+	}
+	AQH_TRY(cudaGetLastError(), "sample kernel launch");
+	if (timing) mark(ctx->ev[2]);
+	launch_filter(fp, ctx->smp, P.store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(), s);
+	if (fp.q_one == 0.0f || (fp.q_min >= 0.0f && fp.q_max <= 255.0f)) {
+		AQH_TRY(cudaMemcpyAsync(ctx->d_qchan.p, kDefaultDisplay, sizeof kDefaultDisplay, cudaMemcpyHostToDevice, s),
+		        "upload display channels");
+		launch_quantize_u8(fp, ctx->smp, ctx->d_chan.as<float>(), ctx->d_qchan.as<int>(), 4, ctx->d_q8.as<uint8_t>(), s);
+	}
+	AQH_TRY(cudaGetLastError(), "filter kernel launch");
+	if (timing) mark(ctx->ev[3]);
+	return AQH_OK;
+}
+
+static void read_stage_times(aqh_ctx* ctx) {
+	float a = 0, b = 0, c = 0;
+	if (cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]) != cudaSuccess) a = 0;
+	if (cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]) != cudaSuccess) b = 0;
+	if (cudaEventElapsedTime(&c, ctx->ev[2], ctx->ev[3]) != cudaSuccess) c = 0;
+	cudaGetLastError();  // a failed timing query is not an error of the next launch
+	ctx->stats.ms_bin = a;
+	ctx->stats.ms_sample = b;
+	ctx->stats.ms_filter = c;
+	ctx->stats.ms_total = a + b + c;
+}
+
+// One frame, one launch per stage, with the host reading binning's list size
+// and the fragment count back between stages (the plain path).
+static aqh_status render_plain(aqh_ctx* ctx, RenderPlan& P, bool sync) {
+	cudaStream_t s = ctx->stream;
+	const FrameParams& fp = P.fp;
+	cudaEventRecord(ctx->ev[0], s);
+	int32_t total = 0;
+	if (P.g.ngrids > 0) {
+		launch_grid_rects(fp, P.g, P.bb.grid_rect, P.bb.grid_minz, s);
+		launch_st_count(fp, P.g, P.bb, s);
+		launch_scan_i32(P.bb.st_count, P.bb.st_offset, P.nst * P.bb.nranges, nullptr, s);
+		AQH_TRY(cudaMemcpyAsync(&total, P.bb.st_offset + (size_t)P.nst * P.bb.nranges, 4, cudaMemcpyDeviceToHost, s),
+		        "readback");
+		AQH_TRY(cudaStreamSynchronize(s), "bin");
+	}
+	AQH_TRY(ctx->d_stlist.ensure(sizeof(int32_t) * std::max<int64_t>(total, 1)), "alloc tile lists");
+	ctx->st_list_cap = std::max<int64_t>(ctx->st_list_cap, ctx->d_stlist.cap / sizeof(int32_t));
+	P.bb.st_list = ctx->d_stlist.as<int32_t>();
+	P.bb.list_capacity = ctx->d_stlist.cap / sizeof(int32_t);
+	if (P.g.ngrids > 0) launch_st_write(fp, P.g, P.bb, s);
+	else AQH_TRY(cudaMemsetAsync(P.bb.st_offset, 0, sizeof(int32_t) * ((size_t)P.nst * P.bb.nranges + 1), s), "memset");
 	for (int attempt = 0; attempt < 4; ++attempt) {
-		if (pool.capacity > 0) {
-			AQH_TRY(cudaMemsetAsync(pool.count, 0, 8, s), "memset");
-			AQH_TRY(cudaMemsetAsync(pool.overflow, 0, 4, s), "memset");
+		if (P.pool.capacity > 0) {
+			AQH_TRY(cudaMemsetAsync(P.pool.count, 0, 8, s), "memset");
+			AQH_TRY(cudaMemsetAsync(P.pool.overflow, 0, 4, s), "memset");
 		}
 		cudaEventRecord(ctx->ev[1], s);
-		if (mbdof)
-			launch_sample_mb(fp, g, ctx->smp, bb, store, pool, ctx->d_dofb.as<float4>(), s);
+		if (P.mbdof)
+			launch_sample_mb(fp, P.g, ctx->smp, P.bb, P.store, P.pool, ctx->d_dofb.as<float4>(), ctx->d_slices.as<float>(), s);
 		else
-			launch_sample_tiles(fp, g, ctx->smp, bb, store, pool, ctx->d_err.as<int32_t>(), s);
+			launch_sample_tiles(fp, P.g, ctx->smp, P.bb, P.store, P.pool, ctx->d_err.as<int32_t>(), s);
 		AQH_TRY(cudaGetLastError(), "sample kernel launch");
-		if (pool.capacity == 0) break;
+		if (P.pool.capacity == 0) break;
 		int32_t ovf = 0;
 		unsigned long long used = 0;
-		AQH_TRY(cudaMemcpyAsync(&ovf, pool.overflow, 4, cudaMemcpyDeviceToHost, s), "readback");
-		AQH_TRY(cudaMemcpyAsync(&used, pool.count, 8, cudaMemcpyDeviceToHost, s), "readback");
+		AQH_TRY(cudaMemcpyAsync(&ovf, P.pool.overflow, 4, cudaMemcpyDeviceToHost, s), "readback");
+		AQH_TRY(cudaMemcpyAsync(&used, P.pool.count, 8, cudaMemcpyDeviceToHost, s), "readback");
 		AQH_TRY(cudaStreamSynchronize(s), "sample");
 		ctx->stats.fragments = (int64_t)used;
 		if (!ovf) break;
@@ -866,36 +985,127 @@ aqh_status aqh_render(aqh_ctx* ctx, int sync) {
 		ctx->frag_capacity = (int64_t)used + (int64_t)used / 4 + 1024;
 		AQH_TRY(ctx->d_frag.ensure(ctx->frag_capacity * sizeof(float4)), "alloc fragments");
 		AQH_TRY(ctx->d_next.ensure(ctx->frag_capacity * sizeof(int32_t)), "alloc fragments");
-		pool.frag = ctx->d_frag.as<float4>();
-		pool.next = ctx->d_next.as<int32_t>();
-		pool.capacity = ctx->frag_capacity;
+		P.pool.frag = ctx->d_frag.as<float4>();
+		P.pool.next = ctx->d_next.as<int32_t>();
+		P.pool.capacity = ctx->frag_capacity;
+		ctx->graph_valid = false;
 	}
 	cudaEventRecord(ctx->ev[2], s);
-	launch_filter(fp, ctx->smp, store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(), s);
+	launch_filter(fp, ctx->smp, P.store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(), s);
+	if (fp.q_one == 0.0f || (fp.q_min >= 0.0f && fp.q_max <= 255.0f)) {
+		AQH_TRY(cudaMemcpyAsync(ctx->d_qchan.p, kDefaultDisplay, sizeof kDefaultDisplay, cudaMemcpyHostToDevice, s),
+		        "upload display channels");
+		launch_quantize_u8(fp, ctx->smp, ctx->d_chan.as<float>(), ctx->d_qchan.as<int>(), 4, ctx->d_q8.as<uint8_t>(), s);
+	}
 	AQH_TRY(cudaGetLastError(), "filter kernel launch");
 	cudaEventRecord(ctx->ev[3], s);
-	ctx->stats.micropolygons = nmps;
-	ctx->stats.samples = (int64_t)nsamp;
-	ctx->stats.grids = G;
 	ctx->stats.tile_grid_pairs = total;
 	if (sync) {
 		AQH_TRY(cudaStreamSynchronize(s), "render");
-		float a = 0, b = 0, c = 0;
-		cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
-		cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
-		cudaEventElapsedTime(&c, ctx->ev[2], ctx->ev[3]);
-		ctx->stats.ms_bin = a;
-		ctx->stats.ms_sample = b;
-		ctx->stats.ms_filter = c;
-		ctx->stats.ms_total = a + b + c;
+		read_stage_times(ctx);
 	}
 	return AQH_OK;
+}
+
+// Batched path: the list and fragment capacities come from the previous
+// frame (or a bound), overflow is detected on the device, and the whole frame
+// is one CUDA graph replayed while its arguments stay the same.
+static aqh_status render_batched(aqh_ctx* ctx, RenderPlan& P, bool sync) {
+	cudaStream_t s = ctx->stream;
+	const int64_t want = std::max<int64_t>(ctx->st_list_cap, (int64_t)P.g.ngrids * 4 + 1024);
+	AQH_TRY(ctx->d_stlist.ensure(sizeof(int32_t) * want), "alloc tile lists");
+	ctx->st_list_cap = ctx->d_stlist.cap / sizeof(int32_t);
+	P.bb.st_list = ctx->d_stlist.as<int32_t>();
+	P.bb.list_capacity = ctx->st_list_cap;
+	// graph key: every kernel argument of the frame
+	std::vector<unsigned char> key(sizeof(RenderPlan) + sizeof(SamplerDev) + sizeof(void*) * 8);
+	unsigned char* k = key.data();
+	std::memcpy(k, &P, sizeof(RenderPlan));
+	k += sizeof(RenderPlan);
+	std::memcpy(k, &ctx->smp, sizeof(SamplerDev));
+	k += sizeof(SamplerDev);
+	void* ptrs[8] = {ctx->d_ftab.p, ctx->d_chan.p, ctx->d_q8.p, ctx->d_qchan.p, ctx->d_queue.p, ctx->d_dofb.p,
+	                 ctx->d_err.p, (void*)s};
+	std::memcpy(k, ptrs, sizeof ptrs);
+	if (!ctx->graph_valid || ctx->graph_key != key) {
+		if (ctx->graph_exec) {
+			cudaGraphExecDestroy(ctx->graph_exec);
+			ctx->graph_exec = nullptr;
+		}
+		cudaGraph_t graph = nullptr;
+		AQH_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+		aqh_status st = enqueue_frame(ctx, P, true, true);
+		cudaError_t e = cudaStreamEndCapture(s, &graph);
+		if (st != AQH_OK) {
+			if (graph) cudaGraphDestroy(graph);
+			return st;
+		}
+		AQH_TRY(e, "end capture");
+		e = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+		cudaGraphDestroy(graph);
+		AQH_TRY(e, "instantiate graph");
+		ctx->graph_key = key;
+		ctx->graph_valid = true;
+		ctx->graphs_built++;
+	}
+	AQH_TRY(cudaGraphLaunch(ctx->graph_exec, s), "launch graph");
+	ctx->pending_check = true;
+	ctx->pending_plan = P;
+	if (sync) return aqh_synchronize(ctx);
+	return AQH_OK;
+}
+
+aqh_status aqh_render(aqh_ctx* ctx, int sync) {
+	if (!ctx) return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	if (!ctx->samples_set) return ctx->fail(AQH_EINVAL, "aqh_set_samples was not called");
+	cudaSetDevice(ctx->device);
+	RenderPlan P;
+	aqh_status st = plan_render(ctx, P);
+	if (st != AQH_OK) return st;
+	ctx->stats.micropolygons = P.nmps;
+	ctx->stats.samples = (int64_t)P.nsamp;
+	ctx->stats.grids = P.g.ngrids;
+	if (ctx->mode == AQH_MODE_BATCHED) return render_batched(ctx, P, sync != 0);
+	return render_plain(ctx, P, sync != 0);
 }
 
 aqh_status aqh_synchronize(aqh_ctx* ctx) {
 	if (!ctx) return AQH_EINVAL;
 	cudaSetDevice(ctx->device);
 	AQH_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
+	if (ctx->pending_check) {
+		// batched frame: did binning or the fragment pool outgrow its capacity?
+		ctx->pending_check = false;
+		RenderPlan& P = ctx->pending_plan;
+		int32_t total = 0;
+		if (P.g.ngrids > 0)
+			AQH_TRY(cudaMemcpy(&total, P.bb.st_offset + (size_t)P.nst * P.bb.nranges, 4, cudaMemcpyDeviceToHost), "readback");
+		int32_t ovf = 0;
+		if (P.pool.capacity > 0) {
+			unsigned long long used = 0;
+			AQH_TRY(cudaMemcpy(&ovf, P.pool.overflow, 4, cudaMemcpyDeviceToHost), "readback");
+			AQH_TRY(cudaMemcpy(&used, P.pool.count, 8, cudaMemcpyDeviceToHost), "readback");
+			ctx->stats.fragments = (int64_t)used;
+		}
+		ctx->stats.tile_grid_pairs = total;
+		read_stage_times(ctx);
+		if (total > ctx->st_list_cap || ovf) {
+			// render this frame again on the plain path, which sizes both exactly
+			ctx->st_list_cap = std::max<int64_t>(ctx->st_list_cap, total + total / 8 + 1024);
+			ctx->graph_valid = false;
+			ctx->overflow_rerenders++;
+			return render_plain(ctx, P, true);
+		}
+	}
+	return AQH_OK;
+}
+
+aqh_status aqh_set_mode(aqh_ctx* ctx, int mode) {
+	if (!ctx || (mode != AQH_MODE_PLAIN && mode != AQH_MODE_BATCHED)) return AQH_EINVAL;
+	cudaSetDevice(ctx->device);
+	AQH_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
+	ctx->mode = mode;
 	return AQH_OK;
 }
 
@@ -943,6 +1153,7 @@ aqh_status aqh_read_quantized_u8(aqh_ctx* ctx, const int* channels, int nchan, u
 	AQH_TRY(ctx->d_qchan.ensure(64), "alloc");
 	AQH_TRY(ctx->d_q8.ensure(npix * nchan), "alloc");
 	AQH_TRY(cudaMemcpyAsync(ctx->d_qchan.p, channels, nchan * 4, cudaMemcpyHostToDevice, ctx->stream), "upload");
+	cudaGetLastError();
 	launch_quantize_u8(fp, ctx->smp, ctx->d_chan.as<float>(), ctx->d_qchan.as<int>(), nchan, ctx->d_q8.as<uint8_t>(),
 	                   ctx->stream);
 	AQH_TRY(cudaGetLastError(), "quantize launch");

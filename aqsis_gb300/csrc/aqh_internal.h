@@ -104,6 +104,7 @@ struct FragPool {
 
 struct BinBuffers {
 	int4* grid_rect;       // pixel rectangle [x0,x1) x [y0,y1) touched by each grid (empty: x0 >= x1)
+	float* grid_minz;      // smallest camera z over each grid's vertices (all keys)
 	int32_t* st_count;     // [nst][nranges]
 	int32_t* st_offset;    // exclusive scan of st_count, plus total at the end
 	int32_t* st_list;      // grid ids per super-tile, in grid order
@@ -112,16 +113,40 @@ struct BinBuffers {
 	int64_t list_capacity;
 };
 
+// Everything one render of a context needs: uploads done, buffers sized, kernel arguments filled.
+struct RenderPlan {
+	FrameParams fp;
+	GridsDev g;
+	BinBuffers bb;
+	SampleStore store;
+	FragPool pool;
+	bool mbdof;
+	int nst;
+	int nctas;     // persistent sampling CTAs (batched form)
+	size_t nsamp;
+	int64_t nmps;
+};
+
 // Kernel launchers (implemented in the .cu files).
-void launch_grid_rects(const FrameParams& fp, const GridsDev& g, int4* rect, cudaStream_t s);
+void launch_grid_rects(const FrameParams& fp, const GridsDev& g, int4* rect, float* minz, cudaStream_t s);
 void launch_st_count(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);
 void launch_scan_i32(const int32_t* in, int32_t* out, int n, int32_t* scratch, cudaStream_t s);
 void launch_st_write(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);
 void launch_sample_tiles(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
                          SampleStore st, FragPool pool, int32_t* err, cudaStream_t s);
+// Persistent form: `nctas` CTAs pull tiles from queue[0] (zeroed by the
+// caller), in `order` when given.
+void launch_sample_tiles_q(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
+                           SampleStore st, FragPool pool, int* queue, const int* order, int nctas, cudaStream_t s);
+int sample_static_ctas_per_sm(bool transp);
+void configure_sample_kernels();
+void configure_sample_mb_kernels();
+// `slice_times`: for every slice count d in 1..max(4, spp), the d accumulated
+// slice end times of CqMicroPolygonMotion::BuildBoundList, at offset d*(d-1)/2.
 void launch_sample_mb(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
-                      SampleStore st, FragPool pool, const float4* dof_bounds, cudaStream_t s);
-int mb_samples_per_thread();
+                      SampleStore st, FragPool pool, const float4* dof_bounds, const float* slice_times,
+                      cudaStream_t s);
+void slice_times_h(float open, float close, int spp, std::vector<float>& out);
 void static_tiling(FrameParams& fp);
 // Frame options resolved from an aqh_frame_desc (plus the host filter table).
 aqh_status resolve_frame(const aqh_frame_desc& d, FrameParams& fp, std::vector<float>& ftab, std::string& err);

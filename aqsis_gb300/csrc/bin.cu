@@ -17,7 +17,7 @@ namespace aqh {
 // by the largest circle of confusion in the grid's depth range when depth of
 // field is on, turned into the pixel rectangle [floor(min), ceil(max)] + 1
 // clipped to the sample region.
-__global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect) {
+__global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect, float* minz) {
 	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const int lane = threadIdx.x & 31;
 	if (warp >= g.ngrids) return;
@@ -42,6 +42,7 @@ __global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect) {
 		mxz = fmaxf(mxz, __shfl_xor_sync(0xffffffffu, mxz, o));
 	}
 	if (lane != 0) return;
+	minz[warp] = mnz;
 	if (fp.use_dof) {
 		float2 c1 = coc(mnz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
 		float2 c2 = coc(mxz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
@@ -105,7 +106,7 @@ __global__ void st_count_kernel(FrameParams fp, int ngrids, const int4* rect, in
 // Ordered compaction: write the range's touching grids at the super-tile's
 // offset, in grid order.
 __global__ void st_write_kernel(FrameParams fp, int ngrids, const int4* rect, int nranges, int range_size,
-                                const int32_t* offset, int32_t* list) {
+                                const int32_t* offset, int32_t* list, long long capacity) {
 	const int st = blockIdx.x, r = blockIdx.y;
 	int x0, x1, y0, y1;
 	st_rect(fp, st, x0, x1, y0, y1);
@@ -127,7 +128,8 @@ __global__ void st_write_kernel(FrameParams fp, int ngrids, const int4* rect, in
 			pre += (w < wid) ? t : 0;
 			tot += t;
 		}
-		if (f) list[base + pre + __popc(bal & ((1u << lane) - 1u))] = gi;
+		const long long idx = (long long)base + pre + __popc(bal & ((1u << lane) - 1u));
+		if (f && idx < capacity) list[idx] = gi;  // a short list is detected by the host and re-binned
 		__syncthreads();
 		if (threadIdx.x == 0) base += tot;
 		__syncthreads();
@@ -165,10 +167,10 @@ __global__ void scan_i32_kernel(const int32_t* in, int32_t* out, int n) {
 	if (threadIdx.x == 0) out[n] = carry;
 }
 
-void launch_grid_rects(const FrameParams& fp, const GridsDev& g, int4* rect, cudaStream_t s) {
+void launch_grid_rects(const FrameParams& fp, const GridsDev& g, int4* rect, float* minz, cudaStream_t s) {
 	if (g.ngrids == 0) return;
 	const int wpb = kBlock / 32;
-	grid_rects_kernel<<<(g.ngrids + wpb - 1) / wpb, kBlock, 0, s>>>(fp, g, rect);
+	grid_rects_kernel<<<(g.ngrids + wpb - 1) / wpb, kBlock, 0, s>>>(fp, g, rect, minz);
 }
 
 void launch_st_count(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s) {
@@ -183,7 +185,7 @@ void launch_scan_i32(const int32_t* in, int32_t* out, int n, int32_t*, cudaStrea
 void launch_st_write(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s) {
 	dim3 grid(fp.nstx * fp.nsty, b.nranges);
 	st_write_kernel<<<grid, kBlock, 0, s>>>(fp, g.ngrids, b.grid_rect, b.nranges, b.range_size, b.st_offset,
-	                                        b.st_list);
+	                                        b.st_list, (long long)b.list_capacity);
 }
 
 }  // namespace aqh

@@ -66,7 +66,8 @@ struct SmemS {
 	float warp_max[32];
 	int first_reject;
 	int qn;
-	float tile_ozmax;                     // largest occluding depth over the tile's samples
+	float pixmax[kTilePixMax];            // largest occluding depth over each pixel's samples
+	float blkmax[16];                     // ... over each 4x4-pixel block of the tile
 	float soz[kTileSampMax];              // occlZ per tile sample
 	int swin[kTileSampMax];               // occluding micropolygon per tile sample (-1 none)
 };
@@ -182,14 +183,31 @@ __device__ __forceinline__ void resolve_sample(const FrameParams& fp, const Grid
 	if (st.nfrag) st.nfrag[sidx] = nf;
 }
 
-template <bool TRANSP>
+// PERSIST: a fixed grid of CTAs pulls tiles from a device work queue
+// (`queue[0]` counts tiles handed out, `order` lists tiles costliest first);
+// otherwise one CTA per tile.
+template <bool TRANSP, bool PERSIST>
 __global__ void __launch_bounds__(kThreadsS, 2)
-sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, SampleStore st, FragPool pool) {
+sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, SampleStore st, FragPool pool,
+                     int* queue, const int* order) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	SmemS& sm = *reinterpret_cast<SmemS*>(smem_raw);
 	int32_t* fhead = reinterpret_cast<int32_t*>(smem_raw + sizeof(SmemS));  // TRANSP: fragment lists
-
-	const int tile = blockIdx.x;
+	__shared__ int next_tile;
+	const int ntiles = fp.ntx * fp.nty;
+	for (int job = 0;; ++job) {
+	int tile;
+	if (PERSIST) {
+		__syncthreads();
+		if (threadIdx.x == 0) next_tile = atomicAdd(queue, 1);
+		__syncthreads();
+		tile = next_tile;
+		if (tile >= ntiles) break;
+		if (order) tile = order[tile];
+	} else {
+		if (job > 0) break;
+		tile = blockIdx.x;
+	}
 	const int tx = tile % fp.ntx, ty = tile / fp.ntx;
 	const int tpx0 = fp.sx0 + tx * fp.tile_w, tpy0 = fp.sy0 + ty * fp.tile_h;
 	const int tpx1 = min(tpx0 + fp.tile_w, fp.sx0 + fp.sw), tpy1 = min(tpy0 + fp.tile_h, fp.sy0 + fp.sh);
@@ -207,15 +225,16 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		if (TRANSP) fhead[i] = -1;
 	}
 	for (int i = t; i < kTilePixMax * kWordsS; i += kThreadsS) (&sm.mask[0][0])[i] = 0u;
+	for (int i = t; i < kTilePixMax; i += kThreadsS) sm.pixmax[i] = FLT_MAX;
+	if (t < 16) sm.blkmax[t] = FLT_MAX;
 	if (t == 0) {
-		sm.tile_ozmax = FLT_MAX;
 		sm.qn = 0;
 		sm.qcum[0] = 0;
 	}
 	__syncthreads();
 
 	const int lbeg = bb.st_offset[st_idx * bb.nranges];
-	const int lend = bb.st_offset[(st_idx + 1) * bb.nranges];
+	const int lend = (int)min((long long)bb.st_offset[(st_idx + 1) * bb.nranges], (long long)bb.list_capacity);
 
 	// Stream cursor (uniform over the block): next list chunk, position in
 	// the micropolygon stream of the queued grids.
@@ -235,6 +254,16 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 					gid = bb.st_list[li];
 					const int4 rc = bb.grid_rect[gid];
 					f = rc.x < rc.y && rc.x < tpx1 && rc.y > tpx0 && rc.z < tpy1 && rc.w > tpy0;
+					if (f && cullable) {
+						// whole grid behind every sample of the 4x4-pixel blocks it overlaps
+						const int bx0 = (max(rc.x, tpx0) - tpx0) >> 2, bx1 = (min(rc.y, tpx1) - 1 - tpx0) >> 2;
+						const int by0 = (max(rc.z, tpy0) - tpy0) >> 2, by1 = (min(rc.w, tpy1) - 1 - tpy0) >> 2;
+						const int nbx = (fp.tile_w + 3) >> 2;
+						float mx = -FLT_MAX;
+						for (int by = by0; by <= by1; ++by)
+							for (int bx = bx0; bx <= bx1; ++bx) mx = fmaxf(mx, sm.blkmax[by * nbx + bx]);
+						if (__ldg(bb.grid_minz + gid) > mx) f = false;
+					}
 					if (f) nmp = __ldg(g.cu + gid) * __ldg(g.cv + gid);
 				}
 				int total;
@@ -286,11 +315,16 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 				// AddMPG crop cull (imagebuffer.cpp:533-539)
 				const bool cropped =
 				    bmaxx < fp.cull_x0 || bmaxy < fp.cull_y0 || bminx > fp.cull_x1 || bminy > fp.cull_y1;
-				// early-z for the whole tile: behind every sample's occluding depth
-				const bool hidden = cullable && bminz > sm.tile_ozmax;
 				const int sX = max((int)floorf(bminx), tpx0), eX = min(lceil_f(bmaxx), tpx1);
 				const int sY = max((int)floorf(bminy), tpy0), eY = min(lceil_f(bmaxy), tpy1);
-				active = !culled && !cropped && !hidden && sX < eX && sY < eY;
+				active = !culled && !cropped && sX < eX && sY < eY;
+				if (active && cullable) {
+					// early-z for every pixel it visits: behind all their samples' occluding depths
+					float mx = -FLT_MAX;
+					for (int yy = sY; yy < eY; ++yy)
+						for (int xx = sX; xx < eX; ++xx) mx = fmaxf(mx, sm.pixmax[(yy - tpy0) * fp.tile_w + (xx - tpx0)]);
+					if (bminz > mx) active = false;
+				}
 			}
 			int total;
 			const int rank = block_excl_scan(sm.warp_tot, active, total);
@@ -406,15 +440,25 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 			}
 			wmax = fmaxf(wmax, gmax);
 		}
-		// tile-wide largest occluding depth, then clear the masks
-		if (lane == 0) sm.warp_max[warp] = wmax;
+		(void)wmax;
+		// largest occluding depth per pixel and per 4x4 block, then clear the masks
 		__syncthreads();
-		if (t == 0) {
+		for (int pp = t; pp < tpix; pp += kThreadsS) {
 			float mx = -FLT_MAX;
-			for (int k = 0; k < kWarpsS; ++k) mx = fmaxf(mx, sm.warp_max[k]);
-			sm.tile_ozmax = mx;
+			for (int k = 0; k < spp; ++k) mx = fmaxf(mx, sm.soz[pp * spp + k]);
+			sm.pixmax[pp] = mx;
 		}
 		for (int i = t; i < kTilePixMax * kWordsS; i += kThreadsS) (&sm.mask[0][0])[i] = 0u;
+		__syncthreads();
+		if (t < 16) {
+			const int nbx = (fp.tile_w + 3) >> 2;
+			const int bx = t % nbx, by = t / nbx;
+			float mx = -FLT_MAX;
+			if (by * 4 < fp.tile_h)
+				for (int yy = by * 4; yy < min(by * 4 + 4, fp.tile_h); ++yy)
+					for (int xx = bx * 4; xx < min(bx * 4 + 4, fp.tile_w); ++xx) mx = fmaxf(mx, sm.pixmax[yy * fp.tile_w + xx]);
+			sm.blkmax[t] = mx;
+		}
 		__syncthreads();
 		npend = 0;
 		if (exhausted) break;
@@ -432,6 +476,7 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		resolve_sample<TRANSP>(fp, g, pool, st, pix * spp + si, (float)px + o.x, (float)py + o.y, sm.soz[s],
 		                       sm.swin[s], TRANSP ? fhead[s] : -1);
 	}
+	}  // tile loop
 }
 
 }  // namespace
@@ -448,19 +493,52 @@ void static_tiling(FrameParams& fp) {
 void launch_sample_tiles(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
                          SampleStore st, FragPool pool, int32_t* err, cudaStream_t s) {
 	(void)err;
+	launch_sample_tiles_q(fp, g, sm, b, st, pool, nullptr, nullptr, 0, s);
+}
+
+void launch_sample_tiles_q(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
+                           SampleStore st, FragPool pool, int* queue, const int* order, int nctas, cudaStream_t s) {
 	const int ntiles = fp.ntx * fp.nty;
 	const size_t smem_opaque = sizeof(SmemS);
 	const size_t smem_transp = smem_opaque + sizeof(int32_t) * kTileSampMax;
-	static bool configured = false;
-	if (!configured) {
-		cudaFuncSetAttribute(sample_static_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_opaque);
-		cudaFuncSetAttribute(sample_static_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_transp);
-		configured = true;
+	configure_sample_kernels();
+	const bool transp = pool.capacity > 0;
+	if (queue) {
+		if (transp)
+			sample_static_kernel<true, true><<<nctas, kThreadsS, smem_transp, s>>>(fp, g, sm, b, st, pool, queue, order);
+		else
+			sample_static_kernel<false, true><<<nctas, kThreadsS, smem_opaque, s>>>(fp, g, sm, b, st, pool, queue, order);
+	} else {
+		if (transp)
+			sample_static_kernel<true, false><<<ntiles, kThreadsS, smem_transp, s>>>(fp, g, sm, b, st, pool, nullptr, nullptr);
+		else
+			sample_static_kernel<false, false><<<ntiles, kThreadsS, smem_opaque, s>>>(fp, g, sm, b, st, pool, nullptr, nullptr);
 	}
-	if (pool.capacity > 0)
-		sample_static_kernel<true><<<ntiles, kThreadsS, smem_transp, s>>>(fp, g, sm, b, st, pool);
+}
+
+// Shared-memory limits of the sampling kernels; safe to call repeatedly, and
+// done before any graph capture (context creation calls it).
+void configure_sample_kernels() {
+	static bool configured = false;
+	if (configured) return;
+	const int smem_opaque = (int)sizeof(SmemS);
+	const int smem_transp = smem_opaque + (int)(sizeof(int32_t) * kTileSampMax);
+	cudaFuncSetAttribute(sample_static_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_opaque);
+	cudaFuncSetAttribute(sample_static_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_transp);
+	cudaFuncSetAttribute(sample_static_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_opaque);
+	cudaFuncSetAttribute(sample_static_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_transp);
+	configure_sample_mb_kernels();
+	configured = true;
+}
+
+int sample_static_ctas_per_sm(bool transp) {
+	const size_t smem = sizeof(SmemS) + (transp ? sizeof(int32_t) * kTileSampMax : 0);
+	int n = 0;
+	if (transp)
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sample_static_kernel<true, true>, kThreadsS, smem);
 	else
-		sample_static_kernel<false><<<ntiles, kThreadsS, smem_opaque, s>>>(fp, g, sm, b, st, pool);
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sample_static_kernel<false, true>, kThreadsS, smem);
+	return n > 0 ? n : 1;
 }
 
 }  // namespace aqh

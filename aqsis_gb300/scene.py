@@ -355,3 +355,39 @@ def scaled(scene_fn, scale: float, **kw) -> Scene:
         n = {"opaque_stream": 200_000, "transparent_stream": 16_200, "motion_dof_stream": 100_000}[scene_fn.__name__]
     n = max(1, int(round(n * scale * scale)))
     return scene_fn(width=w, height=h, ngrids=n, **kw)
+
+
+# ---------------------------------------------------------------------------
+# Served request stream
+
+SERVED_RESOLUTIONS = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
+
+
+def served_job(rng: np.random.Generator, seed: int, max_mps: float = 8e6) -> Scene:
+    """One request of the served mixed stream: resolution from the five sizes,
+    PixelSamples n n with n in {2, 4, 8}, micropolygons log-uniform in
+    [50k, 8M] (16x16-quad grids), 20% motion blur + depth of field (two keys,
+    displacement U[0,20] px), 30% transparency (Oi ~ U[0.1,0.9]^3, centre
+    window), the rest opaque; filters as the stream's base configurations."""
+    w, h = SERVED_RESOLUTIONS[int(rng.integers(0, len(SERVED_RESOLUTIONS)))]
+    n = int(rng.choice([2, 4, 8]))
+    mps = float(np.exp(rng.uniform(np.log(5e4), np.log(max_mps))))
+    ngrids = max(1, int(mps / 256))
+    kind = rng.choice(["mb", "transparent", "opaque"], p=[0.2, 0.3, 0.5])
+    sub = np.random.default_rng(seed)
+    if kind == "mb":
+        fr = Frame(width=w, height=h, xsamples=n, ysamples=n, filter="box", xfilter=1.0, yfilter=1.0,
+                   q_dither=0.0, shutter=(0.0, 1.0), fstop=2.8, focal_length=0.05, focal_distance=50.0,
+                   dof_scale=(h / 2.0, h / 2.0))
+        g = regular_grids(ngrids, w, h, sub, motion=20.0)
+    elif kind == "transparent":
+        fr = Frame(width=w, height=h, xsamples=n, ysamples=n, filter="catmull-rom", xfilter=3.0, yfilter=3.0,
+                   q_dither=0.0)
+        win = (w * 0.25, w * 0.75, h * 0.25, h * 0.75)
+        g = regular_grids(ngrids, w, h, sub, window=win, opacity=(0.1, 0.9))
+    else:
+        fr = Frame(width=w, height=h, xsamples=n, ysamples=n, q_dither=0.0)
+        g = regular_grids(ngrids, w, h, sub)
+    sc = Scene(fr, g, make_samples(fr, sub, 250))
+    sc.kind = str(kind)
+    return sc

@@ -112,11 +112,26 @@ def peaks() -> dict:
         return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+WORKLOADS = {
+    "opaque": ("opaque_stream", 0xC1, {"workload": "opaque_stream_1080p_16spp"}),
+    "transparent": ("transparent_stream", 0xC2,
+                    {"workload": "transparent_stream_1080p_64spp", "pixel_samples": [8, 8], "grids": 16200,
+                     "micropolygons": 4_147_200, "filter": "catmull-rom 3x3",
+                     "window": "960x540 centre, ~8 layers", "opacity": "U[0.1,0.9]^3"}),
+    "mbdof": ("motion_dof_stream", 0xC3,
+              {"workload": "motion_dof_stream_1080p_36spp", "pixel_samples": [6, 6], "grids": 100000,
+               "micropolygons": 25_600_000, "filter": "box 1x1", "shutter": [0, 1],
+               "dof": {"fstop": 2.8, "focal_length": 0.05, "focal_distance": 50}, "motion_px": 20}),
+}
+
+
 def make_scene(args):
     from aqsis_gb300 import scene as S
+    fn, seed, _ = WORKLOADS[args.workload]
+    fn = getattr(S, fn)
     if args.scale == 1.0:
-        return S.opaque_stream(seed=0xC1)
-    return S.scaled(S.opaque_stream, args.scale, seed=0xC1)
+        return fn(seed=seed)
+    return S.scaled(fn, args.scale, seed=seed)
 
 
 def cpu_baseline(args) -> dict:
@@ -125,7 +140,8 @@ def cpu_baseline(args) -> dict:
     from aqsis_gb300 import scene as S
     from oracle import oracle as O
     O.build()
-    sc = S.scaled(S.opaque_stream, args.cpu_scale, seed=0xC1)
+    fn, seed, _ = WORKLOADS[args.workload]
+    sc = S.scaled(getattr(S, fn), args.cpu_scale if args.workload == "opaque" else args.cpu_scale / 4, seed=seed)
     t0 = time.perf_counter()
     O.render(sc, want_samples=False)
     dt = time.perf_counter() - t0
@@ -214,41 +230,50 @@ def run_gpu(args):
          for k in ("cu", "cv", "nkeys", "flags", "pbase", "cbase", "tbase", "times", "P", "Ci", "Oi")}
     stream = torch.cuda.Stream(dev)  # the hider's work and the timing events share this stream
     h = aqh.Hider(local)
-    h.L.aqh_set_stream(h.ctx, stream.cuda_stream)
+    h.set_stream(stream.cuda_stream)
     h.frame_begin(fr)
     h.set_samples(smp)
     h.submit_grids_device(G, t["cu"].data_ptr(), t["cv"].data_ptr(), t["nkeys"].data_ptr(), t["flags"].data_ptr(),
                           t["pbase"].data_ptr(), t["cbase"].data_ptr(), t["tbase"].data_ptr(), t["times"].data_ptr(),
                           t["P"].data_ptr(), t["Ci"].data_ptr(), t["Oi"].data_ptr(), mps)
     qch = np.array([0, 1, 2, 6], np.int32)
-    for _ in range(args.warmup):
-        h.render(sync=True)
-    barrier()
-    torch.cuda.synchronize(dev)
+
+    def timed_frames(batched: bool, steps: int, warmup: int):
+        """Device time of `steps` frames (CUDA events on the hider's stream) and
+        per-frame latencies; plain = one launch per stage with host round trips."""
+        h.set_mode(batched)
+        for _ in range(warmup):
+            h.render(sync=True)
+        barrier()
+        torch.cuda.synchronize(dev)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        stage = {"bin": [], "sample": [], "filter": []}
+        ev[0].record(stream)
+        for i in range(steps):
+            h.render(sync=True)
+            ev[i + 1].record(stream)
+            st = h.stats()
+            stage["bin"].append(st["ms_bin"])
+            stage["sample"].append(st["ms_sample"])
+            stage["filter"].append(st["ms_filter"])
+        torch.cuda.synchronize(dev)
+        barrier()
+        lat = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+        return ev[0].elapsed_time(ev[steps]) / steps, lat, stage
+
+    plain_ms, plain_lat, _ = timed_frames(False, max(2, args.steps // 2), 1)
     clocks = ClockSampler(local)
     clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    sample_ms, bin_ms, filt_ms = [], [], []
-    e0.record(stream)
-    for _ in range(args.steps):
-        h.render(sync=True)
-        st = h.stats()
-        sample_ms.append(st["ms_sample"])
-        bin_ms.append(st["ms_bin"])
-        filt_ms.append(st["ms_filter"])
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    barrier()
+    ms, lat, stage = timed_frames(True, args.steps, args.warmup)
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1) / args.steps
+    sample_ms, bin_ms, filt_ms = stage["sample"], stage["bin"], stage["filter"]
     ms_t = torch.tensor([ms], device=dev)
     if dist is not None:
         dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
     ms_max = float(ms_t.item())
     value = mps * world / (ms_max / 1e3)
-    launches_per_step = 6  # grid rects, super-tile count, scan, super-tile write, sample, filter
-    st = h.stats()
-    img = h.read_quantized(qch)  # exercise the quantize path once on the resident frame
+    launches_per_step = 7  # grid rects, super-tile count, scan, super-tile write, sample, filter, quantize
+    img = h.read_quantized(qch)  # exercise the readback of the resident frame
     h.close()
     del t
     torch.cuda.empty_cache()
@@ -261,19 +286,21 @@ def run_gpu(args):
         pt = torch.from_numpy(a).pin_memory()
         pin[k] = pt
     h2 = aqh.Hider(local)
-    h2.L.aqh_set_stream(h2.ctx, stream.cuda_stream)
+    h2.set_stream(stream.cuda_stream)
+    h2.set_mode(True)
     h2.frame_begin(fr)
     h2.set_samples(smp)
     L = h2.L
     L.aqh_submit_grids_host.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 8 + [C.c_size_t, C.c_void_p,
                                                                                   C.c_size_t, C.c_void_p,
-                                                                                  C.c_void_p, C.c_size_t, C.c_int64]
+                                                                                  C.c_void_p, C.c_size_t, C.c_void_p,
+                                                                                  C.c_int64]
     L.aqh_submit_grids_host.restype = C.c_int
     rc = L.aqh_submit_grids_host(h2.ctx, G, pin["cu"].data_ptr(), pin["cv"].data_ptr(), pin["nkeys"].data_ptr(),
                                  pin["flags"].data_ptr(), pin["pbase"].data_ptr(), pin["cbase"].data_ptr(),
                                  pin["tbase"].data_ptr(), pin["times"].data_ptr(), int(g.times.size),
                                  pin["P"].data_ptr(), int(g.P.shape[0]), pin["Ci"].data_ptr(), pin["Oi"].data_ptr(),
-                                 int(g.Ci.shape[0]), mps)
+                                 int(g.Ci.shape[0]), None, mps)
     if rc != 0:
         raise RuntimeError("aqh_submit_grids_host: " + L.aqh_last_error(h2.ctx).decode())
     out = np.zeros((fr.height, fr.width, 4), np.uint8)
@@ -310,14 +337,19 @@ def run_gpu(args):
     achieved = alg_bytes / (ms_sample / 1e3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / pk["hbm_gbs"], "traffic": None,
-            "kernel": "sample_static_kernel", "algorithmic_bytes": alg_bytes,
+            "kernel": "sample_mb_kernel" if args.workload == "mbdof" else "sample_static_kernel", "algorithmic_bytes": alg_bytes,
             "kernel_ms": ms_sample, "peak_source": pk["source"]}
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(CONFIG, parallelism="replicas" if world > 1 else "single"),
+            "config": dict(CONFIG, **WORKLOADS[args.workload][2], parallelism="replicas" if world > 1 else "single"),
             "samples_per_s": fr.width * fr.height * fr.spp * world / (ms_max / 1e3),
             "stage_ms": {"bin": float(np.mean(bin_ms)), "sample": ms_sample, "filter": float(np.mean(filt_ms))},
+            "mode": "batched (persistent tile queue, one CUDA graph per frame)",
+            "frame_latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+            "plain": {"value": mps * world / (plain_ms / 1e3), "ms_per_step": plain_ms,
+                      "frame_latency_ms": {"p50": float(np.percentile(plain_lat, 50)),
+                                           "p99": float(np.percentile(plain_lat, 99))}},
             "roofline": roof, "clocks": clk, "gpu_launches": launches_per_step * args.steps,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": float(e2t.item())}}
@@ -326,6 +358,100 @@ def run_gpu(args):
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+    return 0
+
+
+def run_served(args):
+    """The served mixed request stream: `args.jobs` requests (drawn from
+    `args.distinct` generated scenes, cycled), Poisson arrivals with a mean gap
+    of `args.gap_ms`.  Plain = one frame at a time on one context in plain mode
+    (one launch per stage); served = the batched server (continuous admission
+    onto resident slots, persistent kernels, CUDA graphs).  Reports p50/p99
+    latency (arrival -> image on the host) under the Poisson schedule and
+    frames/s with every request queued at once (saturated)."""
+    import torch
+    from aqsis_gb300 import aqh, scene as S
+    aqh.load(build_if_missing=True)
+    rng = np.random.default_rng(0xC4)
+    t0 = time.perf_counter()
+    scenes = [S.served_job(rng, 1000 + i, max_mps=args.max_mps) for i in range(args.distinct)]
+    gen_s = time.perf_counter() - t0
+    # page-locked copies of every input array (the requests' host buffers)
+    for sc in scenes:
+        g = sc.grids
+        for k in ("P", "Ci", "Oi"):
+            setattr(g, k, torch.from_numpy(getattr(g, k)).pin_memory().numpy())
+    order = [i % args.distinct for i in range(args.jobs)]
+    gaps = rng.exponential(args.gap_ms / 1e3, args.jobs)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    mps_total = sum(scenes[i].grids.micropolygons for i in order)
+
+    # warm both paths on every distinct scene (context buffers, graphs, JIT)
+    h = aqh.Hider(0)
+    h.set_mode(False)
+    sv = aqh.Server(0, slots=args.slots, batched=True)
+    for sc in scenes:
+        h.render_scene(sc, samples=False)
+        jid = sv.submit(sc)
+        sv.wait(jid)
+        sv.release(jid)
+
+    def plain_run(poisson: bool):
+        lat, t_free = [], 0.0
+        start = time.perf_counter()
+        for k, i in enumerate(order):
+            arr = arrivals[k] if poisson else 0.0
+            now = time.perf_counter() - start
+            if poisson and now < arr:
+                time.sleep(arr - now)
+            h.render_scene(scenes[i], samples=False)
+            lat.append(time.perf_counter() - start - arr)
+        return time.perf_counter() - start, lat
+
+    def served_run(poisson: bool):
+        ids = []
+        start = time.perf_counter()
+        for k, i in enumerate(order):
+            if poisson:
+                now = time.perf_counter() - start
+                if now < arrivals[k]:
+                    time.sleep(arrivals[k] - now)
+            ids.append((sv.submit(scenes[i]), arrivals[k] if poisson else 0.0))
+        lat = []
+        for jid, arr in ids:
+            rc, info = sv.wait(jid)
+            if rc != 0:
+                raise RuntimeError("served job failed: " + sv.error(jid))
+            lat.append(time.perf_counter() - start - arr)  # upper bound: waits are in submit order
+            sv.release(jid)
+        return time.perf_counter() - start, lat
+
+    plain_sat, _ = plain_run(False)
+    served_sat, _ = served_run(False)
+    plain_p, plain_lat = plain_run(True)
+    served_p, served_lat = served_run(True)
+    st = sv.stats()
+    sv.close()
+    h.close()
+    kinds = {k: sum(1 for i in order if scenes[i].kind == k) for k in ("opaque", "transparent", "mb")}
+    line = {"metric": "frames/s", "value": args.jobs / served_sat, "unit": "frames/s", "n_gpus": 1,
+            "steps": args.jobs, "warmup": args.distinct, "ms_per_step": 1e3 * served_sat / args.jobs,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "workload": "served_mixed_stream",
+            "config": {"workload": "served_mixed_stream", "jobs": args.jobs, "distinct_scenes": args.distinct,
+                       "mean_gap_ms": args.gap_ms, "slots": args.slots, "kinds": kinds,
+                       "max_micropolygons": args.max_mps, "generation_s": gen_s},
+            "served": {"frames_per_s_saturated": args.jobs / served_sat,
+                       "micropolygons_per_s_saturated": mps_total / served_sat,
+                       "latency_ms_poisson": {"p50": 1e3 * float(np.percentile(served_lat, 50)),
+                                              "p99": 1e3 * float(np.percentile(served_lat, 99))},
+                       "peak_jobs_in_flight": st["peak_running"], "peak_hbm_bytes": st["peak_in_use"]},
+            "plain": {"frames_per_s_saturated": args.jobs / plain_sat,
+                      "micropolygons_per_s_saturated": mps_total / plain_sat,
+                      "latency_ms_poisson": {"p50": 1e3 * float(np.percentile(plain_lat, 50)),
+                                             "p99": 1e3 * float(np.percentile(plain_lat, 99))}},
+            "speedup_saturated": plain_sat / served_sat}
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -338,7 +464,15 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="scale the workload (1.0 = the full configuration)")
     ap.add_argument("--cpu-scale", type=float, default=0.4)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="opaque", choices=["opaque", "transparent", "mbdof", "served"])
+    ap.add_argument("--jobs", type=int, default=256)
+    ap.add_argument("--distinct", type=int, default=32)
+    ap.add_argument("--gap-ms", type=float, default=20.0)
+    ap.add_argument("--slots", type=int, default=6)
+    ap.add_argument("--max-mps", type=float, default=8e6)
     args = ap.parse_args()
+    if args.workload == "served":
+        sys.exit(run_served(args))
     if args.warmup < 3 and args.impl == "gb300" and args.scale == 1.0:
         args.warmup = 3
     if args.impl == "reference":

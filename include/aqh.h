@@ -180,7 +180,7 @@ aqh_status aqh_submit_grids_device(aqh_ctx* ctx, int ngrids,
                                    const int32_t* d_flags, const int64_t* d_pbase, const int64_t* d_cbase,
                                    const int32_t* d_tbase, const float* d_times,
                                    const float* d_P, const float* d_Ci, const float* d_Oi,
-                                   int64_t total_micropolygons);
+                                   const uint8_t* d_culled, int64_t total_micropolygons);
 /* Append many grids from packed HOST arrays (same layout as
  * aqh_submit_grids_device).  Nothing is copied until aqh_render, which
  * uploads them in one transfer per array; the arrays must stay valid until
@@ -190,7 +190,7 @@ aqh_status aqh_submit_grids_host(aqh_ctx* ctx, int ngrids,
                                  const int32_t* flags, const int64_t* pbase, const int64_t* cbase,
                                  const int32_t* tbase, const float* times, size_t ntimes,
                                  const float* P, size_t nP, const float* Ci, const float* Oi, size_t nC,
-                                 int64_t total_micropolygons);
+                                 const uint8_t* culled, int64_t total_micropolygons);
 /* Page-locked host memory for grid arrays. */
 void* aqh_host_alloc(size_t bytes);
 void aqh_host_free(void* p);
@@ -202,6 +202,16 @@ aqh_status aqh_set_stream(aqh_ctx* ctx, void* stream);
  * (bucketprocessor.cpp:95-359) done on the device.  Asynchronous on the
  * context's stream unless `sync` is nonzero. */
 aqh_status aqh_render(aqh_ctx* ctx, int sync);
+/* Execution form of aqh_render.  PLAIN: one launch per stage, the host reads
+ * binning's list size and the fragment count back between stages.  BATCHED:
+ * a persistent sampling kernel pulls tiles from a device work queue, nothing
+ * synchronizes with the host inside a frame, and the frame's whole
+ * bin -> sample -> filter -> quantize sequence is one CUDA graph, captured on
+ * the first render and replayed while the frame's arguments are unchanged;
+ * capacities come from the previous frame and an overflow found at
+ * aqh_synchronize re-renders that frame on the plain path.  Same pixels. */
+enum { AQH_MODE_PLAIN = 0, AQH_MODE_BATCHED = 1 };
+aqh_status aqh_set_mode(aqh_ctx* ctx, int mode);
 aqh_status aqh_synchronize(aqh_ctx* ctx);
 
 /* ---- results ------------------------------------------------------------- */
@@ -237,6 +247,69 @@ typedef struct {
 	float ms_bin, ms_sample, ms_filter, ms_total;  /* device time per stage of the last render */
 } aqh_frame_stats;
 aqh_status aqh_get_stats(aqh_ctx* ctx, aqh_frame_stats* st);
+
+/* ---- serving --------------------------------------------------------------- */
+/* No counterpart in the reference, which renders one frame per process.  A
+ * server keeps `slots` contexts resident on one GPU, each with its own
+ * stream and device buffers reused from job to job; jobs are admitted in
+ * arrival order when a slot is free and their estimated HBM footprint fits
+ * in the budget the running jobs leave, and jobs on different slots run
+ * concurrently on the device.  A job that can never fit is rejected at
+ * submission (AQH_EREJECTED). */
+typedef struct aqh_server aqh_server;
+typedef struct {
+	int device;
+	size_t hbm_budget;   /* bytes the admitted jobs may hold together; 0 = 80% of free memory */
+	int slots;           /* jobs in flight at once (1..64) */
+	int mode;            /* AQH_MODE_BATCHED or AQH_MODE_PLAIN for every slot */
+} aqh_server_opts;
+/* One render request.  Every pointer is host memory that must stay valid
+ * until the job completes; grids use the aqh_submit_grids_host layout. */
+typedef struct {
+	aqh_frame_desc frame;
+	aqh_samples samples;
+	int ngrids;
+	const int32_t *cu, *cv, *nkeys, *flags;
+	const int64_t *pbase, *cbase;
+	const int32_t* tbase;
+	const float* times;
+	size_t ntimes;
+	const float* P;
+	size_t nP;
+	const float *Ci, *Oi;
+	size_t nC;
+	const uint8_t* culled;   /* one byte per micropolygon, nonzero = culled; may be NULL */
+	int64_t micropolygons;
+	uint8_t* rgba;       /* out: crop window x 4 bytes (r, g, b, a quantized), or NULL */
+	float* channels;     /* out: crop window x AQH_NCHANNELS floats, or NULL */
+} aqh_job;
+typedef struct {
+	int64_t id;
+	int status;          /* aqh_status of the job once done */
+	int state;           /* 0 pending, 1 running, 2 done, 3 failed, 4 cancelled */
+	double t_submit, t_admit, t_done;  /* seconds on the server's clock */
+	size_t footprint;    /* estimated HBM bytes while running */
+	float ms_device;     /* device time of the frame */
+	int slot;
+} aqh_job_info;
+typedef struct {
+	size_t budget, in_use, peak_in_use;
+	int64_t pending, completed;
+	int running, peak_running;
+} aqh_server_info;
+aqh_status aqh_server_create(const aqh_server_opts* opts, aqh_server** out);
+void aqh_server_destroy(aqh_server* s);
+aqh_status aqh_server_submit(aqh_server* s, const aqh_job* job, int64_t* id);
+/* AQH_ENOTREADY while pending or running; the job's status once finished. */
+aqh_status aqh_server_poll(aqh_server* s, int64_t id, aqh_job_info* info);
+/* Waits up to timeout_ms; AQH_ETIMEDOUT if the job has not finished. */
+aqh_status aqh_server_wait(aqh_server* s, int64_t id, int timeout_ms, aqh_job_info* info);
+/* Removes a job that has not been admitted yet (AQH_ENOTREADY if it has). */
+aqh_status aqh_server_cancel(aqh_server* s, int64_t id);
+const char* aqh_server_job_error(aqh_server* s, int64_t id);
+aqh_status aqh_server_stats(aqh_server* s, aqh_server_info* info);
+/* Estimated HBM footprint of a job (host arithmetic, no GPU needed); 0 if invalid. */
+size_t aqh_job_footprint(const aqh_job* job);
 
 /* ---- weight table and test hooks ----------------------------------------- */
 /* Host-side filter weight table [(2*sy+1)*(2*sx+1)][spp] evaluated at sub-pixel

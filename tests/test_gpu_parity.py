@@ -155,3 +155,25 @@ def test_dof_only(hider, oracle):
 def test_motion_blur_transparent(hider, oracle):
     res, ref = run_both(hider, oracle, SS.motion_dof_small(seed=84, dof=False, xs=3, ys=3, transparent=True))
     compare(res, ref)
+
+
+@pytest.mark.parametrize("scene_fn", [lambda: SS.opaque_small(seed=101), lambda: SS.transparent_small(seed=102),
+                                      lambda: SS.edge_cases(seed=103), lambda: SS.motion_dof_small(seed=104)],
+                         ids=["opaque", "transparent", "edge", "mbdof"])
+def test_batched_mode_matches_oracle_and_replays(hider, oracle, scene_fn):
+    """AQH_MODE_BATCHED (persistent tile queue, CUDA graph) gives the oracle's
+    pixels, and replaying the captured graph gives the same bits again."""
+    sc = scene_fn()
+    ref = oracle.render(sc)
+    hider.set_mode(True)
+    try:
+        res = hider.render_scene(sc)
+        compare(res, ref)
+        again = []
+        for _ in range(2):
+            hider.render(sync=True)
+            again.append(hider.read_channels())
+        for a in again:
+            assert np.array_equal(a.view(np.uint32), res["channels"].view(np.uint32))
+    finally:
+        hider.set_mode(False)
