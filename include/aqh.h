@@ -311,6 +311,36 @@ aqh_status aqh_server_stats(aqh_server* s, aqh_server_info* info);
 /* Estimated HBM footprint of a job (host arithmetic, no GPU needed); 0 if invalid. */
 size_t aqh_job_footprint(const aqh_job* job);
 
+/* ---- rendering without allocation ---------------------------------------- */
+/* No counterpart in the reference (aqsis renders into memory it allocates
+ * per bucket).  For callers that cannot allocate device memory: a host whose
+ * device memory belongs to another allocator, a plugin running inside
+ * someone else's CUDA context, or code that must not grow the process's
+ * footprint.  Renders one small, static, opaque frame with no cudaMalloc,
+ * cudaFree or other allocation: the caller passes the grids (table on the
+ * host, P/Ci/Oi in device memory) and a device output of
+ * (crop width x crop height x AQH_NCHANNELS) floats; all intermediate data
+ * lives in fixed device arrays of about 19 MB that every GPU loading this
+ * library holds until the process exits.  Limits: AQH_NOALLOC_MAX_GRIDS
+ * grids, AQH_NOALLOC_MAX_REGION_PIXELS pixels and AQH_NOALLOC_MAX_SAMPLES
+ * samples in the sample region (at most 16 super-tiles of 128x128 pixels),
+ * AQH_NOALLOC_MAX_PATTERN_SAMPLES pattern entries; no motion blur, no depth of field, every grid AQH_GRID_OPAQUE;
+ * larger inputs return AQH_ELIMIT with a message in `err`.
+ * The first call on a device looks up the arrays' device addresses with that
+ * device current, so make it before any stream capture.  Calls share the
+ * arrays: calls whose work overlaps on the GPU (other streams, other threads)
+ * race.  `pos`/`pos_index` follow aqh_samples (host arrays); the work is
+ * queued on `stream` (a cudaStream_t, NULL = default stream). */
+#define AQH_NOALLOC_MAX_GRIDS 65536
+#define AQH_NOALLOC_MAX_REGION_PIXELS 36864
+#define AQH_NOALLOC_MAX_SAMPLES 300000
+#define AQH_NOALLOC_MAX_PATTERN_SAMPLES 65536
+aqh_status aqh_render_noalloc(const aqh_frame_desc* desc, const float* pos, int npatterns,
+                              const uint32_t* pos_index, int ngrids, const int32_t* cu, const int32_t* cv,
+                              const int32_t* flags, const int64_t* pbase, const int64_t* cbase,
+                              const float* d_P, const float* d_Ci, const float* d_Oi,
+                              float* d_channels, void* stream, char* err, size_t err_len);
+
 /* ---- weight table and test hooks ----------------------------------------- */
 /* Host-side filter weight table [(2*sy+1)*(2*sx+1)][spp] evaluated at sub-pixel
  * centres (CqBucketProcessor::InitialiseFilterValues, bucketprocessor.cpp:811-856).
