@@ -391,3 +391,56 @@ def served_job(rng: np.random.Generator, seed: int, max_mps: float = 8e6) -> Sce
     sc = Scene(fr, g, make_samples(fr, sub, 250))
     sc.kind = str(kind)
     return sc
+
+
+# ---------------------------------------------------------------------------
+# Scene files
+
+_GRID_KEYS = ("cu", "cv", "nkeys", "flags", "pbase", "cbase", "tbase", "times", "P", "Ci", "Oi", "culled")
+_SAMPLE_KEYS = ("pos", "time", "dof", "shuffle", "lod", "pos_index", "dof_index", "time_index",
+                "shuffle_index", "lod_index", "dither")
+
+
+def scene_arrays(scene: Scene) -> dict:
+    """Flatten a Scene into named arrays (frame options as a JSON string)."""
+    import json
+    out = {"frame": np.array(json.dumps(dataclasses.asdict(scene.frame)))}
+    for k in _GRID_KEYS:
+        a = getattr(scene.grids, k)
+        if a is not None:
+            out["g_" + k] = np.asarray(a)
+    out["s_npatterns"] = np.array(scene.samples.npatterns, np.int64)
+    for k in _SAMPLE_KEYS:
+        a = getattr(scene.samples, k)
+        if a is not None:
+            out["s_" + k] = np.asarray(a)
+    return out
+
+
+def scene_from_arrays(d) -> Scene:
+    """Inverse of scene_arrays (accepts an NpzFile or a dict)."""
+    import json
+    fd = json.loads(str(d["frame"]))
+    for k in ("crop", "bucket", "shutter", "dof_scale", "zthreshold"):
+        if fd.get(k) is not None:
+            fd[k] = tuple(fd[k])
+    fr = Frame(**fd)
+    keys = set(d.keys()) if hasattr(d, "keys") else set(d.files)
+    g = Grids(**{k: (np.array(d["g_" + k]) if ("g_" + k) in keys else None) for k in _GRID_KEYS})
+    s = Samples(npatterns=int(d["s_npatterns"]),
+                **{k: (np.array(d["s_" + k]) if ("s_" + k) in keys else None) for k in _SAMPLE_KEYS})
+    return Scene(fr, g, s)
+
+
+def save_scene(path: str, scene: Scene, **extra) -> None:
+    """Write a Scene (plus any extra named arrays) to a compressed .npz file."""
+    np.savez_compressed(path, **scene_arrays(scene), **extra)
+
+
+def load_scene(path: str):
+    """Read a Scene written by save_scene; returns (scene, extra arrays)."""
+    with np.load(path, allow_pickle=False) as d:
+        sc = scene_from_arrays(d)
+        extra = {k: np.array(d[k]) for k in d.files if k == "frame" or not (k.startswith("g_") or k.startswith("s_"))}
+    extra.pop("frame", None)
+    return sc, extra

@@ -1195,6 +1195,9 @@ unsigned randomInt(unsigned range) {
 extern "C" void orc_mt_seed(uint32_t s) { init_genrand(s); }
 extern "C" uint32_t orc_mt_int32(void) { return genrand_int32(); }
 extern "C" float orc_mt_float(void) { return randomFloat(); }
+extern "C" long orc_lfloor(float x) { return lfloor(x); }
+extern "C" long orc_lceil(float x) { return lceil(x); }
+extern "C" long orc_lround(double x) { return lroundd(x); }
 
 // multijitter.cpp:83-202, multijitter.h:89-101 (the pattern cache; Reseed(19) is
 // left to the caller).

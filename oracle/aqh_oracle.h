@@ -128,6 +128,12 @@ float orc_mt_float(void);
  * pos: [250*spp*2], t1d: [250*spp], shuffle: [250*spp]. Consumes the global MT. */
 void orc_multijitter_tables(int xs, int ys, float* pos, float* t1d, int32_t* shuffle);
 
+/* The rounding helpers of libs/math/math.h:46-70 as the oracle uses them
+ * (lfloor/lceil of a float, lround of a double). */
+long orc_lfloor(float x);
+long orc_lceil(float x);
+long orc_lround(double x);
+
 #ifdef __cplusplus
 }
 #endif

@@ -89,6 +89,12 @@ def lib():
         L.orc_mt_int32.restype = C.c_uint32
         L.orc_mt_float.restype = C.c_float
         L.orc_multijitter_tables.argtypes = [C.c_int, C.c_int, _f32p, _f32p, _i32p]
+        L.orc_lfloor.argtypes = [C.c_float]
+        L.orc_lfloor.restype = C.c_long
+        L.orc_lceil.argtypes = [C.c_float]
+        L.orc_lceil.restype = C.c_long
+        L.orc_lround.argtypes = [C.c_double]
+        L.orc_lround.restype = C.c_long
         _lib = L
     return _lib
 
