@@ -255,10 +255,6 @@ aqh_status resolve_frame(const aqh_frame_desc& dd, FrameParams& fp, std::vector<
 		err = "bad filter width";
 		return AQH_EINVAL;
 	}
-	if (d->display_z && d->depth_filter == AQH_DEPTH_MIDPOINT) {
-		err = "midpoint depth filter with a z display is not supported";
-		return AQH_EINVAL;
-	}
 	std::memset(&fp, 0, sizeof fp);
 	int cx0 = d->crop_xmin, cx1 = d->crop_xmax, cy0 = d->crop_ymin, cy1 = d->crop_ymax;
 	if (cx0 == 0 && cx1 == 0 && cy0 == 0 && cy1 == 0) { cx1 = d->width; cy1 = d->height; }
@@ -289,7 +285,7 @@ aqh_status resolve_frame(const aqh_frame_desc& dd, FrameParams& fp, std::vector<
 	fp.shutter_close = d->shutter_close;
 	fp.depth_filter = d->depth_filter;
 	fp.cullable = !(d->display_z && (d->depth_filter == AQH_DEPTH_MAX || d->depth_filter == AQH_DEPTH_AVERAGE));
-	fp.midpoint_store = 0;
+	fp.midpoint_store = (d->display_z && d->depth_filter == AQH_DEPTH_MIDPOINT) ? 1 : 0;
 	for (int k = 0; k < 3; ++k) fp.zthr[k] = d->zthreshold[k];
 	fp.gain = d->gain; fp.gamma = d->gamma;
 	fp.q_one = d->q_one; fp.q_min = d->q_min; fp.q_max = d->q_max; fp.q_dither = d->q_dither;
@@ -343,8 +339,8 @@ struct aqh_ctx {
 	// device buffers
 	DevBuf d_cu, d_cv, d_nkeys, d_flags, d_tbase, d_pbase, d_cbase, d_mpbase, d_times, d_culled, d_P, d_Ci, d_Oi;
 	DevBuf d_mpcount;
-	DevBuf d_rect, d_minz, d_stcount, d_stoffset, d_stlist;
-	DevBuf d_sa, d_sb, d_win, d_oz, d_nf;
+	DevBuf d_rect, d_minz, d_strips, d_stcount, d_stoffset, d_stlist;
+	DevBuf d_sa, d_sb, d_win, d_oz, d_nf, d_hz;
 	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err;
 	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb;
 	bool dev_motion = false;
@@ -834,6 +830,8 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	AQH_TRY(ctx->d_stoffset.ensure(sizeof(int32_t) * ((size_t)P.nst * bb.nranges + 1)), "alloc bins");
 	bb.grid_rect = ctx->d_rect.as<int4>();
 	bb.grid_minz = ctx->d_minz.as<float>();
+	AQH_TRY(ctx->d_strips.ensure(sizeof(uint32_t) * 64 * std::max(G, 1)), "alloc strips");
+	bb.strips = ctx->d_strips.as<uint32_t>();
 	bb.st_count = ctx->d_stcount.as<int32_t>();
 	bb.st_offset = ctx->d_stoffset.as<int32_t>();
 	AQH_TRY(ctx->d_sa.ensure(P.nsamp * sizeof(float4)), "alloc sample store");
@@ -850,6 +848,10 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 		store.occlz = ctx->d_oz.as<float>();
 		store.nfrag = ctx->d_nf.as<int32_t>();
 	}
+	if (fp.midpoint_store) {
+		AQH_TRY(ctx->d_hz.ensure(P.nsamp * 4), "alloc");
+		store.hitz = ctx->d_hz.as<float>();
+	}
 	AQH_TRY(ctx->d_ftab.ensure(ctx->ftab.size() * 4), "alloc");
 	AQH_TRY(cudaMemcpyAsync(ctx->d_ftab.p, ctx->ftab.data(), ctx->ftab.size() * 4, cudaMemcpyHostToDevice, s), "ftab");
 	const size_t ndisp = (size_t)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
@@ -860,7 +862,7 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	AQH_TRY(ctx->d_queue.ensure(64), "alloc");
 	FragPool& pool = P.pool;
 	pool = FragPool{};
-	if (ctx->any_transparent || !fp.cullable) {
+	if (ctx->any_transparent || !fp.cullable || fp.midpoint_store) {
 		if (ctx->frag_capacity == 0) ctx->frag_capacity = std::max<int64_t>(1 << 20, (int64_t)P.nsamp * 2);
 		AQH_TRY(ctx->d_frag.ensure(ctx->frag_capacity * sizeof(float4)), "alloc fragments");
 		AQH_TRY(ctx->d_next.ensure(ctx->frag_capacity * sizeof(int32_t)), "alloc fragments");
@@ -896,7 +898,7 @@ static aqh_status enqueue_frame(aqh_ctx* ctx, RenderPlan& P, bool batched, bool 
 	};
 	if (timing) mark(ctx->ev[0]);
 	if (P.g.ngrids > 0) {
-		launch_grid_rects(fp, P.g, P.bb.grid_rect, P.bb.grid_minz, s);
+		launch_grid_rects(fp, P.g, P.bb, s);
 		launch_st_count(fp, P.g, P.bb, s);
 		launch_scan_i32(P.bb.st_count, P.bb.st_offset, P.nst * P.bb.nranges, nullptr, s);
 		launch_st_write(fp, P.g, P.bb, s);
@@ -949,7 +951,7 @@ static aqh_status render_plain(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 	cudaEventRecord(ctx->ev[0], s);
 	int32_t total = 0;
 	if (P.g.ngrids > 0) {
-		launch_grid_rects(fp, P.g, P.bb.grid_rect, P.bb.grid_minz, s);
+		launch_grid_rects(fp, P.g, P.bb, s);
 		launch_st_count(fp, P.g, P.bb, s);
 		launch_scan_i32(P.bb.st_count, P.bb.st_offset, P.nst * P.bb.nranges, nullptr, s);
 		AQH_TRY(cudaMemcpyAsync(&total, P.bb.st_offset + (size_t)P.nst * P.bb.nranges, 4, cudaMemcpyDeviceToHost, s),
@@ -1179,12 +1181,15 @@ aqh_status aqh_read_samples(aqh_ctx* ctx, int32_t* winner, float* occlz, int32_t
 		AQH_TRY(cudaMemcpyAsync(a.data(), ctx->d_sa.p, n * 16, cudaMemcpyDeviceToHost, s), "read");
 		AQH_TRY(cudaMemcpyAsync(b.data(), ctx->d_sb.p, n * 16, cudaMemcpyDeviceToHost, s), "read");
 		AQH_TRY(cudaStreamSynchronize(s), "read");
+		// the device store is sample-major: [sample index][sample-region pixel]
+		const size_t spp = (size_t)fp.spp, npix = n / spp;
 		for (size_t i = 0; i < n; ++i) {
-			if (valid) valid[i] = b[i].w != 0.0f ? 1 : 0;
+			const size_t j = (i % spp) * npix + i / spp;
+			if (valid) valid[i] = b[j].w != 0.0f ? 1 : 0;
 			if (sdata) {
 				float* d = sdata + 7 * i;
-				d[0] = a[i].x; d[1] = a[i].y; d[2] = a[i].z;
-				d[3] = b[i].x; d[4] = b[i].y; d[5] = b[i].z; d[6] = a[i].w;
+				d[0] = a[j].x; d[1] = a[j].y; d[2] = a[j].z;
+				d[3] = b[j].x; d[4] = b[j].y; d[5] = b[j].z; d[6] = a[j].w;
 			}
 		}
 	}

@@ -85,12 +85,17 @@ struct SamplerDev {
 };
 
 // Per-sample resolved store (after Combine): R G B depth / OR OG OB flags.
+// Sample-major: a and b hold [sample index][sample-region pixel], so the
+// filter's loads of one sample index over neighbouring pixels coalesce; the
+// debug arrays are pixel-major ([pixel][sample index]).
 struct SampleStore {
 	float4* a;        // r, g, b, depth
 	float4* b;        // or, og, ob, valid (1.0f / 0.0f)
 	int32_t* winner;  // debug: occluding hit id before Combine (or null)
 	float* occlz;     // debug: occlZ (or null)
 	int32_t* nfrag;   // debug: transparent fragment count (or null)
+	float* hitz;      // depth of the occluding hit when occlZ tracks the second-nearest
+	                  // depth (midpoint depth filter with a z display), else null
 };
 
 // Transparent fragment pool: {depth, micropolygon id bits, u, v} + next link.
@@ -108,6 +113,9 @@ struct BinBuffers {
 	int32_t* st_count;     // [nst][nranges]
 	int32_t* st_offset;    // exclusive scan of st_count, plus total at the end
 	int32_t* st_list;      // grid ids per super-tile, in grid order
+	uint32_t* strips;      // per grid 64 words, or null: [0, 32) the pixel range [lo, hi) of each
+	                       // micropolygon column, [32, 63) of each row (lo | hi << 16, int16 each);
+	                       // word 63 = 1 when present (one motion key, cu and cv at most 31)
 	int nranges;
 	int range_size;
 	int64_t list_capacity;
@@ -128,7 +136,7 @@ struct RenderPlan {
 };
 
 // Kernel launchers (implemented in the .cu files).
-void launch_grid_rects(const FrameParams& fp, const GridsDev& g, int4* rect, float* minz, cudaStream_t s);
+void launch_grid_rects(const FrameParams& fp, const GridsDev& g, const BinBuffers& b, cudaStream_t s);
 void launch_st_count(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);
 void launch_scan_i32(const int32_t* in, int32_t* out, int n, int32_t* scratch, cudaStream_t s);
 void launch_st_write(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);

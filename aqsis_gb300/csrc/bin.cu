@@ -17,7 +17,54 @@ namespace aqh {
 // by the largest circle of confusion in the grid's depth range when depth of
 // field is on, turned into the pixel rectangle [floor(min), ceil(max)] + 1
 // clipped to the sample region.
-__global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect, float* minz) {
+// Pixel range [floor(mn), lceil(mx)) packed as two int16, widened to the
+// whole int16 range where the floats are out of range or NaN.
+__device__ __forceinline__ uint32_t pack_range(float mn, float mx, bool bad) {
+	int lo = -32768, hi = 32767;
+	if (!bad) {
+		if (mn > -32768.0f) lo = (int)floorf(mn);
+		if (mx < 32767.0f) hi = lceil_f(mx);
+	}
+	return (uint32_t)(lo & 0xffff) | ((uint32_t)hi << 16);
+}
+
+// Strips: the pixel ranges each micropolygon column and row of a static grid
+// can touch (x over vertex columns iu, iu+1; y over vertex rows iv, iv+1), so
+// the sampler streams only the micropolygons whose column and row both meet
+// its tile -- a superset of those whose bound does.  Lane = vertex column.
+__device__ __forceinline__ void grid_strips(const float4* P, int cu, int cv, int lane, uint32_t* S) {
+	const bool on = lane <= cu;
+	float cmn = FLT_MAX, cmx = -FLT_MAX, pmn = FLT_MAX, pmx = -FLT_MAX;
+	bool cbad = false, pbad = false;
+	for (int j = 0; j <= cv; ++j) {
+		float x = 0.0f, y = 0.0f;
+		if (on) {
+			const float4 p = __ldg(P + j * (cu + 1) + lane);
+			x = p.x;
+			y = p.y;
+			cbad |= (x != x);
+			cmn = fminf(cmn, x);
+			cmx = fmaxf(cmx, x);
+		}
+		float ymn = on ? y : FLT_MAX, ymx = on ? y : -FLT_MAX;
+		bool ybad = on && (y != y);
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			ymn = fminf(ymn, __shfl_xor_sync(0xffffffffu, ymn, o));
+			ymx = fmaxf(ymx, __shfl_xor_sync(0xffffffffu, ymx, o));
+		}
+		ybad = __any_sync(0xffffffffu, ybad);
+		if (j > 0 && lane == 0) S[32 + j - 1] = pack_range(fminf(pmn, ymn), fmaxf(pmx, ymx), pbad || ybad);
+		pmn = ymn;
+		pmx = ymx;
+		pbad = ybad;
+	}
+	const float nmn = __shfl_down_sync(0xffffffffu, cmn, 1), nmx = __shfl_down_sync(0xffffffffu, cmx, 1);
+	const bool nbad = __shfl_down_sync(0xffffffffu, cbad, 1);
+	if (lane < cu) S[lane] = pack_range(fminf(cmn, nmn), fmaxf(cmx, nmx), cbad || nbad);
+}
+
+__global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect, float* minz, uint32_t* strips) {
 	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const int lane = threadIdx.x & 31;
 	if (warp >= g.ngrids) return;
@@ -40,6 +87,12 @@ __global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect, float*
 		mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
 		mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
 		mxz = fmaxf(mxz, __shfl_xor_sync(0xffffffffu, mxz, o));
+	}
+	if (strips) {
+		uint32_t* S = strips + (long long)warp * 64;
+		const bool has = nk == 1 && cu <= 31 && cv <= 31;
+		if (has) grid_strips(P, cu, cv, lane, S);
+		if (lane == 0) S[63] = has ? 1u : 0u;
 	}
 	if (lane != 0) return;
 	minz[warp] = mnz;
@@ -167,10 +220,10 @@ __global__ void scan_i32_kernel(const int32_t* in, int32_t* out, int n) {
 	if (threadIdx.x == 0) out[n] = carry;
 }
 
-void launch_grid_rects(const FrameParams& fp, const GridsDev& g, int4* rect, float* minz, cudaStream_t s) {
+void launch_grid_rects(const FrameParams& fp, const GridsDev& g, const BinBuffers& b, cudaStream_t s) {
 	if (g.ngrids == 0) return;
 	const int wpb = kBlock / 32;
-	grid_rects_kernel<<<(g.ngrids + wpb - 1) / wpb, kBlock, 0, s>>>(fp, g, rect, minz);
+	grid_rects_kernel<<<(g.ngrids + wpb - 1) / wpb, kBlock, 0, s>>>(fp, g, b.grid_rect, b.grid_minz, b.strips);
 }
 
 void launch_st_count(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s) {

@@ -22,6 +22,7 @@ filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __res
 	const float xcent = x + 0.5f, ycent = y + 0.5f;
 	const int xmax = fp.shiftX, ymax = fp.shiftY;
 	const int spp = fp.spp;
+	const long long npix = (long long)fp.sw * fp.sh;  // the sample store is sample-major
 	float gTot = 0.0f;
 	int count = 0;
 	float acc[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -40,9 +41,9 @@ filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __res
 				if (vx >= -fp.xfwo2 && vy >= -fp.yfwo2 && vx <= fp.xfwo2 && vy <= fp.yfwo2) {
 					const float gw = __ldg(ftab + index + i);
 					gTot += gw;
-					const float4 b = st.b[pix * spp + i];
+					const float4 b = st.b[i * npix + pix];
 					if (b.w != 0.0f) {
-						const float4 a = st.a[pix * spp + i];
+						const float4 a = st.a[i * npix + pix];
 						acc[0] += a.x * gw;
 						acc[1] += a.y * gw;
 						acc[2] += a.z * gw;

@@ -135,6 +135,9 @@ extern "C" aqh_status aqh_render_noalloc(const aqh_frame_desc* desc, const float
 	const long long npix = (long long)fp.sw * fp.sh;
 	const long long nsamp = npix * fp.spp;
 	if (fp.use_dof) return na_fail(err, err_len, AQH_ELIMIT, "aqh_render_noalloc: depth of field is not supported");
+	if (!fp.cullable || fp.midpoint_store)
+		return na_fail(err, err_len, AQH_ELIMIT,
+		               "aqh_render_noalloc: a z display with the midpoint, max or average depth filter is not supported");
 	if (npix > kNaMaxRegionPixels || nsamp > kNaMaxSamples) {
 		snprintf(buf, sizeof buf,
 		         "aqh_render_noalloc: sample region %dx%d x %d samples exceeds the limit of %d pixels / %d samples",
@@ -228,7 +231,7 @@ extern "C" aqh_status aqh_render_noalloc(const aqh_frame_desc* desc, const float
 	store.b = a.sb;
 	FragPool pool{};
 	if (ngrids > 0) {
-		launch_grid_rects(fp, g, bb.grid_rect, bb.grid_minz, s);
+		launch_grid_rects(fp, g, bb, s);
 		launch_st_count(fp, g, bb, s);
 		launch_scan_i32(bb.st_count, bb.st_offset, nst * bb.nranges, nullptr, s);
 		launch_st_write(fp, g, bb, s);

@@ -62,6 +62,7 @@ struct SmemS {
 	int2 pend[kSlotsS];                   // (grid, micropolygon) of the staged candidates
 	int qgrid[kThreadsS];                 // grids of the current list chunk that touch the tile
 	int qcum[kThreadsS + 1];              // running micropolygon counts of those grids
+	int qsub[kThreadsS];                  // their micropolygon sub-rectangles (see stage_candidates)
 	int warp_tot[32];
 	float warp_max[32];
 	int first_reject;
@@ -72,7 +73,12 @@ struct SmemS {
 	int swin[kTileSampMax];               // occluding micropolygon per tile sample (-1 none)
 };
 
+// Running maximum of occluding depths for the early-z culls.  A NaN depth
+// never passes `bminz > occlZ`, so it must never cull: it counts as +inf.
+__device__ __forceinline__ float max_depth(float mx, float d) { return (d != d) ? INFINITY : fmaxf(mx, d); }
+
 __device__ __forceinline__ float warp_max_f(float v) {
+	v = (v != v) ? INFINITY : v;
 #pragma unroll
 	for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
 	return v;
@@ -142,8 +148,8 @@ __device__ __forceinline__ void build_record(const FrameParams& fp, const GridsD
 // Combine of its transparent fragments; written to the sample store.
 template <bool TRANSP>
 __device__ __forceinline__ void resolve_sample(const FrameParams& fp, const GridsDev& g, const FragPool& pool,
-                                               const SampleStore& st, long long sidx, float x, float y, float oz,
-                                               int w, int head) {
+                                               const SampleStore& st, long long sidx, long long aidx, float x,
+                                               float y, float oz, int w, int head) {
 	float occl[7] = {0, 0, 0, 0, 0, 0, 0};
 	int occl_flags = 0;
 	if (w >= 0) {
@@ -161,7 +167,7 @@ __device__ __forceinline__ void resolve_sample(const FrameParams& fp, const Grid
 		float u, vv;
 		inv_bilinear(h.ax, h.ay, h.e_x, h.e_y, h.f_x, h.f_y, h.g_x, h.g_y, h.linear, x, y, u, vv);
 		hit_colour(g, wg, m, u, vv, occl, occl_flags);
-		occl[6] = oz;
+		occl[6] = (TRANSP && fp.midpoint_store) ? st.hitz[sidx] : oz;
 	}
 	int nf = 0;
 	bool valid = w >= 0;
@@ -176,11 +182,155 @@ __device__ __forceinline__ void resolve_sample(const FrameParams& fp, const Grid
 			for (int q = 0; q < 6; ++q) occl[q] = 0.0f;
 		if (fp.depth_filter == 1) occl[6] = (float)(0.5 * ((double)occl[6] + (double)oz));
 	}
-	st.a[sidx] = make_float4(occl[0], occl[1], occl[2], occl[6]);
-	st.b[sidx] = make_float4(occl[3], occl[4], occl[5], valid ? 1.0f : 0.0f);
+	st.a[aidx] = make_float4(occl[0], occl[1], occl[2], occl[6]);
+	st.b[aidx] = make_float4(occl[3], occl[4], occl[5], valid ? 1.0f : 0.0f);
 	if (st.winner) st.winner[sidx] = w;
 	if (st.occlz) st.occlz[sidx] = oz;
 	if (st.nfrag) st.nfrag[sidx] = nf;
+}
+
+// Phase A: stream the super-tile's grid list from the cursor (lp, r0,
+// qtotal) and append the micropolygons that are candidates of the tile to
+// sm.pend, in insertion order, until kSlots are staged or the list ends
+// (returns true then).  One micropolygon per thread tests bound, crop cull
+// and early-z against the largest occluding depth of every pixel it visits;
+// whole grids behind every sample of the 4x4-pixel blocks they overlap are
+// skipped.  Survivors are compacted with block scans, so the staged order is
+// the insertion order.
+template <int kSlots, class Smem>
+__device__ __forceinline__ bool stage_candidates(const FrameParams& fp, const GridsDev& g, const BinBuffers& bb,
+                                                 Smem& sm, int tpx0, int tpy0, int tpx1, int tpy1, int lend, int& lp,
+                                                 int& r0, int& qtotal, int& npend) {
+	const int t = threadIdx.x;
+	const int cullable = fp.cullable;
+	while (npend < kSlots) {
+		if (r0 >= qtotal) {
+			if (lp >= lend) return true;
+			// grids of the next list chunk that touch the tile, in order
+			const int li = lp + t;
+			int gid = -1, nmp = 0, sub = -1;  // sub: first column, first row, width; -1 = whole grid
+			bool f = false;
+			if (li < lend) {
+				gid = bb.st_list[li];
+				const int4 rc = bb.grid_rect[gid];
+				f = rc.x < rc.y && rc.x < tpx1 && rc.y > tpx0 && rc.z < tpy1 && rc.w > tpy0;
+				if (f && cullable) {
+					// whole grid behind every sample of the 4x4-pixel blocks it overlaps
+					const int bx0 = (max(rc.x, tpx0) - tpx0) >> 2, bx1 = (min(rc.y, tpx1) - 1 - tpx0) >> 2;
+					const int by0 = (max(rc.z, tpy0) - tpy0) >> 2, by1 = (min(rc.w, tpy1) - 1 - tpy0) >> 2;
+					const int nbx = (fp.tile_w + 3) >> 2;
+					float mx = -FLT_MAX;
+					for (int by = by0; by <= by1; ++by)
+						for (int bx = bx0; bx <= bx1; ++bx) mx = fmaxf(mx, sm.blkmax[by * nbx + bx]);
+					if (__ldg(bb.grid_minz + gid) > mx) f = false;
+				}
+				if (f) {
+					const int cu = __ldg(g.cu + gid), cv = __ldg(g.cv + gid);
+					nmp = cu * cv;
+					if (bb.strips && __ldg(bb.strips + (long long)gid * 64 + 63)) {
+						// the columns and rows of micropolygons that can meet the tile
+						const uint32_t* S = bb.strips + (long long)gid * 64;
+						int iu0 = 64, iu1 = -1, iv0 = 64, iv1 = -1;
+						for (int k = 0; k < cu; ++k) {
+							const uint32_t w = __ldg(S + k);
+							if ((int)(int16_t)(w & 0xffffu) < tpx1 && (int)(int16_t)(w >> 16) > tpx0) {
+								iu0 = min(iu0, k);
+								iu1 = k;
+							}
+						}
+						for (int k = 0; k < cv; ++k) {
+							const uint32_t w = __ldg(S + 32 + k);
+							if ((int)(int16_t)(w & 0xffffu) < tpy1 && (int)(int16_t)(w >> 16) > tpy0) {
+								iv0 = min(iv0, k);
+								iv1 = k;
+							}
+						}
+						if (iu1 < 0 || iv1 < 0) {
+							f = false;
+							nmp = 0;
+						} else {
+							nmp = (iu1 - iu0 + 1) * (iv1 - iv0 + 1);
+							sub = iu0 | (iv0 << 8) | ((iu1 - iu0 + 1) << 16);
+						}
+					}
+				}
+			}
+			int total, sum;
+			const int pos = block_excl_scan(sm.warp_tot, f, total);
+			__syncthreads();
+			// running micropolygon counts of the queued grids
+			const int pre = block_excl_sum(sm.warp_tot, nmp, sum);
+			if (f) {
+				sm.qgrid[pos] = gid;
+				sm.qcum[pos] = pre;
+				sm.qsub[pos] = sub;
+			}
+			if (t == 0) {
+				sm.qcum[total] = sum;
+				sm.qn = total;
+			}
+			__syncthreads();
+			qtotal = sm.qcum[sm.qn];
+			r0 = 0;
+			lp += kThreadsS;
+			continue;
+		}
+		// one micropolygon of the stream per thread: is it a candidate of this tile?
+		const int p = r0 + t;
+		bool active = false;
+		int gid = 0, m = 0;
+		if (p < qtotal) {
+			int lo = 0, hi = sm.qn - 1;
+			while (lo < hi) {
+				const int mid = (lo + hi + 1) >> 1;
+				if (sm.qcum[mid] <= p) lo = mid; else hi = mid - 1;
+			}
+			gid = sm.qgrid[lo];
+			m = p - sm.qcum[lo];
+			const int cu = __ldg(g.cu + gid);
+			const int sub = sm.qsub[lo];
+			if (sub >= 0) {
+				const int w = sub >> 16, jv = m / w;
+				m = ((sub >> 8) & 0xff) * cu + jv * cu + (sub & 0xff) + (m - jv * w);
+			}
+			const long long pb = __ldg(g.pbase + gid);
+			const int iv = m / cu, iu = m - iv * cu;
+			const int index = iv * (cu + 1) + iu;
+			const V3f a = ld3(g.P, pb + index), b = ld3(g.P, pb + index + 1);
+			const V3f c = ld3(g.P, pb + index + cu + 1), d = ld3(g.P, pb + index + cu + 2);
+			const float bminx = amin(amin(amin(a.x, b.x), d.x), c.x);
+			const float bminy = amin(amin(amin(a.y, b.y), d.y), c.y);
+			const float bminz = amin(amin(amin(a.z, b.z), d.z), c.z);
+			const float bmaxx = amax(amax(amax(a.x, b.x), d.x), c.x);
+			const float bmaxy = amax(amax(amax(a.y, b.y), d.y), c.y);
+			const bool culled = g.culled && g.culled[__ldg(g.mpbase + gid) + m];
+			// AddMPG crop cull (imagebuffer.cpp:533-539)
+			const bool cropped =
+			    bmaxx < fp.cull_x0 || bmaxy < fp.cull_y0 || bminx > fp.cull_x1 || bminy > fp.cull_y1;
+			const int sX = max((int)floorf(bminx), tpx0), eX = min(lceil_f(bmaxx), tpx1);
+			const int sY = max((int)floorf(bminy), tpy0), eY = min(lceil_f(bmaxy), tpy1);
+			active = !culled && !cropped && sX < eX && sY < eY;
+			if (active && cullable) {
+				// early-z for every pixel it visits: behind all their samples' occluding depths
+				float mx = -FLT_MAX;
+				for (int yy = sY; yy < eY; ++yy)
+					for (int xx = sX; xx < eX; ++xx) mx = fmaxf(mx, sm.pixmax[(yy - tpy0) * fp.tile_w + (xx - tpx0)]);
+				if (bminz > mx) active = false;
+			}
+		}
+		int total;
+		const int rank = block_excl_scan(sm.warp_tot, active, total);
+		const int navail = kSlots - npend;
+		if (t == 0) sm.first_reject = kThreadsS;
+		__syncthreads();
+		if (active && rank == navail) sm.first_reject = t;
+		if (active && rank < navail) sm.pend[npend + rank] = make_int2(gid, m);
+		__syncthreads();
+		const int consumed = (total > navail) ? sm.first_reject : min(kThreadsS, qtotal - r0);
+		npend += min(total, navail);
+		r0 += consumed;
+	}
+	return false;
 }
 
 // PERSIST: a fixed grid of CTAs pulls tiles from a device work queue
@@ -241,103 +391,9 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 	int lp = lbeg, r0 = 0, qtotal = 0;
 	int npend = 0;
 	for (;;) {
-		// ---- phase A: stage up to kSlotsS candidates, in insertion order ----
-		bool exhausted = false;
-		while (npend < kSlotsS) {
-			if (r0 >= qtotal) {
-				if (lp >= lend) { exhausted = true; break; }
-				// grids of the next list chunk that touch the tile, in order
-				const int li = lp + t;
-				int gid = -1, nmp = 0;
-				bool f = false;
-				if (li < lend) {
-					gid = bb.st_list[li];
-					const int4 rc = bb.grid_rect[gid];
-					f = rc.x < rc.y && rc.x < tpx1 && rc.y > tpx0 && rc.z < tpy1 && rc.w > tpy0;
-					if (f && cullable) {
-						// whole grid behind every sample of the 4x4-pixel blocks it overlaps
-						const int bx0 = (max(rc.x, tpx0) - tpx0) >> 2, bx1 = (min(rc.y, tpx1) - 1 - tpx0) >> 2;
-						const int by0 = (max(rc.z, tpy0) - tpy0) >> 2, by1 = (min(rc.w, tpy1) - 1 - tpy0) >> 2;
-						const int nbx = (fp.tile_w + 3) >> 2;
-						float mx = -FLT_MAX;
-						for (int by = by0; by <= by1; ++by)
-							for (int bx = bx0; bx <= bx1; ++bx) mx = fmaxf(mx, sm.blkmax[by * nbx + bx]);
-						if (__ldg(bb.grid_minz + gid) > mx) f = false;
-					}
-					if (f) nmp = __ldg(g.cu + gid) * __ldg(g.cv + gid);
-				}
-				int total;
-				const int pos = block_excl_scan(sm.warp_tot, f, total);
-				if (f) sm.qgrid[pos] = gid;
-				__syncthreads();
-				// running micropolygon counts of the queued grids
-				if (t == 0) {
-					int acc = 0;
-					for (int k = 0; k < total; ++k) {
-						sm.qcum[k] = acc;
-						const int q = sm.qgrid[k];
-						acc += __ldg(g.cu + q) * __ldg(g.cv + q);
-					}
-					sm.qcum[total] = acc;
-					sm.qn = total;
-				}
-				(void)nmp;
-				__syncthreads();
-				qtotal = sm.qcum[sm.qn];
-				r0 = 0;
-				lp += kThreadsS;
-				continue;
-			}
-			// one micropolygon of the stream per thread: is it a candidate of this tile?
-			const int p = r0 + t;
-			bool active = false;
-			int gid = 0, m = 0;
-			if (p < qtotal) {
-				int lo = 0, hi = sm.qn - 1;
-				while (lo < hi) {
-					const int mid = (lo + hi + 1) >> 1;
-					if (sm.qcum[mid] <= p) lo = mid; else hi = mid - 1;
-				}
-				gid = sm.qgrid[lo];
-				m = p - sm.qcum[lo];
-				const int cu = __ldg(g.cu + gid);
-				const long long pb = __ldg(g.pbase + gid);
-				const int iv = m / cu, iu = m - iv * cu;
-				const int index = iv * (cu + 1) + iu;
-				const V3f a = ld3(g.P, pb + index), b = ld3(g.P, pb + index + 1);
-				const V3f c = ld3(g.P, pb + index + cu + 1), d = ld3(g.P, pb + index + cu + 2);
-				const float bminx = amin(amin(amin(a.x, b.x), d.x), c.x);
-				const float bminy = amin(amin(amin(a.y, b.y), d.y), c.y);
-				const float bminz = amin(amin(amin(a.z, b.z), d.z), c.z);
-				const float bmaxx = amax(amax(amax(a.x, b.x), d.x), c.x);
-				const float bmaxy = amax(amax(amax(a.y, b.y), d.y), c.y);
-				const bool culled = g.culled && g.culled[__ldg(g.mpbase + gid) + m];
-				// AddMPG crop cull (imagebuffer.cpp:533-539)
-				const bool cropped =
-				    bmaxx < fp.cull_x0 || bmaxy < fp.cull_y0 || bminx > fp.cull_x1 || bminy > fp.cull_y1;
-				const int sX = max((int)floorf(bminx), tpx0), eX = min(lceil_f(bmaxx), tpx1);
-				const int sY = max((int)floorf(bminy), tpy0), eY = min(lceil_f(bmaxy), tpy1);
-				active = !culled && !cropped && sX < eX && sY < eY;
-				if (active && cullable) {
-					// early-z for every pixel it visits: behind all their samples' occluding depths
-					float mx = -FLT_MAX;
-					for (int yy = sY; yy < eY; ++yy)
-						for (int xx = sX; xx < eX; ++xx) mx = fmaxf(mx, sm.pixmax[(yy - tpy0) * fp.tile_w + (xx - tpx0)]);
-					if (bminz > mx) active = false;
-				}
-			}
-			int total;
-			const int rank = block_excl_scan(sm.warp_tot, active, total);
-			const int navail = kSlotsS - npend;
-			if (t == 0) sm.first_reject = kThreadsS;
-			__syncthreads();
-			if (active && rank == navail) sm.first_reject = t;
-			if (active && rank < navail) sm.pend[npend + rank] = make_int2(gid, m);
-			__syncthreads();
-			const int consumed = (total > navail) ? sm.first_reject : min(kThreadsS, qtotal - r0);
-			npend += min(total, navail);
-			r0 += consumed;
-		}
+		// ---- phase A ----
+		const bool exhausted =
+		    stage_candidates<kSlotsS>(fp, g, bb, sm, tpx0, tpy0, tpx1, tpy1, lend, lp, r0, qtotal, npend);
 		if (npend == 0) break;
 
 		// ---- build the staged records with every thread busy ----
@@ -365,8 +421,9 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 			const int px = tpx0 + lx, py = tpy0 + ly;
 			const bool valid = s < tsamp && px < tpx1 && py < tpy1;
 			const int sn = si / fp.xs, smm = si - sn * fp.xs;
-			float x = 0.0f, y = 0.0f, oz = -FLT_MAX;
+			float x = 0.0f, y = 0.0f, oz = -FLT_MAX, hz = FLT_MAX;
 			int w = -1, fh = -1;
+			long long sidx = 0;
 			if (valid) {
 				const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
 				const long long pat = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
@@ -376,6 +433,8 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 				oz = sm.soz[s];
 				w = sm.swin[s];
 				if (TRANSP) fh = fhead[s];
+				sidx = pix * spp + si;
+				if (TRANSP && fp.midpoint_store && w >= 0) hz = st.hitz[sidx];
 			}
 			float gmax = warp_max_f(oz);
 #pragma unroll 1
@@ -408,8 +467,21 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 						// StoreSample (bucketprocessor.cpp:1471-1569)
 						if (!(cullable && oz <= D)) {
 							if ((r.bits & kRecOccluding) && cullable) {
-								oz = D;
-								w = r.id;
+								if (TRANSP && fp.midpoint_store) {
+									// midpoint filter with a z display (bucketprocessor.cpp:1502-1530):
+									// occlZ follows the second-nearest opaque depth, the hit the nearest
+									const float hp = (w >= 0) ? hz : FLT_MAX;
+									if (hp < D) {
+										oz = D;
+									} else {
+										oz = hp;
+										hz = D;
+										w = r.id;
+									}
+								} else {
+									oz = D;
+									w = r.id;
+								}
 								stored = true;
 							} else if (TRANSP) {
 								// append a fragment {depth, id, u, v}; lists are newest-first
@@ -437,6 +509,7 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 				sm.soz[s] = oz;
 				sm.swin[s] = w;
 				if (TRANSP) fhead[s] = fh;
+				if (TRANSP && fp.midpoint_store && w >= 0) st.hitz[sidx] = hz;
 			}
 			wmax = fmaxf(wmax, gmax);
 		}
@@ -445,7 +518,7 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		__syncthreads();
 		for (int pp = t; pp < tpix; pp += kThreadsS) {
 			float mx = -FLT_MAX;
-			for (int k = 0; k < spp; ++k) mx = fmaxf(mx, sm.soz[pp * spp + k]);
+			for (int k = 0; k < spp; ++k) mx = max_depth(mx, sm.soz[pp * spp + k]);
 			sm.pixmax[pp] = mx;
 		}
 		for (int i = t; i < kTilePixMax * kWordsS; i += kThreadsS) (&sm.mask[0][0])[i] = 0u;
@@ -465,16 +538,327 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 	}
 
 	// ---- resolve: colours of the occluding hits, Combine of fragment lists ----
-	for (int s = t; s < tsamp; s += kThreadsS) {
-		const int pl = s / spp;
-		const int si = s - pl * spp;
+	// (consecutive threads take consecutive pixels of one sample index: the
+	// sample store is sample-major)
+	const long long npix = (long long)fp.sw * fp.sh;
+	for (int q = t; q < tsamp; q += kThreadsS) {
+		const int si = q / tpix;
+		const int pl = q - si * tpix;
+		const int s = pl * spp + si;
 		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 		if (px >= tpx1 || py >= tpy1) continue;
 		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
 		const long long pat = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
 		const float2 o = __ldg(smp.pos + pat * spp + si);
-		resolve_sample<TRANSP>(fp, g, pool, st, pix * spp + si, (float)px + o.x, (float)py + o.y, sm.soz[s],
-		                       sm.swin[s], TRANSP ? fhead[s] : -1);
+		resolve_sample<TRANSP>(fp, g, pool, st, pix * spp + si, si * npix + pix, (float)px + o.x, (float)py + o.y,
+		                       sm.soz[s], sm.swin[s], TRANSP ? fhead[s] : -1);
+	}
+	}  // tile loop
+}
+
+
+// ---- opaque frames: parallel hit tests with an ordered fallback ----------
+//
+// When every micropolygon is opaque, StoreSample's early-z and store rule
+// (bucketprocessor.cpp:1179, 1475: skip if bound.min.z > occlZ, keep the hit
+// only if D < occlZ) reduce, for every hit whose depth D is not below its own
+// bound's minimum z, to "occlZ = min(occlZ, D), first of equal depths wins":
+// such a hit skipped by early-z has D >= min.z > occlZ and would not have
+// been kept anyway.  So the winner of a sample is the least (D, insertion
+// order) over those hits, which does not depend on the order in which they
+// are visited: (candidate, sample) pairs are tested in parallel and folded
+// with a 64-bit shared-memory atomicMin on (ordered depth bits, id + 1).
+// A hit with D below its bound's minimum (rounding or Newton error), a NaN
+// or a zero depth (the signs of zero compare equal) may behave differently
+// in order, so the sample is flagged and replayed in insertion order over
+// the round's candidates from its state at the start of the round.  A
+// sample whose occlZ becomes NaN or zero stays on the ordered replay for
+// the rest of the tile.  Early-z in the parallel pass tests the depth at the
+// start of the round, which is never below the depth the ordered sequence
+// would see, so it only skips what the reference skips.
+constexpr int kSlotsO = 192;
+
+__device__ __forceinline__ unsigned long long depth_key(float z, int w) {
+	const uint32_t u = __float_as_uint(z);
+	const uint32_t o = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+	return ((unsigned long long)o << 32) | (uint32_t)(w + 1);
+}
+__device__ __forceinline__ float key_depth(unsigned long long k) {
+	const uint32_t o = (uint32_t)(k >> 32);
+	return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+__device__ __forceinline__ int key_winner(unsigned long long k) { return (int)(uint32_t)k - 1; }
+
+struct SmemO {
+	unsigned long long key[kTileSampMax];   // occluding hit of each tile sample (depth_key)
+	unsigned long long prev[kTileSampMax];  // ... at the start of the round
+	RecS rec[kSlotsO];
+	int2 pend[kSlotsO];
+	int pref[kSlotsO + 1];                  // running count of (candidate, sample) tests
+	int rng[kSlotsO][3];                    // tests in the first column, the first row, and per row
+	int qgrid[kThreadsS];
+	int qcum[kThreadsS + 1];
+	int qsub[kThreadsS];
+	int patidx[kTilePixMax];                // sample pattern of each tile pixel
+	int warp_tot[32];
+	int first_reject;
+	int qn;
+	float pixmax[kTilePixMax];
+	float blkmax[16];
+	uint32_t flag[kTileSampMax / 32];       // samples replayed in order this round
+	uint32_t sticky[kTileSampMax / 32];     // samples replayed in order for the rest of the tile
+};
+
+template <bool PERSIST>
+__global__ void __launch_bounds__(kThreadsS, 2)
+sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, SampleStore st, int* queue,
+                     const int* order) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	SmemO& sm = *reinterpret_cast<SmemO*>(smem_raw);
+	__shared__ int next_tile;
+	const int ntiles = fp.ntx * fp.nty;
+	const FragPool nopool{};
+	for (int job = 0;; ++job) {
+	int tile;
+	if (PERSIST) {
+		__syncthreads();
+		if (threadIdx.x == 0) next_tile = atomicAdd(queue, 1);
+		__syncthreads();
+		tile = next_tile;
+		if (tile >= ntiles) break;
+		if (order) tile = order[tile];
+	} else {
+		if (job > 0) break;
+		tile = blockIdx.x;
+	}
+	const int tx = tile % fp.ntx, ty = tile / fp.ntx;
+	const int tpx0 = fp.sx0 + tx * fp.tile_w, tpy0 = fp.sy0 + ty * fp.tile_h;
+	const int tpx1 = min(tpx0 + fp.tile_w, fp.sx0 + fp.sw), tpy1 = min(tpy0 + fp.tile_h, fp.sy0 + fp.sh);
+	const int st_idx = (ty / fp.st_tiles) * fp.nstx + (tx / fp.st_tiles);
+	const int t = threadIdx.x;
+	const int spp = fp.spp, xs = fp.xs, ys = fp.ys;
+	const int tpix = fp.tile_w * fp.tile_h;
+	const int tsamp = tpix * spp;
+	const int nflagw = (tsamp + 31) >> 5;
+	const unsigned long long kinit = depth_key(FLT_MAX, -1);
+
+	for (int i = t; i < tsamp; i += kThreadsS) {
+		sm.key[i] = kinit;
+		sm.prev[i] = kinit;
+	}
+	for (int i = t; i < kTileSampMax / 32; i += kThreadsS) {
+		sm.flag[i] = 0u;
+		sm.sticky[i] = 0u;
+	}
+	for (int i = t; i < kTilePixMax; i += kThreadsS) {
+		sm.pixmax[i] = FLT_MAX;
+		const int px = tpx0 + i % fp.tile_w, py = tpy0 + i / fp.tile_w;
+		int pat = 0;
+		if (i < tpix && px < tpx1 && py < tpy1) {
+			const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
+			pat = smp.pos_index ? (int)__ldg(smp.pos_index + pix) : (int)pix;
+		}
+		sm.patidx[i] = pat;
+	}
+	if (t < 16) sm.blkmax[t] = FLT_MAX;
+	if (t == 0) {
+		sm.qn = 0;
+		sm.qcum[0] = 0;
+	}
+	__syncthreads();
+
+	const int lbeg = bb.st_offset[st_idx * bb.nranges];
+	const int lend = (int)min((long long)bb.st_offset[(st_idx + 1) * bb.nranges], (long long)bb.list_capacity);
+	int lp = lbeg, r0 = 0, qtotal = 0, npend = 0;
+	for (;;) {
+		const bool exhausted =
+		    stage_candidates<kSlotsO>(fp, g, bb, sm, tpx0, tpy0, tpx1, tpy1, lend, lp, r0, qtotal, npend);
+		if (npend == 0) break;
+
+		// ---- records, and the (candidate, sample) tests RenderMPG_Static makes ----
+		// The samples a candidate visits form a product set: columns of the
+		// clipped pixel range with their sub-sample ranges (the first and last
+		// pixel trimmed, bucketprocessor.cpp:1135-1153) times the same in y.
+		int ntests = 0;
+		if (t < npend) {
+			const int2 e = sm.pend[t];
+			RecS& r = sm.rec[t];
+			build_record(fp, g, e.x, e.y, r);
+			const int sX = max(r.px0, tpx0), eX = min(r.px1, tpx1);
+			const int sY = max(r.py0, tpy0), eY = min(r.py1, tpy1);
+			// per-axis counts: first pixel, then full pixels, the last one trimmed
+			int cx0 = ((sX == r.px1 - 1) ? r.em : xs) - ((sX == r.px0) ? r.im : 0);
+			int totx = cx0;
+			if (eX - sX > 1) totx += (eX - sX - 2) * xs + ((eX - 1 == r.px1 - 1) ? r.em : xs);
+			int cy0 = ((sY == r.py1 - 1) ? r.en : ys) - ((sY == r.py0) ? r.in_ : 0);
+			int toty = cy0;
+			if (eY - sY > 1) toty += (eY - sY - 2) * ys + ((eY - 1 == r.py1 - 1) ? r.en : ys);
+			totx = max(totx, 0);
+			toty = max(toty, 0);
+			ntests = totx * toty;
+			sm.rng[t][0] = cx0;
+			sm.rng[t][1] = cy0;
+			sm.rng[t][2] = totx;
+		}
+		int total;
+		const int pre = block_excl_sum(sm.warp_tot, ntests, total);
+		if (t < npend) sm.pref[t] = pre;
+		__syncthreads();
+
+		// ---- parallel pass: one (candidate, sample) test per thread ----
+		for (int p = t; p < total; p += kThreadsS) {
+			int lo = 0, hi = npend - 1;
+			while (lo < hi) {
+				const int mid = (lo + hi + 1) >> 1;
+				if (sm.pref[mid] <= p) lo = mid; else hi = mid - 1;
+			}
+			const RecS& r = sm.rec[lo];
+			const int k = p - sm.pref[lo];
+			const int cx0 = sm.rng[lo][0], cy0 = sm.rng[lo][1], totx = sm.rng[lo][2];
+			const int sX = max(r.px0, tpx0), sY = max(r.py0, tpy0);
+			const int ky = k / totx, kx = k - ky * totx;
+			int px, m, py, n;
+			if (kx < cx0) {
+				px = sX;
+				m = ((sX == r.px0) ? r.im : 0) + kx;
+			} else {
+				const int q = kx - cx0;
+				px = sX + 1 + q / xs;
+				m = q - (q / xs) * xs;
+			}
+			if (ky < cy0) {
+				py = sY;
+				n = ((sY == r.py0) ? r.in_ : 0) + ky;
+			} else {
+				const int q = ky - cy0;
+				py = sY + 1 + q / ys;
+				n = q - (q / ys) * ys;
+			}
+			const int si = n * xs + m;
+			const int pl = (py - tpy0) * fp.tile_w + (px - tpx0);
+			const int s = pl * spp + si;
+			if (sm.flag[s >> 5] & (1u << (s & 31))) continue;  // replayed in order below
+			const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + si);
+			const float x = (float)px + o.x, y = (float)py + o.y;
+			// CqBound::Contains2D (bound.h:144-151), early-z, fContains
+			if ((x < r.bminx || x > r.bmaxx) || (y < r.bminy || y > r.bmaxy)) continue;
+			if (r.bminz > key_depth(sm.prev[s])) continue;
+			if (!edges_inside(r.ym, r.xm, r.ex, r.ey, x, y)) continue;
+			float u, v;
+			inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y, (r.bits & kRecLinear) != 0, x, y, u,
+			             v);
+			const float D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
+			if (!(D >= r.bminz) || D == 0.0f)
+				atomicOr(&sm.flag[s >> 5], 1u << (s & 31));
+			else
+				atomicMin(&sm.key[s], depth_key(D, r.id));
+		}
+		__syncthreads();
+		int anyf = 0;
+		for (int i = t; i < nflagw; i += kThreadsS) anyf |= (int)(sm.flag[i] != 0u);
+
+		// ---- ordered replay of flagged samples: a warp per sample ----
+		// Lanes test 32 candidates at a time (the tests do not depend on
+		// occlZ); lane order then applies early-z and the store rule in
+		// insertion order.
+		if (__syncthreads_or(anyf)) {
+			const int lane = t & 31, warp = t >> 5;
+			for (int wd = warp; wd < nflagw; wd += kWarpsS) {
+				uint32_t fb = sm.flag[wd];
+				while (fb) {
+					const int s = wd * 32 + __ffs(fb) - 1;
+					fb &= fb - 1u;
+					const int pl = s / spp, si = s - pl * spp;
+					const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
+					if (px >= tpx1 || py >= tpy1) continue;
+					const int sn = si / xs, smm = si - sn * xs;
+					const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + si);
+					const float x = (float)px + o.x, y = (float)py + o.y;
+					float oz = key_depth(sm.prev[s]);
+					int w = key_winner(sm.prev[s]);
+					for (int c0 = 0; c0 < npend; c0 += 32) {
+						const int c = c0 + lane;
+						bool hit = false;
+						float D = 0.0f, bz = 0.0f;
+						int id = 0;
+						if (c < npend) {
+							const RecS& r = sm.rec[c];
+							const int m_lo = (px == r.px0) ? r.im : 0, m_hi = (px == r.px1 - 1) ? r.em : xs;
+							const int n_lo = (py == r.py0) ? r.in_ : 0, n_hi = (py == r.py1 - 1) ? r.en : ys;
+							hit = px >= r.px0 && px < r.px1 && py >= r.py0 && py < r.py1 && smm >= m_lo && smm < m_hi &&
+							      sn >= n_lo && sn < n_hi &&
+							      !((x < r.bminx || x > r.bmaxx) || (y < r.bminy || y > r.bmaxy)) &&
+							      edges_inside(r.ym, r.xm, r.ex, r.ey, x, y);
+							if (hit) {
+								float u, v;
+								inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y,
+								             (r.bits & kRecLinear) != 0, x, y, u, v);
+								D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
+								bz = r.bminz;
+								id = r.id;
+							}
+						}
+						uint32_t hb = __ballot_sync(0xffffffffu, hit);
+						while (hb) {
+							const int b = __ffs(hb) - 1;
+							hb &= hb - 1u;
+							const float Db = __shfl_sync(0xffffffffu, D, b);
+							const float bzb = __shfl_sync(0xffffffffu, bz, b);
+							const int idb = __shfl_sync(0xffffffffu, id, b);
+							if (!(bzb > oz) && !(oz <= Db)) {
+								oz = Db;
+								w = idb;
+							}
+						}
+					}
+					if (lane == 0) {
+						sm.key[s] = depth_key(oz, w);
+						if (oz != oz || oz == 0.0f) atomicOr(&sm.sticky[s >> 5], 1u << (s & 31));
+					}
+				}
+			}
+		}
+		__syncthreads();
+
+		// ---- end of round: state, largest occluding depths, flags ----
+		for (int pp = t; pp < tpix; pp += kThreadsS) {
+			float mx = -FLT_MAX;
+			for (int k = 0; k < spp; ++k) {
+				const unsigned long long kk = sm.key[pp * spp + k];
+				sm.prev[pp * spp + k] = kk;
+				mx = max_depth(mx, key_depth(kk));
+			}
+			sm.pixmax[pp] = mx;
+		}
+		for (int i = t; i < nflagw; i += kThreadsS) sm.flag[i] = sm.sticky[i];
+		__syncthreads();
+		if (t < 16) {
+			const int nbx = (fp.tile_w + 3) >> 2;
+			const int bx = t % nbx, by = t / nbx;
+			float mx = -FLT_MAX;
+			if (by * 4 < fp.tile_h)
+				for (int yy = by * 4; yy < min(by * 4 + 4, fp.tile_h); ++yy)
+					for (int xx = bx * 4; xx < min(bx * 4 + 4, fp.tile_w); ++xx)
+						mx = max_depth(mx, sm.pixmax[yy * fp.tile_w + xx]);
+			sm.blkmax[t] = mx;
+		}
+		__syncthreads();
+		npend = 0;
+		if (exhausted) break;
+	}
+
+	// ---- resolve: colours of the occluding hits (sample-major, as above) ----
+	const long long npix = (long long)fp.sw * fp.sh;
+	for (int q = t; q < tsamp; q += kThreadsS) {
+		const int si = q / tpix;
+		const int pl = q - si * tpix;
+		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
+		if (px >= tpx1 || py >= tpy1) continue;
+		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
+		const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + si);
+		const unsigned long long kk = sm.key[pl * spp + si];
+		resolve_sample<false>(fp, g, nopool, st, pix * spp + si, si * npix + pix, (float)px + o.x, (float)py + o.y,
+		                      key_depth(kk), key_winner(kk), -1);
 	}
 	}  // tile loop
 }
@@ -499,20 +883,19 @@ void launch_sample_tiles(const FrameParams& fp, const GridsDev& g, const Sampler
 void launch_sample_tiles_q(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
                            SampleStore st, FragPool pool, int* queue, const int* order, int nctas, cudaStream_t s) {
 	const int ntiles = fp.ntx * fp.nty;
-	const size_t smem_opaque = sizeof(SmemS);
-	const size_t smem_transp = smem_opaque + sizeof(int32_t) * kTileSampMax;
+	const size_t smem_transp = sizeof(SmemS) + sizeof(int32_t) * kTileSampMax;
 	configure_sample_kernels();
 	const bool transp = pool.capacity > 0;
 	if (queue) {
 		if (transp)
 			sample_static_kernel<true, true><<<nctas, kThreadsS, smem_transp, s>>>(fp, g, sm, b, st, pool, queue, order);
 		else
-			sample_static_kernel<false, true><<<nctas, kThreadsS, smem_opaque, s>>>(fp, g, sm, b, st, pool, queue, order);
+			sample_opaque_kernel<true><<<nctas, kThreadsS, sizeof(SmemO), s>>>(fp, g, sm, b, st, queue, order);
 	} else {
 		if (transp)
 			sample_static_kernel<true, false><<<ntiles, kThreadsS, smem_transp, s>>>(fp, g, sm, b, st, pool, nullptr, nullptr);
 		else
-			sample_static_kernel<false, false><<<ntiles, kThreadsS, smem_opaque, s>>>(fp, g, sm, b, st, pool, nullptr, nullptr);
+			sample_opaque_kernel<false><<<ntiles, kThreadsS, sizeof(SmemO), s>>>(fp, g, sm, b, st, nullptr, nullptr);
 	}
 }
 
@@ -521,23 +904,22 @@ void launch_sample_tiles_q(const FrameParams& fp, const GridsDev& g, const Sampl
 void configure_sample_kernels() {
 	static bool configured = false;
 	if (configured) return;
-	const int smem_opaque = (int)sizeof(SmemS);
-	const int smem_transp = smem_opaque + (int)(sizeof(int32_t) * kTileSampMax);
-	cudaFuncSetAttribute(sample_static_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_opaque);
+	const int smem_transp = (int)(sizeof(SmemS) + sizeof(int32_t) * kTileSampMax);
+	cudaFuncSetAttribute(sample_opaque_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemO));
 	cudaFuncSetAttribute(sample_static_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_transp);
-	cudaFuncSetAttribute(sample_static_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_opaque);
+	cudaFuncSetAttribute(sample_opaque_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemO));
 	cudaFuncSetAttribute(sample_static_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_transp);
 	configure_sample_mb_kernels();
 	configured = true;
 }
 
 int sample_static_ctas_per_sm(bool transp) {
-	const size_t smem = sizeof(SmemS) + (transp ? sizeof(int32_t) * kTileSampMax : 0);
 	int n = 0;
 	if (transp)
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sample_static_kernel<true, true>, kThreadsS, smem);
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sample_static_kernel<true, true>, kThreadsS,
+		                                              sizeof(SmemS) + sizeof(int32_t) * kTileSampMax);
 	else
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sample_static_kernel<false, true>, kThreadsS, smem);
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sample_opaque_kernel<true>, kThreadsS, sizeof(SmemO));
 	return n > 0 ? n : 1;
 }
 

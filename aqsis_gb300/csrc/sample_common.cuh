@@ -24,6 +24,28 @@ __device__ __forceinline__ int block_excl_scan(int* warp_tot, bool f, int& total
 	return pre + __popc(bal & ((1u << lane) - 1u));
 }
 
+// Exclusive prefix sum of `v` over the block (same layout rules as
+// block_excl_scan).
+__device__ __forceinline__ int block_excl_sum(int* warp_tot, int v, int& total) {
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	int inc = v;
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1) {
+		const int n = __shfl_up_sync(0xffffffffu, inc, o);
+		if (lane >= o) inc += n;
+	}
+	if (lane == 31) warp_tot[wid] = inc;
+	__syncthreads();
+	int pre = 0, tot = 0;
+	for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+		const int t = warp_tot[w];
+		pre += (w < wid) ? t : 0;
+		tot += t;
+	}
+	total = tot;
+	return pre + inc - v;
+}
+
 // Sub-sample index range of pixel `p` inside [s, e) of a bound edge
 // (bucketprocessor.cpp:1119-1138, 1149-1153), for one axis.
 __device__ __forceinline__ void sub_range(int p, float bmin, float bmax, int ns, int& lo, int& hi) {

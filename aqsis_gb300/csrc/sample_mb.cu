@@ -480,8 +480,9 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 			const int j = s - pl * spp;
 			const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 			const bool valid = s < tsamp && px < tpx1 && py < tpy1;
-			float x = 0.0f, y = 0.0f, stime = 0.0f, sdx = 0.0f, sdy = 0.0f, oz = -FLT_MAX;
+			float x = 0.0f, y = 0.0f, stime = 0.0f, sdx = 0.0f, sdy = 0.0f, oz = -FLT_MAX, hz = FLT_MAX;
 			int w = -1, fh = -1, kinv = 0;
+			long long sidx = 0;
 			if (valid) {
 				const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
 				const long long pp = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
@@ -506,6 +507,8 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 				oz = sm.soz[s];
 				w = sm.swin[s];
 				if (TRANSP) fh = fhead[s];
+				sidx = pix * spp + j;
+				if (TRANSP && fp.midpoint_store && w >= 0) hz = st.hitz[sidx];
 			}
 			float gmax = warp_max_m(oz);
 #pragma unroll 1
@@ -585,8 +588,20 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 							if (!mb_sample(fp, r, moving, usingDof, x, y, stime, sdx, sdy, D, u, v)) continue;
 							if (cullable && oz <= D) continue;
 							if ((r.bits & 2) && cullable) {
-								oz = D;
-								w = r.id;
+								if (TRANSP && fp.midpoint_store) {
+									// midpoint filter with a z display (bucketprocessor.cpp:1502-1530)
+									const float hp = (w >= 0) ? hz : FLT_MAX;
+									if (hp < D) {
+										oz = D;
+									} else {
+										oz = hp;
+										hz = D;
+										w = r.id;
+									}
+								} else {
+									oz = D;
+									w = r.id;
+								}
 								stored = true;
 							} else if (TRANSP) {
 								const unsigned act = __activemask();
@@ -613,6 +628,7 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 				sm.soz[s] = oz;
 				sm.swin[s] = w;
 				if (TRANSP) fhead[s] = fh;
+				if (TRANSP && fp.midpoint_store && w >= 0) st.hitz[sidx] = hz;
 			}
 		}
 		__syncthreads();
@@ -623,13 +639,18 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 	}
 
 	// ---- resolve: repeat the winner's hit test for its (u,v) ----
-	for (int s = t; s < tsamp; s += kThreadsM) {
-		const int pl = s / spp;
-		const int j = s - pl * spp;
+	// (consecutive threads take consecutive pixels of one sample index: the
+	// sample store is sample-major)
+	const long long npix = (long long)fp.sw * fp.sh;
+	for (int q = t; q < tsamp; q += kThreadsM) {
+		const int j = q / tpix;
+		const int pl = q - j * tpix;
+		const int s = pl * spp + j;
 		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 		if (px >= tpx1 || py >= tpy1) continue;
 		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
 		const long long sidx = pix * spp + j;
+		const long long aidx = (long long)j * npix + pix;
 		const float ozv = sm.soz[s];
 		const int w = sm.swin[s];
 		float occl[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -661,7 +682,7 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 			float D, u, v;
 			mb_sample(fp, rr, rr.nkeys > 1, usingDof, x, y, stime, sdx, sdy, D, u, v);
 			hit_colour(g, gi, m, u, v, occl, occl_flags);
-			occl[6] = ozv;
+			occl[6] = (TRANSP && fp.midpoint_store) ? st.hitz[sidx] : ozv;
 		}
 		int nf = 0;
 		bool valid = w >= 0;
@@ -677,8 +698,8 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 				for (int q = 0; q < 6; ++q) occl[q] = 0.0f;
 			if (fp.depth_filter == 1) occl[6] = (float)(0.5 * ((double)occl[6] + (double)ozv));
 		}
-		st.a[sidx] = make_float4(occl[0], occl[1], occl[2], occl[6]);
-		st.b[sidx] = make_float4(occl[3], occl[4], occl[5], valid ? 1.0f : 0.0f);
+		st.a[aidx] = make_float4(occl[0], occl[1], occl[2], occl[6]);
+		st.b[aidx] = make_float4(occl[3], occl[4], occl[5], valid ? 1.0f : 0.0f);
 		if (st.winner) st.winner[sidx] = w;
 		if (st.occlz) st.occlz[sidx] = ozv;
 		if (st.nfrag) st.nfrag[sidx] = nf;
