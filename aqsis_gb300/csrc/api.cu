@@ -339,7 +339,7 @@ struct aqh_ctx {
 	// device buffers
 	DevBuf d_cu, d_cv, d_nkeys, d_flags, d_tbase, d_pbase, d_cbase, d_mpbase, d_times, d_culled, d_P, d_Ci, d_Oi;
 	DevBuf d_mpcount;
-	DevBuf d_rect, d_minz, d_strips, d_stcount, d_stoffset, d_stlist;
+	DevBuf d_rect, d_minz, d_strips, d_stcount, d_stoffset, d_stlist, d_idgrid;
 	DevBuf d_sa, d_sb, d_win, d_oz, d_nf, d_hz;
 	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err;
 	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb;
@@ -879,6 +879,8 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	P.nctas = std::max(1, std::min(fp.ntx * fp.nty, nsm * sample_static_ctas_per_sm(pool.capacity > 0)));
 	P.fp = fp;
 	P.g = g;
+	AQH_TRY(ctx->d_idgrid.ensure(sizeof(int32_t) * (size_t)((P.nmps + 255) / 256 + 1)), "alloc id table");
+	P.g.id_grid = ctx->d_idgrid.as<int32_t>();
 	return AQH_OK;
 }
 
@@ -898,6 +900,7 @@ static aqh_status enqueue_frame(aqh_ctx* ctx, RenderPlan& P, bool batched, bool 
 	};
 	if (timing) mark(ctx->ev[0]);
 	if (P.g.ngrids > 0) {
+		launch_id_grid(P.g, P.nmps, const_cast<int32_t*>(P.g.id_grid), s);
 		launch_grid_rects(fp, P.g, P.bb, s);
 		launch_st_count(fp, P.g, P.bb, s);
 		launch_scan_i32(P.bb.st_count, P.bb.st_offset, P.nst * P.bb.nranges, nullptr, s);
@@ -951,6 +954,7 @@ static aqh_status render_plain(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 	cudaEventRecord(ctx->ev[0], s);
 	int32_t total = 0;
 	if (P.g.ngrids > 0) {
+		launch_id_grid(P.g, P.nmps, const_cast<int32_t*>(P.g.id_grid), s);
 		launch_grid_rects(fp, P.g, P.bb, s);
 		launch_st_count(fp, P.g, P.bb, s);
 		launch_scan_i32(P.bb.st_count, P.bb.st_offset, P.nst * P.bb.nranges, nullptr, s);

@@ -66,6 +66,7 @@ struct GridsDev {
 	const float4* Ci;
 	const float4* Oi;
 	const uint8_t* culled;   // per global micropolygon id, may be null
+	const int32_t* id_grid;  // grid holding micropolygon id k * 256, for each k; may be null
 };
 
 // Sample pattern caches (aqh_samples) in device memory.
@@ -137,6 +138,7 @@ struct RenderPlan {
 
 // Kernel launchers (implemented in the .cu files).
 void launch_grid_rects(const FrameParams& fp, const GridsDev& g, const BinBuffers& b, cudaStream_t s);
+void launch_id_grid(const GridsDev& g, int64_t nmps, int32_t* table, cudaStream_t s);
 void launch_st_count(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);
 void launch_scan_i32(const int32_t* in, int32_t* out, int n, int32_t* scratch, cudaStream_t s);
 void launch_st_write(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);

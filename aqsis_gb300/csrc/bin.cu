@@ -220,6 +220,21 @@ __global__ void scan_i32_kernel(const int32_t* in, int32_t* out, int n) {
 	if (threadIdx.x == 0) out[n] = carry;
 }
 
+// Lookup table from micropolygon id to grid: entry k is the grid holding id
+// k * 256 (thread per grid writes the entries whose id falls in it).
+__global__ void id_grid_kernel(GridsDev g, int64_t nmps, int32_t* table) {
+	const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+	if (gi >= g.ngrids) return;
+	const int64_t s = g.mpbase[gi];
+	const int64_t e = (gi + 1 < g.ngrids) ? g.mpbase[gi + 1] : nmps;
+	for (int64_t k = (s + 255) >> 8; (k << 8) < e; ++k) table[k] = gi;
+}
+
+void launch_id_grid(const GridsDev& g, int64_t nmps, int32_t* table, cudaStream_t s) {
+	if (g.ngrids == 0) return;
+	id_grid_kernel<<<(g.ngrids + 255) / 256, 256, 0, s>>>(g, nmps, table);
+}
+
 void launch_grid_rects(const FrameParams& fp, const GridsDev& g, const BinBuffers& b, cudaStream_t s) {
 	if (g.ngrids == 0) return;
 	const int wpb = kBlock / 32;

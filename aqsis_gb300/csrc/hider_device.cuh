@@ -79,6 +79,21 @@ struct HitCoeffs {
 	bool linear;
 };
 
+// CqInvBilinear's "almost rectangular" test `irregularity < 1e-2*patchSize`
+// (bilinear.h:271-274), evaluated in double like the reference.  FP64 issues
+// slowly on this GPU, so clear cases are decided in float: 0.01f * patch is
+// within 2^-22 relative of the double product for normal values, far inside
+// the 1e-5 margins, and everything else (near ties, zeros, denormals, inf,
+// NaN) takes the double comparison.
+__device__ __forceinline__ bool linear_test(float irr, float patch) {
+	const float b = 0.01f * patch;
+	if (b >= 1e-30f && b <= 1e30f && irr >= 0.0f) {
+		if (irr < b * 0.99999f) return true;
+		if (irr > b * 1.00001f) return false;
+	}
+	return static_cast<double>(irr) < 1e-2 * static_cast<double>(patch);
+}
+
 __device__ __forceinline__ void hit_setup(const V3f p[4], int code, HitCoeffs& h) {
 	h.z[0] = p[0].z; h.z[1] = p[1].z; h.z[2] = p[2].z; h.z[3] = p[3].z;
 	// setVertices(A, B, C, D) with A=p0, B=p1, C=p2, D=p3
@@ -90,7 +105,7 @@ __device__ __forceinline__ void hit_setup(const V3f p[4], int code, HitCoeffs& h
 	h.g_y = ((-h.e_y) - p[2].y) + p[3].y;
 	float patch = amax(amax(fabsf(h.f_x), fabsf(h.f_y)), amax(fabsf(h.e_x), fabsf(h.e_y)));
 	float irr = amax(fabsf(h.g_x), fabsf(h.g_y));
-	h.linear = static_cast<double>(irr) < 1e-2 * static_cast<double>(patch);
+	h.linear = linear_test(irr, patch);
 	// reorder by the vertex code (selects keep the points in registers)
 	auto pick = [&](int k) -> V3f { return k == 0 ? p[0] : (k == 1 ? p[1] : (k == 2 ? p[2] : p[3])); };
 	V3f q[4] = {pick((code >> 2) & 3), pick((code >> 4) & 3), pick((code >> 6) & 3), pick(code & 3)};

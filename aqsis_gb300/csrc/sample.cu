@@ -421,9 +421,8 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 			const int px = tpx0 + lx, py = tpy0 + ly;
 			const bool valid = s < tsamp && px < tpx1 && py < tpy1;
 			const int sn = si / fp.xs, smm = si - sn * fp.xs;
-			float x = 0.0f, y = 0.0f, oz = -FLT_MAX, hz = FLT_MAX;
+			float x = 0.0f, y = 0.0f, oz = -FLT_MAX;
 			int w = -1, fh = -1;
-			long long sidx = 0;
 			if (valid) {
 				const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
 				const long long pat = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
@@ -433,8 +432,6 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 				oz = sm.soz[s];
 				w = sm.swin[s];
 				if (TRANSP) fh = fhead[s];
-				sidx = pix * spp + si;
-				if (TRANSP && fp.midpoint_store && w >= 0) hz = st.hitz[sidx];
 			}
 			float gmax = warp_max_f(oz);
 #pragma unroll 1
@@ -470,12 +467,14 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 								if (TRANSP && fp.midpoint_store) {
 									// midpoint filter with a z display (bucketprocessor.cpp:1502-1530):
 									// occlZ follows the second-nearest opaque depth, the hit the nearest
-									const float hp = (w >= 0) ? hz : FLT_MAX;
+									const long long hx =
+									    ((long long)(py - fp.sy0) * fp.sw + (px - fp.sx0)) * spp + si;
+									const float hp = (w >= 0) ? st.hitz[hx] : FLT_MAX;
 									if (hp < D) {
 										oz = D;
 									} else {
 										oz = hp;
-										hz = D;
+										st.hitz[hx] = D;
 										w = r.id;
 									}
 								} else {
@@ -509,7 +508,6 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 				sm.soz[s] = oz;
 				sm.swin[s] = w;
 				if (TRANSP) fhead[s] = fh;
-				if (TRANSP && fp.midpoint_store && w >= 0) st.hitz[sidx] = hz;
 			}
 			wmax = fmaxf(wmax, gmax);
 		}
@@ -538,13 +536,12 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 	}
 
 	// ---- resolve: colours of the occluding hits, Combine of fragment lists ----
-	// (consecutive threads take consecutive pixels of one sample index: the
-	// sample store is sample-major)
+	// (consecutive threads take the samples of one pixel, whose fragments the
+	// same warp allocated together; the sample store is sample-major)
 	const long long npix = (long long)fp.sw * fp.sh;
-	for (int q = t; q < tsamp; q += kThreadsS) {
-		const int si = q / tpix;
-		const int pl = q - si * tpix;
-		const int s = pl * spp + si;
+	for (int s = t; s < tsamp; s += kThreadsS) {
+		const int pl = s / spp;
+		const int si = s - pl * spp;
 		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 		if (px >= tpx1 || py >= tpy1) continue;
 		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
@@ -578,6 +575,12 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 // would see, so it only skips what the reference skips.
 constexpr int kSlotsO = 192;
 
+// Division of k < 2^16 by 1 <= d < 2^16 with a multiply: m = ceil(2^32 / d)
+// makes floor(k * m / 2^32) exact (the error k * (m - 2^32/d) / 2^32 < 2^-16 <
+// 1/d); d = 1 has no 32-bit m and is passed through.
+__device__ __forceinline__ uint32_t div_magic(int d) { return d > 1 ? 0xffffffffu / (uint32_t)d + 1u : 0u; }
+__device__ __forceinline__ int div_small(int k, int d, uint32_t m) { return d > 1 ? (int)__umulhi((uint32_t)k, m) : k; }
+
 __device__ __forceinline__ unsigned long long depth_key(float z, int w) {
 	const uint32_t u = __float_as_uint(z);
 	const uint32_t o = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
@@ -595,7 +598,7 @@ struct SmemO {
 	RecS rec[kSlotsO];
 	int2 pend[kSlotsO];
 	int pref[kSlotsO + 1];                  // running count of (candidate, sample) tests
-	int rng[kSlotsO][3];                    // tests in the first column, the first row, and per row
+	int rng[kSlotsO][4];                    // tests in the first column, the first row, per row; divisor magic
 	int qgrid[kThreadsS];
 	int qcum[kThreadsS + 1];
 	int qsub[kThreadsS];
@@ -637,6 +640,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 	const int st_idx = (ty / fp.st_tiles) * fp.nstx + (tx / fp.st_tiles);
 	const int t = threadIdx.x;
 	const int spp = fp.spp, xs = fp.xs, ys = fp.ys;
+	const uint32_t mxs = div_magic(xs), mys = div_magic(ys);
 	const int tpix = fp.tile_w * fp.tile_h;
 	const int tsamp = tpix * spp;
 	const int nflagw = (tsamp + 31) >> 5;
@@ -699,6 +703,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 			sm.rng[t][0] = cx0;
 			sm.rng[t][1] = cy0;
 			sm.rng[t][2] = totx;
+			sm.rng[t][3] = (int)div_magic(totx);
 		}
 		int total;
 		const int pre = block_excl_sum(sm.warp_tot, ntests, total);
@@ -715,24 +720,27 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 			const RecS& r = sm.rec[lo];
 			const int k = p - sm.pref[lo];
 			const int cx0 = sm.rng[lo][0], cy0 = sm.rng[lo][1], totx = sm.rng[lo][2];
+			const uint32_t mtot = (uint32_t)sm.rng[lo][3];
 			const int sX = max(r.px0, tpx0), sY = max(r.py0, tpy0);
-			const int ky = k / totx, kx = k - ky * totx;
+			const int ky = div_small(k, totx, mtot), kx = k - ky * totx;
 			int px, m, py, n;
 			if (kx < cx0) {
 				px = sX;
 				m = ((sX == r.px0) ? r.im : 0) + kx;
 			} else {
 				const int q = kx - cx0;
-				px = sX + 1 + q / xs;
-				m = q - (q / xs) * xs;
+				const int qd = div_small(q, xs, mxs);
+				px = sX + 1 + qd;
+				m = q - qd * xs;
 			}
 			if (ky < cy0) {
 				py = sY;
 				n = ((sY == r.py0) ? r.in_ : 0) + ky;
 			} else {
 				const int q = ky - cy0;
-				py = sY + 1 + q / ys;
-				n = q - (q / ys) * ys;
+				const int qd = div_small(q, ys, mys);
+				py = sY + 1 + qd;
+				n = q - qd * ys;
 			}
 			const int si = n * xs + m;
 			const int pl = (py - tpy0) * fp.tile_w + (px - tpx0);

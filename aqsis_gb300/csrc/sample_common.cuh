@@ -93,8 +93,15 @@ __device__ __forceinline__ void hit_colour(const GridsDev& g, int gi, int m, flo
 	flg = ((gflags & 2) ? 1 : 0) | ((gflags & 4) ? 2 : 0);
 }
 
-// Grid owning a global micropolygon id (binary search over first ids).
+// Grid owning a global micropolygon id: from the id table when there is one,
+// else by binary search over the grids' first ids.
 __device__ __forceinline__ int grid_of(const GridsDev& g, int id) {
+	if (g.id_grid) {
+		// the grid holding id & ~255, then forward over grids that start later
+		int gi = __ldg(g.id_grid + (id >> 8));
+		while (gi + 1 < g.ngrids && __ldg(g.mpbase + gi + 1) <= id) ++gi;
+		return gi;
+	}
 	int lo = 0, hi = g.ngrids - 1;
 	while (lo < hi) {
 		const int mid = (lo + hi + 1) >> 1;

@@ -175,7 +175,11 @@ __device__ void load_mb_record(const FrameParams& fp, const GridsDev& g, int gi,
 		for (int k = 1; k < nk; ++k)
 			for (int c = 0; c < 3; ++c) { r.bmn[c] = amin(r.bmn[c], r.kbmn[k][c]); r.bmx[c] = amax(r.bmx[c], r.kbmx[k][c]); }
 	}
-	if (fp.use_dof) {
+	if (!fp.use_dof) {
+		// no lens offsets: a static micropolygon is tested at its own vertices
+		for (int q = 0; q < 4; ++q) r.cocm[q][0] = r.cocm[q][1] = 0.0f;
+		r.cocmin[0] = r.cocmin[1] = r.cocmax[0] = r.cocmax[1] = 0.0f;
+	} else {
 		if (nk == 1) {
 			// CacheHitTestValues with DoF (micropolygon.cpp:1409-1422)
 			for (int q = 0; q < 4; ++q) {
@@ -207,6 +211,96 @@ __device__ void load_mb_record(const FrameParams& fp, const GridsDev& g, int gi,
 			r.cocmax[1] = amax(c1.y, c2.y);
 		}
 	}
+}
+
+// Record of micropolygon m of grid gi with its occluding flag
+// (SqMpgSampleInfo::isOpaque, micropolygon.cpp:1477-1529) and global id.
+__device__ __forceinline__ void build_mb_record(const FrameParams& fp, const GridsDev& g, int gi, int m, MbRec& rr) {
+	load_mb_record(fp, g, gi, m, rr);
+	const int gflags = __ldg(g.flags + gi);
+	bool opaque = true;
+	const bool smooth = (gflags & 1) != 0;
+	if (!(gflags & 8) && g.Oi) {
+		const int cu = __ldg(g.cu + gi);
+		const int iv = m / cu, iu = m - iv * cu;
+		const int index = iv * (cu + 1) + iu;
+		const long long cb = __ldg(g.cbase + gi);
+		const int vi[4] = {index, index + 1, index + cu + 1, index + cu + 2};
+		for (int q = 0; q < (smooth ? 4 : 1); ++q) {
+			const float4 o = __ldg(g.Oi + cb + vi[q]);
+			opaque = opaque && (o.x >= 1.0f && o.y >= 1.0f && o.z >= 1.0f);
+		}
+	}
+	rr.bits = (opaque || (gflags & 4)) ? 2 : 0;
+	rr.id = (int)(__ldg(g.mpbase + gi) + m);
+	rr.grid = gi;
+}
+
+// Position, time, lens offset and lens stratum of sample j of pixel (px, py)
+// (CqImagePixel::setSamples, imagepixel.cpp:334-359: the lens offset of
+// sample j is the one whose shuffled index is j).
+__device__ __forceinline__ void mb_sample_attrs(const FrameParams& fp, const SamplerDev& smp, int px, int py, int j,
+                                                long long pix, float& x, float& y, float& stime, float& sdx,
+                                                float& sdy, int& kinv) {
+	const int spp = fp.spp;
+	const long long pp = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
+	const long long tp = smp.time_index ? (long long)__ldg(smp.time_index + pix) : pix;
+	const long long dp = smp.dof_index ? (long long)__ldg(smp.dof_index + pix) : pix;
+	const long long sp = smp.shuffle_index ? (long long)__ldg(smp.shuffle_index + pix) : pix;
+	const float2 o = __ldg(smp.pos + pp * spp + j);
+	x = (float)px + o.x;
+	y = (float)py + o.y;
+	const float tt = smp.time ? __ldg(smp.time + tp * spp + j) : 0.0f;
+	stime = (fp.shutter_close - fp.shutter_open) * tt + fp.shutter_open;
+	kinv = j;
+	if (smp.shuffle)
+		for (int q = 0; q < spp; ++q)
+			if (__ldg(smp.shuffle + sp * spp + q) == j) kinv = q;
+	sdx = 0.0f;
+	sdy = 0.0f;
+	if (smp.dof) {
+		const float2 d = __ldg(smp.dof + dp * spp + kinv);
+		const float2 c = project_to_circle(-1.0f + 2.0f * d.x, -1.0f + 2.0f * d.y);
+		sdx = c.x;
+		sdy = c.y;
+	}
+}
+
+// Final value of one sample: the occluding hit's colour at its (u,v) --
+// the winner's hit test repeated at the sample's time and lens offset -- or
+// the Combine of its fragments; written to the sample store.
+template <bool TRANSP>
+__device__ __forceinline__ void mb_resolve(const FrameParams& fp, const GridsDev& g, const FragPool& pool,
+                                           const SampleStore& st, long long sidx, long long aidx, float x, float y,
+                                           float stime, float sdx, float sdy, float ozv, int w, int head) {
+	float occl[7] = {0, 0, 0, 0, 0, 0, 0};
+	int occl_flags = 0;
+	if (w >= 0) {
+		const int gi = grid_of(g, w);
+		const int m = w - (int)__ldg(g.mpbase + gi);
+		MbRec rr;
+		load_mb_record(fp, g, gi, m, rr);
+		float D, u, v;
+		mb_sample(fp, rr, rr.nkeys > 1, fp.use_dof != 0, x, y, stime, sdx, sdy, D, u, v);
+		hit_colour(g, gi, m, u, v, occl, occl_flags);
+		occl[6] = (TRANSP && fp.midpoint_store) ? st.hitz[sidx] : ozv;
+	}
+	int nf = 0;
+	bool valid = w >= 0;
+	if (TRANSP && head >= 0) {
+		nf = combine_fragments(fp, g, pool, head, w >= 0, ozv, occl, occl_flags);
+		valid = true;
+	}
+	if (nf == 0 && valid) {
+		if (occl_flags & 1)
+			for (int q = 0; q < 6; ++q) occl[q] = 0.0f;
+		if (fp.depth_filter == 1) occl[6] = (float)(0.5 * ((double)occl[6] + (double)ozv));
+	}
+	st.a[aidx] = make_float4(occl[0], occl[1], occl[2], occl[6]);
+	st.b[aidx] = make_float4(occl[3], occl[4], occl[5], valid ? 1.0f : 0.0f);
+	if (st.winner) st.winner[sidx] = w;
+	if (st.occlz) st.occlz[sidx] = ozv;
+	if (st.nfrag) st.nfrag[sidx] = nf;
 }
 
 constexpr int kThreadsM = 512;
@@ -299,6 +393,106 @@ __device__ Bnd sub_bound(const MbRec& r, const float* T, int b) {
 	return bound;
 }
 
+// Phase A of the motion blur / depth of field kernels: stream the
+// super-tile's grid list from the cursor (lp, r0, qtotal) and stage, in
+// insertion order, the micropolygons whose bound over the whole shutter --
+// grown by the largest circle of confusion in their depth range -- meets the
+// tile and passes AddMPG's crop cull.  Returns true when the list is
+// exhausted.
+template <int kSlots, class Smem>
+__device__ __forceinline__ bool stage_mb(const FrameParams& fp, const GridsDev& g, const BinBuffers& bb, Smem& sm,
+                                         int tpx0, int tpy0, int tpx1, int tpy1, int lend, int& lp, int& r0,
+                                         int& qtotal, int& npend) {
+	const int t = threadIdx.x;
+	const bool usingDof = fp.use_dof != 0;
+	while (npend < kSlots) {
+		if (r0 >= qtotal) {
+			if (lp >= lend) return true;
+			const int li = lp + t;
+			int gid = -1;
+			bool f = false;
+			if (li < lend) {
+				gid = bb.st_list[li];
+				const int4 rc = bb.grid_rect[gid];
+				f = rc.x < rc.y && rc.x < tpx1 && rc.y > tpx0 && rc.z < tpy1 && rc.w > tpy0;
+			}
+			const int nmp = f ? __ldg(g.cu + gid) * __ldg(g.cv + gid) : 0;
+			int total, sum;
+			const int pos = block_excl_scan(sm.warp_tot, f, total);
+			__syncthreads();
+			const int pre = block_excl_sum(sm.warp_tot, nmp, sum);
+			if (f) {
+				sm.qgrid[pos] = gid;
+				sm.qcum[pos] = pre;
+			}
+			if (t == 0) {
+				sm.qcum[total] = sum;
+				sm.qn = total;
+			}
+			__syncthreads();
+			qtotal = sm.qcum[sm.qn];
+			r0 = 0;
+			lp += kThreadsM;
+			continue;
+		}
+		const int p = r0 + t;
+		bool active = false;
+		int gid = 0, m = 0;
+		if (p < qtotal) {
+			int lo = 0, hi = sm.qn - 1;
+			while (lo < hi) {
+				const int mid = (lo + hi + 1) >> 1;
+				if (sm.qcum[mid] <= p) lo = mid; else hi = mid - 1;
+			}
+			gid = sm.qgrid[lo];
+			m = p - sm.qcum[lo];
+			const int cu = __ldg(g.cu + gid), nk = __ldg(g.nkeys + gid);
+			const long long nv = (long long)(cu + 1) * (__ldg(g.cv + gid) + 1);
+			const long long pb = __ldg(g.pbase + gid);
+			const int iv = m / cu, iu = m - iv * cu;
+			const int index = iv * (cu + 1) + iu;
+			float mnx = FLT_MAX, mny = FLT_MAX, mnz = FLT_MAX, mxx = -FLT_MAX, mxy = -FLT_MAX, mxz = -FLT_MAX;
+			for (int k = 0; k < nk; ++k) {
+				const long long kb = pb + k * nv + index;
+				const V3f a = ld3(g.P, kb), b = ld3(g.P, kb + 1), c = ld3(g.P, kb + cu + 1), d = ld3(g.P, kb + cu + 2);
+				mnx = amin(mnx, amin(amin(amin(a.x, b.x), c.x), d.x));
+				mny = amin(mny, amin(amin(amin(a.y, b.y), c.y), d.y));
+				mnz = amin(mnz, amin(amin(amin(a.z, b.z), c.z), d.z));
+				mxx = amax(mxx, amax(amax(amax(a.x, b.x), c.x), d.x));
+				mxy = amax(mxy, amax(amax(amax(a.y, b.y), c.y), d.y));
+				mxz = amax(mxz, amax(amax(amax(a.z, b.z), c.z), d.z));
+			}
+			const bool culled = g.culled && g.culled[__ldg(g.mpbase + gid) + m];
+			float gx = 0.0f, gy = 0.0f;
+			if (usingDof) {
+				const float2 c1 = coc(mnz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+				const float2 c2 = coc(mxz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+				gx = amax(c1.x, c2.x);
+				gy = amax(c1.y, c2.y);
+			}
+			// AddMPG (imagebuffer.cpp:514-539): DoF-grown bound against the crop cull window
+			const bool cropped = (mxx + gx) < fp.cull_x0 || (mxy + gy) < fp.cull_y0 || (mnx - gx) > fp.cull_x1 ||
+			                     (mny - gy) > fp.cull_y1;
+			// conservative pixel rectangle over every time slice and lens stratum
+			const int sX = max((int)floorf(mnx - gx) - 1, tpx0), eX = min(lceil_f(mxx + gx) + 1, tpx1);
+			const int sY = max((int)floorf(mny - gy) - 1, tpy0), eY = min(lceil_f(mxy + gy) + 1, tpy1);
+			active = !culled && !cropped && sX < eX && sY < eY;
+		}
+		int total;
+		const int rank = block_excl_scan(sm.warp_tot, active, total);
+		const int navail = kSlots - npend;
+		if (t == 0) sm.first_reject = kThreadsM;
+		__syncthreads();
+		if (active && rank == navail) sm.first_reject = t;
+		if (active && rank < navail) sm.pend[npend + rank] = make_int2(gid, m);
+		__syncthreads();
+		const int consumed = (total > navail) ? sm.first_reject : min(kThreadsM, qtotal - r0);
+		npend += min(total, navail);
+		r0 += consumed;
+	}
+	return false;
+}
+
 template <bool TRANSP>
 __global__ void __launch_bounds__(kThreadsM, 1)
 sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, SampleStore st, FragPool pool,
@@ -344,118 +538,16 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 	const int lend = (int)min((long long)bb.st_offset[(st_idx + 1) * bb.nranges], (long long)bb.list_capacity);
 	int lp = lbeg, r0 = 0, qtotal = 0, npend = 0;
 	for (;;) {
-		// ---- phase A: stage candidates in insertion order ----
-		bool exhausted = false;
-		while (npend < kSlotsM) {
-			if (r0 >= qtotal) {
-				if (lp >= lend) { exhausted = true; break; }
-				const int li = lp + t;
-				int gid = -1;
-				bool f = false;
-				if (li < lend) {
-					gid = bb.st_list[li];
-					const int4 rc = bb.grid_rect[gid];
-					f = rc.x < rc.y && rc.x < tpx1 && rc.y > tpx0 && rc.z < tpy1 && rc.w > tpy0;
-				}
-				int total;
-				const int pos = block_excl_scan(sm.warp_tot, f, total);
-				if (f) sm.qgrid[pos] = gid;
-				__syncthreads();
-				if (t == 0) {
-					int acc = 0;
-					for (int k = 0; k < total; ++k) {
-						sm.qcum[k] = acc;
-						const int q = sm.qgrid[k];
-						acc += __ldg(g.cu + q) * __ldg(g.cv + q);
-					}
-					sm.qcum[total] = acc;
-					sm.qn = total;
-				}
-				__syncthreads();
-				qtotal = sm.qcum[sm.qn];
-				r0 = 0;
-				lp += kThreadsM;
-				continue;
-			}
-			const int p = r0 + t;
-			bool active = false;
-			int gid = 0, m = 0;
-			if (p < qtotal) {
-				int lo = 0, hi = sm.qn - 1;
-				while (lo < hi) {
-					const int mid = (lo + hi + 1) >> 1;
-					if (sm.qcum[mid] <= p) lo = mid; else hi = mid - 1;
-				}
-				gid = sm.qgrid[lo];
-				m = p - sm.qcum[lo];
-				const int cu = __ldg(g.cu + gid), nk = __ldg(g.nkeys + gid);
-				const long long nv = (long long)(cu + 1) * (__ldg(g.cv + gid) + 1);
-				const long long pb = __ldg(g.pbase + gid);
-				const int iv = m / cu, iu = m - iv * cu;
-				const int index = iv * (cu + 1) + iu;
-				float mnx = FLT_MAX, mny = FLT_MAX, mnz = FLT_MAX, mxx = -FLT_MAX, mxy = -FLT_MAX, mxz = -FLT_MAX;
-				for (int k = 0; k < nk; ++k) {
-					const long long kb = pb + k * nv + index;
-					const V3f a = ld3(g.P, kb), b = ld3(g.P, kb + 1), c = ld3(g.P, kb + cu + 1), d = ld3(g.P, kb + cu + 2);
-					mnx = amin(mnx, amin(amin(amin(a.x, b.x), c.x), d.x));
-					mny = amin(mny, amin(amin(amin(a.y, b.y), c.y), d.y));
-					mnz = amin(mnz, amin(amin(amin(a.z, b.z), c.z), d.z));
-					mxx = amax(mxx, amax(amax(amax(a.x, b.x), c.x), d.x));
-					mxy = amax(mxy, amax(amax(amax(a.y, b.y), c.y), d.y));
-					mxz = amax(mxz, amax(amax(amax(a.z, b.z), c.z), d.z));
-				}
-				const bool culled = g.culled && g.culled[__ldg(g.mpbase + gid) + m];
-				float gx = 0.0f, gy = 0.0f;
-				if (usingDof) {
-					const float2 c1 = coc(mnz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
-					const float2 c2 = coc(mxz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
-					gx = amax(c1.x, c2.x);
-					gy = amax(c1.y, c2.y);
-				}
-				// AddMPG (imagebuffer.cpp:514-539): DoF-grown bound against the crop cull window
-				const bool cropped = (mxx + gx) < fp.cull_x0 || (mxy + gy) < fp.cull_y0 || (mnx - gx) > fp.cull_x1 ||
-				                     (mny - gy) > fp.cull_y1;
-				// conservative pixel rectangle over every time slice and lens stratum
-				const int sX = max((int)floorf(mnx - gx) - 1, tpx0), eX = min(lceil_f(mxx + gx) + 1, tpx1);
-				const int sY = max((int)floorf(mny - gy) - 1, tpy0), eY = min(lceil_f(mxy + gy) + 1, tpy1);
-				active = !culled && !cropped && sX < eX && sY < eY;
-			}
-			int total;
-			const int rank = block_excl_scan(sm.warp_tot, active, total);
-			const int navail = kSlotsM - npend;
-			if (t == 0) sm.first_reject = kThreadsM;
-			__syncthreads();
-			if (active && rank == navail) sm.first_reject = t;
-			if (active && rank < navail) sm.pend[npend + rank] = make_int2(gid, m);
-			__syncthreads();
-			const int consumed = (total > navail) ? sm.first_reject : min(kThreadsM, qtotal - r0);
-			npend += min(total, navail);
-			r0 += consumed;
-		}
+		// ---- phase A ----
+		const bool exhausted =
+		    stage_mb<kSlotsM>(fp, g, bb, sm, tpx0, tpy0, tpx1, tpy1, lend, lp, r0, qtotal, npend);
 		if (npend == 0) break;
 
 		// ---- records, one per thread ----
 		for (int slot = t; slot < npend; slot += kThreadsM) {
 			const int2 e = sm.pend[slot];
 			MbRec& rr = sm.rec[slot];
-			load_mb_record(fp, g, e.x, e.y, rr);
-			const int gflags = __ldg(g.flags + e.x);
-			bool opaque = true;
-			const bool smooth = (gflags & 1) != 0;
-			if (!(gflags & 8) && g.Oi) {
-				const int cu = __ldg(g.cu + e.x);
-				const int iv = e.y / cu, iu = e.y - iv * cu;
-				const int index = iv * (cu + 1) + iu;
-				const long long cb = __ldg(g.cbase + e.x);
-				const int vi[4] = {index, index + 1, index + cu + 1, index + cu + 2};
-				for (int q = 0; q < (smooth ? 4 : 1); ++q) {
-					const float4 o = __ldg(g.Oi + cb + vi[q]);
-					opaque = opaque && (o.x >= 1.0f && o.y >= 1.0f && o.z >= 1.0f);
-				}
-			}
-			rr.bits = (opaque || (gflags & 4)) ? 2 : 0;
-			rr.id = (int)(__ldg(g.mpbase + e.x) + e.y);
-			rr.grid = e.x;
+			build_mb_record(fp, g, e.x, e.y, rr);
 			float gx = 0.0f, gy = 0.0f;
 			if (usingDof) {
 				const float2 c1 = coc(rr.bmn[2], fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
@@ -480,35 +572,14 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 			const int j = s - pl * spp;
 			const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 			const bool valid = s < tsamp && px < tpx1 && py < tpy1;
-			float x = 0.0f, y = 0.0f, stime = 0.0f, sdx = 0.0f, sdy = 0.0f, oz = -FLT_MAX, hz = FLT_MAX;
+			float x = 0.0f, y = 0.0f, stime = 0.0f, sdx = 0.0f, sdy = 0.0f, oz = -FLT_MAX;
 			int w = -1, fh = -1, kinv = 0;
-			long long sidx = 0;
 			if (valid) {
 				const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
-				const long long pp = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
-				const long long tp = smp.time_index ? (long long)__ldg(smp.time_index + pix) : pix;
-				const long long dp = smp.dof_index ? (long long)__ldg(smp.dof_index + pix) : pix;
-				const long long sp = smp.shuffle_index ? (long long)__ldg(smp.shuffle_index + pix) : pix;
-				const float2 o = __ldg(smp.pos + pp * spp + j);
-				x = (float)px + o.x;
-				y = (float)py + o.y;
-				const float tt = smp.time ? __ldg(smp.time + tp * spp + j) : 0.0f;
-				stime = (closetime - opentime) * tt + opentime;
-				kinv = j;
-				if (smp.shuffle)
-					for (int q = 0; q < spp; ++q)
-						if (__ldg(smp.shuffle + sp * spp + q) == j) kinv = q;
-				if (smp.dof) {
-					const float2 d = __ldg(smp.dof + dp * spp + kinv);
-					const float2 c = project_to_circle(-1.0f + 2.0f * d.x, -1.0f + 2.0f * d.y);
-					sdx = c.x;
-					sdy = c.y;
-				}
+				mb_sample_attrs(fp, smp, px, py, j, pix, x, y, stime, sdx, sdy, kinv);
 				oz = sm.soz[s];
 				w = sm.swin[s];
 				if (TRANSP) fh = fhead[s];
-				sidx = pix * spp + j;
-				if (TRANSP && fp.midpoint_store && w >= 0) hz = st.hitz[sidx];
 			}
 			float gmax = warp_max_m(oz);
 #pragma unroll 1
@@ -590,12 +661,14 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 							if ((r.bits & 2) && cullable) {
 								if (TRANSP && fp.midpoint_store) {
 									// midpoint filter with a z display (bucketprocessor.cpp:1502-1530)
-									const float hp = (w >= 0) ? hz : FLT_MAX;
+									const long long hx =
+									    ((long long)(py - fp.sy0) * fp.sw + (px - fp.sx0)) * spp + j;
+									const float hp = (w >= 0) ? st.hitz[hx] : FLT_MAX;
 									if (hp < D) {
 										oz = D;
 									} else {
 										oz = hp;
-										hz = D;
+										st.hitz[hx] = D;
 										w = r.id;
 									}
 								} else {
@@ -628,7 +701,6 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 				sm.soz[s] = oz;
 				sm.swin[s] = w;
 				if (TRANSP) fhead[s] = fh;
-				if (TRANSP && fp.midpoint_store && w >= 0) st.hitz[sidx] = hz;
 			}
 		}
 		__syncthreads();
@@ -639,8 +711,496 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 	}
 
 	// ---- resolve: repeat the winner's hit test for its (u,v) ----
-	// (consecutive threads take consecutive pixels of one sample index: the
-	// sample store is sample-major)
+	// (opaque: consecutive threads take consecutive pixels of one sample index,
+	// as the sample store is sample-major; transparent: the samples of one
+	// pixel, whose fragments the same warp allocated together)
+	const long long npix = (long long)fp.sw * fp.sh;
+	for (int q = t; q < tsamp; q += kThreadsM) {
+		const int j = TRANSP ? q % spp : q / tpix;
+		const int pl = TRANSP ? q / spp : q - j * tpix;
+		const int s = pl * spp + j;
+		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
+		if (px >= tpx1 || py >= tpy1) continue;
+		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
+		const int w = sm.swin[s];
+		float x = 0.0f, y = 0.0f, stime = 0.0f, sdx = 0.0f, sdy = 0.0f;
+		int kinv = 0;
+		if (w >= 0) mb_sample_attrs(fp, smp, px, py, j, pix, x, y, stime, sdx, sdy, kinv);
+		mb_resolve<TRANSP>(fp, g, pool, st, pix * spp + j, (long long)j * npix + pix, x, y, stime, sdx, sdy,
+		                   sm.soz[s], w, TRANSP ? fhead[s] : -1);
+	}
+}
+
+
+// ---- opaque frames: parallel (slice, sample) tests with an ordered replay ----
+//
+// The order argument of the static opaque kernel (sample.cu) carries over:
+// RenderMPG_MBOrDof skips a (slice, sample) test when the slice's bound has
+// min.z > occlZ and keeps a hit only if D < occlZ, so for every hit with D
+// at or above its slice bound's min.z the winner is the least (D, insertion
+// order) whatever the order of visits.  Work items are (micropolygon, time
+// slice) pairs; each walks the pixels and samples RenderMPG_MBOrDof would
+// visit for that slice (the sample-index window without depth of field; with
+// depth of field every sample of the pixels covered by some lens stratum's
+// shifted bound, then the sample's own stratum) and folds hits into a 64-bit
+// shared-memory atomicMin.  Hits below their slice's min.z, NaN or zero
+// depths flag the sample for an in-order replay from the round's start.
+constexpr int kSlotsP = 128;
+constexpr int kSurvivors = 2048;
+
+__device__ __forceinline__ unsigned long long depth_key_m(float z, int w) {
+	const uint32_t u = __float_as_uint(z);
+	const uint32_t o = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+	return ((unsigned long long)o << 32) | (uint32_t)(w + 1);
+}
+__device__ __forceinline__ float key_depth_m(unsigned long long k) {
+	const uint32_t o = (uint32_t)(k >> 32);
+	return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+__device__ __forceinline__ int key_winner_m(unsigned long long k) { return (int)(uint32_t)k - 1; }
+
+// Shutter constants of RenderMPG_MBOrDof (bucketprocessor.cpp:1237-1246).
+struct Shutter {
+	float open, close, timePerSample;
+	bool fast;
+	int timeRanges;
+};
+
+__device__ __forceinline__ Shutter shutter_of(const FrameParams& fp) {
+	Shutter sh;
+	sh.open = fp.shutter_open;
+	sh.close = fp.shutter_close;
+	// isClose (math.h:174-182)
+	const float dclose = fabsf(sh.close - sh.open);
+	const float tol = 10 * FLT_EPSILON;
+	sh.fast = dclose <= tol * fabsf(sh.close) || dclose <= tol * fabsf(sh.open);
+	sh.timePerSample = sh.fast ? 0.0f : (float)fp.spp / (sh.close - sh.open);
+	sh.timeRanges = max(4, fp.spp);
+	return sh;
+}
+
+// Slice b of micropolygon r: its bound, time window and (without depth of
+// field) sample-index window.  False when the reference skips the slice.
+__device__ __forceinline__ bool mb_slice(const FrameParams& fp, const Shutter& sh, const MbRec& r, const float* T,
+                                         int div, float dt, int b, Bnd& B, float& time0, float& time1, int& j0,
+                                         int& j1) {
+	const bool moving = r.nkeys > 1;
+	j0 = 0;
+	j1 = fp.spp;
+	time0 = 0.0f;
+	time1 = 0.0f;
+	if (moving) {
+		B = sub_bound(r, T, b);
+		time0 = T[b] - dt;
+		time1 = (b != div - 1) ? (T[b + 1] - dt) : sh.close;
+		if (time1 < sh.open || time0 > sh.close) return false;
+		if (!fp.use_dof) {
+			int indexT0, indexT1;
+			if (sh.fast) {
+				indexT0 = 0;
+				indexT1 = fp.spp;
+			} else {
+				indexT0 = max(0, lfloor_f((time0 - sh.open) * sh.timePerSample));
+				indexT1 = lceil_f((time1 - sh.open) * sh.timePerSample);
+			}
+			if (indexT1 > fp.spp) indexT1 = fp.spp;
+			j0 = indexT0;
+			j1 = min(fp.spp, max(indexT1, indexT0 + 1));
+		}
+	} else {
+		B = Bnd{r.bmn[0], r.bmn[1], r.bmn[2], r.bmx[0], r.bmx[1], r.bmx[2]};
+	}
+	// Clipping defaults (FLT_EPSILON, FLT_MAX), options.cpp:296
+	return !(B.mnz > FLT_MAX || B.mxz < FLT_EPSILON);
+}
+
+// The bound of slice B as lens stratum k sees it (bucketprocessor.cpp:1299-1321).
+__device__ __forceinline__ Bnd stratum_bound(const FrameParams& fp, const Bnd& B, const float* dofb) {
+	const float2 c1 = coc(B.mnz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+	const float2 c2 = coc(B.mxz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+	const float maxCocX = amax(c1.x, c2.x), maxCocY = amax(c1.y, c2.y);
+	Bnd TB = B;
+	TB.mnx = B.mnx - dofb[2] * maxCocX;
+	TB.mxx = B.mxx - dofb[0] * maxCocX;
+	TB.mny = B.mny - dofb[3] * maxCocY;
+	TB.mxy = B.mxy - dofb[1] * maxCocY;
+	return TB;
+}
+
+// One (candidate, slice) item of the parallel pass: the slice's bound, time
+// and sample-index windows, the largest CoC of its depth range and the tile
+// pixels some lens stratum's shifted bound covers (all strata shift by the
+// same CoC, so the union takes the extreme shifts).  False when the
+// reference skips the slice or no covered pixel is in the tile.
+struct MbItem {
+	Bnd B;
+	float time0, time1, maxCocX, maxCocY;
+	int j0, j1, sX, eX, sY, eY;
+};
+
+__device__ __forceinline__ bool mb_item(const FrameParams& fp, const Shutter& sh, const MbRec& r,
+                                        const float* slice_times, int b, const float* dext, int tpx0, int tpy0,
+                                        int tpx1, int tpy1, MbItem& it) {
+	const bool moving = r.nkeys > 1;
+	const int div = moving ? motion_divisions(r, sh.timeRanges) : 1;
+	const float dt = (sh.close - sh.open) / div;
+	const float* T = slice_times + (div * (div - 1)) / 2;
+	if (!mb_slice(fp, sh, r, T, div, dt, b, it.B, it.time0, it.time1, it.j0, it.j1)) return false;
+	const Bnd& B = it.B;
+	Bnd U = B;
+	it.maxCocX = 0.0f;
+	it.maxCocY = 0.0f;
+	if (fp.use_dof) {
+		const float2 c1 = coc(B.mnz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+		const float2 c2 = coc(B.mxz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+		it.maxCocX = amax(c1.x, c2.x);
+		it.maxCocY = amax(c1.y, c2.y);
+		U.mnx = B.mnx - dext[2] * it.maxCocX;
+		U.mxx = B.mxx - dext[0] * it.maxCocX;
+		U.mny = B.mny - dext[3] * it.maxCocY;
+		U.mxy = B.mxy - dext[1] * it.maxCocY;
+	}
+	if (!(U.mnx <= U.mxx && U.mny <= U.mxy)) return false;  // empty or NaN
+	it.sX = (int)fmaxf(floorf(U.mnx), (float)tpx0);
+	it.eX = (int)fminf(ceilf(U.mxx), (float)tpx1);
+	it.sY = (int)fmaxf(floorf(U.mny), (float)tpy0);
+	it.eY = (int)fminf(ceilf(U.mxy), (float)tpy1);
+	return it.sX < it.eX && it.sY < it.eY && it.j0 < it.j1;
+}
+
+struct SmemP {
+	unsigned long long key[kTileSampM];   // occluding hit of each tile sample (depth_key_m)
+	unsigned long long prev[kTileSampM];  // ... at the start of the round
+	MbRec rec[kSlotsP];
+	float2 sd[kTileSampM];                // lens offset of each tile sample
+	float stime[kTileSampM];              // time of each tile sample
+	float dofb[AQH_MAX_SPP_DEV][4];
+	int2 pend[kSlotsP];
+	int pref[kSlotsP + 1];                // running count of (candidate, slice) items
+	int qgrid[kThreadsM];
+	int qcum[kThreadsM + 1];
+	int patidx[kTilePixM];
+	int warp_tot[32];
+	int first_reject;
+	int qn;
+	float dext[4];                        // min dofb[.][0], min [.][1], max [.][2], max [.][3]
+	uint32_t surv[kSurvivors];            // kept (candidate, slice) items: slot | slice << 8
+	int nsurv;
+	uint32_t wq[kWarpsM][64];             // per-warp queue of (candidate, sample) tests
+	float wz[kWarpsM][64];                // ... with their slice bound's min z
+	uint32_t flag[kTileSampM / 32];
+	uint32_t sticky[kTileSampM / 32];
+	uint8_t kinv[kTileSampM];             // lens stratum of each tile sample
+};
+
+// One (slice, sample) test as RenderMPG_MBOrDof makes it, given occlZ:
+// returns true with D when the sample is hit and not skipped by early-z.
+__device__ __forceinline__ bool mb_slice_test(const FrameParams& fp, const MbRec& r, const Bnd& B, bool moving,
+                                              float time0, float time1, const float* dofb_k, int px, int py,
+                                              float x, float y, float stime, float sdx, float sdy, float oz,
+                                              float& D) {
+	if (moving && (stime < time0 || stime > time1)) return false;
+	const Bnd TB = fp.use_dof ? stratum_bound(fp, B, dofb_k) : B;
+	if (px < (int)floorf(TB.mnx) || px >= lceil_f(TB.mxx) || py < (int)floorf(TB.mny) || py >= lceil_f(TB.mxy))
+		return false;
+	if ((x < TB.mnx || x > TB.mxx) || (y < TB.mny || y > TB.mxy)) return false;
+	if (B.mnz > oz) return false;
+	float u, v;
+	return mb_sample(fp, r, moving, fp.use_dof != 0, x, y, stime, sdx, sdy, D, u, v);
+}
+
+__global__ void __launch_bounds__(kThreadsM, 1)
+sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, SampleStore st,
+                  const float4* dof_bounds, const float* slice_times) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	SmemP& sm = *reinterpret_cast<SmemP*>(smem_raw);
+	const int tile = blockIdx.x;
+	const int tx = tile % fp.ntx, ty = tile / fp.ntx;
+	const int tpx0 = fp.sx0 + tx * fp.tile_w, tpy0 = fp.sy0 + ty * fp.tile_h;
+	const int tpx1 = min(tpx0 + fp.tile_w, fp.sx0 + fp.sw), tpy1 = min(tpy0 + fp.tile_h, fp.sy0 + fp.sh);
+	const int st_idx = (ty / fp.st_tiles) * fp.nstx + (tx / fp.st_tiles);
+	const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+	const int spp = fp.spp;
+	const int tpix = fp.tile_w * fp.tile_h;
+	const int tsamp = tpix * spp;
+	const int nflagw = (tsamp + 31) >> 5;
+	const bool usingDof = fp.use_dof != 0;
+	const Shutter sh = shutter_of(fp);
+	const unsigned long long kinit = depth_key_m(FLT_MAX, -1);
+
+	for (int i = t; i < spp; i += kThreadsM) {
+		const float4 b = dof_bounds[i];
+		sm.dofb[i][0] = b.x; sm.dofb[i][1] = b.y; sm.dofb[i][2] = b.z; sm.dofb[i][3] = b.w;
+	}
+	for (int i = t; i < tsamp; i += kThreadsM) {
+		sm.key[i] = kinit;
+		sm.prev[i] = kinit;
+		sm.kinv[i] = (uint8_t)(i % spp);
+	}
+	for (int i = t; i < kTileSampM / 32; i += kThreadsM) {
+		sm.flag[i] = 0u;
+		sm.sticky[i] = 0u;
+	}
+	if (t == 0) {
+		sm.qn = 0;
+		sm.qcum[0] = 0;
+	}
+	__syncthreads();
+	// pattern of each pixel and the lens stratum of each sample (the shuffle
+	// table inverted: the stratum of sample j is the q with shuffle[q] == j)
+	for (int pl = t; pl < tpix; pl += kThreadsM) {
+		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
+		int pat = 0;
+		if (px < tpx1 && py < tpy1) {
+			const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
+			pat = smp.pos_index ? (int)__ldg(smp.pos_index + pix) : (int)pix;
+			if (smp.shuffle) {
+				const long long sp = smp.shuffle_index ? (long long)__ldg(smp.shuffle_index + pix) : pix;
+				for (int q = 0; q < spp; ++q) {
+					const int j = __ldg(smp.shuffle + sp * spp + q);
+					if (j >= 0 && j < spp) sm.kinv[pl * spp + j] = (uint8_t)q;
+				}
+			}
+		}
+		sm.patidx[pl] = pat;
+	}
+	if (t < 32) {
+		float a0 = FLT_MAX, a1 = FLT_MAX, a2 = -FLT_MAX, a3 = -FLT_MAX;
+		for (int k = lane; k < spp; k += 32) {
+			a0 = fminf(a0, sm.dofb[k][0]);
+			a1 = fminf(a1, sm.dofb[k][1]);
+			a2 = fmaxf(a2, sm.dofb[k][2]);
+			a3 = fmaxf(a3, sm.dofb[k][3]);
+		}
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			a0 = fminf(a0, __shfl_xor_sync(0xffffffffu, a0, o));
+			a1 = fminf(a1, __shfl_xor_sync(0xffffffffu, a1, o));
+			a2 = fmaxf(a2, __shfl_xor_sync(0xffffffffu, a2, o));
+			a3 = fmaxf(a3, __shfl_xor_sync(0xffffffffu, a3, o));
+		}
+		if (lane == 0) {
+			sm.dext[0] = a0;
+			sm.dext[1] = a1;
+			sm.dext[2] = a2;
+			sm.dext[3] = a3;
+		}
+	}
+	__syncthreads();
+	// time and lens offset of each sample
+	for (int s = t; s < tsamp; s += kThreadsM) {
+		const int pl = s / spp, j = s - pl * spp;
+		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
+		float tm = 0.0f, dx = 0.0f, dy = 0.0f;
+		if (px < tpx1 && py < tpy1) {
+			const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
+			const long long tp = smp.time_index ? (long long)__ldg(smp.time_index + pix) : pix;
+			const float tt = smp.time ? __ldg(smp.time + tp * spp + j) : 0.0f;
+			tm = (sh.close - sh.open) * tt + sh.open;
+			if (smp.dof) {
+				const long long dp = smp.dof_index ? (long long)__ldg(smp.dof_index + pix) : pix;
+				const float2 d = __ldg(smp.dof + dp * spp + sm.kinv[s]);
+				const float2 c = project_to_circle(-1.0f + 2.0f * d.x, -1.0f + 2.0f * d.y);
+				dx = c.x;
+				dy = c.y;
+			}
+		}
+		sm.stime[s] = tm;
+		sm.sd[s] = make_float2(dx, dy);
+	}
+	__syncthreads();
+
+	const int lbeg = bb.st_offset[st_idx * bb.nranges];
+	const int lend = (int)min((long long)bb.st_offset[(st_idx + 1) * bb.nranges], (long long)bb.list_capacity);
+	int lp = lbeg, r0 = 0, qtotal = 0, npend = 0;
+	for (;;) {
+		const bool exhausted = stage_mb<kSlotsP>(fp, g, bb, sm, tpx0, tpy0, tpx1, tpy1, lend, lp, r0, qtotal, npend);
+		if (npend == 0) break;
+
+		// ---- records and (candidate, slice) items ----
+		int nitems = 0;
+		if (t < npend) {
+			const int2 e = sm.pend[t];
+			MbRec& rr = sm.rec[t];
+			build_mb_record(fp, g, e.x, e.y, rr);
+			nitems = (rr.nkeys > 1) ? motion_divisions(rr, sh.timeRanges) : 1;
+		}
+		int total;
+		const int pre = block_excl_sum(sm.warp_tot, nitems, total);
+		if (t < npend) sm.pref[t] = pre;
+		__syncthreads();
+
+		// ---- parallel pass over (candidate, slice) items ----
+		// Most items of a moving micropolygon lie outside the tile, so threads
+		// first keep the items whose pixel rectangle meets it (chunks of at
+		// most kSurvivors items); then a warp takes each kept item: lanes run
+		// the cheap tests of its (pixel, sample) pairs, pairs that pass queue
+		// up per warp, and every 32 of them take the full hit test together,
+		// one per lane.
+		for (int base = 0; base < total; base += kSurvivors) {
+			if (t == 0) sm.nsurv = 0;
+			__syncthreads();
+			for (int p = base + t; p < min(total, base + kSurvivors); p += kThreadsM) {
+				int lo = 0, hi = npend - 1;
+				while (lo < hi) {
+					const int mid = (lo + hi + 1) >> 1;
+					if (sm.pref[mid] <= p) lo = mid; else hi = mid - 1;
+				}
+				MbItem it;
+				if (mb_item(fp, sh, sm.rec[lo], slice_times, p - sm.pref[lo], sm.dext, tpx0, tpy0, tpx1, tpy1, it))
+					sm.surv[atomicAdd(&sm.nsurv, 1)] = (uint32_t)lo | ((uint32_t)(p - sm.pref[lo]) << 8);
+			}
+			__syncthreads();
+			const int nsurv = sm.nsurv;
+			uint32_t* wq = sm.wq[warp];
+			float* wz = sm.wz[warp];
+			int qn = 0;
+			auto drain = [&](int n) {
+				// hit tests of queue entries [0, n), one per lane
+				if (lane < n) {
+					const uint32_t e = wq[lane];
+					const int c = (int)(e & 0xffu), s = (int)(e >> 8);
+					const MbRec& r = sm.rec[c];
+					const int pl = s / spp, j = s - pl * spp;
+					const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
+					const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + j);
+					const float2 d = sm.sd[s];
+					float D, u, v;
+					if (mb_sample(fp, r, r.nkeys > 1, usingDof, (float)px + o.x, (float)py + o.y, sm.stime[s], d.x, d.y,
+					              D, u, v)) {
+						if (!(D >= wz[lane]) || D == 0.0f)
+							atomicOr(&sm.flag[s >> 5], 1u << (s & 31));
+						else
+							atomicMin(&sm.key[s], depth_key_m(D, r.id));
+					}
+				}
+				__syncwarp();
+			};
+			for (int k = warp; k < nsurv; k += kWarpsM) {
+				const uint32_t e = sm.surv[k];
+				const int c = (int)(e & 0xffu);
+				const MbRec& r = sm.rec[c];
+				MbItem it;
+				mb_item(fp, sh, r, slice_times, (int)(e >> 8), sm.dext, tpx0, tpy0, tpx1, tpy1, it);
+				const bool moving = r.nkeys > 1;
+				const Bnd& B = it.B;
+				const int w = it.eX - it.sX, nj = it.j1 - it.j0;
+				const int npairs = w * (it.eY - it.sY) * nj;
+				for (int q0 = 0; q0 < npairs; q0 += 32) {
+					const int q = q0 + lane;
+					bool pass = false;
+					int s = 0;
+					if (q < npairs) {
+						const int pxy = q / nj, j = it.j0 + (q - pxy * nj);
+						const int px = it.sX + pxy % w, py = it.sY + pxy / w;
+						const int pl = (py - tpy0) * fp.tile_w + (px - tpx0);
+						s = pl * spp + j;
+						pass = !(sm.flag[s >> 5] & (1u << (s & 31)));  // else replayed in order below
+						const float stime = sm.stime[s];
+						if (pass && moving) pass = !(stime < it.time0 || stime > it.time1);
+						if (pass) {
+							Bnd TB = B;
+							if (usingDof) {
+								const float* dk = sm.dofb[sm.kinv[s]];
+								TB.mnx = B.mnx - dk[2] * it.maxCocX;
+								TB.mxx = B.mxx - dk[0] * it.maxCocX;
+								TB.mny = B.mny - dk[3] * it.maxCocY;
+								TB.mxy = B.mxy - dk[1] * it.maxCocY;
+							}
+							const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + j);
+							const float x = (float)px + o.x, y = (float)py + o.y;
+							pass = !(px < (int)floorf(TB.mnx) || px >= lceil_f(TB.mxx) || py < (int)floorf(TB.mny) ||
+							         py >= lceil_f(TB.mxy)) &&
+							       !((x < TB.mnx || x > TB.mxx) || (y < TB.mny || y > TB.mxy)) &&
+							       !(B.mnz > key_depth_m(sm.prev[s]));
+						}
+					}
+					const uint32_t bal = __ballot_sync(0xffffffffu, pass);
+					if (pass) {
+						const int at = qn + __popc(bal & ((1u << lane) - 1u));
+						wq[at] = (uint32_t)c | ((uint32_t)s << 8);
+						wz[at] = B.mnz;
+					}
+					qn += __popc(bal);
+					__syncwarp();
+					if (qn >= 32) {
+						drain(32);
+						if (lane < qn - 32) {  // entries [32, qn) move to the front
+							wq[lane] = wq[32 + lane];
+							wz[lane] = wz[32 + lane];
+						}
+						__syncwarp();
+						qn -= 32;
+					}
+				}
+			}
+			drain(qn);
+			__syncthreads();
+		}
+		__syncthreads();
+		int anyf = 0;
+		for (int i = t; i < nflagw; i += kThreadsM) anyf |= (int)(sm.flag[i] != 0u);
+
+		// ---- ordered replay of flagged samples, one thread per sample ----
+		if (__syncthreads_or(anyf)) {
+			for (int s = t; s < tsamp; s += kThreadsM) {
+				if (!(sm.flag[s >> 5] & (1u << (s & 31)))) continue;
+				const int pl = s / spp, j = s - pl * spp;
+				const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
+				if (px >= tpx1 || py >= tpy1) continue;
+				const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + j);
+				const float x = (float)px + o.x, y = (float)py + o.y;
+				const float stime = sm.stime[s];
+				const float2 d = sm.sd[s];
+				const float* dk = sm.dofb[sm.kinv[s]];
+				float oz = key_depth_m(sm.prev[s]);
+				int w = key_winner_m(sm.prev[s]);
+				for (int c = 0; c < npend; ++c) {
+					const MbRec& r = sm.rec[c];
+					const bool moving = r.nkeys > 1;
+					const int div = moving ? motion_divisions(r, sh.timeRanges) : 1;
+					const float dt = (sh.close - sh.open) / div;
+					const float* T = slice_times + (div * (div - 1)) / 2;
+					int b0 = 0, b1 = 0;
+					if (moving) {
+						// slices whose window can hold the sample's time, in slice order
+						int blo = 0, bhi = div - 1;
+						while (blo < bhi) {
+							const int mid = (blo + bhi + 1) >> 1;
+							if (T[mid] - dt <= stime) blo = mid; else bhi = mid - 1;
+						}
+						b1 = blo;
+						b0 = b1;
+						while (b0 > 0 && (T[b0] - dt) >= stime) --b0;
+					}
+					for (int sb = b0; sb <= b1; ++sb) {
+						Bnd B;
+						float time0, time1;
+						int j0, j1;
+						if (!mb_slice(fp, sh, r, T, div, dt, sb, B, time0, time1, j0, j1)) continue;
+						if (j < j0 || j >= j1) continue;
+						float D;
+						if (!mb_slice_test(fp, r, B, moving, time0, time1, dk, px, py, x, y, stime, d.x, d.y, oz, D))
+							continue;
+						if (!(oz <= D)) {
+							oz = D;
+							w = r.id;
+						}
+					}
+				}
+				sm.key[s] = depth_key_m(oz, w);
+				if (oz != oz || oz == 0.0f) atomicOr(&sm.sticky[s >> 5], 1u << (s & 31));
+			}
+		}
+		__syncthreads();
+		for (int i = t; i < tsamp; i += kThreadsM) sm.prev[i] = sm.key[i];
+		for (int i = t; i < nflagw; i += kThreadsM) sm.flag[i] = sm.sticky[i];
+		__syncthreads();
+		npend = 0;
+		if (exhausted) break;
+	}
+
+	// ---- resolve (sample-major, see the lane kernel) ----
 	const long long npix = (long long)fp.sw * fp.sh;
 	for (int q = t; q < tsamp; q += kThreadsM) {
 		const int j = q / tpix;
@@ -649,60 +1209,11 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 		if (px >= tpx1 || py >= tpy1) continue;
 		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
-		const long long sidx = pix * spp + j;
-		const long long aidx = (long long)j * npix + pix;
-		const float ozv = sm.soz[s];
-		const int w = sm.swin[s];
-		float occl[7] = {0, 0, 0, 0, 0, 0, 0};
-		int occl_flags = 0;
-		if (w >= 0) {
-			const long long pp = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
-			const long long tp = smp.time_index ? (long long)__ldg(smp.time_index + pix) : pix;
-			const long long dp = smp.dof_index ? (long long)__ldg(smp.dof_index + pix) : pix;
-			const long long sp = smp.shuffle_index ? (long long)__ldg(smp.shuffle_index + pix) : pix;
-			const float2 o = __ldg(smp.pos + pp * spp + j);
-			const float x = (float)px + o.x, y = (float)py + o.y;
-			const float tt = smp.time ? __ldg(smp.time + tp * spp + j) : 0.0f;
-			const float stime = (closetime - opentime) * tt + opentime;
-			float sdx = 0.0f, sdy = 0.0f;
-			if (smp.dof) {
-				int kinv = j;
-				if (smp.shuffle)
-					for (int q = 0; q < spp; ++q)
-						if (__ldg(smp.shuffle + sp * spp + q) == j) kinv = q;
-				const float2 d = __ldg(smp.dof + dp * spp + kinv);
-				const float2 c = project_to_circle(-1.0f + 2.0f * d.x, -1.0f + 2.0f * d.y);
-				sdx = c.x;
-				sdy = c.y;
-			}
-			const int gi = grid_of(g, w);
-			const int m = w - (int)__ldg(g.mpbase + gi);
-			MbRec rr;
-			load_mb_record(fp, g, gi, m, rr);
-			float D, u, v;
-			mb_sample(fp, rr, rr.nkeys > 1, usingDof, x, y, stime, sdx, sdy, D, u, v);
-			hit_colour(g, gi, m, u, v, occl, occl_flags);
-			occl[6] = (TRANSP && fp.midpoint_store) ? st.hitz[sidx] : ozv;
-		}
-		int nf = 0;
-		bool valid = w >= 0;
-		if (TRANSP) {
-			const int head = fhead[s];
-			if (head >= 0) {
-				nf = combine_fragments(fp, g, pool, head, w >= 0, ozv, occl, occl_flags);
-				valid = true;
-			}
-		}
-		if (nf == 0 && valid) {
-			if (occl_flags & 1)
-				for (int q = 0; q < 6; ++q) occl[q] = 0.0f;
-			if (fp.depth_filter == 1) occl[6] = (float)(0.5 * ((double)occl[6] + (double)ozv));
-		}
-		st.a[aidx] = make_float4(occl[0], occl[1], occl[2], occl[6]);
-		st.b[aidx] = make_float4(occl[3], occl[4], occl[5], valid ? 1.0f : 0.0f);
-		if (st.winner) st.winner[sidx] = w;
-		if (st.occlz) st.occlz[sidx] = ozv;
-		if (st.nfrag) st.nfrag[sidx] = nf;
+		const unsigned long long kk = sm.key[s];
+		const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + j);
+		const float2 d = sm.sd[s];
+		mb_resolve<false>(fp, g, FragPool{}, st, pix * spp + j, (long long)j * npix + pix, (float)px + o.x,
+		                  (float)py + o.y, sm.stime[s], d.x, d.y, key_depth_m(kk), key_winner_m(kk), -1);
 	}
 }
 
@@ -721,14 +1232,13 @@ void launch_sample_mb(const FrameParams& fp, const GridsDev& g, const SamplerDev
 		sample_mb_kernel<true><<<ntiles, kThreadsM, sample_mb_smem(true), s>>>(fp, g, sm, b, st, pool, dof_bounds,
 		                                                                      slice_times);
 	else
-		sample_mb_kernel<false><<<ntiles, kThreadsM, sample_mb_smem(false), s>>>(fp, g, sm, b, st, pool, dof_bounds,
-		                                                                        slice_times);
+		sample_mbp_kernel<<<ntiles, kThreadsM, sizeof(SmemP), s>>>(fp, g, sm, b, st, dof_bounds, slice_times);
 }
 
 void configure_sample_mb_kernels() {
 	static bool configured = false;
 	if (configured) return;
-	cudaFuncSetAttribute(sample_mb_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sample_mb_smem(false));
+	cudaFuncSetAttribute(sample_mbp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemP));
 	cudaFuncSetAttribute(sample_mb_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sample_mb_smem(true));
 	configured = true;
 }

@@ -129,3 +129,32 @@ def motion_dof_small(seed=5, motion=20.0, dof=True, xs=6, ys=6, scale=0.04, tran
 def dof_only_small(seed=6, xs=4, ys=4, scale=0.04):
     sc = S.scaled(S.motion_dof_stream, scale, seed=seed, motion=None, dof=True, xs=xs, ys=ys)
     return sc
+
+
+def motion_mixed_small(seed=7, dof=False, xs=4, ys=4, scale=0.04):
+    """A motion-blurred frame whose grids alternate between moving and
+    static (one key), as a scene with a camera-fixed prop would give."""
+    sc = S.scaled(S.motion_dof_stream, scale, seed=seed, motion=20.0, dof=dof, xs=xs, ys=ys)
+    rng = np.random.default_rng(seed + 200)
+    fr = sc.frame
+    n = max(4, sc.grids.ngrids // 2)
+    moving = S.regular_grids(n, fr.width, fr.height, rng, motion=20.0)
+    still = S.regular_grids(n, fr.width, fr.height, rng)
+    parts = []
+    for k in range(0, n, 8):
+        parts.append(_take(moving, k, min(n, k + 8)))
+        parts.append(_take(still, k, min(n, k + 8)))
+    sc.grids = S.concat_grids(parts)
+    return sc
+
+
+def _take(g, a, b):
+    """Grids [a, b) of a packed stream as their own stream."""
+    nv = (g.cu.astype(np.int64) + 1) * (g.cv.astype(np.int64) + 1)
+    p0, p1 = int(g.pbase[a]), int(g.pbase[b - 1] + nv[b - 1] * g.nkeys[b - 1])
+    c0, c1 = int(g.cbase[a]), int(g.cbase[b - 1] + nv[b - 1])
+    t0 = int(g.tbase[a])
+    t1 = int(g.tbase[b - 1] + g.nkeys[b - 1]) if len(g.times) > 1 else 1
+    sub = S._pack(g.cu[a:b], g.cv[a:b], g.nkeys[a:b], g.flags[a:b], g.P[p0:p1], g.Ci[c0:c1], g.Oi[c0:c1],
+                  g.times[t0:t1], (g.tbase[a:b] - t0))
+    return sub

@@ -152,6 +152,12 @@ def test_dof_only(hider, oracle):
     compare(res, ref, exact_pixels=True)
 
 
+@pytest.mark.parametrize("dof", [False, True], ids=["motion", "motion_dof"])
+def test_motion_blur_with_static_grids(hider, oracle, dof):
+    res, ref = run_both(hider, oracle, SS.motion_mixed_small(seed=85, dof=dof))
+    compare(res, ref, exact_pixels=True)
+
+
 def test_motion_blur_transparent(hider, oracle):
     res, ref = run_both(hider, oracle, SS.motion_dof_small(seed=84, dof=False, xs=3, ys=3, transparent=True))
     compare(res, ref)
