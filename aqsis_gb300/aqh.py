@@ -248,6 +248,33 @@ class Hider:
                              kt, cl)
             mpbase += cu * cv
 
+    def submit_grids_host(self, g):
+        """Submit a whole packed scene.Grids in one aqh_submit_grids_host call
+        (the arrays are copied to the device at render time, so they must stay
+        alive until then; they are kept on the object)."""
+        L = self.L
+        if not getattr(L, "_packed_bound", False):
+            vp = C.c_void_p
+            L.aqh_submit_grids_host.argtypes = [vp, C.c_int] + [vp] * 8 + [C.c_size_t, vp, C.c_size_t, vp, vp,
+                                                                         C.c_size_t, vp, C.c_int64]
+            L.aqh_submit_grids_host.restype = C.c_int
+            L._packed_bound = True
+        keep = []
+
+        def a(x, dt):
+            x = np.ascontiguousarray(x, dt)
+            keep.append(x)
+            return x.ctypes.data
+        culled = a(g.culled, np.uint8) if g.culled is not None else None
+        self._check(L.aqh_submit_grids_host(self.ctx, g.ngrids, a(g.cu, np.int32), a(g.cv, np.int32),
+                                            a(g.nkeys, np.int32), a(g.flags, np.int32), a(g.pbase, np.int64),
+                                            a(g.cbase, np.int64), a(g.tbase, np.int32), a(g.times, np.float32),
+                                            int(g.times.size), a(g.P, np.float32), int(g.P.shape[0]),
+                                            a(g.Ci, np.float32), a(g.Oi, np.float32), int(g.Ci.shape[0]), culled,
+                                            g.micropolygons),
+                    "aqh_submit_grids_host")
+        self._packed_keep = keep
+
     def submit_grids_device(self, ngrids, d_cu, d_cv, d_nkeys, d_flags, d_pbase, d_cbase, d_tbase, d_times,
                             d_P, d_Ci, d_Oi, total_mps, d_culled=None):
         """Device-resident grids: every argument is a device pointer (int)."""

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <list>
 #include <vector>
 
 #include "../../include/aqh.h"
@@ -303,6 +304,11 @@ struct aqh_ctx {
 	int device = 0;
 	cudaStream_t stream = nullptr;
 	cudaEvent_t ev[6] = {};
+	// packed host grids: Ci/Oi go up on their own stream so the sampler, which
+	// reads only P, overlaps the copy; `ev_cioi` marks them resident
+	cudaStream_t cstream = nullptr;
+	cudaEvent_t ev_before_up = nullptr, ev_cioi = nullptr;
+	bool cioi_pending = false;
 	std::string err;
 	bool frame_open = false;
 	aqh_frame_desc desc{};
@@ -340,7 +346,7 @@ struct aqh_ctx {
 	DevBuf d_cu, d_cv, d_nkeys, d_flags, d_tbase, d_pbase, d_cbase, d_mpbase, d_times, d_culled, d_P, d_Ci, d_Oi;
 	DevBuf d_mpcount;
 	DevBuf d_rect, d_minz, d_strips, d_stcount, d_stoffset, d_stlist, d_idgrid;
-	DevBuf d_sa, d_sb, d_win, d_oz, d_nf, d_hz;
+	DevBuf d_sa, d_sb, d_win, d_oz, d_nf, d_hz, d_keys;
 	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err;
 	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb;
 	bool dev_motion = false;
@@ -348,9 +354,14 @@ struct aqh_ctx {
 	std::vector<float4> h_dofb;
 	std::vector<float> h_slices;
 	int mode = AQH_MODE_PLAIN;
-	cudaGraphExec_t graph_exec = nullptr;
-	bool graph_valid = false;
-	std::vector<unsigned char> graph_key;
+	// batched mode: instantiated frame graphs keyed by every kernel argument of
+	// the frame, most recently used first (a server slot sees many job shapes)
+	struct GraphEntry {
+		std::vector<unsigned char> key;
+		cudaGraphExec_t exec;
+	};
+	std::list<GraphEntry> graphs;
+	bool graph_valid = true;  // false: buffers moved, drop every cached graph
 	int64_t graphs_built = 0, overflow_rerenders = 0;
 	bool pending_check = false;
 	aqh::RenderPlan pending_plan{};
@@ -427,6 +438,9 @@ aqh_status aqh_create(const aqh_device_opts* opts, aqh_ctx** out) {
 	ctx->own_stream = ctx->stream;
 	if (e == cudaSuccess) aqh::configure_sample_kernels();
 	for (int i = 0; e == cudaSuccess && i < 6; ++i) e = cudaEventCreate(&ctx->ev[i]);
+	if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->cstream, cudaStreamNonBlocking);
+	if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_before_up, cudaEventDisableTiming);
+	if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_cioi, cudaEventDisableTiming);
 	if (e != cudaSuccess) {
 		delete ctx;
 		return e == cudaErrorMemoryAllocation ? AQH_ENOMEM : AQH_EDEVICE;
@@ -440,9 +454,13 @@ void aqh_destroy(aqh_ctx* ctx) {
 	cudaSetDevice(ctx->device);
 	if (ctx->stream) cudaStreamSynchronize(ctx->stream);
 	if (ctx->own_stream && ctx->own_stream != ctx->stream) cudaStreamSynchronize(ctx->own_stream);
+	if (ctx->cstream) cudaStreamSynchronize(ctx->cstream);
 	for (auto& ev : ctx->ev)
 		if (ev) cudaEventDestroy(ev);
-	if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+	if (ctx->ev_before_up) cudaEventDestroy(ctx->ev_before_up);
+	if (ctx->ev_cioi) cudaEventDestroy(ctx->ev_cioi);
+	if (ctx->cstream) cudaStreamDestroy(ctx->cstream);
+	for (auto& ge : ctx->graphs) cudaGraphExecDestroy(ge.exec);
 	if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
 	delete ctx;
 }
@@ -733,8 +751,18 @@ static aqh_status upload_packed_grids(aqh_ctx* ctx) {
 	AQH_TRY(up(ctx->d_mpbase, ctx->h_mpbase.data(), G * 8), "upload grids");
 	AQH_TRY(up(ctx->d_times, hp.times, std::max<size_t>(hp.ntimes, 1) * 4), "upload grids");
 	AQH_TRY(up(ctx->d_P, hp.P, hp.nP * 16), "upload P");
-	AQH_TRY(up(ctx->d_Ci, hp.Ci, hp.nC * 16), "upload Ci");
-	AQH_TRY(up(ctx->d_Oi, hp.Oi, hp.nC * 16), "upload Oi");
+	// Ci/Oi on the copy stream, after everything already queued on the main
+	// stream (the previous frame may still read the old colours)
+	AQH_TRY(ctx->d_Ci.ensure(hp.nC * 16), "upload Ci");
+	AQH_TRY(ctx->d_Oi.ensure(hp.nC * 16), "upload Oi");
+	AQH_TRY(cudaEventRecord(ctx->ev_before_up, ctx->stream), "upload Ci");
+	AQH_TRY(cudaStreamWaitEvent(ctx->cstream, ctx->ev_before_up, 0), "upload Ci");
+	if (hp.Ci && hp.nC)
+		AQH_TRY(cudaMemcpyAsync(ctx->d_Ci.p, hp.Ci, hp.nC * 16, cudaMemcpyHostToDevice, ctx->cstream), "upload Ci");
+	if (hp.Oi && hp.nC)
+		AQH_TRY(cudaMemcpyAsync(ctx->d_Oi.p, hp.Oi, hp.nC * 16, cudaMemcpyHostToDevice, ctx->cstream), "upload Oi");
+	AQH_TRY(cudaEventRecord(ctx->ev_cioi, ctx->cstream), "upload Ci");
+	ctx->cioi_pending = true;
 	if (hp.culled) AQH_TRY(up(ctx->d_culled, hp.culled, (size_t)ctx->h_mps), "upload culled");
 	GridsDev& g = ctx->dg;
 	g.ngrids = G;
@@ -874,6 +902,12 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 		pool.overflow = ctx->d_foverflow.as<int32_t>();
 		pool.capacity = ctx->frag_capacity;
 	}
+	if (pool.capacity == 0 && !P.mbdof && ctx->host_packed) {
+		// colours still on their way from the host: the sampler hands its
+		// hits to a separate resolve kernel, which alone waits for Ci/Oi
+		AQH_TRY(ctx->d_keys.ensure(P.nsamp * sizeof(unsigned long long)), "alloc hit keys");
+		store.keys = ctx->d_keys.as<unsigned long long>();
+	}
 	int nsm = 0;
 	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
 	P.nctas = std::max(1, std::min(fp.ntx * fp.nty, nsm * sample_static_ctas_per_sm(pool.capacity > 0)));
@@ -913,13 +947,19 @@ static aqh_status enqueue_frame(aqh_ctx* ctx, RenderPlan& P, bool batched, bool 
 		AQH_TRY(cudaMemsetAsync(P.pool.overflow, 0, 4, s), "memset");
 	}
 	if (timing) mark(ctx->ev[1]);
+	// host-packed colours arrive on the copy stream (ev_cioi); inside a
+	// capture the wait is an external-event node, so every replay waits for
+	// the latest upload
+	const unsigned wflags = batched ? cudaEventWaitExternal : cudaEventWaitDefault;
 	if (P.mbdof) {
+		AQH_TRY(cudaStreamWaitEvent(s, ctx->ev_cioi, wflags), "wait for colours");
 		launch_sample_mb(fp, P.g, ctx->smp, P.bb, P.store, P.pool, ctx->d_dofb.as<float4>(), ctx->d_slices.as<float>(), s);
 	} else if (batched) {
 		AQH_TRY(cudaMemsetAsync(ctx->d_queue.p, 0, 4, s), "memset");
-		launch_sample_tiles_q(fp, P.g, ctx->smp, P.bb, P.store, P.pool, ctx->d_queue.as<int>(), nullptr, P.nctas, s);
+		launch_sample_tiles_q(fp, P.g, ctx->smp, P.bb, P.store, P.pool, ctx->d_queue.as<int>(), nullptr, P.nctas, s,
+		                      ctx->ev_cioi, wflags);
 	} else {
-		launch_sample_tiles(fp, P.g, ctx->smp, P.bb, P.store, P.pool, ctx->d_err.as<int32_t>(), s);
+		launch_sample_tiles(fp, P.g, ctx->smp, P.bb, P.store, P.pool, ctx->d_err.as<int32_t>(), s, ctx->ev_cioi, wflags);
 	}
 	AQH_TRY(cudaGetLastError(), "sample kernel launch");
 	if (timing) mark(ctx->ev[2]);
@@ -974,10 +1014,14 @@ static aqh_status render_plain(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 			AQH_TRY(cudaMemsetAsync(P.pool.overflow, 0, 4, s), "memset");
 		}
 		cudaEventRecord(ctx->ev[1], s);
-		if (P.mbdof)
+		if (P.mbdof) {
+			if (ctx->cioi_pending) AQH_TRY(cudaStreamWaitEvent(s, ctx->ev_cioi, 0), "wait for colours");
 			launch_sample_mb(fp, P.g, ctx->smp, P.bb, P.store, P.pool, ctx->d_dofb.as<float4>(), ctx->d_slices.as<float>(), s);
-		else
-			launch_sample_tiles(fp, P.g, ctx->smp, P.bb, P.store, P.pool, ctx->d_err.as<int32_t>(), s);
+		} else {
+			launch_sample_tiles(fp, P.g, ctx->smp, P.bb, P.store, P.pool, ctx->d_err.as<int32_t>(), s,
+			                    ctx->cioi_pending ? ctx->ev_cioi : nullptr);
+		}
+		ctx->cioi_pending = false;
 		AQH_TRY(cudaGetLastError(), "sample kernel launch");
 		if (P.pool.capacity == 0) break;
 		int32_t ovf = 0;
@@ -1016,6 +1060,8 @@ static aqh_status render_plain(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 // Batched path: the list and fragment capacities come from the previous
 // frame (or a bound), overflow is detected on the device, and the whole frame
 // is one CUDA graph replayed while its arguments stay the same.
+constexpr size_t kMaxGraphs = 16;
+
 static aqh_status render_batched(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 	cudaStream_t s = ctx->stream;
 	const int64_t want = std::max<int64_t>(ctx->st_list_cap, (int64_t)P.g.ngrids * 4 + 1024);
@@ -1033,11 +1079,15 @@ static aqh_status render_batched(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 	void* ptrs[8] = {ctx->d_ftab.p, ctx->d_chan.p, ctx->d_q8.p, ctx->d_qchan.p, ctx->d_queue.p, ctx->d_dofb.p,
 	                 ctx->d_err.p, (void*)s};
 	std::memcpy(k, ptrs, sizeof ptrs);
-	if (!ctx->graph_valid || ctx->graph_key != key) {
-		if (ctx->graph_exec) {
-			cudaGraphExecDestroy(ctx->graph_exec);
-			ctx->graph_exec = nullptr;
-		}
+	if (!ctx->graph_valid) {
+		for (auto& ge : ctx->graphs) cudaGraphExecDestroy(ge.exec);
+		ctx->graphs.clear();
+		ctx->graph_valid = true;
+	}
+	auto hit = std::find_if(ctx->graphs.begin(), ctx->graphs.end(), [&](const aqh_ctx::GraphEntry& ge) { return ge.key == key; });
+	if (hit != ctx->graphs.end()) {
+		ctx->graphs.splice(ctx->graphs.begin(), ctx->graphs, hit);
+	} else {
 		cudaGraph_t graph = nullptr;
 		AQH_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
 		aqh_status st = enqueue_frame(ctx, P, true, true);
@@ -1047,14 +1097,19 @@ static aqh_status render_batched(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 			return st;
 		}
 		AQH_TRY(e, "end capture");
-		e = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+		cudaGraphExec_t exec = nullptr;
+		e = cudaGraphInstantiate(&exec, graph, 0);
 		cudaGraphDestroy(graph);
 		AQH_TRY(e, "instantiate graph");
-		ctx->graph_key = key;
-		ctx->graph_valid = true;
+		ctx->graphs.push_front(aqh_ctx::GraphEntry{key, exec});
+		while (ctx->graphs.size() > kMaxGraphs) {
+			cudaGraphExecDestroy(ctx->graphs.back().exec);
+			ctx->graphs.pop_back();
+		}
 		ctx->graphs_built++;
 	}
-	AQH_TRY(cudaGraphLaunch(ctx->graph_exec, s), "launch graph");
+	ctx->cioi_pending = false;  // the graph waits for ev_cioi itself
+	AQH_TRY(cudaGraphLaunch(ctx->graphs.front().exec, s), "launch graph");
 	ctx->pending_check = true;
 	ctx->pending_plan = P;
 	if (sync) return aqh_synchronize(ctx);

@@ -97,6 +97,9 @@ struct SampleStore {
 	int32_t* nfrag;   // debug: transparent fragment count (or null)
 	float* hitz;      // depth of the occluding hit when occlZ tracks the second-nearest
 	                  // depth (midpoint depth filter with a z display), else null
+	unsigned long long* keys;  // opaque frames: (ordered depth, id + 1) of each sample's occluding
+	                           // hit, sample-major, resolved by a separate kernel; null: the
+	                           // sampler resolves in place
 };
 
 // Transparent fragment pool: {depth, micropolygon id bits, u, v} + next link.
@@ -142,12 +145,17 @@ void launch_id_grid(const GridsDev& g, int64_t nmps, int32_t* table, cudaStream_
 void launch_st_count(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);
 void launch_scan_i32(const int32_t* in, int32_t* out, int n, int32_t* scratch, cudaStream_t s);
 void launch_st_write(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);
+// `colours_ready`, when given, is an event the first kernel that reads Ci/Oi
+// waits for (on an opaque frame, the resolve after the sampler), with
+// cudaStreamWaitEvent flags `wait_flags` (cudaEventWaitExternal in a capture).
 void launch_sample_tiles(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
-                         SampleStore st, FragPool pool, int32_t* err, cudaStream_t s);
+                         SampleStore st, FragPool pool, int32_t* err, cudaStream_t s,
+                         cudaEvent_t colours_ready = nullptr, unsigned wait_flags = 0);
 // Persistent form: `nctas` CTAs pull tiles from queue[0] (zeroed by the
 // caller), in `order` when given.
 void launch_sample_tiles_q(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
-                           SampleStore st, FragPool pool, int* queue, const int* order, int nctas, cudaStream_t s);
+                           SampleStore st, FragPool pool, int* queue, const int* order, int nctas, cudaStream_t s,
+                           cudaEvent_t colours_ready = nullptr, unsigned wait_flags = 0);
 int sample_static_ctas_per_sm(bool transp);
 void configure_sample_kernels();
 void configure_sample_mb_kernels();

@@ -857,6 +857,17 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 
 	// ---- resolve: colours of the occluding hits (sample-major, as above) ----
 	const long long npix = (long long)fp.sw * fp.sh;
+	if (st.keys) {
+		// hand the occluding hits to resolve_opaque_kernel
+		for (int q = t; q < tsamp; q += kThreadsS) {
+			const int si = q / tpix;
+			const int pl = q - si * tpix;
+			const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
+			if (px >= tpx1 || py >= tpy1) continue;
+			st.keys[si * npix + (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0)] = sm.key[pl * spp + si];
+		}
+		continue;
+	}
 	for (int q = t; q < tsamp; q += kThreadsS) {
 		const int si = q / tpix;
 		const int pl = q - si * tpix;
@@ -871,7 +882,30 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 	}  // tile loop
 }
 
+// Colours of the occluding hits of an opaque frame: one thread per sample,
+// sample-major (consecutive threads, consecutive pixels of one sample index).
+__global__ void __launch_bounds__(256)
+resolve_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, SampleStore st) {
+	const long long npix = (long long)fp.sw * fp.sh;
+	const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (q >= npix * fp.spp) return;
+	const int si = (int)(q / npix);
+	const long long pix = q - si * npix;
+	const int px = fp.sx0 + (int)(pix % fp.sw), py = fp.sy0 + (int)(pix / fp.sw);
+	const long long pat = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
+	const float2 o = __ldg(smp.pos + pat * fp.spp + si);
+	const unsigned long long kk = st.keys[q];
+	resolve_sample<false>(fp, g, FragPool{}, st, pix * fp.spp + si, q, (float)px + o.x, (float)py + o.y,
+	                      key_depth(kk), key_winner(kk), -1);
+}
+
 }  // namespace
+
+void launch_resolve_opaque(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, SampleStore st,
+                           cudaStream_t s) {
+	const long long n = (long long)fp.sw * fp.sh * fp.spp;
+	if (n > 0) resolve_opaque_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fp, g, sm, st);
+}
 
 void static_tiling(FrameParams& fp) {
 	const int tpix = min(kTilePixMax, max(1, kTileSampMax / fp.spp));
@@ -883,27 +917,39 @@ void static_tiling(FrameParams& fp) {
 }
 
 void launch_sample_tiles(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
-                         SampleStore st, FragPool pool, int32_t* err, cudaStream_t s) {
+                         SampleStore st, FragPool pool, int32_t* err, cudaStream_t s, cudaEvent_t colours_ready,
+                         unsigned wait_flags) {
 	(void)err;
-	launch_sample_tiles_q(fp, g, sm, b, st, pool, nullptr, nullptr, 0, s);
+	launch_sample_tiles_q(fp, g, sm, b, st, pool, nullptr, nullptr, 0, s, colours_ready, wait_flags);
 }
 
 void launch_sample_tiles_q(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
-                           SampleStore st, FragPool pool, int* queue, const int* order, int nctas, cudaStream_t s) {
+                           SampleStore st, FragPool pool, int* queue, const int* order, int nctas, cudaStream_t s,
+                           cudaEvent_t colours_ready, unsigned wait_flags) {
 	const int ntiles = fp.ntx * fp.nty;
 	const size_t smem_transp = sizeof(SmemS) + sizeof(int32_t) * kTileSampMax;
 	configure_sample_kernels();
 	const bool transp = pool.capacity > 0;
+	const bool split = !transp && st.keys;  // the resolve kernel is the first reader of Ci/Oi
+	if (colours_ready && !split) cudaStreamWaitEvent(s, colours_ready, wait_flags);
 	if (queue) {
 		if (transp)
 			sample_static_kernel<true, true><<<nctas, kThreadsS, smem_transp, s>>>(fp, g, sm, b, st, pool, queue, order);
 		else
 			sample_opaque_kernel<true><<<nctas, kThreadsS, sizeof(SmemO), s>>>(fp, g, sm, b, st, queue, order);
+		if (split) {
+			if (colours_ready) cudaStreamWaitEvent(s, colours_ready, wait_flags);
+			launch_resolve_opaque(fp, g, sm, st, s);
+		}
 	} else {
 		if (transp)
 			sample_static_kernel<true, false><<<ntiles, kThreadsS, smem_transp, s>>>(fp, g, sm, b, st, pool, nullptr, nullptr);
 		else
 			sample_opaque_kernel<false><<<ntiles, kThreadsS, sizeof(SmemO), s>>>(fp, g, sm, b, st, nullptr, nullptr);
+		if (split) {
+			if (colours_ready) cudaStreamWaitEvent(s, colours_ready, wait_flags);
+			launch_resolve_opaque(fp, g, sm, st, s);
+		}
 	}
 }
 

@@ -884,6 +884,10 @@ struct SmemP {
 	int first_reject;
 	int qn;
 	float dext[4];                        // min dofb[.][0], min [.][1], max [.][2], max [.][3]
+	float tsort[kTileSampM];              // each pixel's sample times, ascending (NaN last)
+	uint8_t tord[kTileSampM];             // ... and the sample index of each
+	int tval[kTilePixM];                  // non-NaN times per pixel
+	int wpre[kWarpsM][32];                // per-warp running counts of pixel windows
 	uint32_t surv[kSurvivors];            // kept (candidate, slice) items: slot | slice << 8
 	int nsurv;
 	uint32_t wq[kWarpsM][64];             // per-warp queue of (candidate, sample) tests
@@ -1009,6 +1013,35 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 		sm.sd[s] = make_float2(dx, dy);
 	}
 	__syncthreads();
+	// each pixel's samples in time order, so a time slice's samples form a
+	// window (insertion sort, ties by index; NaN times go last)
+	for (int pl = t; pl < tpix; pl += kThreadsM) {
+		float* ts = sm.tsort + pl * spp;
+		uint8_t* ord = sm.tord + pl * spp;
+		const float* tm = sm.stime + pl * spp;
+		int nv = 0;
+		for (int j = 0; j < spp; ++j) {
+			const float v = tm[j];
+			if (v != v) continue;
+			int k = nv++;
+			while (k > 0 && ts[k - 1] > v) {
+				ts[k] = ts[k - 1];
+				ord[k] = ord[k - 1];
+				--k;
+			}
+			ts[k] = v;
+			ord[k] = (uint8_t)j;
+		}
+		int k = nv;
+		for (int j = 0; j < spp; ++j)
+			if (tm[j] != tm[j]) {
+				ts[k] = tm[j];
+				ord[k] = (uint8_t)j;
+				++k;
+			}
+		sm.tval[pl] = nv;
+	}
+	__syncthreads();
 
 	const int lbeg = bb.st_offset[st_idx * bb.nranges];
 	const int lend = (int)min((long long)bb.st_offset[(st_idx + 1) * bb.nranges], (long long)bb.list_capacity);
@@ -1085,15 +1118,75 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 				const bool moving = r.nkeys > 1;
 				const Bnd& B = it.B;
 				const int w = it.eX - it.sX, nj = it.j1 - it.j0;
-				const int npairs = w * (it.eY - it.sY) * nj;
-				for (int q0 = 0; q0 < npairs; q0 += 32) {
+				// the (pixel, sample) pair of queue position q: with motion and depth
+				// of field the samples whose time lies in the slice's window (found
+				// in each pixel's time order, NaN times always included), else the
+				// slice's sample-index window of every pixel
+				const bool windows = moving && usingDof;
+				const int npx = w * (it.eY - it.sY);
+				for (int p0 = 0; p0 < (windows ? npx : 1); p0 += 32) {
+				int wpl = 0, wa = 0, wn = 0, wnv = 0, tot;
+				if (windows) {
+					const int pi = p0 + lane;
+					int cnt = 0;
+					if (pi < npx) {
+						const int px = it.sX + pi % w, py = it.sY + pi / w;
+						wpl = (py - tpy0) * fp.tile_w + (px - tpx0);
+						const float* ts = sm.tsort + wpl * spp;
+						wnv = sm.tval[wpl];
+						int lo = 0, hi = wnv;
+						while (lo < hi) {
+							const int mid = (lo + hi) >> 1;
+							if (ts[mid] < it.time0) lo = mid + 1; else hi = mid;
+						}
+						wa = lo;
+						hi = wnv;
+						while (lo < hi) {
+							const int mid = (lo + hi) >> 1;
+							if (ts[mid] <= it.time1) lo = mid + 1; else hi = mid;
+						}
+						wn = lo - wa;
+						cnt = wn + (spp - wnv);
+					}
+					int inc = cnt;
+#pragma unroll
+					for (int o = 1; o < 32; o <<= 1) {
+						const int v = __shfl_up_sync(0xffffffffu, inc, o);
+						if (lane >= o) inc += v;
+					}
+					sm.wpre[warp][lane] = inc - cnt;
+					tot = __shfl_sync(0xffffffffu, inc, 31);
+					__syncwarp();
+				} else {
+					tot = w * (it.eY - it.sY) * nj;
+				}
+				for (int q0 = 0; q0 < tot; q0 += 32) {
 					const int q = q0 + lane;
 					bool pass = false;
 					int s = 0;
-					if (q < npairs) {
-						const int pxy = q / nj, j = it.j0 + (q - pxy * nj);
-						const int px = it.sX + pxy % w, py = it.sY + pxy / w;
-						const int pl = (py - tpy0) * fp.tile_w + (px - tpx0);
+					int ol = 0;
+					if (windows && q < tot) {
+						int lo = 0, hi = 31;  // last lane whose window starts at or before q
+						while (lo < hi) {
+							const int mid = (lo + hi + 1) >> 1;
+							if (sm.wpre[warp][mid] <= q) lo = mid; else hi = mid - 1;
+						}
+						ol = lo;
+					}
+					const int opl = __shfl_sync(0xffffffffu, wpl, ol), oa = __shfl_sync(0xffffffffu, wa, ol);
+					const int on = __shfl_sync(0xffffffffu, wn, ol), onv = __shfl_sync(0xffffffffu, wnv, ol);
+					if (q < tot) {
+						int pl, j;
+						if (windows) {
+							const int k = q - sm.wpre[warp][ol];
+							pl = opl;
+							j = sm.tord[pl * spp + ((k < on) ? oa + k : onv + (k - on))];
+						} else {
+							const int pxy = q / nj;
+							j = it.j0 + (q - pxy * nj);
+							pl = (it.sY + pxy / w - tpy0) * fp.tile_w + (it.sX + pxy % w - tpx0);
+						}
+						const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 						s = pl * spp + j;
 						pass = !(sm.flag[s >> 5] & (1u << (s & 31)));  // else replayed in order below
 						const float stime = sm.stime[s];
@@ -1132,6 +1225,8 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 						__syncwarp();
 						qn -= 32;
 					}
+				}
+				__syncwarp();  // wpre is rewritten for the next pixels
 				}
 			}
 			drain(qn);

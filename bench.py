@@ -87,7 +87,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -139,6 +139,11 @@ WORKLOADS = {
                "micropolygons": 25_600_000, "filter": "box 1x1", "shutter": [0, 1],
                "dof": {"fstop": 2.8, "focal_length": 0.05, "focal_distance": 50}, "motion_px": 20}),
 }
+
+
+KERNELS = {"opaque": "sample_opaque_kernel", "transparent": "sample_static_kernel", "mbdof": "sample_mbp_kernel"}
+# measured DRAM bytes per micropolygon of the sampler launch (ncu, 0.35 scale)
+TRAFFIC_PER_MP = {"opaque": (97.556224e6 + 126.517504e6) / 6_272_000}
 
 
 def make_scene(args):
@@ -344,11 +349,16 @@ def run_gpu(args):
         return 0
     pk = peaks()
     alg_bytes = g.nbytes_algorithmic()  # P + Ci + Oi float4 per vertex, read once
+    # DRAM bytes (read + write) of one sampler launch from an ncu capture of the
+    # same kernel on a smaller frame of the same stream, scaled by micropolygons
+    # (profiles/sample_opaque_kernel_opaque_stream_scale035.md); None where no
+    # capture of that kernel exists
+    traffic = TRAFFIC_PER_MP[args.workload] * mps if TRAFFIC_PER_MP.get(args.workload) else None
     ms_sample = float(np.mean(sample_ms))
     achieved = alg_bytes / (ms_sample / 1e3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-            "frac": achieved / pk["hbm_gbs"], "traffic": None,
-            "kernel": "sample_mb_kernel" if args.workload == "mbdof" else "sample_static_kernel", "algorithmic_bytes": alg_bytes,
+            "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
+            "kernel": KERNELS[args.workload], "algorithmic_bytes": alg_bytes,
             "kernel_ms": ms_sample, "peak_source": pk["source"]}
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
@@ -400,22 +410,33 @@ def run_served(args):
     # warm both paths on every distinct scene (context buffers, graphs, JIT)
     h = aqh.Hider(0)
     h.set_mode(False)
-    sv = aqh.Server(0, slots=args.slots, batched=True)
+    sv = aqh.Server(0, slots=args.slots, batched=args.slot_mode == "batched")
+    qch = (0, 1, 2, 6)
+
+    def plain_frame(sc):
+        """One request the way a served job runs it (packed host grids in one
+        call, RGBA8 read back), one frame at a time in plain mode."""
+        h.frame_begin(sc.frame)
+        h.set_samples(sc.samples)
+        h.submit_grids_host(sc.grids)
+        h.render(sync=True)
+        return h.read_quantized(qch)
+
     for sc in scenes:
-        h.render_scene(sc, samples=False)
+        plain_frame(sc)
         jid = sv.submit(sc)
         sv.wait(jid)
         sv.release(jid)
 
     def plain_run(poisson: bool):
-        lat, t_free = [], 0.0
+        lat = []
         start = time.perf_counter()
         for k, i in enumerate(order):
             arr = arrivals[k] if poisson else 0.0
             now = time.perf_counter() - start
             if poisson and now < arr:
                 time.sleep(arr - now)
-            h.render_scene(scenes[i], samples=False)
+            plain_frame(scenes[i])
             lat.append(time.perf_counter() - start - arr)
         return time.perf_counter() - start, lat
 
@@ -450,7 +471,7 @@ def run_served(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "workload": "served_mixed_stream",
             "config": {"workload": "served_mixed_stream", "jobs": args.jobs, "distinct_scenes": args.distinct,
-                       "mean_gap_ms": args.gap_ms, "slots": args.slots, "kinds": kinds,
+                       "mean_gap_ms": args.gap_ms, "slots": args.slots, "slot_mode": args.slot_mode, "kinds": kinds,
                        "max_micropolygons": args.max_mps, "generation_s": gen_s},
             "served": {"frames_per_s_saturated": args.jobs / served_sat,
                        "micropolygons_per_s_saturated": mps_total / served_sat,
@@ -481,6 +502,8 @@ def main():
     ap.add_argument("--gap-ms", type=float, default=20.0)
     ap.add_argument("--slots", type=int, default=6)
     ap.add_argument("--max-mps", type=float, default=8e6)
+    ap.add_argument("--slot-mode", default="batched", choices=["batched", "plain"],
+                    help="served slots: persistent kernel + CUDA graph (batched) or one launch per stage")
     args = ap.parse_args()
     if args.workload == "served":
         sys.exit(run_served(args))
