@@ -65,7 +65,8 @@ class Samples(C.Structure):
 class FrameStats(C.Structure):
     _fields_ = [("micropolygons", C.c_int64), ("samples", C.c_int64), ("grids", C.c_int64),
                 ("tile_grid_pairs", C.c_int64), ("fragments", C.c_int64),
-                ("ms_bin", C.c_float), ("ms_sample", C.c_float), ("ms_filter", C.c_float), ("ms_total", C.c_float)]
+                ("ms_bin", C.c_float), ("ms_sample", C.c_float), ("ms_filter", C.c_float), ("ms_total", C.c_float),
+                ("graphs_built", C.c_int64), ("rerenders", C.c_int64)]
 
 
 class DeviceOpts(C.Structure):
@@ -364,7 +365,8 @@ class Job(C.Structure):
 class JobInfo(C.Structure):
     _fields_ = [("id", C.c_int64), ("status", C.c_int), ("state", C.c_int), ("t_submit", C.c_double),
                 ("t_admit", C.c_double), ("t_done", C.c_double), ("footprint", C.c_size_t),
-                ("ms_device", C.c_float), ("slot", C.c_int)]
+                ("ms_device", C.c_float), ("slot", C.c_int), ("ms_prepare", C.c_float), ("ms_render", C.c_float),
+                ("ms_read", C.c_float)]
 
 
 class ServerOpts(C.Structure):
@@ -373,7 +375,8 @@ class ServerOpts(C.Structure):
 
 class ServerInfo(C.Structure):
     _fields_ = [("budget", C.c_size_t), ("in_use", C.c_size_t), ("peak_in_use", C.c_size_t),
-                ("pending", C.c_int64), ("completed", C.c_int64), ("running", C.c_int), ("peak_running", C.c_int)]
+                ("pending", C.c_int64), ("completed", C.c_int64), ("running", C.c_int), ("peak_running", C.c_int),
+                ("graphs_built", C.c_int64), ("rerenders", C.c_int64)]
 
 
 def _bind_server(L):

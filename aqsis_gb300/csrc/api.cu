@@ -36,9 +36,17 @@ struct DevBuf {
 	}
 	cudaError_t ensure(size_t bytes) {
 		if (bytes <= cap) return cudaSuccess;
+		// grow by at least half: a context that sees frames of many sizes (a
+		// server slot) settles after a few frees, each of which stalls the device
+		const size_t grown = cap ? cap + cap / 2 : 0;
 		release();
-		size_t want = std::max<size_t>(bytes, 256);
+		size_t want = std::max<size_t>(std::max(bytes, grown), 256);
 		cudaError_t e = cudaMalloc(&p, want);
+		if (e == cudaErrorMemoryAllocation && want > bytes) {
+			cudaGetLastError();
+			want = std::max<size_t>(bytes, 256);
+			e = cudaMalloc(&p, want);
+		}
 		if (e != cudaSuccess) {
 			p = nullptr;
 			cap = 0;
@@ -862,8 +870,9 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	bb.strips = ctx->d_strips.as<uint32_t>();
 	bb.st_count = ctx->d_stcount.as<int32_t>();
 	bb.st_offset = ctx->d_stoffset.as<int32_t>();
-	AQH_TRY(ctx->d_sa.ensure(P.nsamp * sizeof(float4)), "alloc sample store");
-	AQH_TRY(ctx->d_sb.ensure(P.nsamp * sizeof(float4)), "alloc sample store");
+	const size_t nstore = store_size((long long)fp.sw * fp.sh, fp.spp);
+	AQH_TRY(ctx->d_sa.ensure(nstore * sizeof(float4)), "alloc sample store");
+	AQH_TRY(ctx->d_sb.ensure(nstore * sizeof(float4)), "alloc sample store");
 	SampleStore& store = P.store;
 	store = SampleStore{};
 	store.a = ctx->d_sa.as<float4>();
@@ -905,7 +914,7 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	if (pool.capacity == 0 && !P.mbdof && ctx->host_packed) {
 		// colours still on their way from the host: the sampler hands its
 		// hits to a separate resolve kernel, which alone waits for Ci/Oi
-		AQH_TRY(ctx->d_keys.ensure(P.nsamp * sizeof(unsigned long long)), "alloc hit keys");
+		AQH_TRY(ctx->d_keys.ensure(nstore * sizeof(unsigned long long)), "alloc hit keys");
 		store.keys = ctx->d_keys.as<unsigned long long>();
 	}
 	int nsm = 0;
@@ -1064,7 +1073,9 @@ constexpr size_t kMaxGraphs = 16;
 
 static aqh_status render_batched(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 	cudaStream_t s = ctx->stream;
-	const int64_t want = std::max<int64_t>(ctx->st_list_cap, (int64_t)P.g.ngrids * 4 + 1024);
+	// list room for 16 super-tiles per grid: a frame that needs more is caught
+	// on the device and rendered again on the plain path
+	const int64_t want = std::max<int64_t>(ctx->st_list_cap, (int64_t)P.g.ngrids * 16 + 4096);
 	AQH_TRY(ctx->d_stlist.ensure(sizeof(int32_t) * want), "alloc tile lists");
 	ctx->st_list_cap = ctx->d_stlist.cap / sizeof(int32_t);
 	P.bb.st_list = ctx->d_stlist.as<int32_t>();
@@ -1236,14 +1247,15 @@ aqh_status aqh_read_samples(aqh_ctx* ctx, int32_t* winner, float* occlz, int32_t
 	if (occlz) AQH_TRY(cudaMemcpyAsync(occlz, ctx->d_oz.p, n * 4, cudaMemcpyDeviceToHost, s), "read");
 	if (nfrag) AQH_TRY(cudaMemcpyAsync(nfrag, ctx->d_nf.p, n * 4, cudaMemcpyDeviceToHost, s), "read");
 	if (valid || sdata) {
-		std::vector<float4> a(n), b(n);
-		AQH_TRY(cudaMemcpyAsync(a.data(), ctx->d_sa.p, n * 16, cudaMemcpyDeviceToHost, s), "read");
-		AQH_TRY(cudaMemcpyAsync(b.data(), ctx->d_sb.p, n * 16, cudaMemcpyDeviceToHost, s), "read");
+		const size_t ns = store_size((long long)fp.sw * fp.sh, fp.spp);
+		std::vector<float4> a(ns), b(ns);
+		AQH_TRY(cudaMemcpyAsync(a.data(), ctx->d_sa.p, ns * 16, cudaMemcpyDeviceToHost, s), "read");
+		AQH_TRY(cudaMemcpyAsync(b.data(), ctx->d_sb.p, ns * 16, cudaMemcpyDeviceToHost, s), "read");
 		AQH_TRY(cudaStreamSynchronize(s), "read");
-		// the device store is sample-major: [sample index][sample-region pixel]
-		const size_t spp = (size_t)fp.spp, npix = n / spp;
+		// the device store is in 32-pixel blocks (store_index)
+		const size_t spp = (size_t)fp.spp;
 		for (size_t i = 0; i < n; ++i) {
-			const size_t j = (i % spp) * npix + i / spp;
+			const size_t j = (size_t)store_index((long long)(i / spp), (int)(i % spp), (int)spp);
 			if (valid) valid[i] = b[j].w != 0.0f ? 1 : 0;
 			if (sdata) {
 				float* d = sdata + 7 * i;
@@ -1259,6 +1271,8 @@ aqh_status aqh_read_samples(aqh_ctx* ctx, int32_t* winner, float* occlz, int32_t
 aqh_status aqh_get_stats(aqh_ctx* ctx, aqh_frame_stats* st) {
 	if (!ctx || !st) return AQH_EINVAL;
 	*st = ctx->stats;
+	st->graphs_built = ctx->graphs_built;
+	st->rerenders = ctx->overflow_rerenders;
 	return AQH_OK;
 }
 

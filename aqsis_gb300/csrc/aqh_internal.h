@@ -86,9 +86,19 @@ struct SamplerDev {
 };
 
 // Per-sample resolved store (after Combine): R G B depth / OR OG OB flags.
-// Sample-major: a and b hold [sample index][sample-region pixel], so the
-// filter's loads of one sample index over neighbouring pixels coalesce; the
-// debug arrays are pixel-major ([pixel][sample index]).
+// Sample store layout: sample-region pixels in blocks of 32 consecutive ones,
+// each block holding its samples sample-index-major ([block][sample][32]).
+// Loads of one sample index over neighbouring pixels coalesce, and all of a
+// pixel's samples stay within one block of 512 * spp bytes.
+__host__ __device__ inline long long store_index(long long pix, int si, int spp) {
+	return ((pix >> 5) * spp + si) * 32 + (pix & 31);
+}
+__host__ __device__ inline size_t store_size(long long npix, int spp) {
+	return (size_t)((npix + 31) >> 5) * 32 * (size_t)spp;
+}
+
+// a and b in the store layout above; the debug arrays are pixel-major
+// ([pixel][sample index]).
 struct SampleStore {
 	float4* a;        // r, g, b, depth
 	float4* b;        // or, og, ob, valid (1.0f / 0.0f)

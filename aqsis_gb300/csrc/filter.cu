@@ -13,6 +13,9 @@ namespace aqh {
 
 namespace {
 
+// SPP > 0: samples per pixel known at compile time (the sample loop is
+// unrolled by four so its loads issue together); 0: read from fp.
+template <int SPP>
 __global__ void __launch_bounds__(256)
 filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __restrict__ ftab,
               float* __restrict__ chan) {
@@ -21,8 +24,7 @@ filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __res
 	if (x >= fp.crop_x1 || y >= fp.crop_y1) return;
 	const float xcent = x + 0.5f, ycent = y + 0.5f;
 	const int xmax = fp.shiftX, ymax = fp.shiftY;
-	const int spp = fp.spp;
-	const long long npix = (long long)fp.sw * fp.sh;  // the sample store is sample-major
+	const int spp = SPP > 0 ? SPP : fp.spp;
 	float gTot = 0.0f;
 	int count = 0;
 	float acc[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -34,6 +36,7 @@ filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __res
 			const long long pat = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
 			const int index = ((fy + ymax) * (2 * xmax + 1) + fx + xmax) * spp;
 			const float fpx = (float)px, fpy = (float)py;
+#pragma unroll 4
 			for (int i = 0; i < spp; ++i) {
 				const float2 o = __ldg(smp.pos + pat * spp + i);
 				const float vx = (fpx + o.x) - xcent;
@@ -41,9 +44,9 @@ filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __res
 				if (vx >= -fp.xfwo2 && vy >= -fp.yfwo2 && vx <= fp.xfwo2 && vy <= fp.yfwo2) {
 					const float gw = __ldg(ftab + index + i);
 					gTot += gw;
-					const float4 b = st.b[i * npix + pix];
+					const float4 b = __ldg(st.b + store_index(pix, i, spp));
 					if (b.w != 0.0f) {
-						const float4 a = st.a[i * npix + pix];
+						const float4 a = __ldg(st.a + store_index(pix, i, spp));
 						acc[0] += a.x * gw;
 						acc[1] += a.y * gw;
 						acc[2] += a.z * gw;
@@ -131,7 +134,13 @@ void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStor
 	const int w = fp.crop_x1 - fp.crop_x0, h = fp.crop_y1 - fp.crop_y0;
 	if (w <= 0 || h <= 0) return;
 	dim3 grid((w + 15) / 16, (h + 15) / 16);
-	filter_kernel<<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels);
+	switch (fp.spp) {
+	case 4: filter_kernel<4><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels); break;
+	case 16: filter_kernel<16><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels); break;
+	case 36: filter_kernel<36><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels); break;
+	case 64: filter_kernel<64><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels); break;
+	default: filter_kernel<0><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels); break;
+	}
 }
 
 void launch_quantize_u8(const FrameParams& fp, const SamplerDev& sm, const float* channels, const int* chans,

@@ -138,7 +138,7 @@ extern "C" aqh_status aqh_render_noalloc(const aqh_frame_desc* desc, const float
 	if (!fp.cullable || fp.midpoint_store)
 		return na_fail(err, err_len, AQH_ELIMIT,
 		               "aqh_render_noalloc: a z display with the midpoint, max or average depth filter is not supported");
-	if (npix > kNaMaxRegionPixels || nsamp > kNaMaxSamples) {
+	if (npix > kNaMaxRegionPixels || nsamp > kNaMaxSamples || (long long)store_size(npix, fp.spp) > kNaMaxSamples) {
 		snprintf(buf, sizeof buf,
 		         "aqh_render_noalloc: sample region %dx%d x %d samples exceeds the limit of %d pixels / %d samples",
 		         fp.sw, fp.sh, fp.spp, kNaMaxRegionPixels, kNaMaxSamples);

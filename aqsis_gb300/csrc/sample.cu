@@ -537,8 +537,7 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 
 	// ---- resolve: colours of the occluding hits, Combine of fragment lists ----
 	// (consecutive threads take the samples of one pixel, whose fragments the
-	// same warp allocated together; the sample store is sample-major)
-	const long long npix = (long long)fp.sw * fp.sh;
+	// same warp allocated together)
 	for (int s = t; s < tsamp; s += kThreadsS) {
 		const int pl = s / spp;
 		const int si = s - pl * spp;
@@ -547,7 +546,7 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
 		const long long pat = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
 		const float2 o = __ldg(smp.pos + pat * spp + si);
-		resolve_sample<TRANSP>(fp, g, pool, st, pix * spp + si, si * npix + pix, (float)px + o.x, (float)py + o.y,
+		resolve_sample<TRANSP>(fp, g, pool, st, pix * spp + si, store_index(pix, si, spp), (float)px + o.x, (float)py + o.y,
 		                       sm.soz[s], sm.swin[s], TRANSP ? fhead[s] : -1);
 	}
 	}  // tile loop
@@ -855,8 +854,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		if (exhausted) break;
 	}
 
-	// ---- resolve: colours of the occluding hits (sample-major, as above) ----
-	const long long npix = (long long)fp.sw * fp.sh;
+	// ---- resolve: colours of the occluding hits (sample-major within the tile) ----
 	if (st.keys) {
 		// hand the occluding hits to resolve_opaque_kernel
 		for (int q = t; q < tsamp; q += kThreadsS) {
@@ -864,7 +862,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 			const int pl = q - si * tpix;
 			const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 			if (px >= tpx1 || py >= tpy1) continue;
-			st.keys[si * npix + (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0)] = sm.key[pl * spp + si];
+			st.keys[store_index((long long)(py - fp.sy0) * fp.sw + (px - fp.sx0), si, spp)] = sm.key[pl * spp + si];
 		}
 		continue;
 	}
@@ -876,7 +874,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
 		const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + si);
 		const unsigned long long kk = sm.key[pl * spp + si];
-		resolve_sample<false>(fp, g, nopool, st, pix * spp + si, si * npix + pix, (float)px + o.x, (float)py + o.y,
+		resolve_sample<false>(fp, g, nopool, st, pix * spp + si, store_index(pix, si, spp), (float)px + o.x, (float)py + o.y,
 		                      key_depth(kk), key_winner(kk), -1);
 	}
 	}  // tile loop
@@ -887,10 +885,11 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 __global__ void __launch_bounds__(256)
 resolve_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, SampleStore st) {
 	const long long npix = (long long)fp.sw * fp.sh;
-	const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-	if (q >= npix * fp.spp) return;
-	const int si = (int)(q / npix);
-	const long long pix = q - si * npix;
+	const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // store index
+	if (q >= (long long)store_size(npix, fp.spp)) return;
+	const int si = (int)((q >> 5) % fp.spp);
+	const long long pix = ((q >> 5) / fp.spp) * 32 + (q & 31);
+	if (pix >= npix) return;
 	const int px = fp.sx0 + (int)(pix % fp.sw), py = fp.sy0 + (int)(pix / fp.sw);
 	const long long pat = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
 	const float2 o = __ldg(smp.pos + pat * fp.spp + si);
@@ -903,7 +902,7 @@ resolve_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, SampleStore st
 
 void launch_resolve_opaque(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, SampleStore st,
                            cudaStream_t s) {
-	const long long n = (long long)fp.sw * fp.sh * fp.spp;
+	const long long n = (long long)store_size((long long)fp.sw * fp.sh, fp.spp);
 	if (n > 0) resolve_opaque_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fp, g, sm, st);
 }
 

@@ -714,7 +714,6 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 	// (opaque: consecutive threads take consecutive pixels of one sample index,
 	// as the sample store is sample-major; transparent: the samples of one
 	// pixel, whose fragments the same warp allocated together)
-	const long long npix = (long long)fp.sw * fp.sh;
 	for (int q = t; q < tsamp; q += kThreadsM) {
 		const int j = TRANSP ? q % spp : q / tpix;
 		const int pl = TRANSP ? q / spp : q - j * tpix;
@@ -726,7 +725,7 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 		float x = 0.0f, y = 0.0f, stime = 0.0f, sdx = 0.0f, sdy = 0.0f;
 		int kinv = 0;
 		if (w >= 0) mb_sample_attrs(fp, smp, px, py, j, pix, x, y, stime, sdx, sdy, kinv);
-		mb_resolve<TRANSP>(fp, g, pool, st, pix * spp + j, (long long)j * npix + pix, x, y, stime, sdx, sdy,
+		mb_resolve<TRANSP>(fp, g, pool, st, pix * spp + j, store_index(pix, j, spp), x, y, stime, sdx, sdy,
 		                   sm.soz[s], w, TRANSP ? fhead[s] : -1);
 	}
 }
@@ -746,7 +745,7 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 // shared-memory atomicMin.  Hits below their slice's min.z, NaN or zero
 // depths flag the sample for an in-order replay from the round's start.
 constexpr int kSlotsP = 128;
-constexpr int kSurvivors = 2048;
+constexpr int kSurvivors = 512;
 
 __device__ __forceinline__ unsigned long long depth_key_m(float z, int w) {
 	const uint32_t u = __float_as_uint(z);
@@ -868,11 +867,18 @@ __device__ __forceinline__ bool mb_item(const FrameParams& fp, const Shutter& sh
 	return it.sX < it.eX && it.sY < it.eY && it.j0 < it.j1;
 }
 
+// Lens offset of the sample of lens stratum k in lens pattern dp
+// (projectToCircle of the pattern's [0,1)^2 lens sample, imagepixel.cpp:338-347).
+__device__ __forceinline__ float2 lens_offset(const SamplerDev& smp, int dp, int spp, int k) {
+	if (!smp.dof) return make_float2(0.0f, 0.0f);
+	const float2 d = __ldg(smp.dof + (long long)dp * spp + k);
+	return project_to_circle(-1.0f + 2.0f * d.x, -1.0f + 2.0f * d.y);
+}
+
 struct SmemP {
 	unsigned long long key[kTileSampM];   // occluding hit of each tile sample (depth_key_m)
 	unsigned long long prev[kTileSampM];  // ... at the start of the round
 	MbRec rec[kSlotsP];
-	float2 sd[kTileSampM];                // lens offset of each tile sample
 	float stime[kTileSampM];              // time of each tile sample
 	float dofb[AQH_MAX_SPP_DEV][4];
 	int2 pend[kSlotsP];
@@ -880,6 +886,7 @@ struct SmemP {
 	int qgrid[kThreadsM];
 	int qcum[kThreadsM + 1];
 	int patidx[kTilePixM];
+	int dofidx[kTilePixM];                // lens pattern of each tile pixel
 	int warp_tot[32];
 	int first_reject;
 	int qn;
@@ -889,6 +896,7 @@ struct SmemP {
 	int tval[kTilePixM];                  // non-NaN times per pixel
 	int wpre[kWarpsM][32];                // per-warp running counts of pixel windows
 	uint32_t surv[kSurvivors];            // kept (candidate, slice) items: slot | slice << 8
+	MbItem items[kSurvivors];             // ... and their bounds, windows and pixel ranges
 	int nsurv;
 	uint32_t wq[kWarpsM][64];             // per-warp queue of (candidate, sample) tests
 	float wz[kWarpsM][64];                // ... with their slice bound's min z
@@ -995,22 +1003,15 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 	for (int s = t; s < tsamp; s += kThreadsM) {
 		const int pl = s / spp, j = s - pl * spp;
 		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
-		float tm = 0.0f, dx = 0.0f, dy = 0.0f;
+		float tm = 0.0f;
 		if (px < tpx1 && py < tpy1) {
 			const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
 			const long long tp = smp.time_index ? (long long)__ldg(smp.time_index + pix) : pix;
 			const float tt = smp.time ? __ldg(smp.time + tp * spp + j) : 0.0f;
 			tm = (sh.close - sh.open) * tt + sh.open;
-			if (smp.dof) {
-				const long long dp = smp.dof_index ? (long long)__ldg(smp.dof_index + pix) : pix;
-				const float2 d = __ldg(smp.dof + dp * spp + sm.kinv[s]);
-				const float2 c = project_to_circle(-1.0f + 2.0f * d.x, -1.0f + 2.0f * d.y);
-				dx = c.x;
-				dy = c.y;
-			}
+			if (j == 0) sm.dofidx[pl] = smp.dof_index ? (int)__ldg(smp.dof_index + pix) : (int)pix;
 		}
 		sm.stime[s] = tm;
-		sm.sd[s] = make_float2(dx, dy);
 	}
 	__syncthreads();
 	// each pixel's samples in time order, so a time slice's samples form a
@@ -1080,8 +1081,11 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 					if (sm.pref[mid] <= p) lo = mid; else hi = mid - 1;
 				}
 				MbItem it;
-				if (mb_item(fp, sh, sm.rec[lo], slice_times, p - sm.pref[lo], sm.dext, tpx0, tpy0, tpx1, tpy1, it))
-					sm.surv[atomicAdd(&sm.nsurv, 1)] = (uint32_t)lo | ((uint32_t)(p - sm.pref[lo]) << 8);
+				if (mb_item(fp, sh, sm.rec[lo], slice_times, p - sm.pref[lo], sm.dext, tpx0, tpy0, tpx1, tpy1, it)) {
+					const int at = atomicAdd(&sm.nsurv, 1);
+					sm.surv[at] = (uint32_t)lo | ((uint32_t)(p - sm.pref[lo]) << 8);
+					sm.items[at] = it;
+				}
 			}
 			__syncthreads();
 			const int nsurv = sm.nsurv;
@@ -1097,7 +1101,7 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 					const int pl = s / spp, j = s - pl * spp;
 					const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 					const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + j);
-					const float2 d = sm.sd[s];
+					const float2 d = lens_offset(smp, sm.dofidx[pl], spp, sm.kinv[s]);
 					float D, u, v;
 					if (mb_sample(fp, r, r.nkeys > 1, usingDof, (float)px + o.x, (float)py + o.y, sm.stime[s], d.x, d.y,
 					              D, u, v)) {
@@ -1113,8 +1117,7 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 				const uint32_t e = sm.surv[k];
 				const int c = (int)(e & 0xffu);
 				const MbRec& r = sm.rec[c];
-				MbItem it;
-				mb_item(fp, sh, r, slice_times, (int)(e >> 8), sm.dext, tpx0, tpy0, tpx1, tpy1, it);
+				const MbItem& it = sm.items[k];
 				const bool moving = r.nkeys > 1;
 				const Bnd& B = it.B;
 				const int w = it.eX - it.sX, nj = it.j1 - it.j0;
@@ -1246,7 +1249,7 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 				const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + j);
 				const float x = (float)px + o.x, y = (float)py + o.y;
 				const float stime = sm.stime[s];
-				const float2 d = sm.sd[s];
+				const float2 d = lens_offset(smp, sm.dofidx[pl], spp, sm.kinv[s]);
 				const float* dk = sm.dofb[sm.kinv[s]];
 				float oz = key_depth_m(sm.prev[s]);
 				int w = key_winner_m(sm.prev[s]);
@@ -1296,7 +1299,6 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 	}
 
 	// ---- resolve (sample-major, see the lane kernel) ----
-	const long long npix = (long long)fp.sw * fp.sh;
 	for (int q = t; q < tsamp; q += kThreadsM) {
 		const int j = q / tpix;
 		const int pl = q - j * tpix;
@@ -1306,8 +1308,8 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
 		const unsigned long long kk = sm.key[s];
 		const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + j);
-		const float2 d = sm.sd[s];
-		mb_resolve<false>(fp, g, FragPool{}, st, pix * spp + j, (long long)j * npix + pix, (float)px + o.x,
+		const float2 d = lens_offset(smp, sm.dofidx[pl], spp, sm.kinv[s]);
+		mb_resolve<false>(fp, g, FragPool{}, st, pix * spp + j, store_index(pix, j, spp), (float)px + o.x,
 		                  (float)py + o.y, sm.stime[s], d.x, d.y, key_depth_m(kk), key_winner_m(kk), -1);
 	}
 }

@@ -40,6 +40,7 @@ struct Job {
 	std::string error;
 	double t_submit = 0, t_admit = 0, t_done = 0;
 	float ms_device = 0;
+	float ms_prepare = 0, ms_render = 0, ms_read = 0;
 	int slot = -1;
 };
 
@@ -91,13 +92,15 @@ extern "C" size_t aqh_job_footprint(const aqh_job* j) {
 static void run_job(aqh_server* sv, int slot, Job* job) {
 	aqh_ctx* c = sv->ctx[slot];
 	const aqh_job& j = job->j;
+	const double t0 = sv->now();
 	aqh_status st = aqh_frame_begin(c, &j.frame);
 	if (st == AQH_OK) st = aqh_set_samples(c, &j.samples);
 	if (st == AQH_OK)
 		st = aqh_submit_grids_host(c, j.ngrids, j.cu, j.cv, j.nkeys, j.flags, j.pbase, j.cbase, j.tbase, j.times,
 		                           j.ntimes, j.P, j.nP, j.Ci, j.Oi, j.nC, j.culled, j.micropolygons);
+	const double t1 = sv->now();
 	if (st == AQH_OK) st = aqh_render(c, 1);
-	aqh::FrameParams fp{};
+	const double t2 = sv->now();
 	if (st == AQH_OK && j.rgba) {
 		const int ch[4] = {0, 1, 2, 6};
 		const size_t n = (size_t)(j.frame.crop_xmax - j.frame.crop_xmin) * (j.frame.crop_ymax - j.frame.crop_ymin);
@@ -111,7 +114,11 @@ static void run_job(aqh_server* sv, int slot, Job* job) {
 	}
 	aqh_frame_stats fs{};
 	aqh_get_stats(c, &fs);
+	const double t3 = sv->now();
 	std::lock_guard<std::mutex> lock(sv->mu);
+	job->ms_prepare = (float)(1e3 * (t1 - t0));
+	job->ms_render = (float)(1e3 * (t2 - t1));
+	job->ms_read = (float)(1e3 * (t3 - t2));
 	job->status = st;
 	job->error = st == AQH_OK ? "" : aqh_last_error(c);
 	job->state = st == AQH_OK ? 2 : 3;
@@ -228,6 +235,9 @@ static void fill_info(const Job* job, aqh_job_info* info) {
 	info->footprint = job->footprint;
 	info->ms_device = job->ms_device;
 	info->slot = job->slot;
+	info->ms_prepare = job->ms_prepare;
+	info->ms_render = job->ms_render;
+	info->ms_read = job->ms_read;
 }
 
 aqh_status aqh_server_poll(aqh_server* sv, int64_t id, aqh_job_info* info) {
@@ -283,6 +293,13 @@ aqh_status aqh_server_stats(aqh_server* sv, aqh_server_info* info) {
 	info->pending = (int64_t)sv->pending.size();
 	info->running = sv->running;
 	info->peak_running = sv->peak_running;
+	info->graphs_built = info->rerenders = 0;
+	for (aqh_ctx* c : sv->ctx) {
+		aqh_frame_stats fs{};
+		aqh_get_stats(c, &fs);
+		info->graphs_built += fs.graphs_built;
+		info->rerenders += fs.rerenders;
+	}
 	info->completed = sv->completed;
 	return AQH_OK;
 }

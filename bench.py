@@ -413,20 +413,31 @@ def run_served(args):
     sv = aqh.Server(0, slots=args.slots, batched=args.slot_mode == "batched")
     qch = (0, 1, 2, 6)
 
+    plain_phases = []
+
     def plain_frame(sc):
         """One request the way a served job runs it (packed host grids in one
         call, RGBA8 read back), one frame at a time in plain mode."""
+        t0 = time.perf_counter()
         h.frame_begin(sc.frame)
         h.set_samples(sc.samples)
         h.submit_grids_host(sc.grids)
+        t1 = time.perf_counter()
         h.render(sync=True)
-        return h.read_quantized(qch)
+        t2 = time.perf_counter()
+        out = h.read_quantized(qch)
+        plain_phases.append((t1 - t0, t2 - t1, time.perf_counter() - t2))
+        return out
 
     for sc in scenes:
         plain_frame(sc)
-        jid = sv.submit(sc)
-        sv.wait(jid)
-        sv.release(jid)
+    # every slot meets the requests' sizes before the timed runs (buffers grown,
+    # graphs captured), as on a server that has been up for a while
+    for _ in range(2):
+        ids = [sv.submit(sc) for sc in scenes]
+        for jid in ids:
+            sv.wait(jid)
+            sv.release(jid)
 
     def plain_run(poisson: bool):
         lat = []
@@ -449,16 +460,27 @@ def run_served(args):
                 if now < arrivals[k]:
                     time.sleep(arrivals[k] - now)
             ids.append((sv.submit(scenes[i]), arrivals[k] if poisson else 0.0))
-        lat = []
+        lat, service, device, phases = [], [], [], []
         for jid, arr in ids:
             rc, info = sv.wait(jid)
             if rc != 0:
                 raise RuntimeError("served job failed: " + sv.error(jid))
-            lat.append(time.perf_counter() - start - arr)  # upper bound: waits are in submit order
+            # the server's own clock: submission (= arrival) to completion
+            lat.append(info.t_done - info.t_submit)
+            service.append(info.t_done - info.t_admit)
+            device.append(info.ms_device / 1e3)
+            phases.append((info.ms_prepare, info.ms_render, info.ms_read))
             sv.release(jid)
+        ph = np.mean(np.array(phases), axis=0)
+        served_run.breakdown = {"mean_service_ms": 1e3 * float(np.mean(service)),
+                                "mean_device_ms": 1e3 * float(np.mean(device)),
+                                "mean_prepare_ms": float(ph[0]), "mean_render_ms": float(ph[1]),
+                                "mean_read_ms": float(ph[2])}
         return time.perf_counter() - start, lat
 
+    del plain_phases[:]
     plain_sat, _ = plain_run(False)
+    pph = 1e3 * np.mean(np.array(plain_phases), axis=0)
     served_sat, _ = served_run(False)
     plain_p, plain_lat = plain_run(True)
     served_p, served_lat = served_run(True)
@@ -477,8 +499,12 @@ def run_served(args):
                        "micropolygons_per_s_saturated": mps_total / served_sat,
                        "latency_ms_poisson": {"p50": 1e3 * float(np.percentile(served_lat, 50)),
                                               "p99": 1e3 * float(np.percentile(served_lat, 99))},
-                       "peak_jobs_in_flight": st["peak_running"], "peak_hbm_bytes": st["peak_in_use"]},
-            "plain": {"frames_per_s_saturated": args.jobs / plain_sat,
+                       "peak_jobs_in_flight": st["peak_running"], "peak_hbm_bytes": st["peak_in_use"],
+                       "graphs_built": st["graphs_built"], "rerenders": st["rerenders"],
+                       "poisson_run": served_run.breakdown},
+            "plain": {"saturated_run": {"mean_prepare_ms": float(pph[0]), "mean_render_ms": float(pph[1]),
+                                        "mean_read_ms": float(pph[2])},
+                      "frames_per_s_saturated": args.jobs / plain_sat,
                       "micropolygons_per_s_saturated": mps_total / plain_sat,
                       "latency_ms_poisson": {"p50": 1e3 * float(np.percentile(plain_lat, 50)),
                                              "p99": 1e3 * float(np.percentile(plain_lat, 99))}},
@@ -500,7 +526,7 @@ def main():
     ap.add_argument("--jobs", type=int, default=256)
     ap.add_argument("--distinct", type=int, default=32)
     ap.add_argument("--gap-ms", type=float, default=20.0)
-    ap.add_argument("--slots", type=int, default=6)
+    ap.add_argument("--slots", type=int, default=2)
     ap.add_argument("--max-mps", type=float, default=8e6)
     ap.add_argument("--slot-mode", default="batched", choices=["batched", "plain"],
                     help="served slots: persistent kernel + CUDA graph (batched) or one launch per stage")

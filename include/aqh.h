@@ -245,6 +245,9 @@ typedef struct {
 	int64_t tile_grid_pairs;      /* grid references the tile lists hold */
 	int64_t fragments;            /* transparent fragments stored */
 	float ms_bin, ms_sample, ms_filter, ms_total;  /* device time per stage of the last render */
+	int64_t graphs_built;         /* batched mode: frame graphs captured by this context so far */
+	int64_t rerenders;            /* batched mode: frames rendered again on the plain path because
+	                                 a device list outgrew its capacity */
 } aqh_frame_stats;
 aqh_status aqh_get_stats(aqh_ctx* ctx, aqh_frame_stats* st);
 
@@ -291,11 +294,15 @@ typedef struct {
 	size_t footprint;    /* estimated HBM bytes while running */
 	float ms_device;     /* device time of the frame */
 	int slot;
+	/* host time of the job's phases on its slot: frame options, sample
+	 * patterns and grids in; render to completion; results out */
+	float ms_prepare, ms_render, ms_read;
 } aqh_job_info;
 typedef struct {
 	size_t budget, in_use, peak_in_use;
 	int64_t pending, completed;
 	int running, peak_running;
+	int64_t graphs_built, rerenders;  /* summed over the slots (see aqh_frame_stats) */
 } aqh_server_info;
 aqh_status aqh_server_create(const aqh_server_opts* opts, aqh_server** out);
 void aqh_server_destroy(aqh_server* s);
