@@ -354,7 +354,7 @@ struct aqh_ctx {
 	DevBuf d_cu, d_cv, d_nkeys, d_flags, d_tbase, d_pbase, d_cbase, d_mpbase, d_times, d_culled, d_P, d_Ci, d_Oi;
 	DevBuf d_mpcount;
 	DevBuf d_rect, d_minz, d_strips, d_stcount, d_stoffset, d_stlist, d_idgrid;
-	DevBuf d_sa, d_sb, d_win, d_oz, d_nf, d_hz, d_keys;
+	DevBuf d_sa, d_sb, d_win, d_oz, d_nf, d_hz, d_keys, d_wmask;
 	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err;
 	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb;
 	bool dev_motion = false;
@@ -873,10 +873,16 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	const size_t nstore = store_size((long long)fp.sw * fp.sh, fp.spp);
 	AQH_TRY(ctx->d_sa.ensure(nstore * sizeof(float4)), "alloc sample store");
 	AQH_TRY(ctx->d_sb.ensure(nstore * sizeof(float4)), "alloc sample store");
+	// window masks pay off where positions vary across the filter window and
+	// pixels hold few samples (measured: 16 samples, 3x3 pixels)
+	const bool wmask = fp.spp <= 16 && (fp.shiftX > 0 || fp.shiftY > 0) &&
+	                   (2 * fp.shiftX + 1) * (2 * fp.shiftY + 1) <= 32;
+	if (wmask) AQH_TRY(ctx->d_wmask.ensure(nstore * sizeof(uint32_t)), "alloc window masks");
 	SampleStore& store = P.store;
 	store = SampleStore{};
 	store.a = ctx->d_sa.as<float4>();
 	store.b = ctx->d_sb.as<float4>();
+	if (wmask) store.wmask = ctx->d_wmask.as<uint32_t>();
 	if (ctx->debug_samples) {
 		AQH_TRY(ctx->d_win.ensure(P.nsamp * 4), "alloc");
 		AQH_TRY(ctx->d_oz.ensure(P.nsamp * 4), "alloc");

@@ -107,6 +107,9 @@ struct SampleStore {
 	int32_t* nfrag;   // debug: transparent fragment count (or null)
 	float* hitz;      // depth of the occluding hit when occlZ tracks the second-nearest
 	                  // depth (midpoint depth filter with a z display), else null
+	uint32_t* wmask;  // per sample (store layout): bit (fy + shiftY) * (2 shiftX + 1) + fx + shiftX set
+	                  // when the sample is inside the filter window of the display pixel at
+	                  // offset (-fx, -fy); null: the filter tests sample positions itself
 	unsigned long long* keys;  // opaque frames: (ordered depth, id + 1) of each sample's occluding
 	                           // hit, sample-major, resolved by a separate kernel; null: the
 	                           // sampler resolves in place

@@ -33,15 +33,22 @@ filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __res
 		for (int fx = -xmax; fx <= xmax; fx++) {
 			const int px = x + fx;
 			const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
-			const long long pat = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
-			const int index = ((fy + ymax) * (2 * xmax + 1) + fx + xmax) * spp;
+			const long long pat = (st.wmask || !smp.pos_index) ? pix : (long long)__ldg(smp.pos_index + pix);
+			const int bit = (fy + ymax) * (2 * xmax + 1) + fx + xmax;
+			const int index = bit * spp;
 			const float fpx = (float)px, fpy = (float)py;
 #pragma unroll 4
 			for (int i = 0; i < spp; ++i) {
-				const float2 o = __ldg(smp.pos + pat * spp + i);
-				const float vx = (fpx + o.x) - xcent;
-				const float vy = (fpy + o.y) - ycent;
-				if (vx >= -fp.xfwo2 && vy >= -fp.yfwo2 && vx <= fp.xfwo2 && vy <= fp.yfwo2) {
+				bool inside;
+				if (st.wmask) {
+					inside = (__ldg(st.wmask + store_index(pix, i, spp)) >> bit) & 1u;
+				} else {
+					const float2 o = __ldg(smp.pos + pat * spp + i);
+					const float vx = (fpx + o.x) - xcent;
+					const float vy = (fpy + o.y) - ycent;
+					inside = vx >= -fp.xfwo2 && vy >= -fp.yfwo2 && vx <= fp.xfwo2 && vy <= fp.yfwo2;
+				}
+				if (inside) {
 					const float gw = __ldg(ftab + index + i);
 					gTot += gw;
 					const float4 b = __ldg(st.b + store_index(pix, i, spp));

@@ -548,6 +548,7 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		const float2 o = __ldg(smp.pos + pat * spp + si);
 		resolve_sample<TRANSP>(fp, g, pool, st, pix * spp + si, store_index(pix, si, spp), (float)px + o.x, (float)py + o.y,
 		                       sm.soz[s], sm.swin[s], TRANSP ? fhead[s] : -1);
+		if (st.wmask) st.wmask[store_index(pix, si, spp)] = window_mask(fp, px, py, (float)px + o.x, (float)py + o.y);
 	}
 	}  // tile loop
 }
@@ -609,6 +610,7 @@ struct SmemO {
 	float blkmax[16];
 	uint32_t flag[kTileSampMax / 32];       // samples replayed in order this round
 	uint32_t sticky[kTileSampMax / 32];     // samples replayed in order for the rest of the tile
+	uint32_t dirty[kTilePixMax / 32];       // pixels whose samples changed this round
 };
 
 template <bool PERSIST>
@@ -653,6 +655,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		sm.flag[i] = 0u;
 		sm.sticky[i] = 0u;
 	}
+	if (t < kTilePixMax / 32) sm.dirty[t] = 0u;
 	for (int i = t; i < kTilePixMax; i += kThreadsS) {
 		sm.pixmax[i] = FLT_MAX;
 		const int px = tpx0 + i % fp.tile_w, py = tpy0 + i / fp.tile_w;
@@ -755,10 +758,12 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 			inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y, (r.bits & kRecLinear) != 0, x, y, u,
 			             v);
 			const float D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
-			if (!(D >= r.bminz) || D == 0.0f)
+			if (!(D >= r.bminz) || D == 0.0f) {
 				atomicOr(&sm.flag[s >> 5], 1u << (s & 31));
-			else
-				atomicMin(&sm.key[s], depth_key(D, r.id));
+			} else {
+				const unsigned long long k = depth_key(D, r.id);
+				if (k < atomicMin(&sm.key[s], k)) atomicOr(&sm.dirty[pl >> 5], 1u << (pl & 31));
+			}
 		}
 		__syncthreads();
 		int anyf = 0;
@@ -820,6 +825,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 					}
 					if (lane == 0) {
 						sm.key[s] = depth_key(oz, w);
+						atomicOr(&sm.dirty[pl >> 5], 1u << (pl & 31));
 						if (oz != oz || oz == 0.0f) atomicOr(&sm.sticky[s >> 5], 1u << (s & 31));
 					}
 				}
@@ -827,8 +833,10 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		}
 		__syncthreads();
 
-		// ---- end of round: state, largest occluding depths, flags ----
+		// ---- end of round: state and largest occluding depth of the pixels
+		// whose samples changed, flags ----
 		for (int pp = t; pp < tpix; pp += kThreadsS) {
+			if (!(sm.dirty[pp >> 5] & (1u << (pp & 31)))) continue;
 			float mx = -FLT_MAX;
 			for (int k = 0; k < spp; ++k) {
 				const unsigned long long kk = sm.key[pp * spp + k];
@@ -839,6 +847,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		}
 		for (int i = t; i < nflagw; i += kThreadsS) sm.flag[i] = sm.sticky[i];
 		__syncthreads();
+		if (t < kTilePixMax / 32) sm.dirty[t] = 0u;
 		if (t < 16) {
 			const int nbx = (fp.tile_w + 3) >> 2;
 			const int bx = t % nbx, by = t / nbx;
@@ -876,6 +885,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		const unsigned long long kk = sm.key[pl * spp + si];
 		resolve_sample<false>(fp, g, nopool, st, pix * spp + si, store_index(pix, si, spp), (float)px + o.x, (float)py + o.y,
 		                      key_depth(kk), key_winner(kk), -1);
+		if (st.wmask) st.wmask[store_index(pix, si, spp)] = window_mask(fp, px, py, (float)px + o.x, (float)py + o.y);
 	}
 	}  // tile loop
 }
@@ -896,6 +906,7 @@ resolve_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, SampleStore st
 	const unsigned long long kk = st.keys[q];
 	resolve_sample<false>(fp, g, FragPool{}, st, pix * fp.spp + si, q, (float)px + o.x, (float)py + o.y,
 	                      key_depth(kk), key_winner(kk), -1);
+	if (st.wmask) st.wmask[q] = window_mask(fp, px, py, (float)px + o.x, (float)py + o.y);
 }
 
 }  // namespace

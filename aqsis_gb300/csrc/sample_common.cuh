@@ -93,6 +93,26 @@ __device__ __forceinline__ void hit_colour(const GridsDev& g, int gi, int m, flo
 	flg = ((gflags & 2) ? 1 : 0) | ((gflags & 4) ? 2 : 0);
 }
 
+// FilterBucket's in-window test (bucketprocessor.cpp:609-614) for one sample
+// at (x, y) of pixel (px, py) against every display pixel whose filter
+// reaches it, as a bitmask: bit (fy + shiftY) * (2 shiftX + 1) + fx + shiftX
+// is set when the sample lies inside the window of display pixel
+// (px - fx, py - fy).  The float operations are the filter's own, so the
+// filter reads the bit instead of repeating the test per display pixel.
+__device__ __forceinline__ uint32_t window_mask(const FrameParams& fp, int px, int py, float x, float y) {
+	uint32_t m = 0;
+	const int xmax = fp.shiftX, ymax = fp.shiftY;
+	for (int fy = -ymax; fy <= ymax; ++fy) {
+		const float vy = y - ((float)(py - fy) + 0.5f);
+		for (int fx = -xmax; fx <= xmax; ++fx) {
+			const float vx = x - ((float)(px - fx) + 0.5f);
+			if (vx >= -fp.xfwo2 && vy >= -fp.yfwo2 && vx <= fp.xfwo2 && vy <= fp.yfwo2)
+				m |= 1u << ((fy + ymax) * (2 * xmax + 1) + fx + xmax);
+		}
+	}
+	return m;
+}
+
 // Grid owning a global micropolygon id: from the id table when there is one,
 // else by binary search over the grids' first ids.
 __device__ __forceinline__ int grid_of(const GridsDev& g, int id) {

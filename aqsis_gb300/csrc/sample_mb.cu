@@ -727,6 +727,11 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 		if (w >= 0) mb_sample_attrs(fp, smp, px, py, j, pix, x, y, stime, sdx, sdy, kinv);
 		mb_resolve<TRANSP>(fp, g, pool, st, pix * spp + j, store_index(pix, j, spp), x, y, stime, sdx, sdy,
 		                   sm.soz[s], w, TRANSP ? fhead[s] : -1);
+		if (st.wmask) {
+			const long long pp = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
+			const float2 o = __ldg(smp.pos + pp * spp + j);
+			st.wmask[store_index(pix, j, spp)] = window_mask(fp, px, py, (float)px + o.x, (float)py + o.y);
+		}
 	}
 }
 
@@ -896,6 +901,7 @@ struct SmemP {
 	int tval[kTilePixM];                  // non-NaN times per pixel
 	int wpre[kWarpsM][32];                // per-warp running counts of pixel windows
 	uint32_t surv[kSurvivors];            // kept (candidate, slice) items: slot | slice << 8
+	int ipref[kSurvivors];                // running pixel count of the kept items
 	MbItem items[kSurvivors];             // ... and their bounds, windows and pixel ranges
 	int nsurv;
 	uint32_t wq[kWarpsM][64];             // per-warp queue of (candidate, sample) tests
@@ -1113,83 +1119,95 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 				}
 				__syncwarp();
 			};
-			for (int k = warp; k < nsurv; k += kWarpsM) {
-				const uint32_t e = sm.surv[k];
-				const int c = (int)(e & 0xffu);
-				const MbRec& r = sm.rec[c];
-				const MbItem& it = sm.items[k];
-				const bool moving = r.nkeys > 1;
-				const Bnd& B = it.B;
-				const int w = it.eX - it.sX, nj = it.j1 - it.j0;
-				// the (pixel, sample) pair of queue position q: with motion and depth
-				// of field the samples whose time lies in the slice's window (found
-				// in each pixel's time order, NaN times always included), else the
-				// slice's sample-index window of every pixel
-				const bool windows = moving && usingDof;
-				const int npx = w * (it.eY - it.sY);
-				for (int p0 = 0; p0 < (windows ? npx : 1); p0 += 32) {
-				int wpl = 0, wa = 0, wn = 0, wnv = 0, tot;
-				if (windows) {
-					const int pi = p0 + lane;
-					int cnt = 0;
-					if (pi < npx) {
-						const int px = it.sX + pi % w, py = it.sY + pi / w;
-						wpl = (py - tpy0) * fp.tile_w + (px - tpx0);
+			// pixel counts of the kept items and their running sum: warps take
+			// 32 (item, pixel) slots at a time, several items per warp
+			int npx_t = 0;
+			if (t < nsurv) {
+				const MbItem& it = sm.items[t];
+				npx_t = (it.eX - it.sX) * (it.eY - it.sY);
+			}
+			int totpx;
+			const int ipre = block_excl_sum(sm.warp_tot, npx_t, totpx);
+			if (t < nsurv) sm.ipref[t] = ipre;
+			__syncthreads();
+			for (int g0 = warp * 32; g0 < totpx; g0 += kThreadsM) {
+				// this lane's (item, pixel) and its run of samples: with motion and
+				// depth of field the samples whose time lies in the slice's window
+				// (each pixel's time order; NaN times always included), else the
+				// slice's sample-index window
+				const int gs = g0 + lane;
+				int k = 0, wpl = 0, wa = 0, wn = 0, wnv = 0, cnt = 0, win = 0;
+				if (gs < totpx) {
+					int lo = 0, hi = nsurv - 1;
+					while (lo < hi) {
+						const int mid = (lo + hi + 1) >> 1;
+						if (sm.ipref[mid] <= gs) lo = mid; else hi = mid - 1;
+					}
+					k = lo;
+					const MbItem& it = sm.items[k];
+					const int li = gs - sm.ipref[k], w = it.eX - it.sX;
+					const int px = it.sX + li % w, py = it.sY + li / w;
+					wpl = (py - tpy0) * fp.tile_w + (px - tpx0);
+					win = (sm.rec[sm.surv[k] & 0xffu].nkeys > 1 && usingDof) ? 1 : 0;
+					if (win) {
 						const float* ts = sm.tsort + wpl * spp;
 						wnv = sm.tval[wpl];
-						int lo = 0, hi = wnv;
-						while (lo < hi) {
-							const int mid = (lo + hi) >> 1;
-							if (ts[mid] < it.time0) lo = mid + 1; else hi = mid;
+						int a0 = 0, a1 = wnv;
+						while (a0 < a1) {
+							const int mid = (a0 + a1) >> 1;
+							if (ts[mid] < it.time0) a0 = mid + 1; else a1 = mid;
 						}
-						wa = lo;
-						hi = wnv;
-						while (lo < hi) {
-							const int mid = (lo + hi) >> 1;
-							if (ts[mid] <= it.time1) lo = mid + 1; else hi = mid;
+						wa = a0;
+						a1 = wnv;
+						while (a0 < a1) {
+							const int mid = (a0 + a1) >> 1;
+							if (ts[mid] <= it.time1) a0 = mid + 1; else a1 = mid;
 						}
-						wn = lo - wa;
+						wn = a0 - wa;
 						cnt = wn + (spp - wnv);
+					} else {
+						wa = it.j0;
+						wn = it.j1 - it.j0;
+						wnv = spp;
+						cnt = wn;
 					}
-					int inc = cnt;
-#pragma unroll
-					for (int o = 1; o < 32; o <<= 1) {
-						const int v = __shfl_up_sync(0xffffffffu, inc, o);
-						if (lane >= o) inc += v;
-					}
-					sm.wpre[warp][lane] = inc - cnt;
-					tot = __shfl_sync(0xffffffffu, inc, 31);
-					__syncwarp();
-				} else {
-					tot = w * (it.eY - it.sY) * nj;
 				}
+				int inc = cnt;
+#pragma unroll
+				for (int o = 1; o < 32; o <<= 1) {
+					const int v = __shfl_up_sync(0xffffffffu, inc, o);
+					if (lane >= o) inc += v;
+				}
+				sm.wpre[warp][lane] = inc - cnt;
+				const int tot = __shfl_sync(0xffffffffu, inc, 31);
+				__syncwarp();
 				for (int q0 = 0; q0 < tot; q0 += 32) {
 					const int q = q0 + lane;
-					bool pass = false;
-					int s = 0;
 					int ol = 0;
-					if (windows && q < tot) {
-						int lo = 0, hi = 31;  // last lane whose window starts at or before q
+					if (q < tot) {
+						int lo = 0, hi = 31;  // last lane whose run starts at or before q
 						while (lo < hi) {
 							const int mid = (lo + hi + 1) >> 1;
 							if (sm.wpre[warp][mid] <= q) lo = mid; else hi = mid - 1;
 						}
 						ol = lo;
 					}
-					const int opl = __shfl_sync(0xffffffffu, wpl, ol), oa = __shfl_sync(0xffffffffu, wa, ol);
-					const int on = __shfl_sync(0xffffffffu, wn, ol), onv = __shfl_sync(0xffffffffu, wnv, ol);
+					const int ok = __shfl_sync(0xffffffffu, k, ol), opl = __shfl_sync(0xffffffffu, wpl, ol);
+					const int oa = __shfl_sync(0xffffffffu, wa, ol), on = __shfl_sync(0xffffffffu, wn, ol);
+					const int onv = __shfl_sync(0xffffffffu, wnv, ol), owin = __shfl_sync(0xffffffffu, win, ol);
+					bool pass = false;
+					int s = 0, c = 0;
+					float bz = 0.0f;
 					if (q < tot) {
-						int pl, j;
-						if (windows) {
-							const int k = q - sm.wpre[warp][ol];
-							pl = opl;
-							j = sm.tord[pl * spp + ((k < on) ? oa + k : onv + (k - on))];
-						} else {
-							const int pxy = q / nj;
-							j = it.j0 + (q - pxy * nj);
-							pl = (it.sY + pxy / w - tpy0) * fp.tile_w + (it.sX + pxy % w - tpx0);
-						}
+						const int kk = q - sm.wpre[warp][ol];
+						const int pl = opl;
+						const int j = owin ? sm.tord[pl * spp + ((kk < on) ? oa + kk : onv + (kk - on))] : oa + kk;
 						const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
+						const MbItem& it = sm.items[ok];
+						c = (int)(sm.surv[ok] & 0xffu);
+						const bool moving = sm.rec[c].nkeys > 1;
+						const Bnd& B = it.B;
+						bz = B.mnz;
 						s = pl * spp + j;
 						pass = !(sm.flag[s >> 5] & (1u << (s & 31)));  // else replayed in order below
 						const float stime = sm.stime[s];
@@ -1215,7 +1233,7 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 					if (pass) {
 						const int at = qn + __popc(bal & ((1u << lane) - 1u));
 						wq[at] = (uint32_t)c | ((uint32_t)s << 8);
-						wz[at] = B.mnz;
+						wz[at] = bz;
 					}
 					qn += __popc(bal);
 					__syncwarp();
@@ -1229,8 +1247,7 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 						qn -= 32;
 					}
 				}
-				__syncwarp();  // wpre is rewritten for the next pixels
-				}
+				__syncwarp();  // wpre is rewritten for the next slots
 			}
 			drain(qn);
 			__syncthreads();
@@ -1311,6 +1328,7 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 		const float2 d = lens_offset(smp, sm.dofidx[pl], spp, sm.kinv[s]);
 		mb_resolve<false>(fp, g, FragPool{}, st, pix * spp + j, store_index(pix, j, spp), (float)px + o.x,
 		                  (float)py + o.y, sm.stime[s], d.x, d.y, key_depth_m(kk), key_winner_m(kk), -1);
+		if (st.wmask) st.wmask[store_index(pix, j, spp)] = window_mask(fp, px, py, (float)px + o.x, (float)py + o.y);
 	}
 }
 
