@@ -355,7 +355,7 @@ struct aqh_ctx {
 	DevBuf d_mpcount;
 	DevBuf d_rect, d_minz, d_strips, d_stcount, d_stoffset, d_stlist, d_idgrid;
 	DevBuf d_sa, d_sb, d_win, d_oz, d_nf, d_hz, d_keys, d_wmask;
-	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err;
+	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err, d_occl;
 	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb;
 	bool dev_motion = false;
 	DevBuf d_queue, d_slices;
@@ -905,6 +905,7 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	AQH_TRY(ctx->d_queue.ensure(64), "alloc");
 	FragPool& pool = P.pool;
 	pool = FragPool{};
+	fp.frag_only = 0;
 	if (ctx->any_transparent || !fp.cullable || fp.midpoint_store) {
 		if (ctx->frag_capacity == 0) ctx->frag_capacity = std::max<int64_t>(1 << 20, (int64_t)P.nsamp * 2);
 		AQH_TRY(ctx->d_frag.ensure(ctx->frag_capacity * sizeof(float4)), "alloc fragments");
@@ -916,6 +917,9 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 		pool.count = ctx->d_fcount.as<unsigned long long>();
 		pool.overflow = ctx->d_foverflow.as<int32_t>();
 		pool.capacity = ctx->frag_capacity;
+		AQH_TRY(ctx->d_occl.ensure(16), "alloc");
+		pool.occluders = ctx->d_occl.as<int32_t>();
+		fp.frag_only = (!P.mbdof && !fp.midpoint_store) ? 1 : 0;
 	}
 	if (pool.capacity == 0 && !P.mbdof && ctx->host_packed) {
 		// colours still on their way from the host: the sampler hands its

@@ -39,6 +39,9 @@ struct FrameParams {
 	int cullable;                            // samples are occlusion cullable (depth filter min/midpoint)
 	int depth_filter;
 	int midpoint_store;                      // display_z && depth_filter == midpoint
+	int frag_only;                           // static frame whose hits all become fragments when no
+	                                         // micropolygon occludes (FragPool::occluders == 0) or
+	                                         // samples are not cullable: parallel fragment kernel
 	float zthr[3];
 	float gain, gamma;
 	float q_one, q_min, q_max, q_dither;
@@ -122,6 +125,7 @@ struct FragPool {
 	unsigned long long* count;
 	int64_t capacity;
 	int32_t* overflow;
+	int32_t* occluders;  // nonzero when some micropolygon may be occluding (opaque or matte alpha)
 };
 
 struct BinBuffers {

@@ -340,6 +340,8 @@ template <bool TRANSP, bool PERSIST>
 __global__ void __launch_bounds__(kThreadsS, 2)
 sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, SampleStore st, FragPool pool,
                      int* queue, const int* order) {
+	// a fragment-only frame without occluders is rendered by sample_frag_kernel
+	if (TRANSP && fp.frag_only && !(fp.cullable && *pool.occluders)) return;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	SmemS& sm = *reinterpret_cast<SmemS*>(smem_raw);
 	int32_t* fhead = reinterpret_cast<int32_t*>(smem_raw + sizeof(SmemS));  // TRANSP: fragment lists
@@ -909,6 +911,232 @@ resolve_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, SampleStore st
 	if (st.wmask) st.wmask[q] = window_mask(fp, px, py, (float)px + o.x, (float)py + o.y);
 }
 
+
+// ---- fragment-only frames: parallel hit tests appending fragments --------
+//
+// When no micropolygon of a static frame can be occluding (none opaque, none
+// matte alpha), or samples are not cullable (a z display with the max or
+// average depth filter), StoreSample never sets an occluding hit: occlZ stays
+// FLT_MAX, early-z skips only bounds with min.z > FLT_MAX, and every hit with
+// !(cullable && FLT_MAX <= D) becomes a fragment (bucketprocessor.cpp:
+// 1471-1569).  Which hits are kept then does not depend on order, and Combine
+// orders fragments by (depth, micropolygon id), so (micropolygon, sample)
+// tests run in parallel as on the opaque path and hits are appended to the
+// fragment pool in any order: each block iteration reserves its hits' slots
+// with one atomic and links them into per-sample lists in shared memory.
+constexpr int kSlotsF = 256;
+
+struct SmemF {
+	RecS rec[kSlotsF];
+	int2 pend[kSlotsF];
+	int pref[kSlotsF + 1];
+	int rng[kSlotsF][4];
+	int qgrid[kThreadsS];
+	int qcum[kThreadsS + 1];
+	int qsub[kThreadsS];
+	int patidx[kTilePixMax];
+	int warp_tot[32];
+	int first_reject;
+	int qn;
+	unsigned long long gbase;
+	float pixmax[kTilePixMax];  // stay FLT_MAX: no occluding hits
+	float blkmax[16];
+	int32_t fhead[kTileSampMax];
+};
+
+template <bool PERSIST>
+__global__ void __launch_bounds__(kThreadsS, 2)
+sample_frag_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, SampleStore st, FragPool pool,
+                   int* queue, const int* order) {
+	if (fp.cullable && *pool.occluders) return;  // the ordered kernel renders this frame
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	SmemF& sm = *reinterpret_cast<SmemF*>(smem_raw);
+	__shared__ int next_tile;
+	const int ntiles = fp.ntx * fp.nty;
+	const int cullable = fp.cullable;
+	for (int job = 0;; ++job) {
+	int tile;
+	if (PERSIST) {
+		__syncthreads();
+		if (threadIdx.x == 0) next_tile = atomicAdd(queue, 1);
+		__syncthreads();
+		tile = next_tile;
+		if (tile >= ntiles) break;
+		if (order) tile = order[tile];
+	} else {
+		if (job > 0) break;
+		tile = blockIdx.x;
+	}
+	const int tx = tile % fp.ntx, ty = tile / fp.ntx;
+	const int tpx0 = fp.sx0 + tx * fp.tile_w, tpy0 = fp.sy0 + ty * fp.tile_h;
+	const int tpx1 = min(tpx0 + fp.tile_w, fp.sx0 + fp.sw), tpy1 = min(tpy0 + fp.tile_h, fp.sy0 + fp.sh);
+	const int st_idx = (ty / fp.st_tiles) * fp.nstx + (tx / fp.st_tiles);
+	const int t = threadIdx.x;
+	const int spp = fp.spp, xs = fp.xs, ys = fp.ys;
+	const uint32_t mxs = div_magic(xs), mys = div_magic(ys);
+	const int tpix = fp.tile_w * fp.tile_h;
+	const int tsamp = tpix * spp;
+
+	for (int i = t; i < tsamp; i += kThreadsS) sm.fhead[i] = -1;
+	for (int i = t; i < kTilePixMax; i += kThreadsS) {
+		sm.pixmax[i] = FLT_MAX;
+		const int px = tpx0 + i % fp.tile_w, py = tpy0 + i / fp.tile_w;
+		int pat = 0;
+		if (i < tpix && px < tpx1 && py < tpy1) {
+			const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
+			pat = smp.pos_index ? (int)__ldg(smp.pos_index + pix) : (int)pix;
+		}
+		sm.patidx[i] = pat;
+	}
+	if (t < 16) sm.blkmax[t] = FLT_MAX;
+	if (t == 0) {
+		sm.qn = 0;
+		sm.qcum[0] = 0;
+	}
+	__syncthreads();
+
+	const int lbeg = bb.st_offset[st_idx * bb.nranges];
+	const int lend = (int)min((long long)bb.st_offset[(st_idx + 1) * bb.nranges], (long long)bb.list_capacity);
+	int lp = lbeg, r0 = 0, qtotal = 0, npend = 0;
+	for (;;) {
+		const bool exhausted =
+		    stage_candidates<kSlotsF>(fp, g, bb, sm, tpx0, tpy0, tpx1, tpy1, lend, lp, r0, qtotal, npend);
+		if (npend == 0) break;
+
+		// records and the (candidate, sample) tests, as on the opaque path
+		int ntests = 0;
+		if (t < npend) {
+			const int2 e = sm.pend[t];
+			RecS& r = sm.rec[t];
+			build_record(fp, g, e.x, e.y, r);
+			const int sX = max(r.px0, tpx0), eX = min(r.px1, tpx1);
+			const int sY = max(r.py0, tpy0), eY = min(r.py1, tpy1);
+			int cx0 = ((sX == r.px1 - 1) ? r.em : xs) - ((sX == r.px0) ? r.im : 0);
+			int totx = cx0;
+			if (eX - sX > 1) totx += (eX - sX - 2) * xs + ((eX - 1 == r.px1 - 1) ? r.em : xs);
+			int cy0 = ((sY == r.py1 - 1) ? r.en : ys) - ((sY == r.py0) ? r.in_ : 0);
+			int toty = cy0;
+			if (eY - sY > 1) toty += (eY - sY - 2) * ys + ((eY - 1 == r.py1 - 1) ? r.en : ys);
+			totx = max(totx, 0);
+			toty = max(toty, 0);
+			ntests = totx * toty;
+			sm.rng[t][0] = cx0;
+			sm.rng[t][1] = cy0;
+			sm.rng[t][2] = totx;
+			sm.rng[t][3] = (int)div_magic(totx);
+		}
+		int total;
+		const int pre = block_excl_sum(sm.warp_tot, ntests, total);
+		if (t < npend) sm.pref[t] = pre;
+		__syncthreads();
+
+		// block-uniform sweep: each iteration tests kThreadsS pairs and appends
+		// its hits to the pool with one reservation
+		for (int base = 0; base < total; base += kThreadsS) {
+			const int p = base + t;
+			bool hit = false;
+			int s = 0, id = 0;
+			float D = 0.0f, u = 0.0f, v = 0.0f;
+			if (p < total) {
+				int lo = 0, hi = npend - 1;
+				while (lo < hi) {
+					const int mid = (lo + hi + 1) >> 1;
+					if (sm.pref[mid] <= p) lo = mid; else hi = mid - 1;
+				}
+				const RecS& r = sm.rec[lo];
+				const int k = p - sm.pref[lo];
+				const int cx0 = sm.rng[lo][0], cy0 = sm.rng[lo][1], totx = sm.rng[lo][2];
+				const uint32_t mtot = (uint32_t)sm.rng[lo][3];
+				const int sX = max(r.px0, tpx0), sY = max(r.py0, tpy0);
+				const int ky = div_small(k, totx, mtot), kx = k - ky * totx;
+				int px, m, py, n;
+				if (kx < cx0) {
+					px = sX;
+					m = ((sX == r.px0) ? r.im : 0) + kx;
+				} else {
+					const int q = kx - cx0;
+					const int qd = div_small(q, xs, mxs);
+					px = sX + 1 + qd;
+					m = q - qd * xs;
+				}
+				if (ky < cy0) {
+					py = sY;
+					n = ((sY == r.py0) ? r.in_ : 0) + ky;
+				} else {
+					const int q = ky - cy0;
+					const int qd = div_small(q, ys, mys);
+					py = sY + 1 + qd;
+					n = q - qd * ys;
+				}
+				const int si = n * xs + m;
+				const int pl = (py - tpy0) * fp.tile_w + (px - tpx0);
+				s = pl * spp + si;
+				const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + si);
+				const float x = (float)px + o.x, y = (float)py + o.y;
+				// Contains2D, early-z against occlZ = FLT_MAX, fContains, StoreSample's test
+				hit = !((x < r.bminx || x > r.bmaxx) || (y < r.bminy || y > r.bmaxy)) &&
+				      !(cullable && r.bminz > FLT_MAX) && edges_inside(r.ym, r.xm, r.ex, r.ey, x, y);
+				if (hit) {
+					inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y, (r.bits & kRecLinear) != 0, x,
+					             y, u, v);
+					D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
+					hit = !(cullable && FLT_MAX <= D);
+					id = r.id;
+				}
+			}
+			int nhits;
+			const int rank = block_excl_scan(sm.warp_tot, hit, nhits);
+			if (t == 0 && nhits) sm.gbase = atomicAdd(pool.count, (unsigned long long)nhits);
+			__syncthreads();
+			if (hit) {
+				const long long idx = (long long)sm.gbase + rank;
+				if (idx < pool.capacity) {
+					pool.frag[idx] = make_float4(D, __int_as_float(id), u, v);
+					pool.next[idx] = atomicExch(&sm.fhead[s], (int)idx);
+				} else {
+					atomicOr(pool.overflow, 1);
+				}
+			}
+			__syncthreads();
+		}
+		npend = 0;
+		if (exhausted) break;
+	}
+
+	// ---- resolve: Combine of each sample's fragments ----
+	for (int s = t; s < tsamp; s += kThreadsS) {
+		const int pl = s / spp;
+		const int si = s - pl * spp;
+		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
+		if (px >= tpx1 || py >= tpy1) continue;
+		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
+		const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + si);
+		resolve_sample<true>(fp, g, pool, st, pix * spp + si, store_index(pix, si, spp), (float)px + o.x,
+		                     (float)py + o.y, FLT_MAX, -1, sm.fhead[s]);
+		if (st.wmask) st.wmask[store_index(pix, si, spp)] = window_mask(fp, px, py, (float)px + o.x, (float)py + o.y);
+	}
+	}  // tile loop
+}
+
+// Whether any micropolygon of the frame may be occluding: a grid flagged
+// opaque or matte alpha, no opacity array, or a vertex with every opacity
+// channel at 1 or more (a superset of SqMpgSampleInfo::isOpaque).
+__global__ void occluder_scan_kernel(GridsDev g, int32_t* flag) {
+	const int gi = blockIdx.x;
+	if (gi >= g.ngrids) return;
+	const int gflags = __ldg(g.flags + gi);
+	bool occ = (gflags & (8 | 4)) != 0 || g.Oi == nullptr;
+	if (!occ) {
+		const long long nv = (long long)(__ldg(g.cu + gi) + 1) * (__ldg(g.cv + gi) + 1);
+		const long long cb = __ldg(g.cbase + gi);
+		for (long long i = threadIdx.x; i < nv && !occ; i += blockDim.x) {
+			const float4 o = __ldg(g.Oi + cb + i);
+			occ = o.x >= 1.0f && o.y >= 1.0f && o.z >= 1.0f;
+		}
+	}
+	if (__syncthreads_or(occ) && threadIdx.x == 0) *flag = 1;
+}
+
 }  // namespace
 
 void launch_resolve_opaque(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, SampleStore st,
@@ -942,6 +1170,18 @@ void launch_sample_tiles_q(const FrameParams& fp, const GridsDev& g, const Sampl
 	const bool transp = pool.capacity > 0;
 	const bool split = !transp && st.keys;  // the resolve kernel is the first reader of Ci/Oi
 	if (colours_ready && !split) cudaStreamWaitEvent(s, colours_ready, wait_flags);
+	if (transp && fp.frag_only) {
+		// both kernels are queued; each reads the occluder flag and one returns at once
+		if (fp.cullable) {
+			cudaMemsetAsync(pool.occluders, 0, sizeof(int32_t), s);
+			if (g.ngrids > 0) occluder_scan_kernel<<<g.ngrids, 256, 0, s>>>(g, pool.occluders);
+		}
+		if (queue)
+			sample_frag_kernel<true><<<nctas, kThreadsS, sizeof(SmemF), s>>>(fp, g, sm, b, st, pool, queue, order);
+		else
+			sample_frag_kernel<false><<<ntiles, kThreadsS, sizeof(SmemF), s>>>(fp, g, sm, b, st, pool, nullptr,
+			                                                                  nullptr);
+	}
 	if (queue) {
 		if (transp)
 			sample_static_kernel<true, true><<<nctas, kThreadsS, smem_transp, s>>>(fp, g, sm, b, st, pool, queue, order);
@@ -973,6 +1213,8 @@ void configure_sample_kernels() {
 	cudaFuncSetAttribute(sample_static_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_transp);
 	cudaFuncSetAttribute(sample_opaque_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemO));
 	cudaFuncSetAttribute(sample_static_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_transp);
+	cudaFuncSetAttribute(sample_frag_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemF));
+	cudaFuncSetAttribute(sample_frag_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemF));
 	configure_sample_mb_kernels();
 	configured = true;
 }

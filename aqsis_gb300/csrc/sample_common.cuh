@@ -130,54 +130,55 @@ __device__ __forceinline__ int grid_of(const GridsDev& g, int id) {
 	return lo;
 }
 
-// Entry k of a sample's fragment set in Combine's sort order.  The set is the
-// transparent fragments in insertion order followed by the occluding hit
-// (imagepixel.cpp:155-161), sorted by ascending depth; exact depth ties keep
-// that order.  The list is newest-first, so list position p has sequence
-// n-1-p.  Selection by (depth, sequence) keys needs no per-sample storage.
-struct FragKey { float d; int seq; int idx; };
+// Combine's sort order (imagepixel.cpp:155-161, 188-193): the transparent
+// fragments followed by the occluding hit, sorted by ascending depth; equal
+// depths keep insertion order, which is the micropolygon id order (the
+// occluding hit, id INT_MAX, last).  Entries with the same depth and id are
+// the same micropolygon hit twice at one sample time (a motion slice
+// boundary) and carry the same data.
+struct FragKey { float d; int id; int seq; int idx; };
 
+__device__ __forceinline__ bool key_less(float d, int id, int seq, const FragKey& b) {
+	return d < b.d || (d == b.d && (id < b.id || (id == b.id && seq < b.seq)));
+}
+__device__ __forceinline__ bool key_greater(float d, int id, int seq, const FragKey& b) {
+	return d > b.d || (d == b.d && (id > b.id || (id == b.id && seq > b.seq)));
+}
+
+// Selection form for long lists: the entry after `prev` in ascending order
+// (descending: before it), by a walk over the list.
 __device__ __forceinline__ FragKey next_key(const FragPool& pool, int head, int n, bool has_occl, float occl_d,
                                             FragKey prev, bool first, bool descending) {
-	FragKey best{descending ? -FLT_MAX : FLT_MAX, descending ? -1 : 0x7fffffff, -2};
-	int seq = n - 1;
+	FragKey best{0.0f, 0, 0, -2};
 	bool any = false;
+	auto consider = [&](float d, int id, int seq, int idx) {
+		bool beyond, better;
+		if (descending) {
+			beyond = first || key_less(d, id, seq, prev);
+			better = !any || key_greater(d, id, seq, best);
+		} else {
+			beyond = first || key_greater(d, id, seq, prev);
+			better = !any || key_less(d, id, seq, best);
+		}
+		if (beyond && better) { best = FragKey{d, id, seq, idx}; any = true; }
+	};
+	int seq = n - 1;
 	for (int f = head; f >= 0; f = pool.next[f], --seq) {
-		const float d = pool.frag[f].x;
-		bool beyond, better;
-		if (descending) {
-			beyond = first || d < prev.d || (d == prev.d && seq < prev.seq);
-			better = !any || d > best.d || (d == best.d && seq > best.seq);
-		} else {
-			beyond = first || d > prev.d || (d == prev.d && seq > prev.seq);
-			better = !any || d < best.d || (d == best.d && seq < best.seq);
-		}
-		if (beyond && better) { best = FragKey{d, seq, f}; any = true; }
+		const float4 fr = pool.frag[f];
+		consider(fr.x, __float_as_int(fr.y), seq, f);
 	}
-	if (has_occl) {
-		const float d = occl_d;
-		const int sq = n;
-		bool beyond, better;
-		if (descending) {
-			beyond = first || d < prev.d || (d == prev.d && sq < prev.seq);
-			better = !any || d > best.d || (d == best.d && sq > best.seq);
-		} else {
-			beyond = first || d > prev.d || (d == prev.d && sq > prev.seq);
-			better = !any || d < best.d || (d == best.d && sq < best.seq);
-		}
-		if (beyond && better) best = FragKey{d, sq, -1};
-	}
+	if (has_occl) consider(occl_d, 0x7fffffff, n, -1);
 	return best;
 }
 
-__device__ __forceinline__ void key_data(const GridsDev& g, const FragPool& pool, const FragKey& k,
-                                         const float occl[7], int occl_flags, float dat[7], int& flg) {
-	if (k.idx == -1) {
+__device__ __forceinline__ void key_data(const GridsDev& g, const FragPool& pool, int idx, const float occl[7],
+                                         int occl_flags, float dat[7], int& flg) {
+	if (idx == -1) {
 #pragma unroll
 		for (int q = 0; q < 7; ++q) dat[q] = occl[q];
 		flg = occl_flags;
 	} else {
-		const float4 fr = pool.frag[k.idx];
+		const float4 fr = pool.frag[idx];
 		const int id = __float_as_int(fr.y);
 		const int gi = grid_of(g, id);
 		hit_colour(g, gi, id - (int)__ldg(g.mpbase + gi), fr.z, fr.w, dat, flg);
@@ -185,25 +186,58 @@ __device__ __forceinline__ void key_data(const GridsDev& g, const FragPool& pool
 	}
 }
 
+constexpr int kCombineLocal = 24;  // lists up to this long are sorted in local memory
+
 // CqImagePixel::Combine for a sample with transparent fragments
 // (imagepixel.cpp:155-301).  Returns the fragment count; writes the collapsed
 // sample into occl / occl_flags.
 __device__ inline int combine_fragments(const FrameParams& fp, const GridsDev& g, const FragPool& pool, int head,
-                                 bool has_occl, float occlZ, float occl[7], int& occl_flags) {
+                                        bool has_occl, float occlZ, float occl[7], int& occl_flags) {
 	int n = 0;
-	for (int f = head; f >= 0; f = pool.next[f]) ++n;
+	bool nan = occl[6] != occl[6];
+	for (int f = head; f >= 0; f = pool.next[f]) {
+		++n;
+		const float d = pool.frag[f].x;
+		nan |= d != d;
+	}
 	const int ntot = n + (has_occl ? 1 : 0);
+	// short lists: the entries sorted once (insertion sort, ascending key);
+	// long ones (or NaN depths) are walked in order by selection
+	const bool local = ntot <= kCombineLocal && !nan;
+	FragKey ent[kCombineLocal];
+	if (local) {
+		int m = 0, seq = n - 1;
+		auto insert = [&](float d, int id, int sq, int idx) {
+			int k = m++;
+			while (k > 0 && key_less(d, id, sq, ent[k - 1])) {
+				ent[k] = ent[k - 1];
+				--k;
+			}
+			ent[k] = FragKey{d, id, sq, idx};
+		};
+		for (int f = head; f >= 0; f = pool.next[f], --seq) {
+			const float4 fr = pool.frag[f];
+			insert(fr.x, __float_as_int(fr.y), seq, f);
+		}
+		if (has_occl) insert(occl[6], 0x7fffffff, n, -1);
+	}
 	float sc[3] = {0, 0, 0}, so[3] = {0, 0, 0};
 	float opaque0 = occlZ, opaque1 = FLT_MAX, maxOpaque = FLT_MAX;
 	float top[7] = {0, 0, 0, 0, 0, 0, 0};
 	int top_flags = 0;
-	FragKey prev{0, 0, -2};
+	FragKey prev{0.0f, 0, 0, -2};
+	// back to front (imagepixel.cpp:196-246)
 	for (int k = 0; k < ntot; ++k) {
-		const FragKey key = next_key(pool, head, n, has_occl, occl[6], prev, k == 0, true);
-		prev = key;
+		int idx;
+		if (local) {
+			idx = ent[ntot - 1 - k].idx;
+		} else {
+			prev = next_key(pool, head, n, has_occl, occl[6], prev, k == 0, true);
+			idx = prev.idx;
+		}
 		float dat[7];
 		int flg;
-		key_data(g, pool, key, occl, occl_flags, dat, flg);
+		key_data(g, pool, idx, occl, occl_flags, dat, flg);
 		if (flg & 1) {
 			float nc[3], no[3];
 #pragma unroll
@@ -245,13 +279,18 @@ __device__ inline int combine_fragments(const FrameParams& fp, const GridsDev& g
 		// ascending order (imagepixel.cpp:279-296)
 		float tot = 0.0f;
 		int cnt = 0;
-		FragKey pk{0, 0, -2};
+		FragKey pk{0.0f, 0, 0, -2};
 		for (int k = 0; k < ntot; ++k) {
-			const FragKey key = next_key(pool, head, n, has_occl, occl[6], pk, k == 0, false);
-			pk = key;
+			int idx;
+			if (local) {
+				idx = ent[k].idx;
+			} else {
+				pk = next_key(pool, head, n, has_occl, occl[6], pk, k == 0, false);
+				idx = pk.idx;
+			}
 			float dat[7];
 			int flg;
-			key_data(g, pool, key, occl, occl_flags, dat, flg);
+			key_data(g, pool, idx, occl, occl_flags, dat, flg);
 			if (dat[3] >= fp.zthr[0] || dat[4] >= fp.zthr[1] || dat[5] >= fp.zthr[2]) {
 				tot += dat[6];
 				cnt++;
