@@ -158,3 +158,21 @@ def _take(g, a, b):
     sub = S._pack(g.cu[a:b], g.cv[a:b], g.nkeys[a:b], g.flags[a:b], g.P[p0:p1], g.Ci[c0:c1], g.Oi[c0:c1],
                   g.times[t0:t1], (g.tbase[a:b] - t0))
     return sub
+
+
+def transparent_hidden_occluder(seed=8, xs=4, ys=4):
+    """Transparent grids plus a grid not flagged opaque whose opacity is 1 on
+    every vertex: its micropolygons occlude (SqMpgSampleInfo::isOpaque), so
+    the frame must take the ordered path although no grid says so."""
+    rng = np.random.default_rng(seed)
+    fr = S.Frame(width=40, height=32, xsamples=xs, ysamples=ys, filter="gaussian", xfilter=2.0, yfilter=2.0,
+                 q_dither=0.0)
+    parts = []
+    for k in range(5):
+        op = rng.uniform(0.2, 0.8, (49, 3))
+        parts.append(plane(rng.uniform(0, 30), rng.uniform(0, 22), 6, 6, float(rng.uniform(5, 60)), rng=rng,
+                           jitter=0.3, oi=op))
+    occ = plane(6, 6, 20, 14, 30.0, step=1.3, rng=rng, jitter=0.2)
+    occ.flags = (occ.flags & ~S.GRID_OPAQUE).astype(np.int32)   # opaque by value, not by flag
+    parts.insert(2, occ)
+    return custom(fr, S.concat_grids(parts), seed=seed)

@@ -88,6 +88,12 @@ def test_transparent_edge_cases(hider, oracle, xs, ys):
     compare(res, ref)
 
 
+def test_transparent_frame_with_unflagged_occluder(hider, oracle):
+    res, ref = run_both(hider, oracle, SS.transparent_hidden_occluder())
+    compare(res, ref)
+    assert (res["winner"] >= 0).any()  # the unflagged grid does occlude
+
+
 def test_crop_window_and_exposure(hider, oracle):
     sc = SS.edge_cases(seed=51)
     sc.frame.crop = (7, 50, 5, 40)
