@@ -353,7 +353,7 @@ struct aqh_ctx {
 	// device buffers
 	DevBuf d_cu, d_cv, d_nkeys, d_flags, d_tbase, d_pbase, d_cbase, d_mpbase, d_times, d_culled, d_P, d_Ci, d_Oi;
 	DevBuf d_mpcount;
-	DevBuf d_rect, d_minz, d_strips, d_stcount, d_stoffset, d_stlist, d_idgrid;
+	DevBuf d_rect, d_minz, d_strips, d_tri, d_stcount, d_stoffset, d_stlist, d_idgrid;
 	DevBuf d_sa, d_sb, d_win, d_oz, d_nf, d_hz, d_keys, d_wmask;
 	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err, d_occl;
 	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb;
@@ -868,6 +868,8 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	bb.grid_minz = ctx->d_minz.as<float>();
 	AQH_TRY(ctx->d_strips.ensure(sizeof(uint32_t) * 64 * std::max(G, 1)), "alloc strips");
 	bb.strips = ctx->d_strips.as<uint32_t>();
+	AQH_TRY(ctx->d_tri.ensure(sizeof(float4) * kMaxKeys * std::max(G, 1)), "alloc split lines");
+	bb.tri = ctx->d_tri.as<float4>();
 	bb.st_count = ctx->d_stcount.as<int32_t>();
 	bb.st_offset = ctx->d_stoffset.as<int32_t>();
 	const size_t nstore = store_size((long long)fp.sw * fp.sh, fp.spp);

@@ -134,6 +134,8 @@ struct BinBuffers {
 	int32_t* st_count;     // [nst][nranges]
 	int32_t* st_offset;    // exclusive scan of st_count, plus total at the end
 	int32_t* st_list;      // grid ids per super-tile, in grid order
+	float4* tri;           // per grid and motion key (kMaxKeys each): the triangle split line
+	                       // (A.x, A.y, B.x, B.y) of triangular grids; may be null (no such grids)
 	uint32_t* strips;      // per grid 64 words, or null: [0, 32) the pixel range [lo, hi) of each
 	                       // micropolygon column, [32, 63) of each row (lo | hi << 16, int16 each);
 	                       // word 63 = 1 when present (one motion key, cu and cv at most 31)

@@ -64,7 +64,8 @@ __device__ __forceinline__ void grid_strips(const float4* P, int cu, int cv, int
 	if (lane < cu) S[lane] = pack_range(fminf(cmn, nmn), fmaxf(cmx, nmx), cbad || nbad);
 }
 
-__global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect, float* minz, uint32_t* strips) {
+__global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect, float* minz, uint32_t* strips,
+                                  float4* tri) {
 	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const int lane = threadIdx.x & 31;
 	if (warp >= g.ngrids) return;
@@ -96,6 +97,18 @@ __global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect, float*
 	}
 	if (lane != 0) return;
 	minz[warp] = mnz;
+	if (tri && (g.flags[warp] & 16)) {
+		// triangle split line per key (micropolygon.cpp:703-719, 737-746): through
+		// corners cu and cv*(cu+1), ordered so that the kept side is positive
+		const float4* Pg = g.P + g.pbase[warp];
+		for (int k = 0; k < nk && k < kMaxKeys; ++k) {
+			const long long kb = (long long)k * (cu + 1) * (cv + 1);
+			const float4 v0 = Pg[kb], v1 = Pg[kb + cu], v2 = Pg[kb + (long long)cv * (cu + 1)];
+			const bool cw = ((v1.x - v0.x) * (v2.y - v0.y) - (v1.y - v0.y) * (v2.x - v0.x)) >= 0;
+			tri[(long long)warp * kMaxKeys + k] = cw ? make_float4(v1.x, v1.y, v2.x, v2.y)
+			                                         : make_float4(v2.x, v2.y, v1.x, v1.y);
+		}
+	}
 	if (fp.use_dof) {
 		float2 c1 = coc(mnz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
 		float2 c2 = coc(mxz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
@@ -238,7 +251,7 @@ void launch_id_grid(const GridsDev& g, int64_t nmps, int32_t* table, cudaStream_
 void launch_grid_rects(const FrameParams& fp, const GridsDev& g, const BinBuffers& b, cudaStream_t s) {
 	if (g.ngrids == 0) return;
 	const int wpb = kBlock / 32;
-	grid_rects_kernel<<<(g.ngrids + wpb - 1) / wpb, kBlock, 0, s>>>(fp, g, b.grid_rect, b.grid_minz, b.strips);
+	grid_rects_kernel<<<(g.ngrids + wpb - 1) / wpb, kBlock, 0, s>>>(fp, g, b.grid_rect, b.grid_minz, b.strips, b.tri);
 }
 
 void launch_st_count(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s) {

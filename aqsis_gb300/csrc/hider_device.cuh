@@ -203,4 +203,13 @@ __device__ __forceinline__ float2 project_to_circle(float x, float y) {
 	return make_float2(adj * x, adj * y);
 }
 
+// The triangle split line test of CqMicroPolygon::Sample and
+// CqMicroPolygonMotion::Sample (micropolygon.cpp:1630-1654, 1885-1907): line
+// (A.x, A.y, B.x, B.y); a hit at (hx, hy) on or behind it misses.
+__device__ __forceinline__ bool triangle_keeps(float4 l, float hx, float hy) {
+	const float Ax = l.x, Ay = l.y, Bx = l.z, By = l.w;
+	const float v = (Ay - By) * hx + (Bx - Ax) * hy + (Ax * By - Bx * Ay);
+	return !(v <= 0);
+}
+
 }  // namespace aqh

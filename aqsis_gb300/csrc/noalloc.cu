@@ -168,6 +168,8 @@ extern "C" aqh_status aqh_render_noalloc(const aqh_frame_desc* desc, const float
 			return na_fail(err, err_len, AQH_ELIMIT,
 			               "aqh_render_noalloc: every grid must be opaque (AQH_GRID_OPAQUE); transparency needs "
 			               "the fragment pool of the context path");
+		if (flags[i] & AQH_GRID_TRIANGULAR)
+			return na_fail(err, err_len, AQH_ELIMIT, "aqh_render_noalloc: triangular grids are not supported");
 		mpb[i] = acc;
 		acc += (int64_t)cu[i] * cv[i];
 	}

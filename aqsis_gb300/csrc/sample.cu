@@ -54,7 +54,12 @@ struct RecS {
 	int bits;                      // 1 linear, 2 occluding store
 };  // 43 words: an odd stride spreads neighbouring records over the banks
 
-constexpr int kRecLinear = 1, kRecOccluding = 2;
+constexpr int kRecLinear = 1, kRecOccluding = 2, kRecTriangular = 4;  // RecS::bits; the grid index sits above bit 3
+
+// The triangle split line of the record's grid (key 0: static micropolygons).
+__device__ __forceinline__ bool rec_keeps(const BinBuffers& bb, int bits, float x, float y) {
+	return !(bits & kRecTriangular) || triangle_keeps(__ldg(bb.tri + (size_t)(bits >> 3) * kMaxKeys), x, y);
+}
 
 struct SmemS {
 	RecS rec[kSlotsS];
@@ -141,6 +146,7 @@ __device__ __forceinline__ void build_record(const FrameParams& fp, const GridsD
 	}
 	int bits = h.linear ? kRecLinear : 0;
 	if (opaque || (gflags & 4)) bits |= kRecOccluding;
+	if (gflags & 16) bits |= kRecTriangular | (gi << 3);
 	rec.bits = bits;
 }
 
@@ -463,8 +469,8 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 						inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y,
 						             (r.bits & kRecLinear) != 0, x, y, u, v);
 						const float D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
-						// StoreSample (bucketprocessor.cpp:1471-1569)
-						if (!(cullable && oz <= D)) {
+						// StoreSample (bucketprocessor.cpp:1471-1569) for a hit the split line keeps
+						if (rec_keeps(bb, r.bits, x, y) && !(cullable && oz <= D)) {
 							if ((r.bits & kRecOccluding) && cullable) {
 								if (TRANSP && fp.midpoint_store) {
 									// midpoint filter with a z display (bucketprocessor.cpp:1502-1530):
@@ -760,6 +766,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 			inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y, (r.bits & kRecLinear) != 0, x, y, u,
 			             v);
 			const float D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
+			if (!rec_keeps(bb, r.bits, x, y)) continue;
 			if (!(D >= r.bminz) || D == 0.0f) {
 				atomicOr(&sm.flag[s >> 5], 1u << (s & 31));
 			} else {
@@ -810,6 +817,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 								D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
 								bz = r.bminz;
 								id = r.id;
+								hit = rec_keeps(bb, r.bits, x, y);
 							}
 						}
 						uint32_t hb = __ballot_sync(0xffffffffu, hit);
@@ -1080,7 +1088,7 @@ sample_frag_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sa
 					inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y, (r.bits & kRecLinear) != 0, x,
 					             y, u, v);
 					D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
-					hit = !(cullable && FLT_MAX <= D);
+					hit = rec_keeps(bb, r.bits, x, y) && !(cullable && FLT_MAX <= D);
 					id = r.id;
 				}
 			}

@@ -64,7 +64,7 @@ __device__ __forceinline__ bool dof_in_bound(const Bnd& b, float cminx, float cm
 // (static, with DoF) or CqMicroPolygonMotion::Sample.  On a hit returns depth
 // and (u,v).
 __device__ bool mb_sample(const FrameParams& fp, const MbRec& r, bool moving, bool dof, float px, float py,
-                          float time, float dx, float dy, float& D, float& u, float& v) {
+                          float time, float dx, float dy, float& D, float& u, float& v, const float4* tri = nullptr) {
 	V3f pts[4];
 	if (!moving) {
 		// dof only (the static no-DoF case never reaches this kernel)
@@ -135,6 +135,41 @@ __device__ bool mb_sample(const FrameParams& fp, const MbRec& r, bool moving, bo
 	if (!edges_inside(h.ym, h.xm, h.ex, h.ey, px, py)) return false;
 	inv_bilinear(h.ax, h.ay, h.e_x, h.e_y, h.f_x, h.f_y, h.g_x, h.g_y, h.linear, px, py, u, v);
 	D = bilerp1(h.z[0], h.z[1], h.z[2], h.z[3], u, v);
+	if (tri && (r.bits & 4)) {
+		// triangle split line at the sample time (TriangleSplitPoints,
+		// micropolygon.cpp:895-900, over CqMotionSpec::GetMotionObjectInterpolated,
+		// motion.h:176-228); with depth of field the hit moves back by the
+		// CoC at its depth (micropolygon.cpp:1891-1900)
+		const float4* L = tri + (long long)r.grid * kMaxKeys;
+		const int n = r.nkeys;
+		int i = 0;
+		float F = 0.0f;
+		bool exact = true;
+		if (n > 1) {
+			if (time >= r.kt[n - 1]) {
+				i = n - 1;
+			} else if (time <= r.kt[0]) {
+				i = 0;
+			} else {
+				while (time >= r.kt[i + 1]) i += 1;
+				F = (time - r.kt[i]) / (r.kt[i + 1] - r.kt[i]);
+				exact = (r.kt[i] == time);
+			}
+		}
+		float4 l = __ldg(L + i);
+		if (!exact) {
+			const float4 l1 = __ldg(L + i + 1);
+			l = make_float4(((1.0f - F) * l.x) + (F * l1.x), ((1.0f - F) * l.y) + (F * l1.y),
+			                ((1.0f - F) * l.z) + (F * l1.z), ((1.0f - F) * l.w) + (F * l1.w));
+		}
+		float hx = px, hy = py;
+		if (dof) {
+			const float2 c = coc(D, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+			hx = hx + c.x * dx;
+			hy = hy + c.y * dy;
+		}
+		if (!triangle_keeps(l, hx, hy)) return false;
+	}
 	return true;
 }
 
@@ -231,7 +266,7 @@ __device__ __forceinline__ void build_mb_record(const FrameParams& fp, const Gri
 			opaque = opaque && (o.x >= 1.0f && o.y >= 1.0f && o.z >= 1.0f);
 		}
 	}
-	rr.bits = (opaque || (gflags & 4)) ? 2 : 0;
+	rr.bits = ((opaque || (gflags & 4)) ? 2 : 0) | ((gflags & 16) ? 4 : 0);
 	rr.id = (int)(__ldg(g.mpbase + gi) + m);
 	rr.grid = gi;
 }
@@ -656,7 +691,7 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 							if ((x < TB.mnx || x > TB.mxx) || (y < TB.mny || y > TB.mxy)) continue;
 							if (cullable && B.mnz > oz) continue;
 							float D, u, v;
-							if (!mb_sample(fp, r, moving, usingDof, x, y, stime, sdx, sdy, D, u, v)) continue;
+							if (!mb_sample(fp, r, moving, usingDof, x, y, stime, sdx, sdy, D, u, v, bb.tri)) continue;
 							if (cullable && oz <= D) continue;
 							if ((r.bits & 2) && cullable) {
 								if (TRANSP && fp.midpoint_store) {
@@ -916,7 +951,7 @@ struct SmemP {
 __device__ __forceinline__ bool mb_slice_test(const FrameParams& fp, const MbRec& r, const Bnd& B, bool moving,
                                               float time0, float time1, const float* dofb_k, int px, int py,
                                               float x, float y, float stime, float sdx, float sdy, float oz,
-                                              float& D) {
+                                              float& D, const float4* tri) {
 	if (moving && (stime < time0 || stime > time1)) return false;
 	const Bnd TB = fp.use_dof ? stratum_bound(fp, B, dofb_k) : B;
 	if (px < (int)floorf(TB.mnx) || px >= lceil_f(TB.mxx) || py < (int)floorf(TB.mny) || py >= lceil_f(TB.mxy))
@@ -924,7 +959,7 @@ __device__ __forceinline__ bool mb_slice_test(const FrameParams& fp, const MbRec
 	if ((x < TB.mnx || x > TB.mxx) || (y < TB.mny || y > TB.mxy)) return false;
 	if (B.mnz > oz) return false;
 	float u, v;
-	return mb_sample(fp, r, moving, fp.use_dof != 0, x, y, stime, sdx, sdy, D, u, v);
+	return mb_sample(fp, r, moving, fp.use_dof != 0, x, y, stime, sdx, sdy, D, u, v, tri);
 }
 
 __global__ void __launch_bounds__(kThreadsM, 1)
@@ -1110,7 +1145,7 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 					const float2 d = lens_offset(smp, sm.dofidx[pl], spp, sm.kinv[s]);
 					float D, u, v;
 					if (mb_sample(fp, r, r.nkeys > 1, usingDof, (float)px + o.x, (float)py + o.y, sm.stime[s], d.x, d.y,
-					              D, u, v)) {
+					              D, u, v, bb.tri)) {
 						if (!(D >= wz[lane]) || D == 0.0f)
 							atomicOr(&sm.flag[s >> 5], 1u << (s & 31));
 						else
@@ -1295,7 +1330,7 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 						if (!mb_slice(fp, sh, r, T, div, dt, sb, B, time0, time1, j0, j1)) continue;
 						if (j < j0 || j >= j1) continue;
 						float D;
-						if (!mb_slice_test(fp, r, B, moving, time0, time1, dk, px, py, x, y, stime, d.x, d.y, oz, D))
+						if (!mb_slice_test(fp, r, B, moving, time0, time1, dk, px, py, x, y, stime, d.x, d.y, oz, D, bb.tri))
 							continue;
 						if (!(oz <= D)) {
 							oz = D;

@@ -29,7 +29,7 @@ import numpy as np
 
 FILTERS = {"box": 0, "triangle": 1, "gaussian": 2, "catmull-rom": 3, "sinc": 4,
            "disk": 5, "bessel": 6, "mitchell": 7}
-GRID_SMOOTH, GRID_MATTE, GRID_MATTEALPHA, GRID_OPAQUE = 1, 2, 4, 8
+GRID_SMOOTH, GRID_MATTE, GRID_MATTEALPHA, GRID_OPAQUE, GRID_TRIANGULAR = 1, 2, 4, 8, 16
 FLT_MAX = float(np.finfo(np.float32).max)
 
 

@@ -141,9 +141,9 @@ WORKLOADS = {
 }
 
 
-KERNELS = {"opaque": "sample_opaque_kernel", "transparent": "sample_static_kernel", "mbdof": "sample_mbp_kernel"}
+KERNELS = {"opaque": "sample_opaque_kernel", "transparent": "sample_frag_kernel", "mbdof": "sample_mbp_kernel"}
 # measured DRAM bytes per micropolygon of the sampler launch (ncu, 0.35 scale)
-TRAFFIC_PER_MP = {"opaque": (97.556224e6 + 126.517504e6) / 6_272_000}
+TRAFFIC_PER_MP = {"opaque": (98.411520e6 + 142.133760e6) / 6_272_000}
 
 
 def make_scene(args):

@@ -64,7 +64,9 @@ enum {
 	AQH_GRID_SMOOTH = 1,      /* ShadingInterpolation "smooth": bilinear Ci/Oi across the micropolygon */
 	AQH_GRID_MATTE = 2,       /* Matte 1 (SqImageSample::Flag_Matte) */
 	AQH_GRID_MATTEALPHA = 4,  /* aqsis "matte alpha" (Flag_MatteAlpha) */
-	AQH_GRID_OPAQUE = 8       /* caller guarantees Oi >= 1 on every vertex (skips reading Oi while sampling) */
+	AQH_GRID_OPAQUE = 8,      /* caller guarantees Oi >= 1 on every vertex (skips reading Oi while sampling) */
+	AQH_GRID_TRIANGULAR = 16  /* CqMicroPolyGridBase::fTriangular (micropolygon.h:139-147): hits on or behind
+	                             the line through corners cu and cv*(cu+1) miss (micropolygon.cpp:1630-1654) */
 };
 
 typedef struct aqh_ctx aqh_ctx;

@@ -200,6 +200,9 @@ struct MP {
 	// motion bound list (BuildBoundList)
 	std::vector<Bound> subBounds;
 	std::vector<float> subTimes;
+	// triangle split line per key (CqMicroPolyGridBase::m_TriangleSplitLine)
+	bool triangular;
+	V2 splitA[8], splitB[8];
 	// output cache (SqMpgSampleInfo)
 	float col[4][3], opa[4][3];
 	bool smooth, isOpaque, isCullable;
@@ -386,7 +389,50 @@ static bool dofSampleInBound(const Bound& bound, const HitTestCache& cache, cons
 	return bound.intersects(cocMin, cocMax);
 }
 
-// micropolygon.cpp:1561-1660 (static micropolygon; trimming and triangle grids not modelled).
+// TriangleSplitPoints (micropolygon.cpp:895-900): CqMotionSpec::GetMotionObjectInterpolated
+// (motion.h:176-228) over the per-key split lines, lerped as
+// CqTriangleSplitLine::LinearInterpolateMotionObjects (micropolygon.h:182-188).
+static void triangleSplitPoints(const MP& mp, float time, V2& A, V2& B) {
+	const int n = mp.nkeys;
+	int i = 0;
+	float Fraction = 0.0f;
+	bool exact = true;
+	if (n > 1) {
+		const float* T = mp.keyTimes;
+		if (time >= T[n - 1]) {
+			i = n - 1;
+		} else if (time <= T[0]) {
+			i = 0;
+		} else {
+			i = 0;
+			while (time >= T[i + 1]) i += 1;
+			Fraction = (time - T[i]) / (T[i + 1] - T[i]);
+			exact = (T[i] == time);
+		}
+	}
+	if (exact) {
+		A = mp.splitA[i];
+		B = mp.splitB[i];
+	} else {
+		A = ((1.0f - Fraction) * mp.splitA[i]) + (Fraction * mp.splitA[i + 1]);
+		B = ((1.0f - Fraction) * mp.splitB[i]) + (Fraction * mp.splitB[i + 1]);
+	}
+}
+
+// The triangle split line test of both Sample forms (micropolygon.cpp:1630-1654,
+// 1885-1907): a hit on or behind the line through the grid's far corners misses.
+static bool triangleSplitKeeps(const Ctx& ctx, const MP& mp, const Sample& sample, float D, float time,
+                               bool usingDof) {
+	V2 vA, vB;
+	triangleSplitPoints(mp, time, vA, vB);
+	const float Ax = vA.x, Ay = vA.y, Bx = vB.x, By = vB.y;
+	V2 hitPos = sample.position;
+	if (usingDof) hitPos = hitPos + compMul(ctx.coc(D), sample.dofOffset);
+	const float v = (Ay - By) * hitPos.x + (Bx - Ax) * hitPos.y + (Ax * By - Bx * Ay);
+	return !(v <= 0);
+}
+
+// micropolygon.cpp:1561-1660 (static micropolygon; trimming not modelled).
 static bool sampleStatic(const Ctx& ctx, const MP& mp, HitTestCache& cache, const Sample& sample, float& D, V2& uv,
                          bool usingDof) {
 	V2 vecSample = sample.position;
@@ -402,7 +448,8 @@ static bool sampleStatic(const Ctx& ctx, const MP& mp, HitTestCache& cache, cons
 		}
 		cachePointInPolyTest(mp, cache, points);
 	}
-	return fContains(cache, vecSample, D, uv);
+	if (!fContains(cache, vecSample, D, uv)) return false;
+	return !mp.triangular || triangleSplitKeeps(ctx, mp, sample, D, sample.time, usingDof);
 }
 
 // micropolygon.cpp:1768-1914
@@ -453,7 +500,8 @@ static bool sampleMotion(const Ctx& ctx, const MP& mp, HitTestCache& cache, cons
 		}
 	}
 	cachePointInPolyTest(mp, cache, points);
-	return fContains(cache, vecSample, D, uv);
+	if (!fContains(cache, vecSample, D, uv)) return false;
+	return !mp.triangular || triangleSplitKeeps(ctx, mp, sample, D, time, usingDof);
 }
 
 // Time-sub-bound list (micropolygon.cpp:1689-1756).
@@ -962,6 +1010,22 @@ extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples
 		const long long pb = g->pbase[gi];
 		const long long cb = g->cbase[gi];
 		const int flags = g->flags ? g->flags[gi] : ORC_GRID_SMOOTH;
+		// triangle split line per key (micropolygon.cpp:703-719, 737-746): through the
+		// corners cu and cv*(cu+1), ordered so the kept side is positive
+		mp.triangular = (flags & ORC_GRID_TRIANGULAR) != 0;
+		if (mp.triangular) {
+			for (int k = 0; k < nk; ++k) {
+				const V3 v0 = loadP(g->P, pb + k * nv), v1 = loadP(g->P, pb + k * nv + cu);
+				const V3 v2 = loadP(g->P, pb + k * nv + (long long)cv * (cu + 1));
+				if (((v1.x - v0.x) * (v2.y - v0.y) - (v1.y - v0.y) * (v2.x - v0.x)) >= 0) {
+					mp.splitA[k] = V2(v1.x, v1.y);
+					mp.splitB[k] = V2(v2.x, v2.y);
+				} else {
+					mp.splitA[k] = V2(v2.x, v2.y);
+					mp.splitB[k] = V2(v1.x, v1.y);
+				}
+			}
+		}
 		for (int iv = 0; iv < cv; iv++) {
 			for (int iu = 0; iu < cu; iu++, mpid++) {
 				if (g->culled && g->culled[mpid]) continue;

@@ -34,7 +34,8 @@ enum { ORC_DEPTH_MIN = 0, ORC_DEPTH_MIDPOINT = 1, ORC_DEPTH_MAX = 2, ORC_DEPTH_A
 enum {
 	ORC_GRID_SMOOTH = 1,      /* ShadingInterpolation "smooth" */
 	ORC_GRID_MATTE = 2,       /* SqImageSample::Flag_Matte */
-	ORC_GRID_MATTEALPHA = 4   /* SqImageSample::Flag_MatteAlpha */
+	ORC_GRID_MATTEALPHA = 4,  /* SqImageSample::Flag_MatteAlpha */
+	ORC_GRID_TRIANGULAR = 16  /* CqMicroPolyGridBase::fTriangular: split line through corners cu, cv*(cu+1) */
 };
 
 typedef struct {

@@ -83,6 +83,8 @@ CASES = {
     "dof_only_mini": lambda: SS.dof_only_small(seed=22, scale=0.02),
     "motion_transparent_mini": lambda: SS.motion_dof_small(seed=23, xs=3, ys=3, scale=0.02, transparent=True),
     "reference_patterns": reference_pattern_scene,
+    "triangular_static": lambda: SS.triangular_small(seed=9),
+    "triangular_motion_dof": lambda: SS.triangular(SS.motion_dof_small(seed=10, xs=4, ys=4, scale=0.02), every=2),
 }
 
 

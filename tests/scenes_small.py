@@ -176,3 +176,26 @@ def transparent_hidden_occluder(seed=8, xs=4, ys=4):
     occ.flags = (occ.flags & ~S.GRID_OPAQUE).astype(np.int32)   # opaque by value, not by flag
     parts.insert(2, occ)
     return custom(fr, S.concat_grids(parts), seed=seed)
+
+
+def triangular(sc, every=3):
+    """Mark every `every`-th grid of a scene triangular (fTriangular: the far
+    half of each grid, behind the line through corners cu and cv*(cu+1), is
+    not drawn)."""
+    g = sc.grids
+    f = g.flags.copy()
+    f[::every] |= S.GRID_TRIANGULAR
+    g.flags = f.astype(np.int32)
+    return sc
+
+
+def triangular_small(seed=9):
+    return triangular(edge_cases(seed=seed))
+
+
+def triangular_motion_small(seed=10, dof=True):
+    return triangular(motion_dof_small(seed=seed, dof=dof, xs=4, ys=4, scale=0.03), every=2)
+
+
+def triangular_transparent_small(seed=11):
+    return triangular(transparent_small(seed=seed, scale=0.03), every=2)

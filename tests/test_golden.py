@@ -18,7 +18,7 @@ OUT_KEYS = ("winner", "occlz", "nfrag", "valid", "channels", "quantized")
 
 
 def test_fixtures_present():
-    assert len(FIXTURES) >= 15
+    assert len(FIXTURES) >= 17
 
 
 @pytest.mark.parametrize("path", FIXTURES, ids=NAMES)
@@ -64,10 +64,12 @@ def test_fixtures_cover_the_hider_features():
             feats.add("depth_filter_%d" % fr.depth_filter)
         if fr.q_dither:
             feats.add("dither")
+        if (g.flags & S.GRID_TRIANGULAR).any():
+            feats.add("triangular")
         feats.add("filter_" + fr.filter)
         assert gold["o_valid"].any()
     for f in ("motion", "dof", "transparent", "matte", "culled", "crop", "dither", "depth_filter_1",
-              "depth_filter_2", "depth_filter_3", "filter_box", "filter_gaussian", "filter_catmull-rom"):
+              "depth_filter_2", "depth_filter_3", "filter_box", "filter_gaussian", "filter_catmull-rom", "triangular"):
         assert f in feats, f
 
 

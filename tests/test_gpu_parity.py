@@ -94,6 +94,17 @@ def test_transparent_frame_with_unflagged_occluder(hider, oracle):
     assert (res["winner"] >= 0).any()  # the unflagged grid does occlude
 
 
+@pytest.mark.parametrize("scene_fn", [lambda: SS.triangular_small(),
+                                      lambda: SS.triangular_motion_small(dof=False),
+                                      lambda: SS.triangular_motion_small(dof=True),
+                                      lambda: SS.triangular_transparent_small()],
+                         ids=["static", "motion", "motion_dof", "transparent"])
+def test_triangular_grids(hider, oracle, scene_fn):
+    sc = scene_fn()
+    res, ref = run_both(hider, oracle, sc)
+    compare(res, ref)
+
+
 def test_crop_window_and_exposure(hider, oracle):
     sc = SS.edge_cases(seed=51)
     sc.frame.crop = (7, 50, 5, 40)
