@@ -69,6 +69,11 @@ class FrameStats(C.Structure):
                 ("graphs_built", C.c_int64), ("rerenders", C.c_int64)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("tile_pixels", C.c_int), ("supertile_pixels", C.c_int), ("persistent_ctas", C.c_int),
+                ("ms", C.c_float)]
+
+
 class DeviceOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("vertex_capacity", C.c_size_t), ("grid_capacity", C.c_size_t)]
 
@@ -115,12 +120,16 @@ def load(build_if_missing: bool = False):
     L.aqh_read_quantized_u8.argtypes = [vp, _i32p, C.c_int, _u8p, C.c_size_t]
     L.aqh_read_samples.argtypes = [vp, _i32p, _f32p, _i32p, _u8p, _f32p, C.c_size_t]
     L.aqh_get_stats.argtypes = [vp, C.POINTER(FrameStats)]
+    L.aqh_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    L.aqh_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    L.aqh_autotune.argtypes = [vp, C.c_int, C.POINTER(Tuning)]
     L.aqh_filter_table.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, C.c_int, _f32p, C.c_int]
     L.aqh_filter_table.restype = C.c_int
     L.aqh_test_invbilinear.argtypes = [_f32p, _f32p, C.c_int, _f32p]
     for name in ("aqh_create", "aqh_set_mode", "aqh_set_stream", "aqh_frame_begin", "aqh_set_samples", "aqh_submit_grid", "aqh_submit_grids_device",
                  "aqh_render", "aqh_synchronize", "aqh_read_channels", "aqh_read_bucket", "aqh_read_quantized_u8",
-                 "aqh_read_samples", "aqh_get_stats", "aqh_test_invbilinear"):
+                 "aqh_read_samples", "aqh_get_stats", "aqh_test_invbilinear", "aqh_set_tuning", "aqh_get_tuning",
+                 "aqh_autotune"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -286,6 +295,23 @@ class Hider:
     def set_mode(self, batched: bool):
         """AQH_MODE_BATCHED (persistent work queue + CUDA graph) or AQH_MODE_PLAIN."""
         self._check(self.L.aqh_set_mode(self.ctx, 1 if batched else 0), "aqh_set_mode")
+
+    def set_tuning(self, tile_pixels: int = 0, supertile_pixels: int = 0, persistent_ctas: int = 0):
+        """Launch shape of the sampling stage (aqh_set_tuning); zeros are the defaults."""
+        t = Tuning(tile_pixels, supertile_pixels, persistent_ctas, 0.0)
+        self._check(self.L.aqh_set_tuning(self.ctx, C.byref(t)), "aqh_set_tuning")
+
+    def get_tuning(self) -> dict:
+        t = Tuning()
+        self._check(self.L.aqh_get_tuning(self.ctx, C.byref(t)), "aqh_get_tuning")
+        return {k: getattr(t, k) for k, _ in Tuning._fields_}
+
+    def autotune(self, repeats: int = 3) -> dict:
+        """Time the open frame under each candidate launch shape and keep the
+        fastest (aqh_autotune); returns the choice with its device ms."""
+        t = Tuning()
+        self._check(self.L.aqh_autotune(self.ctx, repeats, C.byref(t)), "aqh_autotune")
+        return {k: getattr(t, k) for k, _ in Tuning._fields_}
 
     def set_stream(self, stream_handle: int):
         self._check(self.L.aqh_set_stream(self.ctx, stream_handle or None), "aqh_set_stream")

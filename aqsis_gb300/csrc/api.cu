@@ -155,23 +155,15 @@ int lfloor_h(float x) { int i = (int)x; return i - ((x < 0 && x != (float)i) ? 1
 
 namespace aqh {
 
-// Tile shape.  spt == 0: the static kernel's shape; else `spt` samples per
-// thread with kBlock threads in near-square tiles (motion blur / DoF kernel).
-void set_tiling(FrameParams& fp, int spt) {
-	if (spt == 0) {
-		static_tiling(fp);
-	} else {
-		fp.tpp = (fp.spp + spt - 1) / spt;
-		const int tpix = kBlock / fp.tpp;
-		int tw = 1;
-		while ((tw + 1) * (tw + 1) <= tpix) ++tw;
-		fp.tile_w = tw;
-		fp.tile_h = tpix / tw;
-	}
+// Tile grid and super-tiles over the sample region.  The tile shape is the
+// static kernel's (every sampler shares it), optionally narrowed to
+// `tile_pixels`; a super-tile is about `supertile_px` pixels on a side.
+void set_tiling(FrameParams& fp, int tile_pixels, int supertile_px) {
+	static_tiling(fp, tile_pixels);
 	const int tw = fp.tile_w, th = fp.tile_h;
 	fp.ntx = (fp.sw + tw - 1) / tw;
 	fp.nty = (fp.sh + th - 1) / th;
-	fp.st_tiles = std::max(1, 128 / std::max(tw, th));
+	fp.st_tiles = std::max(1, (supertile_px > 0 ? supertile_px : 128) / std::max(tw, th));
 	fp.nstx = (fp.ntx + fp.st_tiles - 1) / fp.st_tiles;
 	fp.nsty = (fp.nty + fp.st_tiles - 1) / fp.st_tiles;
 }
@@ -362,6 +354,7 @@ struct aqh_ctx {
 	std::vector<float4> h_dofb;
 	std::vector<float> h_slices;
 	int mode = AQH_MODE_PLAIN;
+	aqh_tuning tune{};  // launch shape of the sampling stage (zeros: defaults)
 	// batched mode: instantiated frame graphs keyed by every kernel argument of
 	// the frame, most recently used first (a server slot sees many job shapes)
 	struct GraphEntry {
@@ -839,7 +832,7 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	if (ctx->dev_grids) motion = ctx->dev_motion;
 	fp.any_motion = motion ? 1 : 0;
 	P.mbdof = fp.use_dof || fp.any_motion;
-	set_tiling(fp, 0);
+	set_tiling(fp, ctx->tune.tile_pixels, ctx->tune.supertile_pixels);
 	if (P.mbdof) {
 		ctx->h_dofb.clear();
 		dof_bounds_h(fp.xs, fp.ys, ctx->h_dofb);
@@ -931,7 +924,9 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	}
 	int nsm = 0;
 	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
-	P.nctas = std::max(1, std::min(fp.ntx * fp.nty, nsm * sample_static_ctas_per_sm(pool.capacity > 0)));
+	int resident = nsm * sample_static_ctas_per_sm(pool.capacity > 0);
+	if (ctx->tune.persistent_ctas > 0) resident = std::min(resident, ctx->tune.persistent_ctas);
+	P.nctas = std::max(1, std::min(fp.ntx * fp.nty, resident));
 	P.fp = fp;
 	P.g = g;
 	AQH_TRY(ctx->d_idgrid.ensure(sizeof(int32_t) * (size_t)((P.nmps + 255) / 256 + 1)), "alloc id table");
@@ -1182,6 +1177,73 @@ aqh_status aqh_synchronize(aqh_ctx* ctx) {
 			return render_plain(ctx, P, true);
 		}
 	}
+	return AQH_OK;
+}
+
+aqh_status aqh_set_tuning(aqh_ctx* ctx, const aqh_tuning* t) {
+	if (!ctx || !t) return AQH_EINVAL;
+	if (t->tile_pixels < 0 || t->tile_pixels > 256 || t->supertile_pixels < 0 || t->supertile_pixels > 65536 ||
+	    t->persistent_ctas < 0)
+		return ctx->fail(AQH_EINVAL, "tuning out of range (tile %d, super-tile %d, ctas %d)", t->tile_pixels,
+		                 t->supertile_pixels, t->persistent_ctas);
+	ctx->tune = *t;
+	ctx->tune.ms = 0.0f;
+	return AQH_OK;
+}
+
+aqh_status aqh_get_tuning(aqh_ctx* ctx, aqh_tuning* t) {
+	if (!ctx || !t) return AQH_EINVAL;
+	*t = ctx->tune;
+	return AQH_OK;
+}
+
+aqh_status aqh_autotune(aqh_ctx* ctx, int repeats, aqh_tuning* best) {
+	if (!ctx) return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	if (!ctx->samples_set) return ctx->fail(AQH_EINVAL, "aqh_set_samples was not called");
+	repeats = std::max(1, std::min(repeats, 64));
+	const int t0 = std::min(256, std::max(1, 4096 / std::max(1, ctx->fp.spp)));
+	std::vector<int> tiles = {0};
+	for (int div : {2, 4})
+		if (t0 / div >= 16) tiles.push_back(t0 / div);
+	std::vector<int> ctas = {0};
+	if (ctx->mode == AQH_MODE_BATCHED) {
+		int nsm = 0;
+		cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+		const int half = nsm * std::max(1, sample_static_ctas_per_sm(ctx->any_transparent)) / 2;
+		if (half >= 1) ctas.push_back(half);
+	}
+	const aqh_tuning keep = ctx->tune;
+	aqh_tuning pick{};
+	float pick_ms = 0.0f;
+	bool have = false;
+	for (int c : ctas)
+		for (int tp : tiles)
+			for (int stp : {128, 64, 256}) {
+				aqh_tuning t{};
+				t.tile_pixels = tp;
+				t.supertile_pixels = stp == 128 ? 0 : stp;
+				t.persistent_ctas = c;
+				ctx->tune = t;
+				float ms = 0.0f;
+				for (int r = 0; r < repeats; ++r) {
+					const aqh_status st = aqh_render(ctx, 1);
+					if (st != AQH_OK) {
+						ctx->tune = keep;
+						return st;
+					}
+					const float m = ctx->stats.ms_total;
+					if (r == 0 || m < ms) ms = m;
+				}
+				if (!have || ms < pick_ms * 0.99f) {
+					pick = t;
+					pick_ms = ms;
+					have = true;
+				}
+			}
+	ctx->tune = pick;
+	pick.ms = pick_ms;
+	if (best) *best = pick;
 	return AQH_OK;
 }
 

@@ -184,11 +184,14 @@ void launch_sample_mb(const FrameParams& fp, const GridsDev& g, const SamplerDev
                       SampleStore st, FragPool pool, const float4* dof_bounds, const float* slice_times,
                       cudaStream_t s);
 void slice_times_h(float open, float close, int spp, std::vector<float>& out);
-void static_tiling(FrameParams& fp);
+void static_tiling(FrameParams& fp, int tile_pixels);
 // Frame options resolved from an aqh_frame_desc (plus the host filter table).
 aqh_status resolve_frame(const aqh_frame_desc& d, FrameParams& fp, std::vector<float>& ftab, std::string& err);
 // Tile grid, super-tiles and the MB/DoF lens-stratum bounds (api.cu).
-void set_tiling(FrameParams& fp, int spt);
+// tile_pixels: pixels per sampling tile (0: the most a CTA holds, min(256,
+// 4096 / samples per pixel)); supertile_px: side of a binning super-tile
+// (0: 128 pixels).  Neither changes any result.
+void set_tiling(FrameParams& fp, int tile_pixels = 0, int supertile_px = 0);
 void dof_bounds_h(int xs, int ys, std::vector<float4>& out);
 void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStore& st, const float* ftab,
                    float* channels, cudaStream_t s);

@@ -1153,12 +1153,13 @@ void launch_resolve_opaque(const FrameParams& fp, const GridsDev& g, const Sampl
 	if (n > 0) resolve_opaque_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fp, g, sm, st);
 }
 
-void static_tiling(FrameParams& fp) {
-	const int tpix = min(kTilePixMax, max(1, kTileSampMax / fp.spp));
+void static_tiling(FrameParams& fp, int tile_pixels) {
+	int tpix = min(kTilePixMax, max(1, kTileSampMax / fp.spp));
+	if (tile_pixels > 0) tpix = min(tpix, tile_pixels);
 	int tw = 1;
 	while ((tw + 1) * (tw + 1) <= tpix) ++tw;
 	fp.tile_w = tw;
-	fp.tile_h = tpix / tw;
+	fp.tile_h = min(16, tpix / tw);  // at most 4x4 blocks of 4x4 pixels (blkmax)
 	fp.tpp = 1;
 }
 

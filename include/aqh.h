@@ -216,6 +216,34 @@ enum { AQH_MODE_PLAIN = 0, AQH_MODE_BATCHED = 1 };
 aqh_status aqh_set_mode(aqh_ctx* ctx, int mode);
 aqh_status aqh_synchronize(aqh_ctx* ctx);
 
+/* ---- launch-shape tuning ---------------------------------------------------- */
+/* The device counterpart of the reference's bucket size (CqImageBuffer's
+ * bucket loop, imagebuffer.cpp): how the sample region is cut for the
+ * sampling kernels.  tile_pixels: pixels per sampling tile (0: the most one
+ * CTA holds, min(256, 4096 / samples per pixel); tiles stay within 16x16
+ * pixels).  supertile_pixels: side of a binning super-tile in pixels (0: 128).
+ * persistent_ctas: CTAs of the batched form's persistent sampling kernel (0:
+ * every CTA that fits on the device at once).  No setting changes a result:
+ * each sample meets its candidate micropolygons in the same order under any
+ * tiling.  `ms` is only written by aqh_autotune. */
+typedef struct {
+	int tile_pixels;
+	int supertile_pixels;
+	int persistent_ctas;
+	float ms;  /* device time of the frame with this tuning (sum of the stage times) */
+} aqh_tuning;
+aqh_status aqh_set_tuning(aqh_ctx* ctx, const aqh_tuning* t);
+aqh_status aqh_get_tuning(aqh_ctx* ctx, aqh_tuning* t);
+/* Render the open frame `repeats` times under each candidate tuning (tile
+ * sizes of 1, 1/2 and 1/4 of the default, super-tiles of 64, 128 and 256
+ * pixels, and in the batched form half the persistent CTAs), in the context's
+ * current mode, and keep the one with the least device time, best of its
+ * repeats; the default is kept unless another is at least 1% faster.  The
+ * choice stays set for later frames and is written to `best` (may be NULL).
+ * The open frame's results are those of its last render, which are the same
+ * under every candidate. */
+aqh_status aqh_autotune(aqh_ctx* ctx, int repeats, aqh_tuning* best);
+
 /* ---- results ------------------------------------------------------------- */
 /* Channel-buffer layout of one display pixel, CqBucketProcessor::FilterBucket
  * (bucketprocessor.cpp:385-398): Ci r g b, Oi r g b, a, z, coverage. */
