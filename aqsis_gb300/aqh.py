@@ -120,6 +120,7 @@ def load(build_if_missing: bool = False):
     L.aqh_read_quantized_u8.argtypes = [vp, _i32p, C.c_int, _u8p, C.c_size_t]
     L.aqh_read_samples.argtypes = [vp, _i32p, _f32p, _i32p, _u8p, _f32p, C.c_size_t]
     L.aqh_get_stats.argtypes = [vp, C.POINTER(FrameStats)]
+    L.aqh_set_camera_to_raster.argtypes = [vp, _f32p]
     L.aqh_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.aqh_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.aqh_autotune.argtypes = [vp, C.c_int, C.POINTER(Tuning)]
@@ -129,7 +130,7 @@ def load(build_if_missing: bool = False):
     for name in ("aqh_create", "aqh_set_mode", "aqh_set_stream", "aqh_frame_begin", "aqh_set_samples", "aqh_submit_grid", "aqh_submit_grids_device",
                  "aqh_render", "aqh_synchronize", "aqh_read_channels", "aqh_read_bucket", "aqh_read_quantized_u8",
                  "aqh_read_samples", "aqh_get_stats", "aqh_test_invbilinear", "aqh_set_tuning", "aqh_get_tuning",
-                 "aqh_autotune"):
+                 "aqh_autotune", "aqh_set_camera_to_raster"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -212,6 +213,17 @@ class Hider:
         self.frame = fr
         self._keep = []
         self._check(self.L.aqh_frame_begin(self.ctx, C.byref(frame_desc(fr))), "aqh_frame_begin")
+        if getattr(fr, "camera_to_raster", None) is not None:
+            self.set_camera_to_raster(fr.camera_to_raster)
+
+    def set_camera_to_raster(self, m):
+        """Camera-to-raster matrix (16 floats, m[row*4 + col]) for GRID_CAMERA
+        grids (aqh_set_camera_to_raster); None clears it."""
+        if m is None:
+            self._check(self.L.aqh_set_camera_to_raster(self.ctx, None), "aqh_set_camera_to_raster")
+            return
+        a = np.ascontiguousarray(np.asarray(m, np.float32).reshape(16))
+        self._check(self.L.aqh_set_camera_to_raster(self.ctx, _p(a, _f32p)), "aqh_set_camera_to_raster")
 
     def set_samples(self, s):
         keep = []

@@ -325,6 +325,10 @@ struct aqh_ctx {
 	int64_t h_verts_p = 0, h_verts_c = 0, h_mps = 0;
 	bool h_has_ci = true, h_has_oi = true;
 	bool any_transparent = false;
+	// Split's projection: grids flagged AQH_GRID_CAMERA and the frame's matrix
+	bool any_camera = false;
+	bool camera_set = false;
+	aqh::CamMatrix camera{};
 
 	// host-submitted packed arrays (caller-owned, uploaded at render)
 	bool host_packed = false;
@@ -507,6 +511,8 @@ aqh_status aqh_frame_begin(aqh_ctx* ctx, const aqh_frame_desc* d) {
 	ctx->h_verts_p = ctx->h_verts_c = ctx->h_mps = 0;
 	ctx->h_has_ci = ctx->h_has_oi = true;
 	ctx->any_transparent = false;
+	ctx->any_camera = false;
+	ctx->camera_set = false;
 	ctx->dev_grids = false;
 	ctx->dev_motion = false;
 	ctx->host_packed = false;
@@ -603,6 +609,7 @@ aqh_status aqh_submit_grid(aqh_ctx* ctx, const aqh_grid* gr) {
 		}
 	}
 	if (e != cudaSuccess) return ctx->cuda_fail(e, "stage grid");
+	if (flags & AQH_GRID_CAMERA) ctx->any_camera = true;
 	ctx->h_flags.push_back(flags);
 	if (gr->culled) {
 		if (!ctx->any_culled) {
@@ -632,6 +639,7 @@ __global__ void any_transparent_kernel(int n, const int32_t* flags, const int32_
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < n && !(flags[i] & AQH_GRID_OPAQUE)) out[0] = 1;
 	if (i < n && nkeys[i] > 1) out[1] = 1;
+	if (i < n && (flags[i] & AQH_GRID_CAMERA)) out[2] = 1;
 }
 }  // namespace
 
@@ -674,6 +682,7 @@ aqh_status aqh_submit_grids_host(aqh_ctx* ctx, int ngrids, const int32_t* cu, co
 			return ctx->fail(AQH_EINVAL, "grid %d: key times out of range", i);
 		mps += (int64_t)cu[i] * cv[i];
 		if (!(flags[i] & AQH_GRID_OPAQUE)) transp = true;
+		if (flags[i] & AQH_GRID_CAMERA) ctx->any_camera = true;
 	}
 	if (mps != total_mps) return ctx->fail(AQH_EINVAL, "total_micropolygons %lld != %lld", (long long)total_mps, (long long)mps);
 	ctx->hp.ngrids = ngrids;
@@ -724,11 +733,12 @@ aqh_status aqh_submit_grids_device(aqh_ctx* ctx, int ngrids, const int32_t* d_cu
 	if (ngrids > 0)
 		any_transparent_kernel<<<(ngrids + 255) / 256, 256, 0, ctx->stream>>>(ngrids, d_flags, d_nkeys,
 		                                                                    ctx->d_err.as<int32_t>() + 8);
-	int32_t anyt[2] = {0, 0};
-	AQH_TRY(cudaMemcpyAsync(anyt, ctx->d_err.as<int32_t>() + 8, 8, cudaMemcpyDeviceToHost, ctx->stream), "readback");
+	int32_t anyt[3] = {0, 0, 0};
+	AQH_TRY(cudaMemcpyAsync(anyt, ctx->d_err.as<int32_t>() + 8, 12, cudaMemcpyDeviceToHost, ctx->stream), "readback");
 	AQH_TRY(cudaStreamSynchronize(ctx->stream), "sync");
 	ctx->any_transparent = anyt[0] != 0;
 	ctx->dev_motion = anyt[1] != 0;
+	ctx->any_camera = anyt[2] != 0;
 	ctx->dev_grids = true;
 	ctx->dev_mps = total_mps;
 	return AQH_OK;
@@ -822,6 +832,10 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 		if (st != AQH_OK) return st;
 	}
 	const GridsDev& g = ctx->dg;
+	if (ctx->any_camera && !ctx->camera_set && !ctx->dev_grids)
+		return ctx->fail(AQH_EINVAL, "grids flagged AQH_GRID_CAMERA but no camera-to-raster matrix is set");
+	P.project = ctx->any_camera && ctx->camera_set;
+	P.cam = ctx->camera;
 	P.nmps = ctx->dev_grids ? ctx->dev_mps : ctx->h_mps;
 	bool motion = false;
 	if (ctx->host_packed) {
@@ -949,6 +963,8 @@ static aqh_status enqueue_frame(aqh_ctx* ctx, RenderPlan& P, bool batched, bool 
 		else cudaEventRecord(e, s);
 	};
 	if (timing) mark(ctx->ev[0]);
+	if (P.project)
+		launch_project_grids(P.g, const_cast<float4*>(P.g.P), const_cast<int32_t*>(P.g.flags), P.cam, s);
 	if (P.g.ngrids > 0) {
 		launch_id_grid(P.g, P.nmps, const_cast<int32_t*>(P.g.id_grid), s);
 		launch_grid_rects(fp, P.g, P.bb, s);
@@ -1009,6 +1025,8 @@ static aqh_status render_plain(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 	const FrameParams& fp = P.fp;
 	cudaEventRecord(ctx->ev[0], s);
 	int32_t total = 0;
+	if (P.project)
+		launch_project_grids(P.g, const_cast<float4*>(P.g.P), const_cast<int32_t*>(P.g.flags), P.cam, s);
 	if (P.g.ngrids > 0) {
 		launch_id_grid(P.g, P.nmps, const_cast<int32_t*>(P.g.id_grid), s);
 		launch_grid_rects(fp, P.g, P.bb, s);
@@ -1177,6 +1195,14 @@ aqh_status aqh_synchronize(aqh_ctx* ctx) {
 			return render_plain(ctx, P, true);
 		}
 	}
+	return AQH_OK;
+}
+
+aqh_status aqh_set_camera_to_raster(aqh_ctx* ctx, const float* m) {
+	if (!ctx) return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	ctx->camera_set = m != nullptr;
+	if (m) std::memcpy(ctx->camera.m, m, sizeof ctx->camera.m);
 	return AQH_OK;
 }
 

@@ -144,6 +144,11 @@ struct BinBuffers {
 	int64_t list_capacity;
 };
 
+// Camera-to-raster matrix of the frame in CqMatrix element order m[row*4 + col].
+struct CamMatrix {
+	float m[16];
+};
+
 // Everything one render of a context needs: uploads done, buffers sized, kernel arguments filled.
 struct RenderPlan {
 	FrameParams fp;
@@ -156,11 +161,16 @@ struct RenderPlan {
 	int nctas;     // persistent sampling CTAs (batched form)
 	size_t nsamp;
 	int64_t nmps;
+	bool project;  // AQH_GRID_CAMERA grids to project before binning (with cam)
+	CamMatrix cam;
 };
 
 // Kernel launchers (implemented in the .cu files).
 void launch_grid_rects(const FrameParams& fp, const GridsDev& g, const BinBuffers& b, cudaStream_t s);
 void launch_id_grid(const GridsDev& g, int64_t nmps, int32_t* table, cudaStream_t s);
+// Split's camera-to-raster projection of AQH_GRID_CAMERA grids, in place in
+// P (the grids' point array, g.P made writable) and clearing the flag.
+void launch_project_grids(const GridsDev& g, float4* P, int32_t* flags, const CamMatrix& m, cudaStream_t s);
 void launch_st_count(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);
 void launch_scan_i32(const int32_t* in, int32_t* out, int n, int32_t* scratch, cudaStream_t s);
 void launch_st_write(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);

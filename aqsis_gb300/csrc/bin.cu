@@ -243,6 +243,25 @@ __global__ void id_grid_kernel(GridsDev g, int64_t nmps, int32_t* table) {
 	for (int64_t k = (s + 255) >> 8; (k << 8) < e; ++k) table[k] = gi;
 }
 
+// Split's projection for grids flagged AQH_GRID_CAMERA: block per grid, every
+// key's points replaced in place by their hybrid raster form, then the flag
+// cleared so a later pass over the same arrays leaves them alone.
+__global__ void project_grids_kernel(GridsDev g, float4* P, int32_t* flags, CamMatrix M) {
+	const int gi = blockIdx.x;
+	if (!(__ldg(g.flags + gi) & AQH_GRID_CAMERA)) return;
+	const int64_t nv = (int64_t)(__ldg(g.cu + gi) + 1) * (__ldg(g.cv + gi) + 1);
+	const int64_t n = nv * __ldg(g.nkeys + gi);
+	float4* p = P + __ldg(g.pbase + gi);
+	for (int64_t i = threadIdx.x; i < n; i += blockDim.x) p[i] = project_point(M.m, p[i]);
+	__syncthreads();
+	if (threadIdx.x == 0) flags[gi] &= ~AQH_GRID_CAMERA;
+}
+
+void launch_project_grids(const GridsDev& g, float4* P, int32_t* flags, const CamMatrix& m, cudaStream_t s) {
+	if (g.ngrids == 0) return;
+	project_grids_kernel<<<g.ngrids, 256, 0, s>>>(g, P, flags, m);
+}
+
 void launch_id_grid(const GridsDev& g, int64_t nmps, int32_t* table, cudaStream_t s) {
 	if (g.ngrids == 0) return;
 	id_grid_kernel<<<(g.ngrids + 255) / 256, 256, 0, s>>>(g, nmps, table);

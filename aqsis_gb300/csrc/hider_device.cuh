@@ -212,4 +212,21 @@ __device__ __forceinline__ bool triangle_keeps(float4 l, float hx, float hy) {
 	return !(v <= 0);
 }
 
+// One point of CqMicroPolyGrid::Split's projection (micropolygon.cpp:735-745,
+// 1023-1032): matCameraToRaster * P with CqMatrix::operator*(CqVector3D)
+// (matrix.h:717-750), x and y divided by h = P.m03 + ... when h != 1; the
+// camera-space z is kept.  m: CqMatrix elements m[row*4 + col], points as row
+// vectors (x' = x m00 + y m10 + z m20 + m30).
+__device__ __forceinline__ float4 project_point(const float* m, float4 p) {
+	const float h = ((m[3] * p.x + m[7] * p.y) + m[11] * p.z) + m[15];
+	float x = ((m[0] * p.x + m[4] * p.y) + m[8] * p.z) + m[12];
+	float y = ((m[1] * p.x + m[5] * p.y) + m[9] * p.z) + m[13];
+	if (h != 1.0f) {
+		const float invh = 1.0f / h;
+		x = x * invh;
+		y = y * invh;
+	}
+	return make_float4(x, y, p.z, p.w);
+}
+
 }  // namespace aqh

@@ -29,7 +29,7 @@ import numpy as np
 
 FILTERS = {"box": 0, "triangle": 1, "gaussian": 2, "catmull-rom": 3, "sinc": 4,
            "disk": 5, "bessel": 6, "mitchell": 7}
-GRID_SMOOTH, GRID_MATTE, GRID_MATTEALPHA, GRID_OPAQUE, GRID_TRIANGULAR = 1, 2, 4, 8, 16
+GRID_SMOOTH, GRID_MATTE, GRID_MATTEALPHA, GRID_OPAQUE, GRID_TRIANGULAR, GRID_CAMERA = 1, 2, 4, 8, 16, 32
 FLT_MAX = float(np.finfo(np.float32).max)
 
 
@@ -60,6 +60,9 @@ class Frame:
     depth_filter: int = 0
     zthreshold: tuple = (1.0, 1.0, 1.0)
     display_z: int = 0
+    # camera-to-raster matrix (16 floats, CqMatrix order m[row*4 + col]) for
+    # GRID_CAMERA grids, whose P is in camera space; None = no projection
+    camera_to_raster: Optional[tuple] = None
 
     @property
     def spp(self) -> int:
@@ -394,6 +397,71 @@ def served_job(rng: np.random.Generator, seed: int, max_mps: float = 8e6) -> Sce
 
 
 # ---------------------------------------------------------------------------
+# Camera-space grids (the input of Split's projection, AQH_GRID_CAMERA)
+
+def camera_to_raster(width: int, height: int, fov_deg: float = 40.0, near: float = 0.1, far: float = 1e4,
+                     orthographic: bool = False, ortho_half_height: float = 100.0) -> tuple:
+    """A camera-to-raster matrix as RiProjection "perspective" (or
+    "orthographic") followed by the screen-to-raster mapping builds it, in
+    CqMatrix element order m[row*4 + col] with points as row vectors.
+    Screen window: [-aspect, aspect] x [-1, 1] (scaled by ortho_half_height
+    for orthographic), raster y down."""
+    aspect = width / height
+    l, r, b, t = -aspect, aspect, -1.0, 1.0
+    m = np.zeros((4, 4), np.float64)
+    if orthographic:
+        l, r, b, t = (v * ortho_half_height for v in (l, r, b, t))
+        m[0, 0] = width / (r - l)
+        m[3, 0] = -l * width / (r - l)
+        m[1, 1] = -height / (t - b)
+        m[3, 1] = t * height / (t - b)
+        m[2, 2] = 1.0 / (far - near)
+        m[3, 2] = -near / (far - near)
+        m[3, 3] = 1.0
+    else:
+        f = 1.0 / math.tan(math.radians(fov_deg) / 2)
+        m[0, 0] = f * width / (r - l)
+        m[2, 0] = -l * width / (r - l)
+        m[1, 1] = -f * height / (t - b)
+        m[2, 1] = t * height / (t - b)
+        m[2, 2] = far / (far - near)
+        m[3, 2] = -near * far / (far - near)
+        m[2, 3] = 1.0
+    return tuple(float(v) for v in m.astype(np.float32).reshape(16))
+
+
+def to_camera_space(scene: Scene, m=None, every: int = 1, **camera_kw) -> Scene:
+    """Turn every `every`-th grid of a raster-space scene into a camera-space
+    grid flagged GRID_CAMERA (P unprojected through `m`, float64, then stored
+    as float32; camera z unchanged) and set the frame's matrix.  Split's
+    projection brings the points back to within rounding of where they were."""
+    fr, g = scene.frame, scene.grids
+    if m is None:
+        m = camera_to_raster(fr.width, fr.height, **camera_kw)
+    M = np.asarray(m, np.float64).reshape(4, 4)
+    P = np.array(g.P, np.float32, copy=True)
+    flags = np.asarray(g.flags, np.int32).copy()
+    for i in range(0, g.ngrids, every):
+        nv = (int(g.cu[i]) + 1) * (int(g.cv[i]) + 1) * int(g.nkeys[i])
+        b = int(g.pbase[i])
+        q = P[b:b + nv].astype(np.float64)
+        xr, yr, z = q[:, 0], q[:, 1], q[:, 2]
+        # h = z m23 + m33; x_r h = x m00 + z m20 + m30 (no x-y coupling in these matrices)
+        h = z * M[2, 3] + M[3, 3]
+        x = (xr * h - z * M[2, 0] - M[3, 0]) / M[0, 0]
+        y = (yr * h - z * M[2, 1] - M[3, 1]) / M[1, 1]
+        P[b:b + nv, 0] = x.astype(np.float32)
+        P[b:b + nv, 1] = y.astype(np.float32)
+        flags[i] |= GRID_CAMERA
+    g2 = dataclasses.replace(g, P=P, flags=flags)
+    fr2 = dataclasses.replace(fr, camera_to_raster=tuple(float(v) for v in np.asarray(m, np.float32)))
+    sc = Scene(fr2, g2, scene.samples)
+    if hasattr(scene, "kind"):
+        sc.kind = scene.kind
+    return sc
+
+
+# ---------------------------------------------------------------------------
 # Scene files
 
 _GRID_KEYS = ("cu", "cv", "nkeys", "flags", "pbase", "cbase", "tbase", "times", "P", "Ci", "Oi", "culled")
@@ -421,7 +489,7 @@ def scene_from_arrays(d) -> Scene:
     """Inverse of scene_arrays (accepts an NpzFile or a dict)."""
     import json
     fd = json.loads(str(d["frame"]))
-    for k in ("crop", "bucket", "shutter", "dof_scale", "zthreshold"):
+    for k in ("crop", "bucket", "shutter", "dof_scale", "zthreshold", "camera_to_raster"):
         if fd.get(k) is not None:
             fd[k] = tuple(fd[k])
     fr = Frame(**fd)

@@ -65,8 +65,10 @@ enum {
 	AQH_GRID_MATTE = 2,       /* Matte 1 (SqImageSample::Flag_Matte) */
 	AQH_GRID_MATTEALPHA = 4,  /* aqsis "matte alpha" (Flag_MatteAlpha) */
 	AQH_GRID_OPAQUE = 8,      /* caller guarantees Oi >= 1 on every vertex (skips reading Oi while sampling) */
-	AQH_GRID_TRIANGULAR = 16  /* CqMicroPolyGridBase::fTriangular (micropolygon.h:139-147): hits on or behind
+	AQH_GRID_TRIANGULAR = 16, /* CqMicroPolyGridBase::fTriangular (micropolygon.h:139-147): hits on or behind
 	                             the line through corners cu and cv*(cu+1) miss (micropolygon.cpp:1630-1654) */
+	AQH_GRID_CAMERA = 32      /* P holds camera-space points: projected on the device with the frame's
+	                             camera-to-raster matrix (aqh_set_camera_to_raster) */
 };
 
 typedef struct aqh_ctx aqh_ctx;
@@ -111,8 +113,9 @@ void aqh_frame_desc_defaults(aqh_frame_desc* d);
  * One shaded grid.  Replaces the per-micropolygon CqImageBuffer::AddMPG()
  * calls made by CqMicroPolyGrid::Split / CqMotionMicroPolyGrid::Split
  * (libs/core/micropolygon.cpp:641-892, 946-1156; imagebuffer.cpp:514-591).
- * P is already in the hybrid raster space Split produces: raster x, raster y,
- * camera-space z.  The library copies the arrays before returning.
+ * P is in the hybrid raster space Split produces (raster x, raster y,
+ * camera-space z), or in camera space with AQH_GRID_CAMERA.  The library
+ * copies the arrays before returning.
  */
 typedef struct {
 	int cu, cv;                  /* micropolygons along u and v; (cu+1)*(cv+1) vertices */
@@ -169,6 +172,19 @@ const char* aqh_status_string(aqh_status s);
 aqh_status aqh_frame_begin(aqh_ctx* ctx, const aqh_frame_desc* desc);
 /* Upload sample patterns; required before aqh_render.  Copies the arrays. */
 aqh_status aqh_set_samples(aqh_ctx* ctx, const aqh_samples* samples);
+/* The projection step of CqMicroPolyGrid::Split / CqMotionMicroPolyGrid::Split
+ * (micropolygon.cpp:649-651, 735-745, 1023-1032) on the device.  Grids flagged
+ * AQH_GRID_CAMERA carry camera-space P for every key; before binning each
+ * point becomes matCameraToRaster * P (CqMatrix::operator*(CqVector3D),
+ * matrix.h:717-750: x and y divided by h when h != 1) with its camera-space z
+ * kept.  `m` is the matrix in CqMatrix element order m[row*4 + col], points
+ * as row vectors (x' = x m[0] + y m[4] + z m[8] + m[12], h = x m[3] + y m[7] +
+ * z m[11] + m[15]); NULL clears it.  Reset by aqh_frame_begin.  Host grids
+ * flagged AQH_GRID_CAMERA without a matrix are rejected at aqh_render.
+ * Device-submitted grids are projected in place, as Split overwrites the
+ * grid's P, and their AQH_GRID_CAMERA flag is cleared in d_flags (without a
+ * matrix they are taken as already projected). */
+aqh_status aqh_set_camera_to_raster(aqh_ctx* ctx, const float* m);
 /* Append one grid (host arrays) in insertion order: CqImageBuffer::AddMPG. */
 aqh_status aqh_submit_grid(aqh_ctx* ctx, const aqh_grid* grid);
 /* Append many grids whose arrays already live in device memory, packed:

@@ -1338,3 +1338,26 @@ extern "C" void orc_multijitter_tables(int xs, int ys, float* pos, float* t1d, i
 		}
 	}
 }
+
+// CqMicroPolyGrid::Split projection (micropolygon.cpp:735-745; motion grids
+// 1023-1032): each point p becomes matCameraToRaster * p by
+// CqMatrix::operator*(const CqVector3D&) (matrix.h:717-750) -- row-vector
+// product, x and y (and z, which Split then discards) multiplied by 1/h when
+// h != 1 -- and keeps its camera-space z.  m[row*4 + col]; float4 points.
+extern "C" void orc_project_points(const float* m, const float* Pin, int64_t n, float* Pout) {
+	for (int64_t i = 0; i < n; ++i) {
+		const float x = Pin[4 * i], y = Pin[4 * i + 1], z = Pin[4 * i + 2], w = Pin[4 * i + 3];
+		const float h = m[0 * 4 + 3] * x + m[1 * 4 + 3] * y + m[2 * 4 + 3] * z + m[3 * 4 + 3];
+		float rx = m[0 * 4 + 0] * x + m[1 * 4 + 0] * y + m[2 * 4 + 0] * z + m[3 * 4 + 0];
+		float ry = m[0 * 4 + 1] * x + m[1 * 4 + 1] * y + m[2 * 4 + 1] * z + m[3 * 4 + 1];
+		if (h != 1) {
+			const float invh = 1 / h;
+			rx = rx * invh;
+			ry = ry * invh;
+		}
+		Pout[4 * i] = rx;
+		Pout[4 * i + 1] = ry;
+		Pout[4 * i + 2] = z;
+		Pout[4 * i + 3] = w;
+	}
+}

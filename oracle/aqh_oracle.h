@@ -35,7 +35,8 @@ enum {
 	ORC_GRID_SMOOTH = 1,      /* ShadingInterpolation "smooth" */
 	ORC_GRID_MATTE = 2,       /* SqImageSample::Flag_Matte */
 	ORC_GRID_MATTEALPHA = 4,  /* SqImageSample::Flag_MatteAlpha */
-	ORC_GRID_TRIANGULAR = 16  /* CqMicroPolyGridBase::fTriangular: split line through corners cu, cv*(cu+1) */
+	ORC_GRID_TRIANGULAR = 16, /* CqMicroPolyGridBase::fTriangular: split line through corners cu, cv*(cu+1) */
+	ORC_GRID_CAMERA = 32      /* P in camera space: orc_project_points first (orc_render itself ignores it) */
 };
 
 typedef struct {
@@ -128,6 +129,11 @@ float orc_mt_float(void);
 /* Fill the 250-pattern caches of CqMultiJitteredSampler (multijitter.cpp:130-202).
  * pos: [250*spp*2], t1d: [250*spp], shuffle: [250*spp]. Consumes the global MT. */
 void orc_multijitter_tables(int xs, int ys, float* pos, float* t1d, int32_t* shuffle);
+
+/* Split's camera-to-raster projection of n float4 points (micropolygon.cpp:
+ * 735-745, 1023-1032; CqMatrix::operator*(CqVector3D), matrix.h:717-750):
+ * raster x, y and the camera-space z.  m: CqMatrix elements m[row*4 + col]. */
+void orc_project_points(const float* m, const float* Pin, int64_t n, float* Pout);
 
 /* The rounding helpers of libs/math/math.h:46-70 as the oracle uses them
  * (lfloor/lceil of a float, lround of a double). */

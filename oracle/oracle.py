@@ -93,6 +93,7 @@ def lib():
         L.orc_lfloor.restype = C.c_long
         L.orc_lceil.argtypes = [C.c_float]
         L.orc_lceil.restype = C.c_long
+        L.orc_project_points.argtypes = [_f32p, _f32p, C.c_int64, _f32p]
         L.orc_lround.argtypes = [C.c_double]
         L.orc_lround.restype = C.c_long
         _lib = L
@@ -139,10 +140,36 @@ def multijitter_tables(xs: int, ys: int, seed: int = 545):
     return pos, t, sh
 
 
+def project_points(m, P) -> np.ndarray:
+    """Split's camera-to-raster projection (orc_project_points) of float4 points."""
+    L = lib()
+    m = np.ascontiguousarray(np.asarray(m, np.float32).reshape(16))
+    Pin = np.ascontiguousarray(P, np.float32).reshape(-1, 4)
+    out = np.empty_like(Pin)
+    L.orc_project_points(_p(m, _f32p), _p(Pin, _f32p), Pin.shape[0], _p(out, _f32p))
+    return out
+
+
+def projected_grids(scene):
+    """The scene's grids with every GRID_CAMERA grid's keys projected to
+    hybrid raster space, as Split leaves them."""
+    from aqsis_gb300.scene import GRID_CAMERA
+    import dataclasses
+    g, m = scene.grids, scene.frame.camera_to_raster
+    if m is None or not (np.asarray(g.flags) & GRID_CAMERA).any():
+        return g
+    P = np.array(g.P, np.float32, copy=True)
+    for i in np.nonzero(np.asarray(g.flags) & GRID_CAMERA)[0]:
+        nv = (int(g.cu[i]) + 1) * (int(g.cv[i]) + 1) * int(g.nkeys[i])
+        b = int(g.pbase[i])
+        P[b:b + nv] = project_points(m, P[b:b + nv])
+    return dataclasses.replace(g, P=P, flags=np.asarray(g.flags) & ~GRID_CAMERA)
+
+
 def render(scene, qchannels=(0, 1, 2, 6), want_samples: bool = True) -> dict:
     """Run the oracle on a Scene (aqsis_gb300.scene).  Returns numpy arrays."""
     from aqsis_gb300.scene import FILTERS
-    fr, g, s = scene.frame, scene.grids, scene.samples
+    fr, g, s = scene.frame, projected_grids(scene), scene.samples
     cx0, cx1, cy0, cy1 = fr.crop_window
     x0, y0, w, h = fr.sample_region
     spp = fr.spp

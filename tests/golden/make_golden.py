@@ -85,6 +85,8 @@ CASES = {
     "reference_patterns": reference_pattern_scene,
     "triangular_static": lambda: SS.triangular_small(seed=9),
     "triangular_motion_dof": lambda: SS.triangular(SS.motion_dof_small(seed=10, xs=4, ys=4, scale=0.02), every=2),
+    "camera_perspective": lambda: S.to_camera_space(SS.triangular_small(seed=12), every=2),
+    "camera_motion_ortho": lambda: S.to_camera_space(SS.motion_mixed_small(seed=13, scale=0.012), orthographic=True),
 }
 
 

@@ -199,3 +199,9 @@ def triangular_motion_small(seed=10, dof=True):
 
 def triangular_transparent_small(seed=11):
     return triangular(transparent_small(seed=seed, scale=0.03), every=2)
+
+
+def camera_small(seed=14, every=2, **kw):
+    """Opaque stream with every `every`-th grid given in camera space
+    (GRID_CAMERA) under a perspective camera-to-raster matrix."""
+    return S.to_camera_space(opaque_small(seed=seed), every=every, **kw)

@@ -18,7 +18,7 @@ OUT_KEYS = ("winner", "occlz", "nfrag", "valid", "channels", "quantized")
 
 
 def test_fixtures_present():
-    assert len(FIXTURES) >= 17
+    assert len(FIXTURES) >= 19
 
 
 @pytest.mark.parametrize("path", FIXTURES, ids=NAMES)
@@ -66,10 +66,13 @@ def test_fixtures_cover_the_hider_features():
             feats.add("dither")
         if (g.flags & S.GRID_TRIANGULAR).any():
             feats.add("triangular")
+        if (g.flags & S.GRID_CAMERA).any() and fr.camera_to_raster is not None:
+            feats.add("camera_space")
         feats.add("filter_" + fr.filter)
         assert gold["o_valid"].any()
     for f in ("motion", "dof", "transparent", "matte", "culled", "crop", "dither", "depth_filter_1",
-              "depth_filter_2", "depth_filter_3", "filter_box", "filter_gaussian", "filter_catmull-rom", "triangular"):
+              "depth_filter_2", "depth_filter_3", "filter_box", "filter_gaussian", "filter_catmull-rom", "triangular",
+              "camera_space"):
         assert f in feats, f
 
 

@@ -99,3 +99,46 @@ def test_filter_table_zero_outside_window(oracle):
     # pixel offset (-1,-1), sub-pixel (0,0): centre at (-1.375, -1.375) -> outside +-1
     assert t[0, 0, 0, 0] == 0.0
     assert t[1, 1].min() > 0.0
+
+
+def test_projection_follows_matrix_vector_product(oracle):
+    """orc_project_points against CqMatrix::operator*(CqVector3D)
+    (matrix.h:717-750) written out in float32 steps: row-vector products,
+    x and y times 1/h only when h != 1, the camera z kept."""
+    from aqsis_gb300 import scene as S
+    f32 = np.float32
+    rng = np.random.default_rng(3)
+    pts = np.zeros((400, 4), np.float32)
+    pts[:, 0] = rng.uniform(-50, 50, 400)
+    pts[:, 1] = rng.uniform(-50, 50, 400)
+    pts[:, 2] = rng.uniform(0.5, 900, 400)
+    pts[:5, 2] = 1.0                      # h == 1 under the perspective matrix: no divide
+    pts[5, 2] = -3.0                      # behind the eye: negative h
+    pts[:, 3] = rng.uniform(0, 1, 400)    # carried through
+    for m in (S.camera_to_raster(64, 48), S.camera_to_raster(64, 48, orthographic=True),
+              tuple(rng.uniform(-2, 2, 16).astype(np.float32))):
+        mm = np.asarray(m, np.float32)
+        got = oracle.project_points(mm, pts)
+        for i in range(pts.shape[0]):
+            x, y, z, w = (f32(v) for v in pts[i])
+            h = f32(f32(f32(mm[3] * x) + f32(mm[7] * y)) + f32(mm[11] * z)) + mm[15]
+            rx = f32(f32(f32(mm[0] * x) + f32(mm[4] * y)) + f32(mm[8] * z)) + mm[12]
+            ry = f32(f32(f32(mm[1] * x) + f32(mm[5] * y)) + f32(mm[9] * z)) + mm[13]
+            if h != f32(1):
+                inv = f32(1) / f32(h)
+                rx, ry = f32(rx * inv), f32(ry * inv)
+            want = np.array([rx, ry, z, w], np.float32)
+            assert np.array_equal(got[i].view(np.uint32), want.view(np.uint32)), (i, got[i], want)
+
+
+def test_camera_space_scene_projects_back(oracle):
+    """Split's projection of a scene unprojected by to_camera_space lands on
+    the raster points within float rounding and keeps z bit for bit."""
+    from aqsis_gb300 import scene as S
+    from tests import scenes_small as SS
+    sc = SS.opaque_small(seed=5)
+    cs = S.to_camera_space(sc, every=3)
+    g = oracle.projected_grids(cs)
+    assert not (g.flags & S.GRID_CAMERA).any()
+    assert np.array_equal(g.P[:, 2], sc.grids.P[:, 2])
+    assert np.abs(g.P[:, :2] - sc.grids.P[:, :2]).max() < 1e-3
