@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libaqh.so")
-SOURCES = ["api.cu", "bin.cu", "sample.cu", "sample_mb.cu", "filter.cu", "noalloc.cu", "server.cu"]
+SOURCES = ["api.cu", "bin.cu", "sample.cu", "sample_mb.cu", "filter.cu", "noalloc.cu", "server.cu", "mpdump.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
               "-Xptxas", "-v"]

@@ -283,6 +283,33 @@ aqh_status aqh_read_quantized_u8(aqh_ctx* ctx, const int* channels, int nchan, u
 aqh_status aqh_read_samples(aqh_ctx* ctx, int32_t* winner, float* occlz, int32_t* nfrag,
                             uint8_t* valid, float* sdata, size_t nsamples);
 
+/* ---- micropolygon dump files ----------------------------------------------- */
+/* The files CqMPDump writes when Option "mpdump" "enabled" is set
+ * (libs/core/mpdump.cpp:40-210; records dumped by CqImageBuffer::AddMPG,
+ * imagebuffer.cpp:541-545, and per bucket by dumpPixelSamples): a stream of
+ * micropolygons in insertion order, each with vertex A's colour and opacity,
+ * plus pixel sample positions and the image resolution.  Host-only; no
+ * context.  Only dumps with sizeof(TqFloat) == 4 are read. */
+typedef struct {
+	int width, height;        /* the image information record (-1 when absent) */
+	int64_t micropolygons;    /* id 1 records */
+	int64_t samples;          /* id 2 records */
+} aqh_mpdump_info;
+aqh_status aqh_mpdump_scan(const char* path, aqh_mpdump_info* info);
+/* Read a scanned file.  P: float4[micropolygons][4] in one-micropolygon grid
+ * order (index, index+1, index+cu+1, index+cu+2; the file's circular order
+ * is undone), Ci / Oi: float4[micropolygons], sample_pix: int[samples][3]
+ * (pixel x, y, sample index), sample_pos: float[samples][2] raster
+ * positions.  Any output may be NULL. */
+aqh_status aqh_mpdump_read(const char* path, const aqh_mpdump_info* info, float* P, float* Ci, float* Oi,
+                           int32_t* sample_pix, float* sample_pos);
+/* Write a dump in the same layout (image record first, then the
+ * micropolygons, then the samples); Ci / Oi NULL write CqMPDump's (0.9, 0.9, 1). */
+aqh_status aqh_mpdump_write(const char* path, int width, int height, int64_t micropolygons, const float* P,
+                            const float* Ci, const float* Oi, int64_t samples, const int32_t* sample_pix,
+                            const float* sample_pos);
+const char* aqh_mpdump_last_error(void);
+
 /* ---- statistics and timing ------------------------------------------------ */
 typedef struct {
 	int64_t micropolygons;        /* micropolygons submitted this frame */

@@ -67,6 +67,26 @@ def depth_filter_scene(mode):
     return sc
 
 
+def mpdump_scene():
+    """A stream replayed from a micropolygon dump file (CqMPDump layout):
+    mpdump_stream.mp is written from a small seeded scene of constant-shaded
+    opaque and transparent grids, and the fixture is the scene read back
+    from it (1x1 grids in dump order, the dumped sample positions)."""
+    from aqsis_gb300 import mpdump
+    rng = np.random.default_rng(0x3D)
+    fr = S.Frame(width=24, height=16, xsamples=2, ysamples=2, filter="gaussian", xfilter=2.0, yfilter=2.0,
+                 q_dither=0.0)
+    parts = []
+    for k in range(8):
+        oi = None if k % 2 == 0 else rng.uniform(0.2, 0.9, (49, 3))
+        parts.append(SS.plane(rng.uniform(-3, 14), rng.uniform(-3, 8), 6, 6, float(rng.uniform(2, 40)), rng=rng,
+                              jitter=0.3, oi=oi, flags=0, step=1.5))
+    sc = SS.custom(fr, S.concat_grids(parts), seed=0x3D)
+    path = os.path.join(HERE, "mpdump_stream.mp")
+    mpdump.write(path, sc)
+    return mpdump.scene_from_dump(path, fr)
+
+
 CASES = {
     "edge_gaussian_4x4": lambda: SS.edge_cases(seed=3),
     "edge_box_3x5": lambda: SS.edge_cases(seed=4, xs=3, ys=5, filt=("box", 1.0, 1.0)),
@@ -86,6 +106,7 @@ CASES = {
     "triangular_static": lambda: SS.triangular_small(seed=9),
     "triangular_motion_dof": lambda: SS.triangular(SS.motion_dof_small(seed=10, xs=4, ys=4, scale=0.02), every=2),
     "camera_perspective": lambda: S.to_camera_space(SS.triangular_small(seed=12), every=2),
+    "mpdump_replay": mpdump_scene,
     "camera_motion_ortho": lambda: S.to_camera_space(SS.motion_mixed_small(seed=13, scale=0.012), orthographic=True),
 }
 
