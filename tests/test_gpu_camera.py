@@ -63,7 +63,9 @@ def test_camera_grids_match_oracle(hider, oracle, name):
     assert (sc.grids.flags & S.GRID_CAMERA).any()
     res = hider.render_scene(sc)
     ref = oracle.render(sc)
-    compare(res, ref, exact_pixels=True)
+    # transparent frames: the z channel's NaNs (FLT_MAX depths under negative
+    # filter lobes) may carry another payload, so compare values, not bits
+    compare(res, ref, exact_pixels="transparent" not in name)
 
 
 def test_camera_grids_packed_host(hider, oracle):
