@@ -54,6 +54,8 @@ SCENES = {
     "perspective_triangular": lambda: S.to_camera_space(SS.triangular_small(seed=33), every=2),
     "perspective_motion_dof": lambda: S.to_camera_space(SS.triangular_motion_small(seed=34)),
     "perspective_transparent": lambda: S.to_camera_space(SS.transparent_small(seed=35, scale=0.03), every=2),
+    "spheres": lambda: __import__("aqsis_gb300.spheres", fromlist=["x"]).sphere_scene(seed=3, nspheres=12,
+                                                                                      width=160, height=120),
 }
 
 
