@@ -74,6 +74,16 @@ class Tuning(C.Structure):
                 ("ms", C.c_float)]
 
 
+class Display(C.Structure):
+    _fields_ = [("nchan", C.c_int), ("channels", C.c_int * 16), ("q_zero", C.c_float), ("q_one", C.c_float),
+                ("q_min", C.c_float), ("q_max", C.c_float), ("q_dither", C.c_float), ("format", C.c_int),
+                ("dither", C.c_void_p)]
+
+
+# AQH_DSPY_* element types (PkDspy* codes) and their numpy dtypes
+DSPY_DTYPES = {1: np.float32, 2: np.uint32, 3: np.int32, 4: np.uint16, 5: np.int16, 6: np.uint8, 7: np.int8}
+
+
 class DeviceOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("vertex_capacity", C.c_size_t), ("grid_capacity", C.c_size_t)]
 
@@ -121,6 +131,9 @@ def load(build_if_missing: bool = False):
     L.aqh_read_samples.argtypes = [vp, _i32p, _f32p, _i32p, _u8p, _f32p, C.c_size_t]
     L.aqh_get_stats.argtypes = [vp, C.POINTER(FrameStats)]
     L.aqh_set_camera_to_raster.argtypes = [vp, _f32p]
+    L.aqh_display_format.argtypes = [C.c_float, C.c_float, C.c_float]
+    L.aqh_display_format.restype = C.c_int
+    L.aqh_read_display.argtypes = [vp, C.POINTER(Display), vp, C.c_size_t, C.POINTER(C.c_int)]
     L.aqh_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.aqh_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.aqh_autotune.argtypes = [vp, C.c_int, C.POINTER(Tuning)]
@@ -130,7 +143,7 @@ def load(build_if_missing: bool = False):
     for name in ("aqh_create", "aqh_set_mode", "aqh_set_stream", "aqh_frame_begin", "aqh_set_samples", "aqh_submit_grid", "aqh_submit_grids_device",
                  "aqh_render", "aqh_synchronize", "aqh_read_channels", "aqh_read_bucket", "aqh_read_quantized_u8",
                  "aqh_read_samples", "aqh_get_stats", "aqh_test_invbilinear", "aqh_set_tuning", "aqh_get_tuning",
-                 "aqh_autotune", "aqh_set_camera_to_raster"):
+                 "aqh_autotune", "aqh_set_camera_to_raster", "aqh_read_display"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -358,6 +371,29 @@ class Hider:
         out = np.zeros((h, w, len(ch)), np.uint8)
         self._check(self.L.aqh_read_quantized_u8(self.ctx, _p(ch, _i32p), len(ch), _p(out, _u8p), out.size),
                     "aqh_read_quantized_u8")
+        return out
+
+    def read_display(self, channels=(0, 1, 2, 6), one=255.0, qmin=0.0, qmax=255.0, dither_amp=0.5, zero=0.0,
+                     fmt=0, dither=None) -> np.ndarray:
+        """One display request (aqh_read_display): the crop window as
+        [h, w, nchan] of the element type the request selects (or `fmt`)."""
+        w, h = self._dims()
+        d = Display()
+        d.nchan = len(channels)
+        for i, c in enumerate(channels):
+            d.channels[i] = int(c)
+        d.q_zero, d.q_one, d.q_min, d.q_max, d.q_dither = zero, one, qmin, qmax, dither_amp
+        d.format = int(fmt)
+        keep = None
+        if dither is not None:
+            keep = np.ascontiguousarray(dither, np.float32).reshape(-1)
+            d.dither = keep.ctypes.data
+        f = fmt or self.L.aqh_display_format(one, qmin, qmax)
+        out = np.zeros((h, w, len(channels)), DSPY_DTYPES[f])
+        used = C.c_int(0)
+        self._check(self.L.aqh_read_display(self.ctx, C.byref(d), out.ctypes.data, out.nbytes, C.byref(used)),
+                    "aqh_read_display")
+        assert used.value == f
         return out
 
     def read_samples(self) -> dict:

@@ -352,7 +352,7 @@ struct aqh_ctx {
 	DevBuf d_rect, d_minz, d_strips, d_tri, d_stcount, d_stoffset, d_stlist, d_idgrid;
 	DevBuf d_sa, d_sb, d_win, d_oz, d_nf, d_hz, d_keys, d_wmask;
 	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err, d_occl;
-	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb;
+	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb, d_disp, d_dither_req;
 	bool dev_motion = false;
 	DevBuf d_queue, d_slices;
 	std::vector<float4> h_dofb;
@@ -1331,6 +1331,51 @@ aqh_status aqh_read_quantized_u8(aqh_ctx* ctx, const int* channels, int nchan, u
 	AQH_TRY(cudaGetLastError(), "quantize launch");
 	AQH_TRY(cudaMemcpyAsync(out, ctx->d_q8.p, npix * nchan, cudaMemcpyDeviceToHost, ctx->stream), "read quantized");
 	AQH_TRY(cudaStreamSynchronize(ctx->stream), "read quantized");
+	return AQH_OK;
+}
+
+int aqh_display_format(float one, float min, float max) {
+	if (one == 0.0f) return AQH_DSPY_FLOAT32;
+	if (min >= 0.0f) {
+		if (max <= 255.0f) return AQH_DSPY_UNSIGNED8;
+		if (max <= 65535.0f) return AQH_DSPY_UNSIGNED16;
+		return AQH_DSPY_UNSIGNED32;
+	}
+	if (min >= -128.0f && max <= 127.0f) return AQH_DSPY_SIGNED8;
+	if (min >= -32768.0f && max <= 32767.0f) return AQH_DSPY_SIGNED16;
+	return AQH_DSPY_SIGNED32;
+}
+
+aqh_status aqh_read_display(aqh_ctx* ctx, const aqh_display* d, void* out, size_t out_bytes, int* format_used) {
+	if (!ctx || !d || !out || d->nchan <= 0 || d->nchan > 16) return AQH_EINVAL;
+	const FrameParams& fp = ctx->fp;
+	for (int c = 0; c < d->nchan; ++c)
+		if (d->channels[c] < 0 || d->channels[c] >= AQH_NCHANNELS)
+			return ctx->fail(AQH_EINVAL, "bad channel %d", d->channels[c]);
+	const int fmt = d->format ? d->format : aqh_display_format(d->q_one, d->q_min, d->q_max);
+	if (fmt < AQH_DSPY_FLOAT32 || fmt > AQH_DSPY_SIGNED8) return ctx->fail(AQH_EINVAL, "bad display format %d", fmt);
+	static const size_t kSize[8] = {0, 4, 4, 4, 2, 2, 1, 1};
+	const size_t npix = (size_t)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
+	const size_t bytes = npix * d->nchan * kSize[fmt];
+	if (out_bytes < bytes) return ctx->fail(AQH_EINVAL, "output holds %zu bytes, %zu needed", out_bytes, bytes);
+	cudaSetDevice(ctx->device);
+	cudaStream_t s = ctx->stream;
+	AQH_TRY(ctx->d_qchan.ensure(64), "alloc");
+	AQH_TRY(ctx->d_disp.ensure(std::max<size_t>(bytes, 16)), "alloc display");
+	AQH_TRY(cudaMemcpyAsync(ctx->d_qchan.p, d->channels, d->nchan * 4, cudaMemcpyHostToDevice, s), "upload");
+	const float* dither = ctx->smp.dither;
+	if (d->dither) {
+		AQH_TRY(ctx->d_dither_req.ensure(npix * 4), "alloc dither");
+		AQH_TRY(cudaMemcpyAsync(ctx->d_dither_req.p, d->dither, npix * 4, cudaMemcpyHostToDevice, s), "upload dither");
+		dither = ctx->d_dither_req.as<float>();
+	}
+	const QuantizeParams q{d->q_zero, d->q_one, d->q_min, d->q_max, d->q_dither};
+	cudaGetLastError();
+	launch_display(fp, q, dither, ctx->d_chan.as<float>(), ctx->d_qchan.as<int>(), d->nchan, fmt, ctx->d_disp.p, s);
+	AQH_TRY(cudaGetLastError(), "display launch");
+	AQH_TRY(cudaMemcpyAsync(out, ctx->d_disp.p, bytes, cudaMemcpyDeviceToHost, s), "read display");
+	AQH_TRY(cudaStreamSynchronize(s), "read display");
+	if (format_used) *format_used = fmt;
 	return AQH_OK;
 }
 

@@ -207,6 +207,12 @@ void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStor
                    float* channels, cudaStream_t s);
 void launch_quantize_u8(const FrameParams& fp, const SamplerDev& sm, const float* channels, const int* chans,
                         int nchan, uint8_t* out, cudaStream_t s);
+// Quantize settings of one display request (CqDisplayRequest, ddmanager.cpp:428-457).
+struct QuantizeParams {
+	float zero, one, min, max, dither;
+};
+void launch_display(const FrameParams& fp, const QuantizeParams& q, const float* dither, const float* channels,
+                    const int* chans, int nchan, int format, void* out, cudaStream_t s);
 void launch_test_invbilinear(const float* quad8, const float2* P, int n, float2* uv, cudaStream_t s);
 
 }  // namespace aqh

@@ -6,6 +6,8 @@
 // (ddmanager/ddmanager.cpp:1022-1119).  One thread per display pixel walks
 // the (2*shift+1)^2 neighbouring pixels and their samples in the reference's
 // loop order (fy, fx, sy, sx), so the float sums round identically.
+#include <type_traits>
+
 #include "aqh_internal.h"
 #include "hider_device.cuh"
 
@@ -123,6 +125,41 @@ __global__ void quantize_u8_kernel(FrameParams fp, SamplerDev smp, const float* 
 	}
 }
 
+// FormatBucketForDisplay (ddmanager.cpp:1054-1114) for one display request:
+// element type T, the request's own quantize settings and dither values.
+template <class T>
+__global__ void display_kernel(FrameParams fp, QuantizeParams q, const float* __restrict__ dither,
+                               const float* __restrict__ chan, const int* __restrict__ chans, int nchan,
+                               T* __restrict__ out) {
+	const long long npix = (long long)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
+	const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (p >= npix) return;
+	const double s = dither ? (double)__ldg(dither + p) : 0.0;
+	for (int c = 0; c < nchan; ++c) {
+		double value = chan[p * 9 + chans[c]];
+		if (q.one != 0.0f) {
+			value = lround_d((double)q.zero + value * (double)(q.one - q.zero) + ((double)q.dither * s));
+			value = value < (double)q.min ? (double)q.min : (value > (double)q.max ? (double)q.max : value);
+		}
+		T v;
+		if constexpr (std::is_floating_point<T>::value) {
+			v = (T)value;                                   // PkDspyFloat32
+		} else if constexpr (sizeof(T) == 4) {
+			// 32-bit integers are clamped to their range first (ddmanager.cpp:1075-1095)
+			const double lo = T(-1) < T(0) ? -2147483648.0 : 0.0;
+			const double hi = T(-1) < T(0) ? 2147483647.0 : 4294967295.0;
+			value = value < lo ? lo : (value > hi ? hi : value);
+			v = T(value == value ? (long long)value : 0);
+		} else {
+			// narrower types: the value is inside the quantize range; outside the
+			// type's range the conversion wraps (through a 64-bit integer)
+			value = value < -9.0e18 ? -9.0e18 : (value > 9.0e18 ? 9.0e18 : value);
+			v = T(value == value ? (long long)value : 0);
+		}
+		out[p * nchan + c] = v;
+	}
+}
+
 __global__ void test_invbilinear_kernel(const float* q, const float2* P, int n, float2* uv) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n) return;
@@ -155,6 +192,22 @@ void launch_quantize_u8(const FrameParams& fp, const SamplerDev& sm, const float
 	const long long npix = (long long)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
 	if (npix <= 0) return;
 	quantize_u8_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(fp, sm, channels, chans, nchan, out);
+}
+
+void launch_display(const FrameParams& fp, const QuantizeParams& q, const float* dither, const float* channels,
+                    const int* chans, int nchan, int format, void* out, cudaStream_t s) {
+	const long long npix = (long long)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
+	if (npix <= 0) return;
+	const unsigned nb = (unsigned)((npix + 255) / 256);
+	switch (format) {
+	case AQH_DSPY_FLOAT32: display_kernel<float><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (float*)out); break;
+	case AQH_DSPY_UNSIGNED32: display_kernel<uint32_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (uint32_t*)out); break;
+	case AQH_DSPY_SIGNED32: display_kernel<int32_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (int32_t*)out); break;
+	case AQH_DSPY_UNSIGNED16: display_kernel<uint16_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (uint16_t*)out); break;
+	case AQH_DSPY_SIGNED16: display_kernel<int16_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (int16_t*)out); break;
+	case AQH_DSPY_UNSIGNED8: display_kernel<uint8_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (uint8_t*)out); break;
+	default: display_kernel<int8_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (int8_t*)out); break;
+	}
 }
 
 void launch_test_invbilinear(const float* quad8, const float2* P, int n, float2* uv, cudaStream_t s) {

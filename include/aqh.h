@@ -276,6 +276,33 @@ aqh_status aqh_read_bucket(aqh_ctx* ctx, int bx, int by, float* out, size_t out_
  * reference's a,r,g,b), lround(v*one + dither*s) clamped to [min,max], stored
  * as uint8 when the range fits (selectDataFormat, ddmanager.cpp:249-285). */
 aqh_status aqh_read_quantized_u8(aqh_ctx* ctx, const int* channels, int nchan, uint8_t* out, size_t out_bytes);
+
+/* Display element types: the PkDspy* codes of ndspy.h:70-76, so a Dspy
+ * driver receives them unchanged. */
+enum {
+	AQH_DSPY_FLOAT32 = 1, AQH_DSPY_UNSIGNED32 = 2, AQH_DSPY_SIGNED32 = 3, AQH_DSPY_UNSIGNED16 = 4,
+	AQH_DSPY_SIGNED16 = 5, AQH_DSPY_UNSIGNED8 = 6, AQH_DSPY_SIGNED8 = 7
+};
+/* selectDataFormat (ddmanager.cpp:249-285): float32 when one == 0, else the
+ * narrowest unsigned (min >= 0) or signed type holding [min, max]. */
+int aqh_display_format(float one, float min, float max);
+/* One display request (CqDisplayRequest) with its own channels and quantize
+ * settings -- an rgba display and a z display of the same frame are two. */
+typedef struct {
+	int nchan;                   /* channels per pixel, at most 16 */
+	int channels[16];            /* channel-buffer indices in display order, e.g. {6,0,1,2} = a,r,g,b */
+	float q_zero, q_one, q_min, q_max, q_dither;  /* the request's quantize; q_one == 0: unquantized */
+	int format;                  /* AQH_DSPY_*; 0 = aqh_display_format(q_one, q_min, q_max) */
+	const float* dither;         /* per display pixel random s in [0,1) (crop window, row-major);
+	                                NULL = the frame's aqh_samples dither (or 0) */
+} aqh_display;
+/* FormatBucketForDisplay (ddmanager.cpp:1022-1119) over the whole crop window
+ * on the device: value = lround(zero + v*(one-zero) + dither*s) in double,
+ * clamped to [min, max] (unsigned/signed 32-bit also to the type's range),
+ * then converted to the element type; with q_one == 0 the channel value as
+ * is.  `out` gets width x height x nchan elements, row-major; `format_used`
+ * (may be NULL) the element type written. */
+aqh_status aqh_read_display(aqh_ctx* ctx, const aqh_display* d, void* out, size_t out_bytes, int* format_used);
 /* Per-sample results for parity checks, over the sample region (pixel-major,
  * sample-minor): occluding-hit micropolygon id before Combine (-1 none), occlZ,
  * transparent fragment count, valid flag after Combine, and the combined

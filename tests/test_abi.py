@@ -52,3 +52,19 @@ def test_filter_tables_match_oracle(aqh_lib, oracle):
             b = oracle.filter_table(fid, xw, yw, xs, ys)
             assert a.shape == b.shape
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (fid, xw, yw, xs, ys)
+
+
+def test_display_format_selection(aqh_lib):
+    """aqh_display_format follows selectDataFormat (ddmanager.cpp:249-285)."""
+    L = aqh_lib.load()
+    f = L.aqh_display_format
+    assert f(0.0, 0.0, 255.0) == 1                  # no quantize: float32
+    assert f(255.0, 0.0, 255.0) == 6                # unsigned 8
+    assert f(255.0, 0.0, 256.0) == 4                # unsigned 16
+    assert f(65535.0, 0.0, 65535.0) == 4
+    assert f(65535.0, 0.0, 65536.0) == 2            # unsigned 32
+    assert f(100.0, -128.0, 127.0) == 7             # signed 8
+    assert f(100.0, -129.0, 127.0) == 5             # signed 16
+    assert f(100.0, -128.0, 128.0) == 5
+    assert f(100.0, -32768.0, 32767.0) == 5
+    assert f(100.0, -32769.0, 0.0) == 3             # signed 32
