@@ -720,13 +720,17 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		if (t < npend) sm.pref[t] = pre;
 		__syncthreads();
 
-		// ---- parallel pass: one (candidate, sample) test per thread ----
-		for (int p = t; p < total; p += kThreadsS) {
-			int lo = 0, hi = npend - 1;
-			while (lo < hi) {
-				const int mid = (lo + hi + 1) >> 1;
-				if (sm.pref[mid] <= p) lo = mid; else hi = mid - 1;
-			}
+		// ---- parallel pass: one (candidate, sample) test per lane, each warp
+		// walking a contiguous run of tests so a lane finds its candidate a
+		// step or two on from where the warp's last lane stopped ----
+		const int chunk = ((total + kThreadsS - 1) / kThreadsS) * 32;
+		const int pw0 = (t >> 5) * chunk, pw1 = min(total, pw0 + chunk);
+		int cur = 0;
+		for (int p0 = pw0; p0 < pw1; p0 += 32) {
+			const int p = p0 + (t & 31);
+			const int lo = advance_item(sm.pref, npend, cur, min(p, pw1 - 1));
+			cur = __shfl_sync(0xffffffffu, lo, 31);
+			if (p >= pw1) continue;
 			const RecS& r = sm.rec[lo];
 			const int k = p - sm.pref[lo];
 			const int cx0 = sm.rng[lo][0], cy0 = sm.rng[lo][1], totx = sm.rng[lo][2];

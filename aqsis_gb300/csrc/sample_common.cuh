@@ -46,6 +46,26 @@ __device__ __forceinline__ int block_excl_sum(int* warp_tot, int v, int& total) 
 	return pre + inc - v;
 }
 
+// The item holding position p of a running count: pref[c] is the first
+// position of item c (nondecreasing, pref[0] = 0), n items.  `c` is an item
+// already known to start at or before p (pref[c] <= p), typically the one a
+// lane of the same warp found for the previous run of positions: a few
+// steps forward, then a binary search for long jumps.  Returns the largest c
+// with pref[c] <= p.
+__device__ __forceinline__ int advance_item(const int* pref, int n, int c, int p) {
+#pragma unroll 1
+	for (int it = 0; it < 4 && c + 1 < n && pref[c + 1] <= p; ++it) ++c;
+	if (c + 1 < n && pref[c + 1] <= p) {
+		int lo = c + 1, hi = n - 1;
+		while (lo < hi) {
+			const int mid = (lo + hi + 1) >> 1;
+			if (pref[mid] <= p) lo = mid; else hi = mid - 1;
+		}
+		c = lo;
+	}
+	return c;
+}
+
 // Sub-sample index range of pixel `p` inside [s, e) of a bound edge
 // (bucketprocessor.cpp:1119-1138, 1149-1153), for one axis.
 __device__ __forceinline__ void sub_range(int p, float bmin, float bmax, int ns, int& lo, int& hi) {
