@@ -71,7 +71,7 @@ class FrameStats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("tile_pixels", C.c_int), ("supertile_pixels", C.c_int), ("persistent_ctas", C.c_int),
-                ("ms", C.c_float)]
+                ("filter_ctas_per_sm", C.c_int), ("ms", C.c_float)]
 
 
 class Display(C.Structure):
@@ -321,9 +321,10 @@ class Hider:
         """AQH_MODE_BATCHED (persistent work queue + CUDA graph) or AQH_MODE_PLAIN."""
         self._check(self.L.aqh_set_mode(self.ctx, 1 if batched else 0), "aqh_set_mode")
 
-    def set_tuning(self, tile_pixels: int = 0, supertile_pixels: int = 0, persistent_ctas: int = 0):
-        """Launch shape of the sampling stage (aqh_set_tuning); zeros are the defaults."""
-        t = Tuning(tile_pixels, supertile_pixels, persistent_ctas, 0.0)
+    def set_tuning(self, tile_pixels: int = 0, supertile_pixels: int = 0, persistent_ctas: int = 0,
+                   filter_ctas_per_sm: int = 0):
+        """Launch shape of the sampling and filter stages (aqh_set_tuning); zeros are the defaults."""
+        t = Tuning(tile_pixels, supertile_pixels, persistent_ctas, filter_ctas_per_sm, 0.0)
         self._check(self.L.aqh_set_tuning(self.ctx, C.byref(t)), "aqh_set_tuning")
 
     def get_tuning(self) -> dict:

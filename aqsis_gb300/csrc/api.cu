@@ -497,7 +497,7 @@ int aqh_filter_table(int filter, float xw, float yw, int xs, int ys, float* out,
 
 aqh_status aqh_frame_begin(aqh_ctx* ctx, const aqh_frame_desc* d) {
 	if (!ctx || !d) return AQH_EINVAL;
-	FrameParams fp;
+	FrameParams fp{};
 	std::string err;
 	const aqh_status st = aqh::resolve_frame(*d, fp, ctx->ftab, err);
 	if (st != AQH_OK) return ctx->fail(st, "%s", err.c_str());
@@ -847,6 +847,7 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	fp.any_motion = motion ? 1 : 0;
 	P.mbdof = fp.use_dof || fp.any_motion;
 	set_tiling(fp, ctx->tune.tile_pixels, ctx->tune.supertile_pixels);
+	fp.filter_ctas = ctx->tune.filter_ctas_per_sm;
 	if (P.mbdof) {
 		ctx->h_dofb.clear();
 		dof_bounds_h(fp.xs, fp.ys, ctx->h_dofb);
@@ -1209,7 +1210,7 @@ aqh_status aqh_set_camera_to_raster(aqh_ctx* ctx, const float* m) {
 aqh_status aqh_set_tuning(aqh_ctx* ctx, const aqh_tuning* t) {
 	if (!ctx || !t) return AQH_EINVAL;
 	if (t->tile_pixels < 0 || t->tile_pixels > 256 || t->supertile_pixels < 0 || t->supertile_pixels > 65536 ||
-	    t->persistent_ctas < 0)
+	    t->persistent_ctas < 0 || t->filter_ctas_per_sm < 0 || t->filter_ctas_per_sm > 8)
 		return ctx->fail(AQH_EINVAL, "tuning out of range (tile %d, super-tile %d, ctas %d)", t->tile_pixels,
 		                 t->supertile_pixels, t->persistent_ctas);
 	ctx->tune = *t;
@@ -1267,6 +1268,36 @@ aqh_status aqh_autotune(aqh_ctx* ctx, int repeats, aqh_tuning* best) {
 					have = true;
 				}
 			}
+	// the filter's tiles in flight, with the sampling shape chosen above
+	// (device time of the filter and quantize stage)
+	auto filter_ms = [&](int fc, float& out) -> aqh_status {
+		ctx->tune = pick;
+		ctx->tune.filter_ctas_per_sm = fc;
+		for (int r = 0; r < repeats; ++r) {
+			const aqh_status st = aqh_render(ctx, 1);
+			if (st != AQH_OK) return st;
+			const float m = ctx->stats.ms_filter;
+			if (r == 0 || m < out) out = m;
+		}
+		return AQH_OK;
+	};
+	float fbest = 0.0f;
+	aqh_status fst = filter_ms(0, fbest);
+	int fpick = 0;
+	for (int fc : {3, 4, 5}) {
+		if (fst != AQH_OK) break;
+		float m = 0.0f;
+		fst = filter_ms(fc, m);
+		if (fst == AQH_OK && m < fbest * 0.99f) {
+			fbest = m;
+			fpick = fc;
+		}
+	}
+	if (fst != AQH_OK) {
+		ctx->tune = keep;
+		return fst;
+	}
+	pick.filter_ctas_per_sm = fpick;
 	ctx->tune = pick;
 	pick.ms = pick_ms;
 	if (best) *best = pick;

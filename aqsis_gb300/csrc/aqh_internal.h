@@ -51,6 +51,7 @@ struct FrameParams {
 	int nstx, nsty;
 	int any_motion;
 	int ftab_n;                              // floats in the filter table
+	int filter_ctas;                         // filter CTAs per SM (0: by the samples' L2 footprint)
 };
 
 // Grid stream in device memory (aqh_submit_grids_device layout).

@@ -6,6 +6,7 @@
 // (ddmanager/ddmanager.cpp:1022-1119).  One thread per display pixel walks
 // the (2*shift+1)^2 neighbouring pixels and their samples in the reference's
 // loop order (fy, fx, sy, sx), so the float sums round identically.
+#include <algorithm>
 #include <type_traits>
 
 #include "aqh_internal.h"
@@ -15,15 +16,12 @@ namespace aqh {
 
 namespace {
 
-// SPP > 0: samples per pixel known at compile time (the sample loop is
-// unrolled by four so its loads issue together); 0: read from fp.
+// One display pixel (x, y).  SPP > 0: samples per pixel known at compile
+// time (the sample loop is unrolled by four so its loads issue together); 0:
+// read from fp.
 template <int SPP>
-__global__ void __launch_bounds__(256)
-filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __restrict__ ftab,
-              float* __restrict__ chan) {
-	const int x = fp.crop_x0 + blockIdx.x * 16 + (threadIdx.x & 15);
-	const int y = fp.crop_y0 + blockIdx.y * 16 + (threadIdx.x >> 4);
-	if (x >= fp.crop_x1 || y >= fp.crop_y1) return;
+__device__ __forceinline__ void filter_pixel(const FrameParams& fp, const SamplerDev& smp, const SampleStore& st,
+                                             const float* __restrict__ ftab, float* __restrict__ chan, int x, int y) {
 	const float xcent = x + 0.5f, ycent = y + 0.5f;
 	const int xmax = fp.shiftX, ymax = fp.shiftY;
 	const int spp = SPP > 0 ? SPP : fp.spp;
@@ -39,31 +37,50 @@ filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __res
 			const int bit = (fy + ymax) * (2 * xmax + 1) + fx + xmax;
 			const int index = bit * spp;
 			const float fpx = (float)px, fpy = (float)py;
-#pragma unroll 4
-			for (int i = 0; i < spp; ++i) {
-				bool inside;
-				if (st.wmask) {
-					inside = (__ldg(st.wmask + store_index(pix, i, spp)) >> bit) & 1u;
-				} else {
-					const float2 o = __ldg(smp.pos + pat * spp + i);
-					const float vx = (fpx + o.x) - xcent;
-					const float vy = (fpy + o.y) - ycent;
-					inside = vx >= -fp.xfwo2 && vy >= -fp.yfwo2 && vx <= fp.xfwo2 && vy <= fp.yfwo2;
+			// samples in groups of four: the window tests of a group first, then
+			// the sample data of the samples inside it, so each group costs two
+			// memory round trips; the sums still run in sample order
+			for (int i0 = 0; i0 < spp; i0 += 4) {
+				bool in[4];
+				float gv[4];
+#pragma unroll
+				for (int j = 0; j < 4; ++j) {
+					const int i = i0 + j;
+					const bool ok = (SPP > 0 && SPP % 4 == 0) || i < spp;
+					const int ic = ok ? i : i0;
+					if (st.wmask) {
+						in[j] = ok && ((__ldg(st.wmask + store_index(pix, ic, spp)) >> bit) & 1u);
+					} else {
+						const float2 o = __ldg(smp.pos + pat * spp + ic);
+						const float vx = (fpx + o.x) - xcent;
+						const float vy = (fpy + o.y) - ycent;
+						in[j] = ok && vx >= -fp.xfwo2 && vy >= -fp.yfwo2 && vx <= fp.xfwo2 && vy <= fp.yfwo2;
+					}
+					gv[j] = __ldg(ftab + index + ic);
 				}
-				if (inside) {
-					const float gw = __ldg(ftab + index + i);
-					gTot += gw;
-					const float4 b = __ldg(st.b + store_index(pix, i, spp));
-					if (b.w != 0.0f) {
-						const float4 a = __ldg(st.a + store_index(pix, i, spp));
-						acc[0] += a.x * gw;
-						acc[1] += a.y * gw;
-						acc[2] += a.z * gw;
-						acc[3] += b.x * gw;
-						acc[4] += b.y * gw;
-						acc[5] += b.z * gw;
-						acc[6] += a.w * gw;
-						count++;
+				float4 av[4], bv[4];
+#pragma unroll
+				for (int j = 0; j < 4; ++j) {
+					const long long si = store_index(pix, in[j] ? i0 + j : i0, spp);
+					bv[j] = in[j] ? __ldg(st.b + si) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+					av[j] = in[j] ? __ldg(st.a + si) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+				}
+#pragma unroll
+				for (int j = 0; j < 4; ++j) {
+					if (in[j]) {
+						const float gw = gv[j];
+						gTot += gw;
+						if (bv[j].w != 0.0f) {
+							const float4 a = av[j], b = bv[j];
+							acc[0] += a.x * gw;
+							acc[1] += a.y * gw;
+							acc[2] += a.z * gw;
+							acc[3] += b.x * gw;
+							acc[4] += b.y * gw;
+							acc[5] += b.z * gw;
+							acc[6] += a.w * gw;
+							count++;
+						}
 					}
 				}
 			}
@@ -99,6 +116,20 @@ filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __res
 	float* out = chan + ((long long)(y - fp.crop_y0) * (fp.crop_x1 - fp.crop_x0) + (x - fp.crop_x0)) * 9;
 #pragma unroll
 	for (int k = 0; k < 9; ++k) out[k] = c[k];
+}
+
+// 16x16-pixel tiles of the crop window in raster order, `gridDim.x` of them
+// in flight at once.
+template <int SPP>
+__global__ void __launch_bounds__(256)
+filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __restrict__ ftab,
+              float* __restrict__ chan) {
+	const int ntx = (fp.crop_x1 - fp.crop_x0 + 15) >> 4, nty = (fp.crop_y1 - fp.crop_y0 + 15) >> 4;
+	for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
+		const int x = fp.crop_x0 + (tile % ntx) * 16 + (threadIdx.x & 15);
+		const int y = fp.crop_y0 + (tile / ntx) * 16 + (threadIdx.x >> 4);
+		if (x < fp.crop_x1 && y < fp.crop_y1) filter_pixel<SPP>(fp, smp, st, ftab, chan, x, y);
+	}
 }
 
 // aqsis lround (math.h:67-70) in double: lfloor(x - 0.5) + 1
@@ -177,7 +208,15 @@ void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStor
                    float* channels, cudaStream_t s) {
 	const int w = fp.crop_x1 - fp.crop_x0, h = fp.crop_y1 - fp.crop_y0;
 	if (w <= 0 || h <= 0) return;
-	dim3 grid((w + 15) / 16, (h + 15) / 16);
+	const int ntiles = ((w + 15) / 16) * ((h + 15) / 16);
+	int dev = 0, nsm = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+	// tiles in flight per SM: by default as many as can be resident (the
+	// filter is latency-bound: fewer tiles in flight, whose samples would stay
+	// in L2 between the passes, measured slower)
+	const int per_sm = fp.filter_ctas > 0 ? std::min(fp.filter_ctas, 8) : 8;
+	const int grid = std::max(1, std::min(ntiles, nsm * per_sm));
 	switch (fp.spp) {
 	case 4: filter_kernel<4><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels); break;
 	case 16: filter_kernel<16><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels); break;

@@ -125,7 +125,7 @@ extern "C" aqh_status aqh_render_noalloc(const aqh_frame_desc* desc, const float
 	if (!desc || !pos || npatterns <= 0 || ngrids < 0 || (ngrids > 0 && (!cu || !cv || !flags || !pbase || !cbase)) ||
 	    !d_P || !d_channels)
 		return na_fail(err, err_len, AQH_EINVAL, "aqh_render_noalloc: null argument");
-	FrameParams fp;
+	FrameParams fp{};
 	std::vector<float> ftab;
 	std::string msg;
 	aqh_status st = resolve_frame(*desc, fp, ftab, msg);

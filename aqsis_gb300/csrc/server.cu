@@ -67,7 +67,7 @@ struct aqh_server {
 
 extern "C" size_t aqh_job_footprint(const aqh_job* j) {
 	if (!j) return 0;
-	aqh::FrameParams fp;
+	aqh::FrameParams fp{};
 	std::vector<float> ftab;
 	std::string err;
 	if (aqh::resolve_frame(j->frame, fp, ftab, err) != AQH_OK) return 0;

@@ -354,7 +354,8 @@ def run_gpu(args):
     h2 = aqh.Hider(local)
     h2.set_stream(stream.cuda_stream)
     h2.set_mode(True)
-    h2.set_tuning(tuning["tile_pixels"], tuning["supertile_pixels"], tuning["persistent_ctas"])
+    h2.set_tuning(tuning["tile_pixels"], tuning["supertile_pixels"], tuning["persistent_ctas"],
+                  tuning["filter_ctas_per_sm"])
     h2.frame_begin(fr)
     h2.set_samples(smp)
     L = h2.L

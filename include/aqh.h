@@ -239,13 +239,16 @@ aqh_status aqh_synchronize(aqh_ctx* ctx);
  * CTA holds, min(256, 4096 / samples per pixel); tiles stay within 16x16
  * pixels).  supertile_pixels: side of a binning super-tile in pixels (0: 128).
  * persistent_ctas: CTAs of the batched form's persistent sampling kernel (0:
- * every CTA that fits on the device at once).  No setting changes a result:
+ * every CTA that fits on the device at once).  filter_ctas_per_sm: 16x16
+ * display tiles the filter keeps in flight per SM (0: as many as fit, else
+ * 1..8).  No setting changes a result:
  * each sample meets its candidate micropolygons in the same order under any
  * tiling.  `ms` is only written by aqh_autotune. */
 typedef struct {
 	int tile_pixels;
 	int supertile_pixels;
 	int persistent_ctas;
+	int filter_ctas_per_sm;  /* filter tiles in flight per SM (0: as many as fit) */
 	float ms;  /* device time of the frame with this tuning (sum of the stage times) */
 } aqh_tuning;
 aqh_status aqh_set_tuning(aqh_ctx* ctx, const aqh_tuning* t);

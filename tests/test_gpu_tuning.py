@@ -20,6 +20,8 @@ SCENES = {
 }
 
 TUNINGS = [
+    (0, 0, 0, 1),   # one filter tile in flight per SM
+    (0, 0, 0, 8),
     (0, 64, 0),
     (0, 256, 0),
     (64, 0, 0),
