@@ -53,7 +53,8 @@ class FrameDesc(C.Structure):
 
 class Grid(C.Structure):
     _fields_ = [("cu", C.c_int), ("cv", C.c_int), ("nkeys", C.c_int), ("key_times", _f32p),
-                ("P", _f32p), ("Ci", _f32p), ("Oi", _f32p), ("culled", _u8p), ("flags", C.c_int)]
+                ("P", _f32p), ("Ci", _f32p), ("Oi", _f32p), ("culled", _u8p), ("flags", C.c_int),
+                ("aov", _f32p)]
 
 
 class Samples(C.Structure):
@@ -131,6 +132,10 @@ def load(build_if_missing: bool = False):
     L.aqh_read_samples.argtypes = [vp, _i32p, _f32p, _i32p, _u8p, _f32p, C.c_size_t]
     L.aqh_get_stats.argtypes = [vp, C.POINTER(FrameStats)]
     L.aqh_set_camera_to_raster.argtypes = [vp, _f32p]
+    L.aqh_set_aov_count.argtypes = [vp, C.c_int]
+    L.aqh_submit_aov_host.argtypes = [vp, _f32p, C.c_size_t]
+    L.aqh_submit_aov_device.argtypes = [vp, vp]
+    L.aqh_read_aov.argtypes = [vp, _f32p, C.c_size_t]
     L.aqh_display_format.argtypes = [C.c_float, C.c_float, C.c_float]
     L.aqh_display_format.restype = C.c_int
     L.aqh_read_display.argtypes = [vp, C.POINTER(Display), vp, C.c_size_t, C.POINTER(C.c_int)]
@@ -143,7 +148,8 @@ def load(build_if_missing: bool = False):
     for name in ("aqh_create", "aqh_set_mode", "aqh_set_stream", "aqh_frame_begin", "aqh_set_samples", "aqh_submit_grid", "aqh_submit_grids_device",
                  "aqh_render", "aqh_synchronize", "aqh_read_channels", "aqh_read_bucket", "aqh_read_quantized_u8",
                  "aqh_read_samples", "aqh_get_stats", "aqh_test_invbilinear", "aqh_set_tuning", "aqh_get_tuning",
-                 "aqh_autotune", "aqh_set_camera_to_raster", "aqh_read_display"):
+                 "aqh_autotune", "aqh_set_camera_to_raster", "aqh_read_display", "aqh_set_aov_count",
+                 "aqh_submit_aov_host", "aqh_submit_aov_device", "aqh_read_aov"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -225,6 +231,7 @@ class Hider:
     def frame_begin(self, fr):
         self.frame = fr
         self._keep = []
+        self.naov = 0
         self._check(self.L.aqh_frame_begin(self.ctx, C.byref(frame_desc(fr))), "aqh_frame_begin")
         if getattr(fr, "camera_to_raster", None) is not None:
             self.set_camera_to_raster(fr.camera_to_raster)
@@ -256,19 +263,36 @@ class Hider:
         self._check(self.L.aqh_set_samples(self.ctx, C.byref(cs)), "aqh_set_samples")
         self._check(self.L.aqh_synchronize(self.ctx), "aqh_synchronize")
 
-    def submit_grid(self, cu, cv, P, Ci=None, Oi=None, flags=1, key_times=None, culled=None):
+    def set_aov_count(self, n: int):
+        """Output variables per vertex for this frame (aqh_set_aov_count), before any grid."""
+        self._check(self.L.aqh_set_aov_count(self.ctx, int(n)), "aqh_set_aov_count")
+        self.naov = int(n)
+
+    def read_aov(self) -> np.ndarray:
+        w, h = self._dims()
+        out = np.zeros((h, w, self.naov), np.float32)
+        self._check(self.L.aqh_read_aov(self.ctx, _p(out, _f32p), out.size), "aqh_read_aov")
+        return out
+
+    def submit_grid(self, cu, cv, P, Ci=None, Oi=None, flags=1, key_times=None, culled=None, aov=None):
         P = np.ascontiguousarray(P, np.float32)
         nkeys = 1 if key_times is None else len(key_times)
         kt = None if key_times is None else np.ascontiguousarray(key_times, np.float32)
         Ci = None if Ci is None else np.ascontiguousarray(Ci, np.float32)
         Oi = None if Oi is None else np.ascontiguousarray(Oi, np.float32)
         cl = None if culled is None else np.ascontiguousarray(culled, np.uint8)
-        g = Grid(cu, cv, nkeys, _p(kt, _f32p), _p(P, _f32p), _p(Ci, _f32p), _p(Oi, _f32p), _p(cl, _u8p), flags)
+        av = None if aov is None else np.ascontiguousarray(aov, np.float32)
+        g = Grid(cu, cv, nkeys, _p(kt, _f32p), _p(P, _f32p), _p(Ci, _f32p), _p(Oi, _f32p), _p(cl, _u8p), flags,
+                 _p(av, _f32p))
         self._check(self.L.aqh_submit_grid(self.ctx, C.byref(g)), "aqh_submit_grid")
 
     def submit_scene_grids(self, g):
         """Submit every grid of a scene.Grids through aqh_submit_grid, in order."""
         mpbase = 0
+        aov = None
+        if getattr(g, "aov", None) is not None:
+            aov = np.asarray(g.aov, np.float32).reshape(len(g.Ci), -1)
+            self.set_aov_count(aov.shape[1])
         for i in range(g.ngrids):
             cu, cv, nk = int(g.cu[i]), int(g.cv[i]), int(g.nkeys[i])
             nv = (cu + 1) * (cv + 1)
@@ -280,7 +304,7 @@ class Hider:
             if g.culled is not None:
                 cl = g.culled[mpbase:mpbase + cu * cv]
             self.submit_grid(cu, cv, g.P[pb:pb + nv * nk], g.Ci[cb:cb + nv], g.Oi[cb:cb + nv], int(g.flags[i]),
-                             kt, cl)
+                             kt, cl, None if aov is None else aov[cb:cb + nv])
             mpbase += cu * cv
 
     def submit_grids_host(self, g):
@@ -301,6 +325,10 @@ class Hider:
             keep.append(x)
             return x.ctypes.data
         culled = a(g.culled, np.uint8) if g.culled is not None else None
+        av = None
+        if getattr(g, "aov", None) is not None:
+            av = np.ascontiguousarray(np.asarray(g.aov, np.float32).reshape(len(g.Ci), -1))
+            self.set_aov_count(av.shape[1])
         self._check(L.aqh_submit_grids_host(self.ctx, g.ngrids, a(g.cu, np.int32), a(g.cv, np.int32),
                                             a(g.nkeys, np.int32), a(g.flags, np.int32), a(g.pbase, np.int64),
                                             a(g.cbase, np.int64), a(g.tbase, np.int32), a(g.times, np.float32),
@@ -308,6 +336,9 @@ class Hider:
                                             a(g.Ci, np.float32), a(g.Oi, np.float32), int(g.Ci.shape[0]), culled,
                                             g.micropolygons),
                     "aqh_submit_grids_host")
+        if av is not None:
+            self._check(L.aqh_submit_aov_host(self.ctx, _p(av, _f32p), av.shape[0]), "aqh_submit_aov_host")
+            keep.append(av)
         self._packed_keep = keep
 
     def submit_grids_device(self, ngrids, d_cu, d_cv, d_nkeys, d_flags, d_pbase, d_cbase, d_tbase, d_times,
@@ -419,6 +450,8 @@ class Hider:
         self.submit_scene_grids(scene.grids)
         self.render(sync=True)
         res = {"channels": self.read_channels(), "quantized": self.read_quantized(qchannels)}
+        if self.naov:
+            res["aov"] = self.read_aov()
         if samples:
             res.update(self.read_samples())
         res["stats"] = self.stats()

@@ -329,6 +329,14 @@ struct aqh_ctx {
 	bool any_camera = false;
 	bool camera_set = false;
 	aqh::CamMatrix camera{};
+	// output variables: count, per-vertex values staged for host grids, the
+	// packed host or device arrays, and the device copies
+	int naov = 0;
+	std::vector<float> h_aov;
+	const float* hp_aov = nullptr;
+	size_t hp_naov_vertices = 0;
+	const float* dev_aov = nullptr;
+	DevBuf d_aov, d_aovsrc, d_aovchan;
 
 	// host-submitted packed arrays (caller-owned, uploaded at render)
 	bool host_packed = false;
@@ -513,6 +521,11 @@ aqh_status aqh_frame_begin(aqh_ctx* ctx, const aqh_frame_desc* d) {
 	ctx->any_transparent = false;
 	ctx->any_camera = false;
 	ctx->camera_set = false;
+	ctx->naov = 0;
+	ctx->h_aov.clear();
+	ctx->hp_aov = nullptr;
+	ctx->hp_naov_vertices = 0;
+	ctx->dev_aov = nullptr;
 	ctx->dev_grids = false;
 	ctx->dev_motion = false;
 	ctx->host_packed = false;
@@ -609,6 +622,10 @@ aqh_status aqh_submit_grid(aqh_ctx* ctx, const aqh_grid* gr) {
 		}
 	}
 	if (e != cudaSuccess) return ctx->cuda_fail(e, "stage grid");
+	if (ctx->naov > 0) {
+		if (gr->aov) ctx->h_aov.insert(ctx->h_aov.end(), gr->aov, gr->aov + (size_t)nv * ctx->naov);
+		else ctx->h_aov.insert(ctx->h_aov.end(), (size_t)nv * ctx->naov, 0.0f);
+	}
 	if (flags & AQH_GRID_CAMERA) ctx->any_camera = true;
 	ctx->h_flags.push_back(flags);
 	if (gr->culled) {
@@ -785,6 +802,18 @@ static aqh_status upload_packed_grids(aqh_ctx* ctx) {
 	g.Ci = hp.Ci ? ctx->d_Ci.as<float4>() : nullptr;
 	g.Oi = hp.Oi ? ctx->d_Oi.as<float4>() : nullptr;
 	g.culled = hp.culled ? ctx->d_culled.as<uint8_t>() : nullptr;
+	g.naov = 0;
+	g.aov = nullptr;
+	if (ctx->naov > 0) {
+		const size_t n = hp.nC * (size_t)ctx->naov;
+		AQH_TRY(ctx->d_aov.ensure(std::max<size_t>(n, 1) * 4), "alloc output variables");
+		if (ctx->hp_aov && ctx->hp_naov_vertices >= hp.nC)
+			AQH_TRY(cudaMemcpyAsync(ctx->d_aov.p, ctx->hp_aov, n * 4, cudaMemcpyHostToDevice, ctx->stream), "upload aov");
+		else
+			AQH_TRY(cudaMemsetAsync(ctx->d_aov.p, 0, n * 4, ctx->stream), "clear aov");
+		g.aov = ctx->d_aov.as<float>();
+		g.naov = ctx->naov;
+	}
 	return AQH_OK;
 }
 
@@ -816,6 +845,13 @@ static aqh_status upload_host_grids(aqh_ctx* ctx) {
 	g.times = ctx->d_times.as<float>();
 	g.P = ctx->d_P.as<float4>(); g.Ci = ctx->d_Ci.as<float4>(); g.Oi = ctx->d_Oi.as<float4>();
 	g.culled = ctx->any_culled ? ctx->d_culled.as<uint8_t>() : nullptr;
+	g.naov = 0;
+	g.aov = nullptr;
+	if (ctx->naov > 0) {
+		AQH_TRY(up(ctx->d_aov, ctx->h_aov.data(), ctx->h_aov.size() * 4), "upload aov");
+		g.aov = ctx->d_aov.as<float>();
+		g.naov = ctx->naov;
+	}
 	return AQH_OK;
 }
 
@@ -946,6 +982,17 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	P.g = g;
 	AQH_TRY(ctx->d_idgrid.ensure(sizeof(int32_t) * (size_t)((P.nmps + 255) / 256 + 1)), "alloc id table");
 	P.g.id_grid = ctx->d_idgrid.as<int32_t>();
+	if (ctx->dev_grids) {
+		if (ctx->naov > 0 && !ctx->dev_aov)
+			return ctx->fail(AQH_EINVAL, "output variables are set but aqh_submit_aov_device was not called");
+		P.g.aov = ctx->dev_aov;
+		P.g.naov = ctx->dev_aov ? ctx->naov : 0;
+	}
+	if (P.g.naov > 0) {
+		AQH_TRY(ctx->d_aovsrc.ensure(nstore * sizeof(int32_t)), "alloc output variable sources");
+		AQH_TRY(ctx->d_aovchan.ensure(ndisp * P.g.naov * sizeof(float)), "alloc output variables");
+		P.store.aovsrc = ctx->d_aovsrc.as<int32_t>();
+	}
 	return AQH_OK;
 }
 
@@ -997,6 +1044,7 @@ static aqh_status enqueue_frame(aqh_ctx* ctx, RenderPlan& P, bool batched, bool 
 	AQH_TRY(cudaGetLastError(), "sample kernel launch");
 	if (timing) mark(ctx->ev[2]);
 	launch_filter(fp, ctx->smp, P.store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(), s);
+	if (P.g.naov > 0) launch_filter_aov(fp, ctx->smp, P.store, P.g, ctx->d_ftab.as<float>(), ctx->d_aovchan.as<float>(), s);
 	if (fp.q_one == 0.0f || (fp.q_min >= 0.0f && fp.q_max <= 255.0f)) {
 		AQH_TRY(cudaMemcpyAsync(ctx->d_qchan.p, kDefaultDisplay, sizeof kDefaultDisplay, cudaMemcpyHostToDevice, s),
 		        "upload display channels");
@@ -1077,6 +1125,7 @@ static aqh_status render_plain(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 	}
 	cudaEventRecord(ctx->ev[2], s);
 	launch_filter(fp, ctx->smp, P.store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(), s);
+	if (P.g.naov > 0) launch_filter_aov(fp, ctx->smp, P.store, P.g, ctx->d_ftab.as<float>(), ctx->d_aovchan.as<float>(), s);
 	if (fp.q_one == 0.0f || (fp.q_min >= 0.0f && fp.q_max <= 255.0f)) {
 		AQH_TRY(cudaMemcpyAsync(ctx->d_qchan.p, kDefaultDisplay, sizeof kDefaultDisplay, cudaMemcpyHostToDevice, s),
 		        "upload display channels");
@@ -1107,14 +1156,14 @@ static aqh_status render_batched(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 	P.bb.st_list = ctx->d_stlist.as<int32_t>();
 	P.bb.list_capacity = ctx->st_list_cap;
 	// graph key: every kernel argument of the frame
-	std::vector<unsigned char> key(sizeof(RenderPlan) + sizeof(SamplerDev) + sizeof(void*) * 8);
+	std::vector<unsigned char> key(sizeof(RenderPlan) + sizeof(SamplerDev) + sizeof(void*) * 9);
 	unsigned char* k = key.data();
 	std::memcpy(k, &P, sizeof(RenderPlan));
 	k += sizeof(RenderPlan);
 	std::memcpy(k, &ctx->smp, sizeof(SamplerDev));
 	k += sizeof(SamplerDev);
-	void* ptrs[8] = {ctx->d_ftab.p, ctx->d_chan.p, ctx->d_q8.p, ctx->d_qchan.p, ctx->d_queue.p, ctx->d_dofb.p,
-	                 ctx->d_err.p, (void*)s};
+	void* ptrs[9] = {ctx->d_ftab.p, ctx->d_chan.p, ctx->d_q8.p, ctx->d_qchan.p, ctx->d_queue.p, ctx->d_dofb.p,
+	                 ctx->d_err.p, ctx->d_aovchan.p, (void*)s};
 	std::memcpy(k, ptrs, sizeof ptrs);
 	if (!ctx->graph_valid) {
 		for (auto& ge : ctx->graphs) cudaGraphExecDestroy(ge.exec);
@@ -1196,6 +1245,43 @@ aqh_status aqh_synchronize(aqh_ctx* ctx) {
 			return render_plain(ctx, P, true);
 		}
 	}
+	return AQH_OK;
+}
+
+aqh_status aqh_set_aov_count(aqh_ctx* ctx, int n) {
+	if (!ctx) return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	if (n < 0 || n > AQH_MAX_AOV) return ctx->fail(AQH_ELIMIT, "%d output variables; 0..%d supported", n, AQH_MAX_AOV);
+	if (!ctx->h_cu.empty() || ctx->host_packed || ctx->dev_grids)
+		return ctx->fail(AQH_EINVAL, "the output variable count is set before grids are submitted");
+	ctx->naov = n;
+	return AQH_OK;
+}
+
+aqh_status aqh_submit_aov_host(aqh_ctx* ctx, const float* aov, size_t nvertices) {
+	if (!ctx || !aov) return AQH_EINVAL;
+	if (ctx->naov == 0) return ctx->fail(AQH_EINVAL, "no output variables set");
+	ctx->hp_aov = aov;
+	ctx->hp_naov_vertices = nvertices;
+	return AQH_OK;
+}
+
+aqh_status aqh_submit_aov_device(aqh_ctx* ctx, const float* d_aov) {
+	if (!ctx || !d_aov) return AQH_EINVAL;
+	if (ctx->naov == 0) return ctx->fail(AQH_EINVAL, "no output variables set");
+	ctx->dev_aov = d_aov;
+	return AQH_OK;
+}
+
+aqh_status aqh_read_aov(aqh_ctx* ctx, float* out, size_t out_floats) {
+	if (!ctx || !out) return AQH_EINVAL;
+	const FrameParams& fp = ctx->fp;
+	const size_t n = (size_t)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0) * ctx->naov;
+	if (ctx->naov == 0) return ctx->fail(AQH_EINVAL, "no output variables set");
+	if (out_floats < n) return ctx->fail(AQH_EINVAL, "output holds %zu floats, %zu needed", out_floats, n);
+	cudaSetDevice(ctx->device);
+	AQH_TRY(cudaMemcpyAsync(out, ctx->d_aovchan.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "read aov");
+	AQH_TRY(cudaStreamSynchronize(ctx->stream), "read aov");
 	return AQH_OK;
 }
 
@@ -1381,7 +1467,7 @@ aqh_status aqh_read_display(aqh_ctx* ctx, const aqh_display* d, void* out, size_
 	if (!ctx || !d || !out || d->nchan <= 0 || d->nchan > 16) return AQH_EINVAL;
 	const FrameParams& fp = ctx->fp;
 	for (int c = 0; c < d->nchan; ++c)
-		if (d->channels[c] < 0 || d->channels[c] >= AQH_NCHANNELS)
+		if (d->channels[c] < 0 || d->channels[c] >= AQH_NCHANNELS + ctx->naov)
 			return ctx->fail(AQH_EINVAL, "bad channel %d", d->channels[c]);
 	const int fmt = d->format ? d->format : aqh_display_format(d->q_one, d->q_min, d->q_max);
 	if (fmt < AQH_DSPY_FLOAT32 || fmt > AQH_DSPY_SIGNED8) return ctx->fail(AQH_EINVAL, "bad display format %d", fmt);
@@ -1402,7 +1488,8 @@ aqh_status aqh_read_display(aqh_ctx* ctx, const aqh_display* d, void* out, size_
 	}
 	const QuantizeParams q{d->q_zero, d->q_one, d->q_min, d->q_max, d->q_dither};
 	cudaGetLastError();
-	launch_display(fp, q, dither, ctx->d_chan.as<float>(), ctx->d_qchan.as<int>(), d->nchan, fmt, ctx->d_disp.p, s);
+	launch_display(fp, q, dither, ctx->d_chan.as<float>(), ctx->d_aovchan.as<float>(), ctx->naov,
+	               ctx->d_qchan.as<int>(), d->nchan, fmt, ctx->d_disp.p, s);
 	AQH_TRY(cudaGetLastError(), "display launch");
 	AQH_TRY(cudaMemcpyAsync(out, ctx->d_disp.p, bytes, cudaMemcpyDeviceToHost, s), "read display");
 	AQH_TRY(cudaStreamSynchronize(s), "read display");

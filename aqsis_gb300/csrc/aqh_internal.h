@@ -71,6 +71,8 @@ struct GridsDev {
 	const float4* Oi;
 	const uint8_t* culled;   // per global micropolygon id, may be null
 	const int32_t* id_grid;  // grid holding micropolygon id k * 256, for each k; may be null
+	const float* aov;        // output variables, float[vertex][naov] indexed like Ci; null when naov == 0
+	int naov;
 };
 
 // Sample pattern caches (aqh_samples) in device memory.
@@ -117,6 +119,8 @@ struct SampleStore {
 	unsigned long long* keys;  // opaque frames: (ordered depth, id + 1) of each sample's occluding
 	                           // hit, sample-major, resolved by a separate kernel; null: the
 	                           // sampler resolves in place
+	int32_t* aovsrc;  // micropolygon whose output variables the sample carries after Combine
+	                  // (store layout; -1 none), or null without output variables
 };
 
 // Transparent fragment pool: {depth, micropolygon id bits, u, v} + next link.
@@ -206,6 +210,9 @@ void set_tiling(FrameParams& fp, int tile_pixels = 0, int supertile_px = 0);
 void dof_bounds_h(int xs, int ys, std::vector<float4>& out);
 void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStore& st, const float* ftab,
                    float* channels, cudaStream_t s);
+// Output variables of the crop window, float[pixel][g.naov], filtered like Ci.
+void launch_filter_aov(const FrameParams& fp, const SamplerDev& sm, const SampleStore& st, const GridsDev& g,
+                       const float* ftab, float* aov_channels, cudaStream_t s);
 void launch_quantize_u8(const FrameParams& fp, const SamplerDev& sm, const float* channels, const int* chans,
                         int nchan, uint8_t* out, cudaStream_t s);
 // Quantize settings of one display request (CqDisplayRequest, ddmanager.cpp:428-457).
@@ -213,7 +220,8 @@ struct QuantizeParams {
 	float zero, one, min, max, dither;
 };
 void launch_display(const FrameParams& fp, const QuantizeParams& q, const float* dither, const float* channels,
-                    const int* chans, int nchan, int format, void* out, cudaStream_t s);
+                    const float* aov_channels, int naov, const int* chans, int nchan, int format, void* out,
+                    cudaStream_t s);
 void launch_test_invbilinear(const float* quad8, const float2* P, int n, float2* uv, cudaStream_t s);
 
 }  // namespace aqh

@@ -11,6 +11,7 @@
 
 #include "aqh_internal.h"
 #include "hider_device.cuh"
+#include "sample_common.cuh"
 
 namespace aqh {
 
@@ -132,6 +133,73 @@ filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __res
 	}
 }
 
+// Output variables of one display pixel: FilterBucket's weighted sum over
+// the same window, weights and order as filter_pixel (gTot included), of the
+// vertex-A values of each valid sample's front micropolygon.
+template <int SPP>
+__global__ void __launch_bounds__(256)
+filter_aov_kernel(FrameParams fp, SamplerDev smp, SampleStore st, GridsDev g, const float* __restrict__ ftab,
+                  float* __restrict__ out) {
+	const int ntx = (fp.crop_x1 - fp.crop_x0 + 15) >> 4, nty = (fp.crop_y1 - fp.crop_y0 + 15) >> 4;
+	const int spp = SPP > 0 ? SPP : fp.spp;
+	const int naov = g.naov;
+	for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
+		const int x = fp.crop_x0 + (tile % ntx) * 16 + (threadIdx.x & 15);
+		const int y = fp.crop_y0 + (tile / ntx) * 16 + (threadIdx.x >> 4);
+		if (x >= fp.crop_x1 || y >= fp.crop_y1) continue;
+		const float xcent = x + 0.5f, ycent = y + 0.5f;
+		const int xmax = fp.shiftX, ymax = fp.shiftY;
+		float gTot = 0.0f;
+		int count = 0;
+		float acc[AQH_MAX_AOV];
+#pragma unroll
+		for (int k = 0; k < AQH_MAX_AOV; ++k) acc[k] = 0.0f;
+		for (int fy = -ymax; fy <= ymax; fy++) {
+			const int py = y + fy;
+			for (int fx = -xmax; fx <= xmax; fx++) {
+				const int px = x + fx;
+				const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
+				const long long pat = (st.wmask || !smp.pos_index) ? pix : (long long)__ldg(smp.pos_index + pix);
+				const int bit = (fy + ymax) * (2 * xmax + 1) + fx + xmax;
+				const int index = bit * spp;
+				const float fpx = (float)px, fpy = (float)py;
+				for (int i = 0; i < spp; ++i) {
+					bool inside;
+					if (st.wmask) {
+						inside = (__ldg(st.wmask + store_index(pix, i, spp)) >> bit) & 1u;
+					} else {
+						const float2 o = __ldg(smp.pos + pat * spp + i);
+						const float vx = (fpx + o.x) - xcent;
+						const float vy = (fpy + o.y) - ycent;
+						inside = vx >= -fp.xfwo2 && vy >= -fp.yfwo2 && vx <= fp.xfwo2 && vy <= fp.yfwo2;
+					}
+					if (!inside) continue;
+					const float gw = __ldg(ftab + index + i);
+					gTot += gw;
+					const long long si = store_index(pix, i, spp);
+					if (__ldg(st.b + si).w == 0.0f) continue;
+					count++;
+					const int id = __ldg(st.aovsrc + si);
+					if (id < 0) continue;
+					const int gi = grid_of(g, id);
+					const int cu = __ldg(g.cu + gi);
+					const int m = id - (int)__ldg(g.mpbase + gi);
+					const int iv = m / cu, iu = m - iv * cu;
+					const float* v = g.aov + (__ldg(g.cbase + gi) + iv * (cu + 1) + iu) * naov;
+#pragma unroll
+					for (int k = 0; k < AQH_MAX_AOV; ++k)
+						if (k < naov) acc[k] += __ldg(v + k) * gw;
+				}
+			}
+		}
+		float* o = out + ((long long)(y - fp.crop_y0) * (fp.crop_x1 - fp.crop_x0) + (x - fp.crop_x0)) * naov;
+		const float inv = count == 0 ? 0.0f : (float)(1.0 / (double)gTot);
+#pragma unroll
+		for (int k = 0; k < AQH_MAX_AOV; ++k)
+			if (k < naov) o[k] = count == 0 ? 0.0f : acc[k] * inv;
+	}
+}
+
 // aqsis lround (math.h:67-70) in double: lfloor(x - 0.5) + 1
 __device__ __forceinline__ double lround_d(double x) {
 	const double y = x - 0.5;
@@ -160,14 +228,15 @@ __global__ void quantize_u8_kernel(FrameParams fp, SamplerDev smp, const float* 
 // element type T, the request's own quantize settings and dither values.
 template <class T>
 __global__ void display_kernel(FrameParams fp, QuantizeParams q, const float* __restrict__ dither,
-                               const float* __restrict__ chan, const int* __restrict__ chans, int nchan,
-                               T* __restrict__ out) {
+                               const float* __restrict__ chan, const float* __restrict__ aov, int naov,
+                               const int* __restrict__ chans, int nchan, T* __restrict__ out) {
 	const long long npix = (long long)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
 	const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
 	if (p >= npix) return;
 	const double s = dither ? (double)__ldg(dither + p) : 0.0;
 	for (int c = 0; c < nchan; ++c) {
-		double value = chan[p * 9 + chans[c]];
+		const int ch = chans[c];
+		double value = ch < 9 ? chan[p * 9 + ch] : aov[p * naov + (ch - 9)];
 		if (q.one != 0.0f) {
 			value = lround_d((double)q.zero + value * (double)(q.one - q.zero) + ((double)q.dither * s));
 			value = value < (double)q.min ? (double)q.min : (value > (double)q.max ? (double)q.max : value);
@@ -226,6 +295,21 @@ void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStor
 	}
 }
 
+void launch_filter_aov(const FrameParams& fp, const SamplerDev& sm, const SampleStore& st, const GridsDev& g,
+                       const float* ftab, float* aov_channels, cudaStream_t s) {
+	const int w = fp.crop_x1 - fp.crop_x0, h = fp.crop_y1 - fp.crop_y0;
+	if (w <= 0 || h <= 0 || g.naov <= 0 || !st.aovsrc) return;
+	const int ntiles = ((w + 15) / 16) * ((h + 15) / 16);
+	int dev = 0, nsm = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+	const int grid = std::max(1, std::min(ntiles, nsm * 8));
+	switch (fp.spp) {
+	case 16: filter_aov_kernel<16><<<grid, 256, 0, s>>>(fp, sm, st, g, ftab, aov_channels); break;
+	default: filter_aov_kernel<0><<<grid, 256, 0, s>>>(fp, sm, st, g, ftab, aov_channels); break;
+	}
+}
+
 void launch_quantize_u8(const FrameParams& fp, const SamplerDev& sm, const float* channels, const int* chans,
                         int nchan, uint8_t* out, cudaStream_t s) {
 	const long long npix = (long long)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
@@ -234,18 +318,19 @@ void launch_quantize_u8(const FrameParams& fp, const SamplerDev& sm, const float
 }
 
 void launch_display(const FrameParams& fp, const QuantizeParams& q, const float* dither, const float* channels,
-                    const int* chans, int nchan, int format, void* out, cudaStream_t s) {
+                    const float* aov_channels, int naov, const int* chans, int nchan, int format, void* out,
+                    cudaStream_t s) {
 	const long long npix = (long long)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
 	if (npix <= 0) return;
 	const unsigned nb = (unsigned)((npix + 255) / 256);
 	switch (format) {
-	case AQH_DSPY_FLOAT32: display_kernel<float><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (float*)out); break;
-	case AQH_DSPY_UNSIGNED32: display_kernel<uint32_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (uint32_t*)out); break;
-	case AQH_DSPY_SIGNED32: display_kernel<int32_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (int32_t*)out); break;
-	case AQH_DSPY_UNSIGNED16: display_kernel<uint16_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (uint16_t*)out); break;
-	case AQH_DSPY_SIGNED16: display_kernel<int16_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (int16_t*)out); break;
-	case AQH_DSPY_UNSIGNED8: display_kernel<uint8_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (uint8_t*)out); break;
-	default: display_kernel<int8_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, chans, nchan, (int8_t*)out); break;
+	case AQH_DSPY_FLOAT32: display_kernel<float><<<nb, 256, 0, s>>>(fp, q, dither, channels, aov_channels, naov, chans, nchan, (float*)out); break;
+	case AQH_DSPY_UNSIGNED32: display_kernel<uint32_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, aov_channels, naov, chans, nchan, (uint32_t*)out); break;
+	case AQH_DSPY_SIGNED32: display_kernel<int32_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, aov_channels, naov, chans, nchan, (int32_t*)out); break;
+	case AQH_DSPY_UNSIGNED16: display_kernel<uint16_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, aov_channels, naov, chans, nchan, (uint16_t*)out); break;
+	case AQH_DSPY_SIGNED16: display_kernel<int16_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, aov_channels, naov, chans, nchan, (int16_t*)out); break;
+	case AQH_DSPY_UNSIGNED8: display_kernel<uint8_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, aov_channels, naov, chans, nchan, (uint8_t*)out); break;
+	default: display_kernel<int8_t><<<nb, 256, 0, s>>>(fp, q, dither, channels, aov_channels, naov, chans, nchan, (int8_t*)out); break;
 	}
 }
 

@@ -210,9 +210,12 @@ constexpr int kCombineLocal = 24;  // lists up to this long are sorted in local 
 
 // CqImagePixel::Combine for a sample with transparent fragments
 // (imagepixel.cpp:155-301).  Returns the fragment count; writes the collapsed
-// sample into occl / occl_flags.
+// sample into occl / occl_flags, and into top_id the micropolygon of the
+// front entry, whose output variables the sample keeps (occl_id for the
+// occluding hit).
 __device__ inline int combine_fragments(const FrameParams& fp, const GridsDev& g, const FragPool& pool, int head,
-                                        bool has_occl, float occlZ, float occl[7], int& occl_flags) {
+                                        bool has_occl, float occlZ, float occl[7], int& occl_flags, int occl_id,
+                                        int& top_id) {
 	int n = 0;
 	bool nan = occl[6] != occl[6];
 	for (int f = head; f >= 0; f = pool.next[f]) {
@@ -285,6 +288,7 @@ __device__ inline int combine_fragments(const FrameParams& fp, const GridsDev& g
 #pragma unroll
 			for (int q = 0; q < 7; ++q) top[q] = dat[q];
 			top_flags = flg;
+			top_id = idx == -1 ? occl_id : __float_as_int(pool.frag[idx].y);
 		}
 	}
 	float depth = top[6];

@@ -322,8 +322,9 @@ __device__ __forceinline__ void mb_resolve(const FrameParams& fp, const GridsDev
 	}
 	int nf = 0;
 	bool valid = w >= 0;
+	int src = w;
 	if (TRANSP && head >= 0) {
-		nf = combine_fragments(fp, g, pool, head, w >= 0, ozv, occl, occl_flags);
+		nf = combine_fragments(fp, g, pool, head, w >= 0, ozv, occl, occl_flags, w, src);
 		valid = true;
 	}
 	if (nf == 0 && valid) {
@@ -333,6 +334,7 @@ __device__ __forceinline__ void mb_resolve(const FrameParams& fp, const GridsDev
 	}
 	st.a[aidx] = make_float4(occl[0], occl[1], occl[2], occl[6]);
 	st.b[aidx] = make_float4(occl[3], occl[4], occl[5], valid ? 1.0f : 0.0f);
+	if (st.aovsrc) st.aovsrc[aidx] = valid ? src : -1;
 	if (st.winner) st.winner[sidx] = w;
 	if (st.occlz) st.occlz[sidx] = ozv;
 	if (st.nfrag) st.nfrag[sidx] = nf;

@@ -116,6 +116,7 @@ class Grids:
     Ci: np.ndarray        # float32[NC, 4]
     Oi: np.ndarray        # float32[NC, 4]
     culled: Optional[np.ndarray] = None  # uint8[total micropolygons]
+    aov: Optional[np.ndarray] = None     # float32[NC, naov] output variables per vertex, indexed like Ci
 
     @property
     def ngrids(self) -> int:
@@ -308,6 +309,13 @@ def concat_grids(parts: list) -> Grids:
     return _pack(cu, cv, nkeys, flags, P, Ci, Oi, times, np.concatenate(tb))
 
 
+def with_aov(scene: Scene, naov: int = 3, seed: int = 0) -> Scene:
+    """The scene with `naov` seeded output variables per vertex, U[-1, 1)."""
+    rng = np.random.default_rng(seed)
+    aov = rng.uniform(-1.0, 1.0, (len(scene.grids.Ci), naov)).astype(np.float32)
+    return Scene(scene.frame, dataclasses.replace(scene.grids, aov=aov), scene.samples)
+
+
 def opaque_stream(width=1920, height=1080, ngrids=200_000, xs=4, ys=4, seed=0xC1,
                   npatterns=250, explicit_samples=False, filt=("gaussian", 2.0, 2.0)) -> Scene:
     """Opaque synthetic stream: 16x16-quad raster grids, Oi = 1, PixelSamples xs ys."""
@@ -464,7 +472,7 @@ def to_camera_space(scene: Scene, m=None, every: int = 1, **camera_kw) -> Scene:
 # ---------------------------------------------------------------------------
 # Scene files
 
-_GRID_KEYS = ("cu", "cv", "nkeys", "flags", "pbase", "cbase", "tbase", "times", "P", "Ci", "Oi", "culled")
+_GRID_KEYS = ("cu", "cv", "nkeys", "flags", "pbase", "cbase", "tbase", "times", "P", "Ci", "Oi", "culled", "aov")
 _SAMPLE_KEYS = ("pos", "time", "dof", "shuffle", "lod", "pos_index", "dof_index", "time_index",
                 "shuffle_index", "lod_index", "dither")
 

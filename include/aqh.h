@@ -126,6 +126,8 @@ typedef struct {
 	const float* Oi;             /* float4[(cu+1)*(cv+1)]: r, g, b, unused; NULL = opaque */
 	const uint8_t* culled;       /* cu*cv bytes, nonzero = culled micropolygon (m_CulledPolys); may be NULL */
 	int flags;                   /* AQH_GRID_* */
+	const float* aov;            /* float[(cu+1)*(cv+1)][n] output variables when aqh_set_aov_count(n > 0);
+	                                NULL = zeros */
 } aqh_grid;
 
 #define AQH_MAX_KEYS 4
@@ -312,6 +314,27 @@ aqh_status aqh_read_display(aqh_ctx* ctx, const aqh_display* d, void* out, size_
  * 7-float sample (R G B OR OG OB depth).  Any pointer may be NULL. */
 aqh_status aqh_read_samples(aqh_ctx* ctx, int32_t* winner, float* occlz, int32_t* nfrag,
                             uint8_t* valid, float* sdata, size_t nsamples);
+
+/* ---- arbitrary output variables ----------------------------------------------- */
+/* Extra float channels per vertex: the shader outputs a display asks for
+ * (CqRenderer's output data map).  Each stored hit carries its
+ * micropolygon's vertex-A values (CqBucketProcessor::StoreExtraData,
+ * bucketprocessor.cpp:1573-1643, GetIndex), Combine keeps the values of the
+ * front entry (imagepixel.cpp:253-262) and FilterBucket averages them with
+ * the same weights as Ci, 0 where a pixel has no valid sample
+ * (bucketprocessor.cpp:620-660).  n = 0..AQH_MAX_AOV floats, set after
+ * aqh_frame_begin and before any grid is submitted.  Unlike the reference,
+ * a grid without values contributes zeros rather than leaving earlier
+ * values in the sample. */
+#define AQH_MAX_AOV 16
+aqh_status aqh_set_aov_count(aqh_ctx* ctx, int n);
+/* Values for packed grids, float[vertices][n] indexed like Ci (cbase):
+ * host arrays (kept by the caller until aqh_render returns) or device. */
+aqh_status aqh_submit_aov_host(aqh_ctx* ctx, const float* aov, size_t nvertices);
+aqh_status aqh_submit_aov_device(aqh_ctx* ctx, const float* d_aov);
+/* The filtered output variables of the crop window: float[h][w][n].  In
+ * aqh_read_display, channel 9 + k is output variable k. */
+aqh_status aqh_read_aov(aqh_ctx* ctx, float* out, size_t out_floats);
 
 /* ---- micropolygon dump files ----------------------------------------------- */
 /* The files CqMPDump writes when Option "mpdump" "enabled" is set

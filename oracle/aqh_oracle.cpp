@@ -318,6 +318,17 @@ struct Frame {
 	int dofIdx(int px, int py, int i) { return dofIndex[((size_t)(py - y0) * w + (px - x0)) * ctx.spp + i]; }
 };
 
+// StoreExtraData (bucketprocessor.cpp:1573-1643): the output variables of
+// micropolygon `id`'s vertex A (GetIndex), found from the grids' micropolygon
+// counts.
+static const float* vertexAValues(const OrcGrids* g, const std::vector<int64_t>& mpStart, int id, int naov) {
+	const int gi = (int)(std::upper_bound(mpStart.begin(), mpStart.end(), (int64_t)id) - mpStart.begin()) - 1;
+	const int cu = g->cu[gi];
+	const int m = id - (int)mpStart[gi];
+	const int iv = m / cu, iu = m - iv * cu;
+	return g->aov + (g->cbase[gi] + (int64_t)iv * (cu + 1) + iu) * naov;
+}
+
 // micropolygon.cpp:1443-1462
 static void interpolateOutputs(const MP& mp, V2 uv, float col[3], float opa[3]) {
 	if (mp.smooth) {
@@ -1117,6 +1128,9 @@ extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples
 	}
 
 	// FilterBucket, non-separable path (bucketprocessor.cpp:584-664, 686-707)
+	const int naov = (g->aov && g->naov > 0) ? (g->naov < ORC_MAX_AOV ? g->naov : ORC_MAX_AOV) : 0;
+	std::vector<int64_t> mpStart((size_t)g->ngrids + 1, 0);
+	for (int gi = 0; gi < g->ngrids; ++gi) mpStart[gi + 1] = mpStart[gi] + (int64_t)g->cu[gi] * g->cv[gi];
 	const int dw = f->crop_xmax - f->crop_xmin, dh = f->crop_ymax - f->crop_ymin;
 	const int xmax = fr.ctx.shiftX, ymax = fr.ctx.shiftY;
 	const float xfwo2 = std::ceil(f->xfilter) * 0.5f;
@@ -1130,6 +1144,10 @@ extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples
 			float gTot = 0.0;
 			int SampleCount = 0;
 			float samples[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+			// output variables: the hit data past the nine standard floats
+			// (StoreExtraData writes vertex A's values, Combine keeps the front
+			// entry's), summed with the same weights
+			float extra[ORC_MAX_AOV] = {0};
 			for (int fy = -ymax; fy <= ymax; fy++) {
 				for (int fx = -xmax; fx <= xmax; fx++) {
 					int index = ((fy + ymax) * (2 * xmax + 1) + fx + xmax) * numSubPixels;
@@ -1147,6 +1165,10 @@ extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples
 									for (int k = 0; k < 7; ++k) samples[k] += sd.occl[k] * gw;
 									samples[7] += 0.0f * gw;
 									samples[8] += 0.0f * gw;
+									if (naov > 0 && sd.occlMp >= 0) {
+										const float* v = vertexAValues(g, mpStart, sd.occlMp, naov);
+										for (int k = 0; k < naov; ++k) extra[k] += v[k] * gw;
+									}
 									SampleCount++;
 								}
 							}
@@ -1175,6 +1197,11 @@ extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples
 			float a = (c[3] + c[4] + c[5]) / 3.0f;
 			c[6] = a * coverage;
 			c[8] = coverage;
+			if (naov > 0 && out->aov_channels) {
+				float* o = out->aov_channels + ((size_t)(y - f->crop_ymin) * dw + (x - f->crop_xmin)) * naov;
+				const float oneOverGTot = SampleCount ? (float)(1.0 / gTot) : 0.0f;
+				for (int k = 0; k < naov; ++k) o[k] = SampleCount ? extra[k] * oneOverGTot : 0.0f;
+			}
 		}
 	}
 	// ExposeBucket (bucketprocessor.cpp:766-806)

@@ -56,6 +56,8 @@ typedef struct {
 	int32_t display_z;                      /* DisplayMode includes DMode_Z */
 } OrcFrame;
 
+#define ORC_MAX_AOV 16
+
 typedef struct {
 	int32_t ngrids;
 	const int32_t* cu;        /* micropolygons along u, per grid */
@@ -70,6 +72,8 @@ typedef struct {
 	const float* Oi;          /* float4: r g b unused (NULL = opaque white) */
 	const int32_t* flags;     /* ORC_GRID_* */
 	const uint8_t* culled;    /* per micropolygon (global mp id) 1 = culled, or NULL */
+	const float* aov;         /* output variables float[vertex][naov] indexed like Ci, or NULL */
+	int32_t naov;
 } OrcGrids;
 
 typedef struct {
@@ -105,6 +109,8 @@ typedef struct {
 	int32_t nqchannels;
 	/* statistics */
 	int64_t spl_count, spl_bound_hits, spl_hits;
+	/* per display pixel: the filtered output variables (naov floats), or NULL */
+	float* aov_channels;
 } OrcOut;
 
 /* Weight table [(2*shiftY+1)*(2*shiftX+1)][spp] (bucketprocessor.cpp:811-856). */

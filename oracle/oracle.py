@@ -41,7 +41,8 @@ class OrcFrame(C.Structure):
 class OrcGrids(C.Structure):
     _fields_ = [("ngrids", C.c_int32), ("cu", _i32p), ("cv", _i32p), ("nkeys", _i32p),
                 ("pbase", _i64p), ("cbase", _i64p), ("tbase", _i64p), ("times", _f32p),
-                ("P", _f32p), ("Ci", _f32p), ("Oi", _f32p), ("flags", _i32p), ("culled", _u8p)]
+                ("P", _f32p), ("Ci", _f32p), ("Oi", _f32p), ("flags", _i32p), ("culled", _u8p),
+                ("aov", _f32p), ("naov", C.c_int32)]
 
 
 class OrcSamples(C.Structure):
@@ -56,7 +57,8 @@ class OrcOut(C.Structure):
     _fields_ = [("winner", _i32p), ("occlz", _f32p), ("nfrag", _i32p), ("valid", _u8p),
                 ("sdata", _f32p), ("channels", _f32p), ("quantized", _f64p),
                 ("qchannels", _i32p), ("nqchannels", C.c_int32),
-                ("spl_count", C.c_int64), ("spl_bound_hits", C.c_int64), ("spl_hits", C.c_int64)]
+                ("spl_count", C.c_int64), ("spl_bound_hits", C.c_int64), ("spl_hits", C.c_int64),
+                ("aov_channels", _f32p)]
 
 
 def build(quiet: bool = True) -> str:
@@ -170,6 +172,7 @@ def render(scene, qchannels=(0, 1, 2, 6), want_samples: bool = True) -> dict:
     """Run the oracle on a Scene (aqsis_gb300.scene).  Returns numpy arrays."""
     from aqsis_gb300.scene import FILTERS
     fr, g, s = scene.frame, projected_grids(scene), scene.samples
+    naov = 0 if getattr(g, "aov", None) is None else int(np.asarray(g.aov).reshape(len(g.Ci), -1).shape[1])
     cx0, cx1, cy0, cy1 = fr.crop_window
     x0, y0, w, h = fr.sample_region
     spp = fr.spp
@@ -194,7 +197,8 @@ def render(scene, qchannels=(0, 1, 2, 6), want_samples: bool = True) -> dict:
                   _p(arr(g.cbase, np.int64), _i64p), _p(tb, _i64p), _p(arr(g.times, np.float32), _f32p),
                   _p(arr(g.P, np.float32), _f32p), _p(arr(g.Ci, np.float32), _f32p),
                   _p(arr(g.Oi, np.float32), _f32p), _p(arr(g.flags, np.int32), _i32p),
-                  _p(arr(g.culled, np.uint8), _u8p))
+                  _p(arr(g.culled, np.uint8), _u8p), _p(arr(getattr(g, "aov", None), np.float32), _f32p),
+                  naov)
     os_ = OrcSamples(x0, y0, w, h, s.npatterns, _p(arr(s.pos, np.float32), _f32p),
                      _p(arr(s.time, np.float32), _f32p), _p(arr(s.dof, np.float32), _f32p),
                      _p(arr(s.shuffle, np.int32), _i32p), _p(arr(s.lod, np.float32), _f32p),
@@ -214,9 +218,11 @@ def render(scene, qchannels=(0, 1, 2, 6), want_samples: bool = True) -> dict:
     res["channels"] = np.zeros((dh, dw, 9), np.float32)
     qc = np.array(qchannels, np.int32)
     res["quantized"] = np.zeros((dh, dw, len(qc)), np.float64)
+    if naov:
+        res["aov"] = np.zeros((dh, dw, naov), np.float32)
     oo = OrcOut(_p(res.get("winner"), _i32p), _p(res.get("occlz"), _f32p), _p(res.get("nfrag"), _i32p),
                 _p(res.get("valid"), _u8p), _p(res.get("sdata"), _f32p), _p(res["channels"], _f32p),
-                _p(res["quantized"], _f64p), _p(qc, _i32p), len(qc), 0, 0, 0)
+                _p(res["quantized"], _f64p), _p(qc, _i32p), len(qc), 0, 0, 0, _p(res.get("aov"), _f32p))
     rc = lib().orc_render(C.byref(of), C.byref(og), C.byref(os_), _p(ftab, _f32p), C.byref(oo))
     if rc != 0:
         raise RuntimeError("oracle render failed: %d" % rc)

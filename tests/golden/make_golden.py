@@ -107,6 +107,9 @@ CASES = {
     "triangular_motion_dof": lambda: SS.triangular(SS.motion_dof_small(seed=10, xs=4, ys=4, scale=0.02), every=2),
     "camera_perspective": lambda: S.to_camera_space(SS.triangular_small(seed=12), every=2),
     "mpdump_replay": mpdump_scene,
+    "output_variables": lambda: S.with_aov(SS.transparent_edge(seed=14), 3, seed=14),
+    "output_variables_motion": lambda: S.with_aov(SS.motion_dof_small(seed=15, xs=3, ys=3, scale=0.015,
+                                                                      transparent=True), 2, seed=15),
     "camera_motion_ortho": lambda: S.to_camera_space(SS.motion_mixed_small(seed=13, scale=0.012), orthographic=True),
 }
 
@@ -114,7 +117,7 @@ CASES = {
 def render_case(scene):
     from oracle import oracle as O
     res = O.render(scene, QCH)
-    return {k: res[k] for k in OUT_KEYS}
+    return {k: res[k] for k in OUT_KEYS + ("aov",) if k in res}
 
 
 def main():
@@ -131,7 +134,7 @@ def main():
         if args.check:
             _, old = S.load_scene(path)
             same = all(np.array_equal(np.asarray(out[k]).view(np.uint8), old["o_" + k].view(np.uint8))
-                       for k in OUT_KEYS)
+                       for k in out)
             print("%-26s %s" % (name, "same" if same else "DIFFERS"))
             bad += not same
         else:

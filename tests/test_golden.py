@@ -18,14 +18,14 @@ OUT_KEYS = ("winner", "occlz", "nfrag", "valid", "channels", "quantized")
 
 
 def test_fixtures_present():
-    assert len(FIXTURES) >= 20
+    assert len(FIXTURES) >= 22
 
 
 @pytest.mark.parametrize("path", FIXTURES, ids=NAMES)
 def test_oracle_reproduces_fixture(oracle, path):
     sc, gold = S.load_scene(path)
     res = oracle.render(sc, tuple(int(c) for c in gold["qchannels"]))
-    for k in OUT_KEYS:
+    for k in OUT_KEYS + (("aov",) if "o_aov" in gold else ()):
         a, b = np.asarray(res[k]), gold["o_" + k]
         assert a.shape == b.shape, k
         assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), "%s differs" % k
@@ -68,11 +68,13 @@ def test_fixtures_cover_the_hider_features():
             feats.add("triangular")
         if (g.flags & S.GRID_CAMERA).any() and fr.camera_to_raster is not None:
             feats.add("camera_space")
+        if g.aov is not None and "o_aov" in gold:
+            feats.add("output_variables")
         feats.add("filter_" + fr.filter)
         assert gold["o_valid"].any()
     for f in ("motion", "dof", "transparent", "matte", "culled", "crop", "dither", "depth_filter_1",
               "depth_filter_2", "depth_filter_3", "filter_box", "filter_gaussian", "filter_catmull-rom", "triangular",
-              "camera_space"):
+              "camera_space", "output_variables"):
         assert f in feats, f
 
 
@@ -89,3 +91,6 @@ def test_device_matches_fixture(hider, path):
     assert ok.all(), "channels differ at %d entries" % int((~ok).sum())
     q = np.abs(res["quantized"].astype(np.int64) - gold["o_quantized"].astype(np.int64))
     assert q.max() <= 1
+    if "o_aov" in gold:
+        ok = close_or_same(res["aov"], gold["o_aov"])
+        assert ok.all(), "output variables differ at %d entries" % int((~ok).sum())
