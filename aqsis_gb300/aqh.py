@@ -85,6 +85,64 @@ class Display(C.Structure):
 DSPY_DTYPES = {1: np.float32, 2: np.uint32, 3: np.int32, 4: np.uint16, 5: np.int16, 6: np.uint8, 7: np.int8}
 
 
+class DspyGeometry(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("origin_x", C.c_int), ("origin_y", C.c_int),
+                ("full_width", C.c_int), ("full_height", C.c_int), ("bucket_x", C.c_int), ("bucket_y", C.c_int)]
+
+
+def capture_driver_path() -> str:
+    """The headless display driver built with the library (writes PPM / raw files)."""
+    import os
+    return os.path.join(os.path.dirname(_build.LIB), "libaqh_dspy_capture.so")
+
+
+def make_display(channels, one=255.0, qmin=0.0, qmax=255.0, dither_amp=0.5, zero=0.0, fmt=0, dither=None):
+    d = Display()
+    d.nchan = len(channels)
+    for i, c in enumerate(channels):
+        d.channels[i] = int(c)
+    d.q_zero, d.q_one, d.q_min, d.q_max, d.q_dither = zero, one, qmin, qmax, dither_amp
+    d.format = int(fmt)
+    keep = None
+    if dither is not None:
+        keep = np.ascontiguousarray(dither, np.float32).reshape(-1)
+        d.dither = keep.ctypes.data
+    return d, keep
+
+
+class DisplayDriver:
+    """A Dspy display driver fed by the library (aqh_dspy_open / _send / _close)."""
+
+    def __init__(self, driver: str, filename: str, geometry: DspyGeometry, channels, names, **quantize):
+        self.L = load()
+        self.d, self._keep = make_display(channels, **quantize)
+        arr = (C.c_char_p * len(names))(*[n.encode() for n in names])
+        self._names = arr
+        self.h = C.c_void_p()
+        rc = self.L.aqh_dspy_open(driver.encode(), filename.encode(), C.byref(geometry), C.byref(self.d), arr,
+                                  C.byref(self.h))
+        if rc != AQH_OK:
+            raise AqhError(rc, "aqh_dspy_open: " + self.L.aqh_dspy_last_error().decode())
+
+    def send(self, hider):
+        rc = self.L.aqh_dspy_send(self.h, hider.ctx)
+        if rc != AQH_OK:
+            raise AqhError(rc, "aqh_dspy_send: " + self.L.aqh_dspy_last_error().decode())
+
+    def send_image(self, image: np.ndarray):
+        image = np.ascontiguousarray(image)
+        rc = self.L.aqh_dspy_send_image(self.h, image.ctypes.data, image.nbytes)
+        if rc != AQH_OK:
+            raise AqhError(rc, "aqh_dspy_send_image: " + self.L.aqh_dspy_last_error().decode())
+
+    def close(self):
+        if self.h:
+            rc = self.L.aqh_dspy_close(self.h)
+            self.h = C.c_void_p()
+            if rc != AQH_OK:
+                raise AqhError(rc, "aqh_dspy_close: " + self.L.aqh_dspy_last_error().decode())
+
+
 class DeviceOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("vertex_capacity", C.c_size_t), ("grid_capacity", C.c_size_t)]
 
@@ -133,6 +191,13 @@ def load(build_if_missing: bool = False):
     L.aqh_get_stats.argtypes = [vp, C.POINTER(FrameStats)]
     L.aqh_set_camera_to_raster.argtypes = [vp, _f32p]
     L.aqh_set_aov_count.argtypes = [vp, C.c_int]
+    L.aqh_dspy_geometry_of.argtypes = [vp, C.POINTER(DspyGeometry)]
+    L.aqh_dspy_open.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(DspyGeometry), C.POINTER(Display),
+                                C.POINTER(C.c_char_p), C.POINTER(vp)]
+    L.aqh_dspy_send.argtypes = [vp, vp]
+    L.aqh_dspy_send_image.argtypes = [vp, vp, C.c_size_t]
+    L.aqh_dspy_close.argtypes = [vp]
+    L.aqh_dspy_last_error.restype = C.c_char_p
     L.aqh_submit_aov_host.argtypes = [vp, _f32p, C.c_size_t]
     L.aqh_submit_aov_device.argtypes = [vp, vp]
     L.aqh_read_aov.argtypes = [vp, _f32p, C.c_size_t]
@@ -149,7 +214,8 @@ def load(build_if_missing: bool = False):
                  "aqh_render", "aqh_synchronize", "aqh_read_channels", "aqh_read_bucket", "aqh_read_quantized_u8",
                  "aqh_read_samples", "aqh_get_stats", "aqh_test_invbilinear", "aqh_set_tuning", "aqh_get_tuning",
                  "aqh_autotune", "aqh_set_camera_to_raster", "aqh_read_display", "aqh_set_aov_count",
-                 "aqh_submit_aov_host", "aqh_submit_aov_device", "aqh_read_aov"):
+                 "aqh_submit_aov_host", "aqh_submit_aov_device", "aqh_read_aov", "aqh_dspy_geometry_of",
+                 "aqh_dspy_open", "aqh_dspy_send", "aqh_dspy_send_image", "aqh_dspy_close"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -404,6 +470,11 @@ class Hider:
         self._check(self.L.aqh_read_quantized_u8(self.ctx, _p(ch, _i32p), len(ch), _p(out, _u8p), out.size),
                     "aqh_read_quantized_u8")
         return out
+
+    def dspy_geometry(self) -> DspyGeometry:
+        g = DspyGeometry()
+        self._check(self.L.aqh_dspy_geometry_of(self.ctx, C.byref(g)), "aqh_dspy_geometry_of")
+        return g
 
     def read_display(self, channels=(0, 1, 2, 6), one=255.0, qmin=0.0, qmax=255.0, dither_amp=0.5, zero=0.0,
                      fmt=0, dither=None) -> np.ndarray:

@@ -17,7 +17,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libaqh.so")
-SOURCES = ["api.cu", "bin.cu", "sample.cu", "sample_mb.cu", "filter.cu", "noalloc.cu", "server.cu", "mpdump.cpp"]
+SOURCES = ["api.cu", "bin.cu", "sample.cu", "sample_mb.cu", "filter.cu", "noalloc.cu", "server.cu", "mpdump.cpp",
+           "dspy_host.cpp"]
+# display drivers built as their own libraries
+DRIVERS = {"dspy_capture.cpp": os.path.join(OUT, "libaqh_dspy_capture.so")}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
               "-Xptxas", "-v"]
@@ -40,7 +43,7 @@ def _compile(src: str, verbose: bool) -> tuple:
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     deps = [os.path.join(SRC, f) for f in os.listdir(SRC)] + [os.path.join(HERE, "..", "include", "aqh.h")]
-    if not force and os.path.exists(LIB):
+    if not force and os.path.exists(LIB) and all(os.path.exists(lib) for lib in DRIVERS.values()):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in deps):
             return LIB
@@ -54,10 +57,15 @@ def build(verbose: bool = False, force: bool = False) -> str:
     with open(os.path.join(OUT, "ptxas.log"), "w") as f:
         f.write("\n".join(logs))
     objs = [r[1] for r in results]
-    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lpthread"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lpthread", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    for src, lib in DRIVERS.items():
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fvisibility=hidden", os.path.join(SRC, src), "-o", lib]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("display driver build failed:\n" + r.stdout + r.stderr)
     if verbose:
         print("\n".join(logs))
     return LIB

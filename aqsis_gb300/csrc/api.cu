@@ -1248,6 +1248,21 @@ aqh_status aqh_synchronize(aqh_ctx* ctx) {
 	return AQH_OK;
 }
 
+aqh_status aqh_dspy_geometry_of(aqh_ctx* ctx, aqh_dspy_geometry* g) {
+	if (!ctx || !g) return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	const FrameParams& fp = ctx->fp;
+	g->width = fp.crop_x1 - fp.crop_x0;
+	g->height = fp.crop_y1 - fp.crop_y0;
+	g->origin_x = fp.crop_x0;
+	g->origin_y = fp.crop_y0;
+	g->full_width = ctx->desc.width;
+	g->full_height = ctx->desc.height;
+	g->bucket_x = ctx->desc.bucket_x > 0 ? ctx->desc.bucket_x : 16;
+	g->bucket_y = ctx->desc.bucket_y > 0 ? ctx->desc.bucket_y : 16;
+	return AQH_OK;
+}
+
 aqh_status aqh_set_aov_count(aqh_ctx* ctx, int n) {
 	if (!ctx) return AQH_EINVAL;
 	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");

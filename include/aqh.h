@@ -336,6 +336,35 @@ aqh_status aqh_submit_aov_device(aqh_ctx* ctx, const float* d_aov);
  * aqh_read_display, channel 9 + k is output variable k. */
 aqh_status aqh_read_aov(aqh_ctx* ctx, float* out, size_t out_floats);
 
+/* ---- display drivers ------------------------------------------------------------ */
+/* A frame sent to a RenderMan display driver library (the Dspy plugin ABI:
+ * DspyImageOpen / DspyImageData / DspyImageClose), as CqDDManager and
+ * CqDisplayRequest do (ddmanager.cpp:560-640, 930-952, 984-1176): the
+ * driver gets the crop window's size, one format per channel of the request
+ * (the request's element type) and the "origin" / "OriginalSize"
+ * parameters; if it reorders the formats the host follows by channel name;
+ * data go out bucket by bucket in row order, or a scanline at a time when the
+ * driver sets PkDspyFlagsWantsScanLineOrder.  Host-only apart from
+ * aqh_dspy_send, which reads the request from a rendered context.  The
+ * library also builds a capture driver (libaqh_dspy_capture.so) that writes
+ * PPM files. */
+typedef struct {
+	int width, height;            /* the image the driver receives: the crop window */
+	int origin_x, origin_y;       /* the crop window's origin in the full image */
+	int full_width, full_height;  /* the full resolution */
+	int bucket_x, bucket_y;       /* bucket size of bucket-order delivery */
+} aqh_dspy_geometry;
+typedef struct aqh_dspy aqh_dspy;
+aqh_status aqh_dspy_geometry_of(aqh_ctx* ctx, aqh_dspy_geometry* g);
+aqh_status aqh_dspy_open(const char* driver_path, const char* filename, const aqh_dspy_geometry* g,
+                         const aqh_display* d, const char* const* channel_names, aqh_dspy** out);
+/* The request's channels of the context's last render (aqh_read_display). */
+aqh_status aqh_dspy_send(aqh_dspy* dd, aqh_ctx* ctx);
+/* A host image in the request's channel order, width x height x nchan elements. */
+aqh_status aqh_dspy_send_image(aqh_dspy* dd, const void* image, size_t bytes);
+aqh_status aqh_dspy_close(aqh_dspy* dd);
+const char* aqh_dspy_last_error(void);
+
 /* ---- micropolygon dump files ----------------------------------------------- */
 /* The files CqMPDump writes when Option "mpdump" "enabled" is set
  * (libs/core/mpdump.cpp:40-210; records dumped by CqImageBuffer::AddMPG,

@@ -64,3 +64,18 @@ def test_u8_request_equals_fused_quantize(hider):
     f = sc.frame
     got = hider.read_display((0, 1, 2, 6), one=f.q_one, qmin=f.q_min, qmax=f.q_max, dither_amp=f.q_dither)
     assert np.array_equal(got, res["quantized"])
+
+
+def test_rendered_frame_to_capture_driver(hider, tmp_path):
+    """aqh_dspy_send: the request read from the device and delivered to the
+    capture driver in buckets equals the fused 8-bit quantize."""
+    from tests.test_dspy import read_ppm
+    sc = SS.opaque_small(seed=53, scale=0.03)
+    res = hider.render_scene(sc, samples=False)
+    path = str(tmp_path / "frame.ppm")
+    f = sc.frame
+    dd = A.DisplayDriver(A.capture_driver_path(), path, hider.dspy_geometry(), (6, 0, 1, 2), ["a", "r", "g", "b"],
+                         one=f.q_one, qmin=f.q_min, qmax=f.q_max, dither_amp=f.q_dither)
+    dd.send(hider)
+    dd.close()
+    assert np.array_equal(read_ppm(path), res["quantized"][..., :3])
