@@ -361,6 +361,8 @@ struct aqh_ctx {
 	DevBuf d_sa, d_sb, d_win, d_oz, d_nf, d_hz, d_keys, d_wmask;
 	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err, d_occl;
 	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb, d_disp, d_dither_req;
+	DevBuf d_q8_req;          // quantized reads with other channel lists
+	bool q8_default = false;  // d_q8 holds the last frame's r g b a display
 	bool dev_motion = false;
 	DevBuf d_queue, d_slices;
 	std::vector<float4> h_dofb;
@@ -1043,13 +1045,12 @@ static aqh_status enqueue_frame(aqh_ctx* ctx, RenderPlan& P, bool batched, bool 
 	}
 	AQH_TRY(cudaGetLastError(), "sample kernel launch");
 	if (timing) mark(ctx->ev[2]);
-	launch_filter(fp, ctx->smp, P.store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(), s);
+	// the frame's r g b a display is quantized in the filter pass when it fits 8 bits
+	const bool fuse_q8 = fp.q_one == 0.0f || (fp.q_min >= 0.0f && fp.q_max <= 255.0f);
+	launch_filter(fp, ctx->smp, P.store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(),
+	              fuse_q8 ? ctx->d_q8.as<uint8_t>() : nullptr, s);
+	ctx->q8_default = fuse_q8;
 	if (P.g.naov > 0) launch_filter_aov(fp, ctx->smp, P.store, P.g, ctx->d_ftab.as<float>(), ctx->d_aovchan.as<float>(), s);
-	if (fp.q_one == 0.0f || (fp.q_min >= 0.0f && fp.q_max <= 255.0f)) {
-		AQH_TRY(cudaMemcpyAsync(ctx->d_qchan.p, kDefaultDisplay, sizeof kDefaultDisplay, cudaMemcpyHostToDevice, s),
-		        "upload display channels");
-		launch_quantize_u8(fp, ctx->smp, ctx->d_chan.as<float>(), ctx->d_qchan.as<int>(), 4, ctx->d_q8.as<uint8_t>(), s);
-	}
 	AQH_TRY(cudaGetLastError(), "filter kernel launch");
 	if (timing) mark(ctx->ev[3]);
 	return AQH_OK;
@@ -1124,13 +1125,12 @@ static aqh_status render_plain(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 		ctx->graph_valid = false;
 	}
 	cudaEventRecord(ctx->ev[2], s);
-	launch_filter(fp, ctx->smp, P.store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(), s);
+	// the frame's r g b a display is quantized in the filter pass when it fits 8 bits
+	const bool fuse_q8 = fp.q_one == 0.0f || (fp.q_min >= 0.0f && fp.q_max <= 255.0f);
+	launch_filter(fp, ctx->smp, P.store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(),
+	              fuse_q8 ? ctx->d_q8.as<uint8_t>() : nullptr, s);
+	ctx->q8_default = fuse_q8;
 	if (P.g.naov > 0) launch_filter_aov(fp, ctx->smp, P.store, P.g, ctx->d_ftab.as<float>(), ctx->d_aovchan.as<float>(), s);
-	if (fp.q_one == 0.0f || (fp.q_min >= 0.0f && fp.q_max <= 255.0f)) {
-		AQH_TRY(cudaMemcpyAsync(ctx->d_qchan.p, kDefaultDisplay, sizeof kDefaultDisplay, cudaMemcpyHostToDevice, s),
-		        "upload display channels");
-		launch_quantize_u8(fp, ctx->smp, ctx->d_chan.as<float>(), ctx->d_qchan.as<int>(), 4, ctx->d_q8.as<uint8_t>(), s);
-	}
 	AQH_TRY(cudaGetLastError(), "filter kernel launch");
 	cudaEventRecord(ctx->ev[3], s);
 	ctx->stats.tile_grid_pairs = total;
@@ -1454,14 +1454,22 @@ aqh_status aqh_read_quantized_u8(aqh_ctx* ctx, const int* channels, int nchan, u
 	for (int c = 0; c < nchan; ++c)
 		if (channels[c] < 0 || channels[c] >= AQH_NCHANNELS) return ctx->fail(AQH_EINVAL, "bad channel %d", channels[c]);
 	cudaSetDevice(ctx->device);
+	const bool rgba = nchan == 4 && channels[0] == kDefaultDisplay[0] && channels[1] == kDefaultDisplay[1] &&
+	                  channels[2] == kDefaultDisplay[2] && channels[3] == kDefaultDisplay[3];
+	if (rgba && ctx->q8_default) {
+		// quantized by the frame's filter pass already
+		AQH_TRY(cudaMemcpyAsync(out, ctx->d_q8.p, npix * 4, cudaMemcpyDeviceToHost, ctx->stream), "read quantized");
+		AQH_TRY(cudaStreamSynchronize(ctx->stream), "read quantized");
+		return AQH_OK;
+	}
 	AQH_TRY(ctx->d_qchan.ensure(64), "alloc");
-	AQH_TRY(ctx->d_q8.ensure(npix * nchan), "alloc");
+	AQH_TRY(ctx->d_q8_req.ensure(npix * nchan), "alloc");
 	AQH_TRY(cudaMemcpyAsync(ctx->d_qchan.p, channels, nchan * 4, cudaMemcpyHostToDevice, ctx->stream), "upload");
 	cudaGetLastError();
-	launch_quantize_u8(fp, ctx->smp, ctx->d_chan.as<float>(), ctx->d_qchan.as<int>(), nchan, ctx->d_q8.as<uint8_t>(),
-	                   ctx->stream);
+	launch_quantize_u8(fp, ctx->smp, ctx->d_chan.as<float>(), ctx->d_qchan.as<int>(), nchan,
+	                   ctx->d_q8_req.as<uint8_t>(), ctx->stream);
 	AQH_TRY(cudaGetLastError(), "quantize launch");
-	AQH_TRY(cudaMemcpyAsync(out, ctx->d_q8.p, npix * nchan, cudaMemcpyDeviceToHost, ctx->stream), "read quantized");
+	AQH_TRY(cudaMemcpyAsync(out, ctx->d_q8_req.p, npix * nchan, cudaMemcpyDeviceToHost, ctx->stream), "read quantized");
 	AQH_TRY(cudaStreamSynchronize(ctx->stream), "read quantized");
 	return AQH_OK;
 }

@@ -208,8 +208,10 @@ aqh_status resolve_frame(const aqh_frame_desc& d, FrameParams& fp, std::vector<f
 // (0: 128 pixels).  Neither changes any result.
 void set_tiling(FrameParams& fp, int tile_pixels = 0, int supertile_px = 0);
 void dof_bounds_h(int xs, int ys, std::vector<float4>& out);
+// `q8` (may be null): the frame's r g b a display quantized to 8 bits,
+// written in the same pass (the quantize of quantize_u8 with channels 0 1 2 6).
 void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStore& st, const float* ftab,
-                   float* channels, cudaStream_t s);
+                   float* channels, uint8_t* q8, cudaStream_t s);
 // Output variables of the crop window, float[pixel][g.naov], filtered like Ci.
 void launch_filter_aov(const FrameParams& fp, const SamplerDev& sm, const SampleStore& st, const GridsDev& g,
                        const float* ftab, float* aov_channels, cudaStream_t s);

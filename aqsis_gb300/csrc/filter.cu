@@ -17,12 +17,21 @@ namespace aqh {
 
 namespace {
 
+// aqsis lround (math.h:67-70) in double: lfloor(x - 0.5) + 1
+__device__ __forceinline__ double lround_d(double x) {
+	const double y = x - 0.5;
+	long long i = (long long)y;
+	i -= (y < 0.0 && y != (double)i) ? 1 : 0;
+	return (double)(i + 1);
+}
+
 // One display pixel (x, y).  SPP > 0: samples per pixel known at compile
 // time (the sample loop is unrolled by four so its loads issue together); 0:
 // read from fp.
 template <int SPP>
 __device__ __forceinline__ void filter_pixel(const FrameParams& fp, const SamplerDev& smp, const SampleStore& st,
-                                             const float* __restrict__ ftab, float* __restrict__ chan, int x, int y) {
+                                             const float* __restrict__ ftab, float* __restrict__ chan,
+                                             uint8_t* __restrict__ q8, int x, int y) {
 	const float xcent = x + 0.5f, ycent = y + 0.5f;
 	const int xmax = fp.shiftX, ymax = fp.shiftY;
 	const int spp = SPP > 0 ? SPP : fp.spp;
@@ -114,9 +123,27 @@ __device__ __forceinline__ void filter_pixel(const FrameParams& fp, const Sample
 			c[2] = (float)pow((double)c[2], (double)oneovergamma);
 		}
 	}
-	float* out = chan + ((long long)(y - fp.crop_y0) * (fp.crop_x1 - fp.crop_x0) + (x - fp.crop_x0)) * 9;
+	const long long p = (long long)(y - fp.crop_y0) * (fp.crop_x1 - fp.crop_x0) + (x - fp.crop_x0);
+	float* out = chan + p * 9;
 #pragma unroll
 	for (int k = 0; k < 9; ++k) out[k] = c[k];
+	if (q8) {
+		// the frame's own display, r g b a, quantized as quantize_u8_kernel does
+		const double s = smp.dither ? (double)__ldg(smp.dither + p) : 0.0;
+		const float src[4] = {c[0], c[1], c[2], c[6]};
+		uchar4 q;
+		unsigned char* qb = reinterpret_cast<unsigned char*>(&q);
+#pragma unroll
+		for (int k = 0; k < 4; ++k) {
+			double value = src[k];
+			if (fp.q_one != 0.0f) {
+				value = lround_d(0.0 + value * (double)(fp.q_one - 0.0f) + ((double)fp.q_dither * s));
+				value = value < (double)fp.q_min ? (double)fp.q_min : (value > (double)fp.q_max ? (double)fp.q_max : value);
+			}
+			qb[k] = (uint8_t)(int)value;
+		}
+		reinterpret_cast<uchar4*>(q8)[p] = q;
+	}
 }
 
 // 16x16-pixel tiles of the crop window in raster order, `gridDim.x` of them
@@ -124,12 +151,12 @@ __device__ __forceinline__ void filter_pixel(const FrameParams& fp, const Sample
 template <int SPP>
 __global__ void __launch_bounds__(256)
 filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __restrict__ ftab,
-              float* __restrict__ chan) {
+              float* __restrict__ chan, uint8_t* __restrict__ q8) {
 	const int ntx = (fp.crop_x1 - fp.crop_x0 + 15) >> 4, nty = (fp.crop_y1 - fp.crop_y0 + 15) >> 4;
 	for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
 		const int x = fp.crop_x0 + (tile % ntx) * 16 + (threadIdx.x & 15);
 		const int y = fp.crop_y0 + (tile / ntx) * 16 + (threadIdx.x >> 4);
-		if (x < fp.crop_x1 && y < fp.crop_y1) filter_pixel<SPP>(fp, smp, st, ftab, chan, x, y);
+		if (x < fp.crop_x1 && y < fp.crop_y1) filter_pixel<SPP>(fp, smp, st, ftab, chan, q8, x, y);
 	}
 }
 
@@ -200,13 +227,6 @@ filter_aov_kernel(FrameParams fp, SamplerDev smp, SampleStore st, GridsDev g, co
 	}
 }
 
-// aqsis lround (math.h:67-70) in double: lfloor(x - 0.5) + 1
-__device__ __forceinline__ double lround_d(double x) {
-	const double y = x - 0.5;
-	long long i = (long long)y;
-	i -= (y < 0.0 && y != (double)i) ? 1 : 0;
-	return (double)(i + 1);
-}
 
 __global__ void quantize_u8_kernel(FrameParams fp, SamplerDev smp, const float* __restrict__ chan,
                                    const int* __restrict__ chans, int nchan, uint8_t* __restrict__ out) {
@@ -274,7 +294,7 @@ __global__ void test_invbilinear_kernel(const float* q, const float2* P, int n, 
 }  // namespace
 
 void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStore& st, const float* ftab,
-                   float* channels, cudaStream_t s) {
+                   float* channels, uint8_t* q8, cudaStream_t s) {
 	const int w = fp.crop_x1 - fp.crop_x0, h = fp.crop_y1 - fp.crop_y0;
 	if (w <= 0 || h <= 0) return;
 	const int ntiles = ((w + 15) / 16) * ((h + 15) / 16);
@@ -287,11 +307,11 @@ void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStor
 	const int per_sm = fp.filter_ctas > 0 ? std::min(fp.filter_ctas, 8) : 8;
 	const int grid = std::max(1, std::min(ntiles, nsm * per_sm));
 	switch (fp.spp) {
-	case 4: filter_kernel<4><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels); break;
-	case 16: filter_kernel<16><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels); break;
-	case 36: filter_kernel<36><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels); break;
-	case 64: filter_kernel<64><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels); break;
-	default: filter_kernel<0><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels); break;
+	case 4: filter_kernel<4><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels, q8); break;
+	case 16: filter_kernel<16><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels, q8); break;
+	case 36: filter_kernel<36><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels, q8); break;
+	case 64: filter_kernel<64><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels, q8); break;
+	default: filter_kernel<0><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels, q8); break;
 	}
 }
 

@@ -242,7 +242,7 @@ extern "C" aqh_status aqh_render_noalloc(const aqh_frame_desc* desc, const float
 		e = cudaMemsetAsync(bb.st_offset, 0, sizeof(int32_t) * ((size_t)nst * bb.nranges + 1), s);
 	}
 	launch_sample_tiles(fp, g, smp, bb, store, pool, nullptr, s);
-	launch_filter(fp, smp, store, a.ftab, d_channels, s);
+	launch_filter(fp, smp, store, a.ftab, d_channels, nullptr, s);
 	if (e == cudaSuccess) e = cudaGetLastError();
 	if (e != cudaSuccess) return na_fail(err, err_len, AQH_EDEVICE, cudaGetErrorString(e));
 	return AQH_OK;
