@@ -373,16 +373,18 @@ class Hider:
                              kt, cl, None if aov is None else aov[cb:cb + nv])
             mpbase += cu * cv
 
-    def submit_grids_host(self, g):
+    def submit_grids_host(self, g, packed3: bool = False):
         """Submit a whole packed scene.Grids in one aqh_submit_grids_host call
         (the arrays are copied to the device at render time, so they must stay
-        alive until then; they are kept on the object)."""
+        alive until then; they are kept on the object).  packed3: P, Ci and Oi
+        as three-float entries (aqh_submit_grids_host3)."""
         L = self.L
         if not getattr(L, "_packed_bound", False):
             vp = C.c_void_p
-            L.aqh_submit_grids_host.argtypes = [vp, C.c_int] + [vp] * 8 + [C.c_size_t, vp, C.c_size_t, vp, vp,
-                                                                         C.c_size_t, vp, C.c_int64]
-            L.aqh_submit_grids_host.restype = C.c_int
+            for fn in (L.aqh_submit_grids_host, L.aqh_submit_grids_host3):
+                fn.argtypes = [vp, C.c_int] + [vp] * 8 + [C.c_size_t, vp, C.c_size_t, vp, vp, C.c_size_t, vp,
+                                                          C.c_int64]
+                fn.restype = C.c_int
             L._packed_bound = True
         keep = []
 
@@ -395,13 +397,15 @@ class Hider:
         if getattr(g, "aov", None) is not None:
             av = np.ascontiguousarray(np.asarray(g.aov, np.float32).reshape(len(g.Ci), -1))
             self.set_aov_count(av.shape[1])
-        self._check(L.aqh_submit_grids_host(self.ctx, g.ngrids, a(g.cu, np.int32), a(g.cv, np.int32),
-                                            a(g.nkeys, np.int32), a(g.flags, np.int32), a(g.pbase, np.int64),
-                                            a(g.cbase, np.int64), a(g.tbase, np.int32), a(g.times, np.float32),
-                                            int(g.times.size), a(g.P, np.float32), int(g.P.shape[0]),
-                                            a(g.Ci, np.float32), a(g.Oi, np.float32), int(g.Ci.shape[0]), culled,
-                                            g.micropolygons),
-                    "aqh_submit_grids_host")
+        fn = L.aqh_submit_grids_host3 if packed3 else L.aqh_submit_grids_host
+        k = 3 if packed3 else 4
+        self._check(fn(self.ctx, g.ngrids, a(g.cu, np.int32), a(g.cv, np.int32),
+                       a(g.nkeys, np.int32), a(g.flags, np.int32), a(g.pbase, np.int64),
+                       a(g.cbase, np.int64), a(g.tbase, np.int32), a(g.times, np.float32),
+                       int(g.times.size), a(np.asarray(g.P)[:, :k], np.float32), int(g.P.shape[0]),
+                       a(np.asarray(g.Ci)[:, :k], np.float32), a(np.asarray(g.Oi)[:, :k], np.float32),
+                       int(g.Ci.shape[0]), culled, g.micropolygons),
+                    "aqh_submit_grids_host3" if packed3 else "aqh_submit_grids_host")
         if av is not None:
             self._check(L.aqh_submit_aov_host(self.ctx, _p(av, _f32p), av.shape[0]), "aqh_submit_aov_host")
             keep.append(av)

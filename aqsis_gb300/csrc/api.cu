@@ -347,6 +347,7 @@ struct aqh_ctx {
 		const float *times, *P, *Ci, *Oi;
 		const uint8_t* culled;
 		size_t ntimes, nP, nC;
+		int comps;  // floats per P / Ci / Oi entry in the host arrays: 4, or 3 (CqVector3D / CqColor)
 	} hp{};
 	cudaStream_t own_stream = nullptr;
 	// device-submitted grids (caller-owned)
@@ -362,6 +363,7 @@ struct aqh_ctx {
 	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err, d_occl;
 	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb, d_disp, d_dither_req;
 	DevBuf d_q8_req;          // quantized reads with other channel lists
+	DevBuf d_P3, d_C3, d_O3;  // three-float host entries before widening
 	bool q8_default = false;  // d_q8 holds the last frame's r g b a display
 	bool dev_motion = false;
 	DevBuf d_queue, d_slices;
@@ -654,6 +656,17 @@ __global__ void widen_kernel(int n, const int32_t* in, int64_t* out) {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i <= n) out[i] = in[i];
 }
+// Packed three-float host entries (P, Ci, Oi as CqVector3D / CqColor) to
+// the float4 device layout.
+__global__ void widen3_kernel(const float* __restrict__ in, float4* __restrict__ out, long long n) {
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+		out[i] = make_float4(in[3 * i], in[3 * i + 1], in[3 * i + 2], 0.0f);
+}
+void launch_widen3(const float* in, float4* out, size_t n, cudaStream_t s) {
+	if (n == 0) return;
+	const long long blocks = std::min<long long>(((long long)n + 255) / 256, 152LL * 16);
+	widen3_kernel<<<(unsigned)blocks, 256, 0, s>>>(in, out, (long long)n);
+}
 __global__ void any_transparent_kernel(int n, const int32_t* flags, const int32_t* nkeys, int32_t* out) {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < n && !(flags[i] & AQH_GRID_OPAQUE)) out[0] = 1;
@@ -680,11 +693,11 @@ void aqh_host_free(void* p) {
 	if (p) cudaFreeHost(p);
 }
 
-aqh_status aqh_submit_grids_host(aqh_ctx* ctx, int ngrids, const int32_t* cu, const int32_t* cv,
-                                 const int32_t* nkeys, const int32_t* flags, const int64_t* pbase,
-                                 const int64_t* cbase, const int32_t* tbase, const float* times, size_t ntimes,
-                                 const float* P, size_t nP, const float* Ci, const float* Oi, size_t nC,
-                                 const uint8_t* culled, int64_t total_mps) {
+static aqh_status submit_grids_host(aqh_ctx* ctx, int comps, int ngrids, const int32_t* cu, const int32_t* cv,
+                                    const int32_t* nkeys, const int32_t* flags, const int64_t* pbase,
+                                    const int64_t* cbase, const int32_t* tbase, const float* times, size_t ntimes,
+                                    const float* P, size_t nP, const float* Ci, const float* Oi, size_t nC,
+                                    const uint8_t* culled, int64_t total_mps) {
 	if (!ctx || ngrids < 0 || !cu || !cv || !nkeys || !flags || !pbase || !cbase || !tbase || !P) return AQH_EINVAL;
 	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
 	if (!ctx->h_cu.empty() || ctx->dev_grids || ctx->host_packed) return ctx->fail(AQH_EINVAL, "frame already holds grids");
@@ -708,6 +721,7 @@ aqh_status aqh_submit_grids_host(aqh_ctx* ctx, int ngrids, const int32_t* cu, co
 	ctx->hp.cu = cu; ctx->hp.cv = cv; ctx->hp.nkeys = nkeys; ctx->hp.flags = flags; ctx->hp.tbase = tbase;
 	ctx->hp.pbase = pbase; ctx->hp.cbase = cbase; ctx->hp.times = times; ctx->hp.ntimes = ntimes;
 	ctx->hp.P = P; ctx->hp.nP = nP; ctx->hp.Ci = Ci; ctx->hp.Oi = Oi; ctx->hp.nC = nC;
+	ctx->hp.comps = comps;
 	ctx->hp.culled = culled;
 	ctx->h_mpbase.resize(ngrids);
 	int64_t acc = 0;
@@ -716,6 +730,24 @@ aqh_status aqh_submit_grids_host(aqh_ctx* ctx, int ngrids, const int32_t* cu, co
 	ctx->any_transparent = transp && Oi;
 	ctx->host_packed = true;
 	return AQH_OK;
+}
+
+aqh_status aqh_submit_grids_host(aqh_ctx* ctx, int ngrids, const int32_t* cu, const int32_t* cv,
+                                 const int32_t* nkeys, const int32_t* flags, const int64_t* pbase,
+                                 const int64_t* cbase, const int32_t* tbase, const float* times, size_t ntimes,
+                                 const float* P, size_t nP, const float* Ci, const float* Oi, size_t nC,
+                                 const uint8_t* culled, int64_t total_mps) {
+	return submit_grids_host(ctx, 4, ngrids, cu, cv, nkeys, flags, pbase, cbase, tbase, times, ntimes, P, nP, Ci, Oi,
+	                         nC, culled, total_mps);
+}
+
+aqh_status aqh_submit_grids_host3(aqh_ctx* ctx, int ngrids, const int32_t* cu, const int32_t* cv,
+                                  const int32_t* nkeys, const int32_t* flags, const int64_t* pbase,
+                                  const int64_t* cbase, const int32_t* tbase, const float* times, size_t ntimes,
+                                  const float* P, size_t nP, const float* Ci, const float* Oi, size_t nC,
+                                  const uint8_t* culled, int64_t total_mps) {
+	return submit_grids_host(ctx, 3, ngrids, cu, cv, nkeys, flags, pbase, cbase, tbase, times, ntimes, P, nP, Ci, Oi,
+	                         nC, culled, total_mps);
 }
 
 aqh_status aqh_submit_grids_device(aqh_ctx* ctx, int ngrids, const int32_t* d_cu, const int32_t* d_cv,
@@ -780,17 +812,34 @@ static aqh_status upload_packed_grids(aqh_ctx* ctx) {
 	AQH_TRY(up(ctx->d_cbase, hp.cbase, G * 8), "upload grids");
 	AQH_TRY(up(ctx->d_mpbase, ctx->h_mpbase.data(), G * 8), "upload grids");
 	AQH_TRY(up(ctx->d_times, hp.times, std::max<size_t>(hp.ntimes, 1) * 4), "upload grids");
-	AQH_TRY(up(ctx->d_P, hp.P, hp.nP * 16), "upload P");
+	const bool packed3 = hp.comps == 3;
+	if (packed3) {
+		// three-float entries go up as they are and are widened on the device
+		AQH_TRY(up(ctx->d_P3, hp.P, hp.nP * 12), "upload P");
+		AQH_TRY(ctx->d_P.ensure(hp.nP * 16), "upload P");
+		launch_widen3(ctx->d_P3.as<float>(), ctx->d_P.as<float4>(), hp.nP, ctx->stream);
+	} else {
+		AQH_TRY(up(ctx->d_P, hp.P, hp.nP * 16), "upload P");
+	}
 	// Ci/Oi on the copy stream, after everything already queued on the main
 	// stream (the previous frame may still read the old colours)
 	AQH_TRY(ctx->d_Ci.ensure(hp.nC * 16), "upload Ci");
 	AQH_TRY(ctx->d_Oi.ensure(hp.nC * 16), "upload Oi");
+	if (packed3) {
+		AQH_TRY(ctx->d_C3.ensure(hp.nC * 12), "upload Ci");
+		AQH_TRY(ctx->d_O3.ensure(hp.nC * 12), "upload Oi");
+	}
 	AQH_TRY(cudaEventRecord(ctx->ev_before_up, ctx->stream), "upload Ci");
 	AQH_TRY(cudaStreamWaitEvent(ctx->cstream, ctx->ev_before_up, 0), "upload Ci");
-	if (hp.Ci && hp.nC)
-		AQH_TRY(cudaMemcpyAsync(ctx->d_Ci.p, hp.Ci, hp.nC * 16, cudaMemcpyHostToDevice, ctx->cstream), "upload Ci");
-	if (hp.Oi && hp.nC)
-		AQH_TRY(cudaMemcpyAsync(ctx->d_Oi.p, hp.Oi, hp.nC * 16, cudaMemcpyHostToDevice, ctx->cstream), "upload Oi");
+	auto colours = [&](DevBuf& dst, DevBuf& stage, const float* src) -> cudaError_t {
+		if (!src || hp.nC == 0) return cudaSuccess;
+		if (!packed3) return cudaMemcpyAsync(dst.p, src, hp.nC * 16, cudaMemcpyHostToDevice, ctx->cstream);
+		cudaError_t e = cudaMemcpyAsync(stage.p, src, hp.nC * 12, cudaMemcpyHostToDevice, ctx->cstream);
+		if (e == cudaSuccess) launch_widen3(stage.as<float>(), dst.as<float4>(), hp.nC, ctx->cstream);
+		return e;
+	};
+	AQH_TRY(colours(ctx->d_Ci, ctx->d_C3, hp.Ci), "upload Ci");
+	AQH_TRY(colours(ctx->d_Oi, ctx->d_O3, hp.Oi), "upload Oi");
 	AQH_TRY(cudaEventRecord(ctx->ev_cioi, ctx->cstream), "upload Ci");
 	ctx->cioi_pending = true;
 	if (hp.culled) AQH_TRY(up(ctx->d_culled, hp.culled, (size_t)ctx->h_mps), "upload culled");

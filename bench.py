@@ -11,9 +11,10 @@ needed between steps.
 
 Legs reported on one JSON line:
   value    micropolygons/s with grids resident in HBM (device-timed, CUDA events)
-  e2e      micropolygons/s through the C-ABI from page-locked host arrays:
-           per step the H2D copy of every grid array, the render and the D2H
-           read of the RGBA8 image are inside the timed region
+  e2e      micropolygons/s through the C-ABI from page-locked host arrays
+           (P, Ci, Oi as three-float entries, the reference's CqVector3D /
+           CqColor layout): per step the H2D copy of every grid array, the
+           render and the D2H read of the RGBA8 image are inside the timed region
   roofline achieved GB/s of the sampling kernel (the dominant one) over its
            algorithmic bytes (P, Ci, Oi float4 per vertex, read once) against
            the measured HBM copy bandwidth
@@ -346,10 +347,14 @@ def run_gpu(args):
 
     # ---- end-to-end leg: host arrays through the C-ABI ----
     import ctypes as C
+    # page-locked host arrays; P, Ci and Oi as three-float entries, the layout
+    # of the reference's CqVector3D / CqColor grid arrays (aqh_submit_grids_host3)
     pin = {}
     for k in ("cu", "cv", "nkeys", "flags", "pbase", "cbase", "tbase", "times", "P", "Ci", "Oi"):
-        a = np.ascontiguousarray(getattr(g, k))
-        pt = torch.from_numpy(a).pin_memory()
+        a = np.asarray(getattr(g, k))
+        if k in ("P", "Ci", "Oi"):
+            a = a[:, :3]
+        pt = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
         pin[k] = pt
     h2 = aqh.Hider(local)
     h2.set_stream(stream.cuda_stream)
@@ -359,18 +364,18 @@ def run_gpu(args):
     h2.frame_begin(fr)
     h2.set_samples(smp)
     L = h2.L
-    L.aqh_submit_grids_host.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 8 + [C.c_size_t, C.c_void_p,
-                                                                                  C.c_size_t, C.c_void_p,
-                                                                                  C.c_void_p, C.c_size_t, C.c_void_p,
-                                                                                  C.c_int64]
-    L.aqh_submit_grids_host.restype = C.c_int
-    rc = L.aqh_submit_grids_host(h2.ctx, G, pin["cu"].data_ptr(), pin["cv"].data_ptr(), pin["nkeys"].data_ptr(),
+    L.aqh_submit_grids_host3.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 8 + [C.c_size_t, C.c_void_p,
+                                                                                   C.c_size_t, C.c_void_p,
+                                                                                   C.c_void_p, C.c_size_t, C.c_void_p,
+                                                                                   C.c_int64]
+    L.aqh_submit_grids_host3.restype = C.c_int
+    rc = L.aqh_submit_grids_host3(h2.ctx, G, pin["cu"].data_ptr(), pin["cv"].data_ptr(), pin["nkeys"].data_ptr(),
                                  pin["flags"].data_ptr(), pin["pbase"].data_ptr(), pin["cbase"].data_ptr(),
                                  pin["tbase"].data_ptr(), pin["times"].data_ptr(), int(g.times.size),
                                  pin["P"].data_ptr(), int(g.P.shape[0]), pin["Ci"].data_ptr(), pin["Oi"].data_ptr(),
                                  int(g.Ci.shape[0]), None, mps)
     if rc != 0:
-        raise RuntimeError("aqh_submit_grids_host: " + L.aqh_last_error(h2.ctx).decode())
+        raise RuntimeError("aqh_submit_grids_host3: " + L.aqh_last_error(h2.ctx).decode())
     out = np.zeros((fr.height, fr.width, 4), np.uint8)
     for _ in range(max(1, args.warmup)):
         h2.render(sync=True)
@@ -431,7 +436,8 @@ def run_gpu(args):
                                            "p99": float(np.percentile(plain_lat, 99))}},
             "roofline": roof, "clocks": clk, "gpu_launches": launches_per_step * args.steps,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": e2e_ms_max}}
+                    "ms_per_step": e2e_ms_max,
+                    "path": "aqh_submit_grids_host3 (P, Ci, Oi as float3) + aqh_render + aqh_read_quantized_u8"}}
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
     print(json.dumps(line), flush=True)

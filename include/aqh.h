@@ -211,6 +211,16 @@ aqh_status aqh_submit_grids_host(aqh_ctx* ctx, int ngrids,
                                  const int32_t* tbase, const float* times, size_t ntimes,
                                  const float* P, size_t nP, const float* Ci, const float* Oi, size_t nC,
                                  const uint8_t* culled, int64_t total_micropolygons);
+/* The same with P, Ci and Oi as packed three-float entries -- the memory
+ * layout of the reference's CqVector3D / CqColor grid arrays -- so they go
+ * up 25% smaller and are widened to float4 on the device; nP and nC count
+ * entries.  The fourth P component is 0. */
+aqh_status aqh_submit_grids_host3(aqh_ctx* ctx, int ngrids,
+                                  const int32_t* cu, const int32_t* cv, const int32_t* nkeys,
+                                  const int32_t* flags, const int64_t* pbase, const int64_t* cbase,
+                                  const int32_t* tbase, const float* times, size_t ntimes,
+                                  const float* P, size_t nP, const float* Ci, const float* Oi, size_t nC,
+                                  const uint8_t* culled, int64_t total_micropolygons);
 /* Page-locked host memory for grid arrays. */
 void* aqh_host_alloc(size_t bytes);
 void aqh_host_free(void* p);

@@ -98,3 +98,21 @@ def test_camera_flag_without_matrix_is_rejected(hider):
     sc = S.Scene(dataclasses.replace(sc.frame, camera_to_raster=None), sc.grids, sc.samples)
     with pytest.raises(AqhError):
         hider.render_scene(sc)
+
+
+@pytest.mark.parametrize("name", ["perspective_static", "perspective_motion_dof", "perspective_transparent"])
+def test_three_float_host_grids(aqh_lib, oracle, name):
+    """aqh_submit_grids_host3 (CqVector3D / CqColor layout, widened on the
+    device) renders exactly what the float4 arrays render."""
+    sc = SCENES[name]()
+    ref = oracle.render(sc)
+    h = aqh_lib.Hider(0)
+    try:
+        for batched in (False, True):
+            h.set_mode(batched)
+            h.frame_begin(sc.frame)
+            h.set_samples(sc.samples)
+            h.submit_grids_host(sc.grids, packed3=True)
+            compare(_finish(h), ref, exact_pixels="transparent" not in name)
+    finally:
+        h.close()
