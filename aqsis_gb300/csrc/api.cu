@@ -768,6 +768,7 @@ aqh_status aqh_submit_grids_device(aqh_ctx* ctx, int ngrids, const int32_t* d_cu
 	g.P = reinterpret_cast<const float4*>(d_P);
 	g.Ci = reinterpret_cast<const float4*>(d_Ci);
 	g.Oi = reinterpret_cast<const float4*>(d_Oi);
+	g.colour3 = 0;
 	g.culled = d_culled;
 	// first micropolygon id of every grid
 	AQH_TRY(ctx->d_mpcount.ensure(sizeof(int32_t) * (ngrids + 1) * 2 + 64), "alloc");
@@ -814,32 +815,37 @@ static aqh_status upload_packed_grids(aqh_ctx* ctx) {
 	AQH_TRY(up(ctx->d_times, hp.times, std::max<size_t>(hp.ntimes, 1) * 4), "upload grids");
 	const bool packed3 = hp.comps == 3;
 	if (packed3) {
-		// three-float entries go up as they are and are widened on the device
-		AQH_TRY(up(ctx->d_P3, hp.P, hp.nP * 12), "upload P");
-		AQH_TRY(ctx->d_P.ensure(hp.nP * 16), "upload P");
-		launch_widen3(ctx->d_P3.as<float>(), ctx->d_P.as<float4>(), hp.nP, ctx->stream);
+		// three-float P: widened to float4 by a kernel that reads the host
+		// array itself when it is page-locked (as fast as the copy engines
+		// over this link, and no second pass), else copied up and widened
+		AQH_TRY(ctx->d_P.ensure(std::max<size_t>(hp.nP, 1) * 16), "upload P");
+		cudaPointerAttributes pa{};
+		const bool mapped = hp.nP && cudaPointerGetAttributes(&pa, hp.P) == cudaSuccess &&
+		                    pa.type == cudaMemoryTypeHost && pa.devicePointer;
+		cudaGetLastError();
+		if (mapped) {
+			launch_widen3(static_cast<const float*>(pa.devicePointer), ctx->d_P.as<float4>(), hp.nP, ctx->stream);
+		} else {
+			AQH_TRY(up(ctx->d_P3, hp.P, hp.nP * 12), "upload P");
+			launch_widen3(ctx->d_P3.as<float>(), ctx->d_P.as<float4>(), hp.nP, ctx->stream);
+		}
 	} else {
 		AQH_TRY(up(ctx->d_P, hp.P, hp.nP * 16), "upload P");
 	}
 	// Ci/Oi on the copy stream, after everything already queued on the main
-	// stream (the previous frame may still read the old colours)
-	AQH_TRY(ctx->d_Ci.ensure(hp.nC * 16), "upload Ci");
-	AQH_TRY(ctx->d_Oi.ensure(hp.nC * 16), "upload Oi");
-	if (packed3) {
-		AQH_TRY(ctx->d_C3.ensure(hp.nC * 12), "upload Ci");
-		AQH_TRY(ctx->d_O3.ensure(hp.nC * 12), "upload Oi");
-	}
+	// stream (the previous frame may still read the old colours); three-float
+	// colours stay packed on the device (GridsDev::colour3)
+	DevBuf& dCi = packed3 ? ctx->d_C3 : ctx->d_Ci;
+	DevBuf& dOi = packed3 ? ctx->d_O3 : ctx->d_Oi;
+	const size_t csz = packed3 ? 12 : 16;
+	AQH_TRY(dCi.ensure(std::max<size_t>(hp.nC, 1) * csz), "upload Ci");
+	AQH_TRY(dOi.ensure(std::max<size_t>(hp.nC, 1) * csz), "upload Oi");
 	AQH_TRY(cudaEventRecord(ctx->ev_before_up, ctx->stream), "upload Ci");
 	AQH_TRY(cudaStreamWaitEvent(ctx->cstream, ctx->ev_before_up, 0), "upload Ci");
-	auto colours = [&](DevBuf& dst, DevBuf& stage, const float* src) -> cudaError_t {
-		if (!src || hp.nC == 0) return cudaSuccess;
-		if (!packed3) return cudaMemcpyAsync(dst.p, src, hp.nC * 16, cudaMemcpyHostToDevice, ctx->cstream);
-		cudaError_t e = cudaMemcpyAsync(stage.p, src, hp.nC * 12, cudaMemcpyHostToDevice, ctx->cstream);
-		if (e == cudaSuccess) launch_widen3(stage.as<float>(), dst.as<float4>(), hp.nC, ctx->cstream);
-		return e;
-	};
-	AQH_TRY(colours(ctx->d_Ci, ctx->d_C3, hp.Ci), "upload Ci");
-	AQH_TRY(colours(ctx->d_Oi, ctx->d_O3, hp.Oi), "upload Oi");
+	if (hp.Ci && hp.nC)
+		AQH_TRY(cudaMemcpyAsync(dCi.p, hp.Ci, hp.nC * csz, cudaMemcpyHostToDevice, ctx->cstream), "upload Ci");
+	if (hp.Oi && hp.nC)
+		AQH_TRY(cudaMemcpyAsync(dOi.p, hp.Oi, hp.nC * csz, cudaMemcpyHostToDevice, ctx->cstream), "upload Oi");
 	AQH_TRY(cudaEventRecord(ctx->ev_cioi, ctx->cstream), "upload Ci");
 	ctx->cioi_pending = true;
 	if (hp.culled) AQH_TRY(up(ctx->d_culled, hp.culled, (size_t)ctx->h_mps), "upload culled");
@@ -850,8 +856,9 @@ static aqh_status upload_packed_grids(aqh_ctx* ctx) {
 	g.pbase = ctx->d_pbase.as<int64_t>(); g.cbase = ctx->d_cbase.as<int64_t>(); g.mpbase = ctx->d_mpbase.as<int64_t>();
 	g.times = hp.times ? ctx->d_times.as<float>() : nullptr;
 	g.P = ctx->d_P.as<float4>();
-	g.Ci = hp.Ci ? ctx->d_Ci.as<float4>() : nullptr;
-	g.Oi = hp.Oi ? ctx->d_Oi.as<float4>() : nullptr;
+	g.Ci = hp.Ci ? dCi.as<float4>() : nullptr;
+	g.Oi = hp.Oi ? dOi.as<float4>() : nullptr;
+	g.colour3 = packed3 ? 1 : 0;
 	g.culled = hp.culled ? ctx->d_culled.as<uint8_t>() : nullptr;
 	g.naov = 0;
 	g.aov = nullptr;
@@ -895,6 +902,7 @@ static aqh_status upload_host_grids(aqh_ctx* ctx) {
 	g.pbase = ctx->d_pbase.as<int64_t>(); g.cbase = ctx->d_cbase.as<int64_t>(); g.mpbase = ctx->d_mpbase.as<int64_t>();
 	g.times = ctx->d_times.as<float>();
 	g.P = ctx->d_P.as<float4>(); g.Ci = ctx->d_Ci.as<float4>(); g.Oi = ctx->d_Oi.as<float4>();
+	g.colour3 = 0;
 	g.culled = ctx->any_culled ? ctx->d_culled.as<uint8_t>() : nullptr;
 	g.naov = 0;
 	g.aov = nullptr;

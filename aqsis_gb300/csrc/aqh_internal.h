@@ -73,6 +73,7 @@ struct GridsDev {
 	const int32_t* id_grid;  // grid holding micropolygon id k * 256, for each k; may be null
 	const float* aov;        // output variables, float[vertex][naov] indexed like Ci; null when naov == 0
 	int naov;
+	int colour3;             // Ci / Oi hold packed three-float entries (float[3 n]) rather than float4
 };
 
 // Sample pattern caches (aqh_samples) in device memory.

@@ -134,12 +134,12 @@ __device__ __forceinline__ void build_record(const FrameParams& fp, const GridsD
 	const bool smooth = (gflags & 1) != 0;
 	if (!(gflags & 8) && g.Oi) {
 		const long long cb = __ldg(g.cbase + gi);
-		const float4 o0 = __ldg(g.Oi + cb + index);
+		const float4 o0 = ld_colour(g, g.Oi, cb + index);
 		opaque = o0.x >= 1.0f && o0.y >= 1.0f && o0.z >= 1.0f;
 		if (smooth) {
-			const float4 o1 = __ldg(g.Oi + cb + index + 1);
-			const float4 o2 = __ldg(g.Oi + cb + index + cu + 1);
-			const float4 o3 = __ldg(g.Oi + cb + index + cu + 2);
+			const float4 o1 = ld_colour(g, g.Oi, cb + index + 1);
+			const float4 o2 = ld_colour(g, g.Oi, cb + index + cu + 1);
+			const float4 o3 = ld_colour(g, g.Oi, cb + index + cu + 2);
 			opaque = opaque && (o1.x >= 1.0f && o1.y >= 1.0f && o1.z >= 1.0f) &&
 			         (o2.x >= 1.0f && o2.y >= 1.0f && o2.z >= 1.0f) && (o3.x >= 1.0f && o3.y >= 1.0f && o3.z >= 1.0f);
 		}
@@ -1144,7 +1144,7 @@ __global__ void occluder_scan_kernel(GridsDev g, int32_t* flag) {
 		const long long nv = (long long)(__ldg(g.cu + gi) + 1) * (__ldg(g.cv + gi) + 1);
 		const long long cb = __ldg(g.cbase + gi);
 		for (long long i = threadIdx.x; i < nv && !occ; i += blockDim.x) {
-			const float4 o = __ldg(g.Oi + cb + i);
+			const float4 o = ld_colour(g, g.Oi, cb + i);
 			occ = o.x >= 1.0f && o.y >= 1.0f && o.z >= 1.0f;
 		}
 	}

@@ -7,6 +7,16 @@
 
 namespace aqh {
 
+// Entry i of a colour array (Ci or Oi): float4, or three packed floats when
+// the grids arrived in the three-float host layout.
+__device__ __forceinline__ float4 ld_colour(const GridsDev& g, const float4* p, long long i) {
+	if (g.colour3) {
+		const float* f = reinterpret_cast<const float*>(p) + 3 * i;
+		return make_float4(__ldg(f), __ldg(f + 1), __ldg(f + 2), 0.0f);
+	}
+	return __ldg(p + i);
+}
+
 // Exclusive prefix count of `f` over the block (blockDim.x a multiple of 32,
 // at most 1024 threads); `warp_tot` is shared scratch of 32 ints.
 __device__ __forceinline__ int block_excl_scan(int* warp_tot, bool f, int& total) {
@@ -95,8 +105,8 @@ __device__ __forceinline__ void hit_colour(const GridsDev& g, int gi, int m, flo
 		float4 c[4], o[4];
 #pragma unroll
 		for (int q = 0; q < 4; ++q) {
-			c[q] = g.Ci ? __ldg(g.Ci + cb + vi[q]) : make_float4(1, 1, 1, 0);
-			o[q] = g.Oi ? __ldg(g.Oi + cb + vi[q]) : make_float4(1, 1, 1, 0);
+			c[q] = g.Ci ? ld_colour(g, g.Ci, cb + vi[q]) : make_float4(1, 1, 1, 0);
+			o[q] = g.Oi ? ld_colour(g, g.Oi, cb + vi[q]) : make_float4(1, 1, 1, 0);
 		}
 		dat[0] = ((wt[0] * c[0].x + wt[1] * c[1].x) + wt[2] * c[2].x) + wt[3] * c[3].x;
 		dat[1] = ((wt[0] * c[0].y + wt[1] * c[1].y) + wt[2] * c[2].y) + wt[3] * c[3].y;
@@ -105,8 +115,8 @@ __device__ __forceinline__ void hit_colour(const GridsDev& g, int gi, int m, flo
 		dat[4] = ((wt[0] * o[0].y + wt[1] * o[1].y) + wt[2] * o[2].y) + wt[3] * o[3].y;
 		dat[5] = ((wt[0] * o[0].z + wt[1] * o[1].z) + wt[2] * o[2].z) + wt[3] * o[3].z;
 	} else {
-		const float4 c = g.Ci ? __ldg(g.Ci + cb + index) : make_float4(1, 1, 1, 0);
-		const float4 o = g.Oi ? __ldg(g.Oi + cb + index) : make_float4(1, 1, 1, 0);
+		const float4 c = g.Ci ? ld_colour(g, g.Ci, cb + index) : make_float4(1, 1, 1, 0);
+		const float4 o = g.Oi ? ld_colour(g, g.Oi, cb + index) : make_float4(1, 1, 1, 0);
 		dat[0] = c.x; dat[1] = c.y; dat[2] = c.z;
 		dat[3] = o.x; dat[4] = o.y; dat[5] = o.z;
 	}

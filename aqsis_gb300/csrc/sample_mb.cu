@@ -262,7 +262,7 @@ __device__ __forceinline__ void build_mb_record(const FrameParams& fp, const Gri
 		const long long cb = __ldg(g.cbase + gi);
 		const int vi[4] = {index, index + 1, index + cu + 1, index + cu + 2};
 		for (int q = 0; q < (smooth ? 4 : 1); ++q) {
-			const float4 o = __ldg(g.Oi + cb + vi[q]);
+			const float4 o = ld_colour(g, g.Oi, cb + vi[q]);
 			opaque = opaque && (o.x >= 1.0f && o.y >= 1.0f && o.z >= 1.0f);
 		}
 	}
