@@ -205,3 +205,75 @@ def camera_small(seed=14, every=2, **kw):
     """Opaque stream with every `every`-th grid given in camera space
     (GRID_CAMERA) under a perspective camera-to-raster matrix."""
     return S.to_camera_space(opaque_small(seed=seed), every=every, **kw)
+
+
+def fuzz(seed):
+    """A small random frame for differential tests: random pixel samples,
+    filter, crop window, depth filter, zthreshold and dither; grids of random
+    size and placement with jitter, exact depth ties, collapsed vertices,
+    mirrored (clockwise) grids, z at and below zero, huge quads, constant and
+    smooth shading, matte flags, transparency (including Oi of 0 and above
+    1), triangular grids, culled micropolygons and, for some seeds, motion
+    and depth of field."""
+    rng = np.random.default_rng(1000 + seed)
+    filters = [("box", 1.0, 1.0), ("gaussian", 2.0, 2.0), ("catmull-rom", 3.0, 3.0), ("triangle", 2.0, 2.0),
+               ("sinc", 4.0, 4.0), ("gaussian", 3.0, 1.0)]
+    filt = filters[int(rng.integers(0, len(filters)))]
+    w, h = int(rng.integers(12, 48)), int(rng.integers(10, 40))
+    crop = None
+    if rng.random() < 0.3:
+        x0, y0 = int(rng.integers(0, w // 2)), int(rng.integers(0, h // 2))
+        crop = (x0, int(rng.integers(x0 + 1, w + 1)), y0, int(rng.integers(y0 + 1, h + 1)))
+    motion = rng.random() < 0.25
+    dof = rng.random() < 0.2
+    fr = S.Frame(width=w, height=h, crop=crop, xsamples=int(rng.integers(1, 7)), ysamples=int(rng.integers(1, 7)),
+                 filter=filt[0], xfilter=filt[1], yfilter=filt[2], q_dither=float(rng.choice([0.0, 0.5])),
+                 depth_filter=int(rng.choice([0, 0, 0, 1, 2, 3])),
+                 zthreshold=tuple(float(v) for v in rng.choice([1.0, 0.5], 3)),
+                 display_z=int(rng.random() < 0.2))
+    if motion:
+        fr.shutter = (0.0, 1.0)
+    if dof:
+        fr.fstop, fr.focal_length, fr.focal_distance = 2.8, 0.5, 20.0
+    parts = []
+    for k in range(int(rng.integers(3, 14))):
+        nx, ny = int(rng.integers(1, 9)), int(rng.integers(1, 9))
+        step = float(rng.choice([0.4, 1.0, 1.7, 6.0]))
+        z = float(rng.choice([rng.uniform(0.5, 60), 20.0, 0.0, -3.0], p=[0.7, 0.2, 0.05, 0.05]))
+        oi = None
+        r = rng.random()
+        if r < 0.3:
+            oi = rng.uniform(0.0, 1.2, ((nx + 1) * (ny + 1), 3))
+        elif r < 0.35:
+            oi = np.zeros(((nx + 1) * (ny + 1), 3))
+        flags = int(rng.choice([S.GRID_SMOOTH, 0, S.GRID_SMOOTH | S.GRID_MATTE, S.GRID_MATTEALPHA | S.GRID_SMOOTH],
+                               p=[0.6, 0.25, 0.1, 0.05]))
+        g = plane(float(rng.uniform(-4, w)), float(rng.uniform(-4, h)), nx, ny, z, step=step, rng=rng,
+                  jitter=float(rng.choice([0.0, 0.3])), oi=oi, flags=flags,
+                  zslope=float(rng.choice([0.0, 0.02, -0.05])))
+        P = g.P.reshape(ny + 1, nx + 1, 4).copy()
+        if rng.random() < 0.2:
+            P = P[:, ::-1, :].copy()                       # clockwise
+        if rng.random() < 0.2 and nx > 1:
+            i, j = int(rng.integers(0, ny + 1)), int(rng.integers(0, nx))
+            P[i, j + 1, :3] = P[i, j, :3]                  # collapsed edge
+        g = grid_from_points(P[..., :3], g.Ci[:, :3], None if oi is None else np.asarray(oi), flags)
+        if rng.random() < 0.15:
+            g.flags = (g.flags | S.GRID_TRIANGULAR).astype(np.int32)
+        if motion and rng.random() < 0.6:
+            d = rng.uniform(-4, 4, 2).astype(np.float32)
+            P1 = g.P.copy()
+            P1[:, 0] += d[0]
+            P1[:, 1] += d[1]
+            g = S._pack(g.cu, g.cv, np.array([2]), g.flags, np.concatenate([g.P, P1]), g.Ci, g.Oi,
+                        np.array([0.0, 1.0], np.float32), np.array([0]))
+        parts.append(g)
+    grids = S.concat_grids(parts)
+    if rng.random() < 0.3:
+        culled = np.zeros(grids.micropolygons, np.uint8)
+        culled[rng.integers(0, grids.micropolygons, max(1, grids.micropolygons // 10))] = 1
+        grids.culled = culled
+    sc = custom(fr, grids, seed=seed, dither=fr.q_dither > 0)
+    if dof:
+        mult, _ = sc.frame.dof_terms()
+    return sc
