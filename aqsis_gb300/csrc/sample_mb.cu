@@ -673,8 +673,10 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 							} else {
 								B = Bnd{r.bmn[0], r.bmn[1], r.bmn[2], r.bmx[0], r.bmx[1], r.bmx[2]};
 							}
-							// Clipping defaults (FLT_EPSILON, FLT_MAX), options.cpp:296
-							if (B.mnz > FLT_MAX || B.mxz < FLT_EPSILON) continue;
+							// RenderMPG_MBOrDof's clipping-range cull (FLT_EPSILON, FLT_MAX,
+							// options.cpp:296); static micropolygons without depth of field
+							// are RenderMPG_Static's and are not culled
+							if ((moving || usingDof) && (B.mnz > FLT_MAX || B.mxz < FLT_EPSILON)) continue;
 							Bnd TB = B;
 							if (usingDof) {
 								// the lens stratum of this sample shifts the bound (bucketprocessor.cpp:1299-1321)
@@ -851,7 +853,11 @@ __device__ __forceinline__ bool mb_slice(const FrameParams& fp, const Shutter& s
 	} else {
 		B = Bnd{r.bmn[0], r.bmn[1], r.bmn[2], r.bmx[0], r.bmx[1], r.bmx[2]};
 	}
-	// Clipping defaults (FLT_EPSILON, FLT_MAX), options.cpp:296
+	// The clipping-range cull of RenderMPG_MBOrDof (bucketprocessor.cpp:1294-1296,
+	// defaults FLT_EPSILON / FLT_MAX, options.cpp:296).  A micropolygon that
+	// neither moves nor sees depth of field is sampled by RenderMPG_Static
+	// (bucketprocessor.cpp:1067-1091), which has no such cull.
+	if (!moving && !fp.use_dof) return true;
 	return !(B.mnz > FLT_MAX || B.mxz < FLT_EPSILON);
 }
 

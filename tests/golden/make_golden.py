@@ -107,6 +107,7 @@ CASES = {
     "triangular_motion_dof": lambda: SS.triangular(SS.motion_dof_small(seed=10, xs=4, ys=4, scale=0.02), every=2),
     "camera_perspective": lambda: S.to_camera_space(SS.triangular_small(seed=12), every=2),
     "mpdump_replay": mpdump_scene,
+    "motion_static_behind_eye": lambda: SS.motion_static_behind_eye(seed=16, transparent=True),
     "output_variables": lambda: S.with_aov(SS.transparent_edge(seed=14), 3, seed=14),
     "output_variables_motion": lambda: S.with_aov(SS.motion_dof_small(seed=15, xs=3, ys=3, scale=0.015,
                                                                       transparent=True), 2, seed=15),

@@ -277,3 +277,22 @@ def fuzz(seed):
     if dof:
         mult, _ = sc.frame.dof_terms()
     return sc
+
+
+def motion_static_behind_eye(seed=16, transparent=False):
+    """A motion-blurred frame with a static grid at negative camera depth
+    beside a moving one.  Only micropolygons that move (or see depth of
+    field) go through RenderMPG_MBOrDof and its clipping-range cull; the
+    static grid is sampled like any static one."""
+    rng = np.random.default_rng(seed)
+    fr = S.Frame(width=28, height=24, xsamples=3, ysamples=3, filter="gaussian", xfilter=2.0, yfilter=2.0,
+                 q_dither=0.0, shutter=(0.0, 1.0))
+    oi = rng.uniform(0.2, 0.8, (49, 3)) if transparent else None
+    still = plane(2, 3, 6, 6, -4.0, step=2.0, rng=rng, jitter=0.3, zslope=0.01, oi=oi)
+    mov = plane(10, 6, 6, 6, 20.0, step=1.5, rng=rng, jitter=0.2)
+    P1 = mov.P.copy()
+    P1[:, 0] += 3.0
+    P1[:, 1] -= 1.5
+    mov = S._pack(mov.cu, mov.cv, np.array([2]), mov.flags, np.concatenate([mov.P, P1]), mov.Ci, mov.Oi,
+                  np.array([0.0, 1.0], np.float32), np.array([0]))
+    return custom(fr, S.concat_grids([still, mov]), seed=seed)

@@ -18,7 +18,7 @@ OUT_KEYS = ("winner", "occlz", "nfrag", "valid", "channels", "quantized")
 
 
 def test_fixtures_present():
-    assert len(FIXTURES) >= 22
+    assert len(FIXTURES) >= 23
 
 
 @pytest.mark.parametrize("path", FIXTURES, ids=NAMES)

@@ -200,3 +200,14 @@ def test_batched_mode_matches_oracle_and_replays(hider, oracle, scene_fn):
             assert np.array_equal(a.view(np.uint32), res["channels"].view(np.uint32))
     finally:
         hider.set_mode(False)
+
+
+@pytest.mark.parametrize("transparent", [False, True])
+def test_static_grid_behind_eye_in_motion_frame(hider, oracle, transparent):
+    """RenderMPG_MBOrDof's clipping-range cull applies to moving micropolygons
+    only; a static grid at negative depth in a motion-blurred frame is still
+    sampled (found by the random differential frames)."""
+    sc = SS.motion_static_behind_eye(transparent=transparent)
+    res, ref = run_both(hider, oracle, sc)
+    compare(res, ref)
+    assert (ref["winner"] >= 0).sum() + (ref["nfrag"] > 0).sum() > 0
