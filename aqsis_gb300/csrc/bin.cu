@@ -89,6 +89,35 @@ __global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect, float*
 		mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
 		mxz = fmaxf(mxz, __shfl_xor_sync(0xffffffffu, mxz, o));
 	}
+	// depth of field: the largest blur AddMPG gives any of the grid's
+	// micropolygons, max(CoC(bound min z), CoC(bound max z)) over its own
+	// bound (imagebuffer.cpp:520-531).  The grid's depth ends do not bound it
+	// when the depth range reaches z = 0, where the blur has its pole.
+	float mcx = 0.0f, mcy = 0.0f;
+	if (fp.use_dof) {
+		const long long nvk = (long long)(cu + 1) * (cv + 1);
+		for (int m = lane; m < cu * cv; m += 32) {
+			const int iv = m / cu, iu = m - iv * cu;
+			const long long idx = (long long)iv * (cu + 1) + iu;
+			float zl = FLT_MAX, zh = -FLT_MAX;
+			for (int k = 0; k < nk; ++k) {
+				const float4* Pk = P + k * nvk;
+				const float za = __ldg(Pk + idx).z, zb = __ldg(Pk + idx + 1).z;
+				const float zc = __ldg(Pk + idx + cu + 1).z, zd = __ldg(Pk + idx + cu + 2).z;
+				zl = amin(zl, amin(amin(amin(za, zb), zc), zd));
+				zh = amax(zh, amax(amax(amax(za, zb), zc), zd));
+			}
+			const float2 c1 = coc(zl, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+			const float2 c2 = coc(zh, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+			mcx = fmaxf(mcx, fmaxf(c1.x, c2.x));
+			mcy = fmaxf(mcy, fmaxf(c1.y, c2.y));
+		}
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			mcx = fmaxf(mcx, __shfl_xor_sync(0xffffffffu, mcx, o));
+			mcy = fmaxf(mcy, __shfl_xor_sync(0xffffffffu, mcy, o));
+		}
+	}
 	if (strips) {
 		uint32_t* S = strips + (long long)warp * 64;
 		const bool has = nk == 1 && cu <= 31 && cv <= 31;
@@ -112,9 +141,7 @@ __global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect, float*
 	if (fp.use_dof) {
 		float2 c1 = coc(mnz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
 		float2 c2 = coc(mxz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
-		float cx = fmaxf(c1.x, c2.x), cy = fmaxf(c1.y, c2.y);
-		// a grid straddling the focal plane has its largest blur at an end of
-		// its depth range as well, so the two ends bound it
+		const float cx = fmaxf(fmaxf(c1.x, c2.x), mcx), cy = fmaxf(fmaxf(c1.y, c2.y), mcy);
 		mnx -= cx; mxx += cx; mny -= cy; mxy += cy;
 	}
 	int4 r;

@@ -240,6 +240,7 @@ def fuzz(seed):
         nx, ny = int(rng.integers(1, 9)), int(rng.integers(1, 9))
         step = float(rng.choice([0.4, 1.0, 1.7, 6.0]))
         z = float(rng.choice([rng.uniform(0.5, 60), 20.0, 0.0, -3.0], p=[0.7, 0.2, 0.05, 0.05]))
+
         oi = None
         r = rng.random()
         if r < 0.3:
@@ -269,6 +270,12 @@ def fuzz(seed):
                         np.array([0.0, 1.0], np.float32), np.array([0]))
         parts.append(g)
     grids = S.concat_grids(parts)
+    if dof:
+        # a vertex at camera depth 0 has an infinite circle of confusion; the
+        # reference's integer conversions of the infinite bounds are undefined
+        # (and differ between hosts), so no parity is defined for it
+        z = grids.P[:, 2]
+        z[z == 0.0] = 1e-3
     if rng.random() < 0.3:
         culled = np.zeros(grids.micropolygons, np.uint8)
         culled[rng.integers(0, grids.micropolygons, max(1, grids.micropolygons // 10))] = 1
