@@ -7,7 +7,7 @@ from tests.test_gpu_parity import compare
 
 pytestmark = pytest.mark.gpu
 
-SEEDS = list(range(60))
+SEEDS = list(range(300))
 
 
 @pytest.mark.parametrize("seed", SEEDS)
@@ -16,7 +16,7 @@ def test_random_frame_matches_oracle(hider, oracle, seed):
     compare(hider.render_scene(sc), oracle.render(sc))
 
 
-@pytest.mark.parametrize("seed", SEEDS[:20])
+@pytest.mark.parametrize("seed", SEEDS[:100])
 def test_random_frame_batched(aqh_lib, oracle, seed):
     sc = SS.fuzz(seed)
     h = aqh_lib.Hider(0)
