@@ -191,6 +191,7 @@ def load(build_if_missing: bool = False):
     L.aqh_get_stats.argtypes = [vp, C.POINTER(FrameStats)]
     L.aqh_set_camera_to_raster.argtypes = [vp, _f32p]
     L.aqh_set_aov_count.argtypes = [vp, C.c_int]
+    L.aqh_set_lod_bounds.argtypes = [vp, _f32p, C.c_int]
     L.aqh_dspy_geometry_of.argtypes = [vp, C.POINTER(DspyGeometry)]
     L.aqh_dspy_open.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(DspyGeometry), C.POINTER(Display),
                                 C.POINTER(C.c_char_p), C.POINTER(vp)]
@@ -215,7 +216,7 @@ def load(build_if_missing: bool = False):
                  "aqh_read_samples", "aqh_get_stats", "aqh_test_invbilinear", "aqh_set_tuning", "aqh_get_tuning",
                  "aqh_autotune", "aqh_set_camera_to_raster", "aqh_read_display", "aqh_set_aov_count",
                  "aqh_submit_aov_host", "aqh_submit_aov_device", "aqh_read_aov", "aqh_dspy_geometry_of",
-                 "aqh_dspy_open", "aqh_dspy_send", "aqh_dspy_send_image", "aqh_dspy_close"):
+                 "aqh_dspy_open", "aqh_dspy_send", "aqh_dspy_send_image", "aqh_dspy_close", "aqh_set_lod_bounds"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -329,6 +330,11 @@ class Hider:
         self._check(self.L.aqh_set_samples(self.ctx, C.byref(cs)), "aqh_set_samples")
         self._check(self.L.aqh_synchronize(self.ctx), "aqh_synchronize")
 
+    def set_lod_bounds(self, bounds):
+        """LevelOfDetailBounds per grid, float[G][2] (aqh_set_lod_bounds)."""
+        b = np.ascontiguousarray(bounds, np.float32).reshape(-1, 2)
+        self._check(self.L.aqh_set_lod_bounds(self.ctx, _p(b, _f32p), b.shape[0]), "aqh_set_lod_bounds")
+
     def set_aov_count(self, n: int):
         """Output variables per vertex for this frame (aqh_set_aov_count), before any grid."""
         self._check(self.L.aqh_set_aov_count(self.ctx, int(n)), "aqh_set_aov_count")
@@ -372,6 +378,8 @@ class Hider:
             self.submit_grid(cu, cv, g.P[pb:pb + nv * nk], g.Ci[cb:cb + nv], g.Oi[cb:cb + nv], int(g.flags[i]),
                              kt, cl, None if aov is None else aov[cb:cb + nv])
             mpbase += cu * cv
+        if getattr(g, "lod", None) is not None:
+            self.set_lod_bounds(g.lod)
 
     def submit_grids_host(self, g, packed3: bool = False):
         """Submit a whole packed scene.Grids in one aqh_submit_grids_host call
@@ -409,6 +417,8 @@ class Hider:
         if av is not None:
             self._check(L.aqh_submit_aov_host(self.ctx, _p(av, _f32p), av.shape[0]), "aqh_submit_aov_host")
             keep.append(av)
+        if getattr(g, "lod", None) is not None:
+            self.set_lod_bounds(g.lod)
         self._packed_keep = keep
 
     def submit_grids_device(self, ngrids, d_cu, d_cv, d_nkeys, d_flags, d_pbase, d_cbase, d_tbase, d_times,

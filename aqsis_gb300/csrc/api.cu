@@ -337,6 +337,10 @@ struct aqh_ctx {
 	size_t hp_naov_vertices = 0;
 	const float* dev_aov = nullptr;
 	DevBuf d_aov, d_aovsrc, d_aovchan;
+	// level-of-detail bounds per grid (min, max), host copy
+	std::vector<float> h_lod;
+	bool lod_set = false;
+	DevBuf d_lod;
 
 	// host-submitted packed arrays (caller-owned, uploaded at render)
 	bool host_packed = false;
@@ -527,6 +531,8 @@ aqh_status aqh_frame_begin(aqh_ctx* ctx, const aqh_frame_desc* d) {
 	ctx->camera_set = false;
 	ctx->naov = 0;
 	ctx->h_aov.clear();
+	ctx->h_lod.clear();
+	ctx->lod_set = false;
 	ctx->hp_aov = nullptr;
 	ctx->hp_naov_vertices = 0;
 	ctx->dev_aov = nullptr;
@@ -943,6 +949,7 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	P.mbdof = fp.use_dof || fp.any_motion;
 	set_tiling(fp, ctx->tune.tile_pixels, ctx->tune.supertile_pixels);
 	fp.filter_ctas = ctx->tune.filter_ctas_per_sm;
+	fp.use_lod = (ctx->smp.lod != nullptr || ctx->lod_set) ? 1 : 0;
 	if (P.mbdof) {
 		ctx->h_dofb.clear();
 		dof_bounds_h(fp.xs, fp.ys, ctx->h_dofb);
@@ -1041,6 +1048,20 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	P.g = g;
 	AQH_TRY(ctx->d_idgrid.ensure(sizeof(int32_t) * (size_t)((P.nmps + 255) / 256 + 1)), "alloc id table");
 	P.g.id_grid = ctx->d_idgrid.as<int32_t>();
+	P.g.lod = nullptr;
+	if (ctx->lod_set && G > 0) {
+		// grids past the given bounds keep the attribute default (0, 1)
+		std::vector<float> b((size_t)G * 2);
+		for (int i = 0; i < G; ++i) {
+			const bool have = (size_t)(2 * i + 1) < ctx->h_lod.size();
+			b[2 * i] = have ? ctx->h_lod[2 * i] : 0.0f;
+			b[2 * i + 1] = have ? ctx->h_lod[2 * i + 1] : 1.0f;
+		}
+		AQH_TRY(ctx->d_lod.ensure(b.size() * 4), "alloc detail bounds");
+		AQH_TRY(cudaMemcpyAsync(ctx->d_lod.p, b.data(), b.size() * 4, cudaMemcpyHostToDevice, s), "upload detail bounds");
+		AQH_TRY(cudaStreamSynchronize(s), "upload detail bounds");
+		P.g.lod = ctx->d_lod.as<float2>();
+	}
 	if (ctx->dev_grids) {
 		if (ctx->naov > 0 && !ctx->dev_aov)
 			return ctx->fail(AQH_EINVAL, "output variables are set but aqh_submit_aov_device was not called");
@@ -1317,6 +1338,14 @@ aqh_status aqh_dspy_geometry_of(aqh_ctx* ctx, aqh_dspy_geometry* g) {
 	g->full_height = ctx->desc.height;
 	g->bucket_x = ctx->desc.bucket_x > 0 ? ctx->desc.bucket_x : 16;
 	g->bucket_y = ctx->desc.bucket_y > 0 ? ctx->desc.bucket_y : 16;
+	return AQH_OK;
+}
+
+aqh_status aqh_set_lod_bounds(aqh_ctx* ctx, const float* bounds, int ngrids) {
+	if (!ctx || ngrids < 0 || (ngrids > 0 && !bounds)) return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	ctx->h_lod.assign(bounds, bounds + (size_t)ngrids * 2);
+	ctx->lod_set = ngrids > 0;
 	return AQH_OK;
 }
 

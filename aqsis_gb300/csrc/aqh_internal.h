@@ -50,6 +50,8 @@ struct FrameParams {
 	int st_tiles;                            // tiles per super-tile side
 	int nstx, nsty;
 	int any_motion;
+	int use_lod;                             // level-of-detail tests can reject samples (sample detail
+	                                         // levels or grid bounds were given)
 	int ftab_n;                              // floats in the filter table
 	int filter_ctas;                         // filter CTAs per SM (0: by the samples' L2 footprint)
 };
@@ -74,6 +76,7 @@ struct GridsDev {
 	const float* aov;        // output variables, float[vertex][naov] indexed like Ci; null when naov == 0
 	int naov;
 	int colour3;             // Ci / Oi hold packed three-float entries (float[3 n]) rather than float4
+	const float2* lod;       // LevelOfDetailBounds (min, max) per grid, or null: (0, 1) for every grid
 };
 
 // Sample pattern caches (aqh_samples) in device memory.

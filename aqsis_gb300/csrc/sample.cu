@@ -54,11 +54,13 @@ struct RecS {
 	int bits;                      // 1 linear, 2 occluding store
 };  // 43 words: an odd stride spreads neighbouring records over the banks
 
-constexpr int kRecLinear = 1, kRecOccluding = 2, kRecTriangular = 4;  // RecS::bits; the grid index sits above bit 3
+// RecS::bits; the grid index sits above bit 4
+constexpr int kRecLinear = 1, kRecOccluding = 2, kRecTriangular = 4, kRecLod = 8;
+constexpr int kRecGridShift = 4;
 
 // The triangle split line of the record's grid (key 0: static micropolygons).
 __device__ __forceinline__ bool rec_keeps(const BinBuffers& bb, int bits, float x, float y) {
-	return !(bits & kRecTriangular) || triangle_keeps(__ldg(bb.tri + (size_t)(bits >> 3) * kMaxKeys), x, y);
+	return !(bits & kRecTriangular) || triangle_keeps(__ldg(bb.tri + (size_t)(bits >> kRecGridShift) * kMaxKeys), x, y);
 }
 
 struct SmemS {
@@ -146,7 +148,9 @@ __device__ __forceinline__ void build_record(const FrameParams& fp, const GridsD
 	}
 	int bits = h.linear ? kRecLinear : 0;
 	if (opaque || (gflags & 4)) bits |= kRecOccluding;
-	if (gflags & 16) bits |= kRecTriangular | (gi << 3);
+	if (gflags & 16) bits |= kRecTriangular;
+	if (lod_active(fp, g, gi)) bits |= kRecLod;
+	bits |= gi << kRecGridShift;
 	rec.bits = bits;
 }
 
@@ -464,6 +468,8 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 					// CqBound::Contains2D (bound.h:144-151) and early-z (bucketprocessor.cpp:1179)
 					ok = ok && !((x < r.bminx || x > r.bmaxx) || (y < r.bminy || y > r.bmaxy));
 					ok = ok && !(cullable && r.bminz > oz);
+					ok = ok && !((r.bits & kRecLod) && lod_rejects(fp, g, smp, r.bits >> kRecGridShift, px, py,
+					                                               sn * fp.xs + smm));
 					ok = ok && edges_inside(r.ym, r.xm, r.ex, r.ey, x, y);
 					bool stored = false;
 					if (ok) {
@@ -767,6 +773,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 			// CqBound::Contains2D (bound.h:144-151), early-z, fContains
 			if ((x < r.bminx || x > r.bmaxx) || (y < r.bminy || y > r.bmaxy)) continue;
 			if (r.bminz > key_depth(sm.prev[s])) continue;
+			if ((r.bits & kRecLod) && lod_rejects(fp, g, smp, r.bits >> kRecGridShift, px, py, si)) continue;
 			if (!edges_inside(r.ym, r.xm, r.ex, r.ey, x, y)) continue;
 			float u, v;
 			inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y, (r.bits & kRecLinear) != 0, x, y, u,
@@ -815,6 +822,8 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 							hit = px >= r.px0 && px < r.px1 && py >= r.py0 && py < r.py1 && smm >= m_lo && smm < m_hi &&
 							      sn >= n_lo && sn < n_hi &&
 							      !((x < r.bminx || x > r.bmaxx) || (y < r.bminy || y > r.bmaxy)) &&
+							      !((r.bits & kRecLod) &&
+							        lod_rejects(fp, g, smp, r.bits >> kRecGridShift, px, py, si)) &&
 							      edges_inside(r.ym, r.xm, r.ex, r.ey, x, y);
 							if (hit) {
 								float u, v;
@@ -1089,7 +1098,9 @@ sample_frag_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sa
 				const float x = (float)px + o.x, y = (float)py + o.y;
 				// Contains2D, early-z against occlZ = FLT_MAX, fContains, StoreSample's test
 				hit = !((x < r.bminx || x > r.bmaxx) || (y < r.bminy || y > r.bmaxy)) &&
-				      !(cullable && r.bminz > FLT_MAX) && edges_inside(r.ym, r.xm, r.ex, r.ey, x, y);
+				      !(cullable && r.bminz > FLT_MAX) &&
+				      !((r.bits & kRecLod) && lod_rejects(fp, g, smp, r.bits >> kRecGridShift, px, py, si)) &&
+				      edges_inside(r.ym, r.xm, r.ex, r.ey, x, y);
 				if (hit) {
 					inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y, (r.bits & kRecLinear) != 0, x,
 					             y, u, v);

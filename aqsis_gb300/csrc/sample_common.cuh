@@ -7,6 +7,28 @@
 
 namespace aqh {
 
+// The level-of-detail test of RenderMPG_Static / RenderMPG_MBOrDof
+// (bucketprocessor.cpp:1182-1190, 1404-1412, 1439-1447): a grid whose
+// LevelOfDetailBounds minimum is >= 0 (the attribute defaults to 0 1,
+// attributes.cpp:127) skips samples whose detail level lies outside
+// [min, max).  True when the grid has such a test that can fire this frame.
+__device__ __forceinline__ bool lod_active(const FrameParams& fp, const GridsDev& g, int gi) {
+	if (!fp.use_lod) return false;
+	return g.lod ? __ldg(g.lod + gi).x >= 0.0f : true;
+}
+// Sample si of sample-region pixel (px, py): is it outside grid gi's bounds?
+__device__ __forceinline__ bool lod_rejects(const FrameParams& fp, const GridsDev& g, const SamplerDev& smp, int gi,
+                                            int px, int py, int si) {
+	const float2 b = g.lod ? __ldg(g.lod + gi) : make_float2(0.0f, 1.0f);
+	float level = 0.0f;
+	if (smp.lod) {
+		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
+		const long long pat = smp.lod_index ? (long long)__ldg(smp.lod_index + pix) : pix;
+		level = __ldg(smp.lod + pat * fp.spp + si);
+	}
+	return b.x > level || level >= b.y;
+}
+
 // Entry i of a colour array (Ci or Oi): float4, or three packed floats when
 // the grids arrived in the three-float host layout.
 __device__ __forceinline__ float4 ld_colour(const GridsDev& g, const float4* p, long long i) {

@@ -266,7 +266,8 @@ __device__ __forceinline__ void build_mb_record(const FrameParams& fp, const Gri
 			opaque = opaque && (o.x >= 1.0f && o.y >= 1.0f && o.z >= 1.0f);
 		}
 	}
-	rr.bits = ((opaque || (gflags & 4)) ? 2 : 0) | ((gflags & 16) ? 4 : 0);
+	// bits: 2 occluding, 4 triangular, 8 level-of-detail test
+	rr.bits = ((opaque || (gflags & 4)) ? 2 : 0) | ((gflags & 16) ? 4 : 0) | (lod_active(fp, g, gi) ? 8 : 0);
 	rr.id = (int)(__ldg(g.mpbase + gi) + m);
 	rr.grid = gi;
 }
@@ -694,6 +695,7 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 								continue;
 							if ((x < TB.mnx || x > TB.mxx) || (y < TB.mny || y > TB.mxy)) continue;
 							if (cullable && B.mnz > oz) continue;
+							if ((r.bits & 8) && lod_rejects(fp, g, smp, r.grid, px, py, j)) continue;
 							float D, u, v;
 							if (!mb_sample(fp, r, moving, usingDof, x, y, stime, sdx, sdy, D, u, v, bb.tri)) continue;
 							if (cullable && oz <= D) continue;
@@ -1152,7 +1154,8 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 					const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + j);
 					const float2 d = lens_offset(smp, sm.dofidx[pl], spp, sm.kinv[s]);
 					float D, u, v;
-					if (mb_sample(fp, r, r.nkeys > 1, usingDof, (float)px + o.x, (float)py + o.y, sm.stime[s], d.x, d.y,
+					if (!((r.bits & 8) && lod_rejects(fp, g, smp, r.grid, px, py, j)) &&
+					    mb_sample(fp, r, r.nkeys > 1, usingDof, (float)px + o.x, (float)py + o.y, sm.stime[s], d.x, d.y,
 					              D, u, v, bb.tri)) {
 						if (!(D >= wz[lane]) || D == 0.0f)
 							atomicOr(&sm.flag[s >> 5], 1u << (s & 31));
@@ -1337,6 +1340,7 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 						int j0, j1;
 						if (!mb_slice(fp, sh, r, T, div, dt, sb, B, time0, time1, j0, j1)) continue;
 						if (j < j0 || j >= j1) continue;
+						if ((r.bits & 8) && lod_rejects(fp, g, smp, r.grid, px, py, j)) continue;
 						float D;
 						if (!mb_slice_test(fp, r, B, moving, time0, time1, dk, px, py, x, y, stime, d.x, d.y, oz, D, bb.tri))
 							continue;

@@ -117,6 +117,7 @@ class Grids:
     Oi: np.ndarray        # float32[NC, 4]
     culled: Optional[np.ndarray] = None  # uint8[total micropolygons]
     aov: Optional[np.ndarray] = None     # float32[NC, naov] output variables per vertex, indexed like Ci
+    lod: Optional[np.ndarray] = None     # float32[G, 2] LevelOfDetailBounds (min, max) per grid
 
     @property
     def ngrids(self) -> int:
@@ -316,6 +317,22 @@ def with_aov(scene: Scene, naov: int = 3, seed: int = 0) -> Scene:
     return Scene(scene.frame, dataclasses.replace(scene.grids, aov=aov), scene.samples)
 
 
+def with_lod(scene: Scene, seed: int = 0) -> Scene:
+    """The scene with seeded sample detail levels U[0, 1) and per-grid
+    LevelOfDetailBounds: a mix of off (-1 0), the default (0 1) and random
+    windows."""
+    rng = np.random.default_rng(seed)
+    n = np.asarray(scene.samples.pos).reshape(-1, 2).shape[0]
+    lod = rng.random(n).astype(np.float32)
+    G = scene.grids.ngrids
+    kind = rng.integers(0, 3, G)
+    lo = rng.uniform(0.0, 0.6, G)
+    hi = lo + rng.uniform(0.2, 0.6, G)
+    b = np.stack([np.where(kind == 0, -1.0, np.where(kind == 1, 0.0, lo)),
+                  np.where(kind == 0, 0.0, np.where(kind == 1, 1.0, hi))], -1).astype(np.float32)
+    return Scene(scene.frame, dataclasses.replace(scene.grids, lod=b), dataclasses.replace(scene.samples, lod=lod))
+
+
 def opaque_stream(width=1920, height=1080, ngrids=200_000, xs=4, ys=4, seed=0xC1,
                   npatterns=250, explicit_samples=False, filt=("gaussian", 2.0, 2.0)) -> Scene:
     """Opaque synthetic stream: 16x16-quad raster grids, Oi = 1, PixelSamples xs ys."""
@@ -472,7 +489,8 @@ def to_camera_space(scene: Scene, m=None, every: int = 1, **camera_kw) -> Scene:
 # ---------------------------------------------------------------------------
 # Scene files
 
-_GRID_KEYS = ("cu", "cv", "nkeys", "flags", "pbase", "cbase", "tbase", "times", "P", "Ci", "Oi", "culled", "aov")
+_GRID_KEYS = ("cu", "cv", "nkeys", "flags", "pbase", "cbase", "tbase", "times", "P", "Ci", "Oi", "culled", "aov",
+              "lod")
 _SAMPLE_KEYS = ("pos", "time", "dof", "shuffle", "lod", "pos_index", "dof_index", "time_index",
                 "shuffle_index", "lod_index", "dither")
 

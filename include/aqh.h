@@ -325,6 +325,15 @@ aqh_status aqh_read_display(aqh_ctx* ctx, const aqh_display* d, void* out, size_
 aqh_status aqh_read_samples(aqh_ctx* ctx, int32_t* winner, float* occlz, int32_t* nfrag,
                             uint8_t* valid, float* sdata, size_t nsamples);
 
+/* ---- level of detail ------------------------------------------------------------ */
+/* LevelOfDetailBounds per grid (RiDetailRange; attribute default 0 1,
+ * attributes.cpp:127): float[ngrids][2] (min, max) in submission order,
+ * copied; grids beyond `ngrids` keep 0 1.  A grid whose min is >= 0 is not
+ * sampled by samples whose detail level (aqh_samples.lod, 0 when NULL) lies
+ * outside [min, max) (RenderMPG_Static / _MBOrDof, bucketprocessor.cpp:
+ * 1182-1190, 1404-1412, 1439-1447).  Reset by aqh_frame_begin. */
+aqh_status aqh_set_lod_bounds(aqh_ctx* ctx, const float* bounds, int ngrids);
+
 /* ---- arbitrary output variables ----------------------------------------------- */
 /* Extra float channels per vertex: the shader outputs a display asks for
  * (CqRenderer's output data map).  Each stored hit carries its

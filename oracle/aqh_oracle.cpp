@@ -207,6 +207,11 @@ struct MP {
 	float col[4][3], opa[4][3];
 	bool smooth, isOpaque, isCullable;
 	int matteFlag;
+	// SqGridInfo::lodBounds (micropolygon.cpp:64-66; attribute default 0 1,
+	// attributes.cpp:127); the test runs when the minimum is >= 0
+	float lodMin, lodMax;
+	bool lodTest() const { return lodMin >= 0.0f; }
+	bool lodRejects(float level) const { return lodMin > level || level >= lodMax; }
 };
 
 static inline V3 loadP(const float* P, long long vtx) {
@@ -591,6 +596,8 @@ static void renderStatic(Frame& fr, MP& mp) {
 					fr.splCount++;
 					if (!Bound.contains2D(sd.position)) continue;
 					if (mp.isCullable && Bound.mn.z > sd.occlZ) continue;
+					// level of detail (bucketprocessor.cpp:1182-1190)
+					if (mp.lodTest() && mp.lodRejects(sd.lod)) continue;
 					fr.splBoundHits++;
 					float D;
 					V2 uv;
@@ -758,6 +765,8 @@ static void renderMBOrDof(Frame& fr, MP& mp, bool isMoving, bool usingDof, const
 							if (!B.contains2D(vecP)) continue;
 						}
 						if (mp.isCullable && B.mn.z > sd.occlZ) continue;
+						// level of detail (bucketprocessor.cpp:1404-1412, 1439-1447)
+						if (mp.lodTest() && mp.lodRejects(sd.lod)) continue;
 						fr.splBoundHits++;
 						float D;
 						V2 uv;
@@ -1089,6 +1098,8 @@ extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples
 				}
 				// Output cache (micropolygon.cpp:1464-1529)
 				mp.smooth = (flags & ORC_GRID_SMOOTH) != 0;
+				mp.lodMin = g->lod ? g->lod[2 * gi] : 0.0f;
+				mp.lodMax = g->lod ? g->lod[2 * gi + 1] : 1.0f;
 				mp.matteFlag = flags & (ORC_GRID_MATTE | ORC_GRID_MATTEALPHA);
 				mp.isCullable = cullable;
 				const int vidx[4] = {index, index + 1, index + cu + 1, index + cu + 2};

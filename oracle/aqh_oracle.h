@@ -74,6 +74,7 @@ typedef struct {
 	const uint8_t* culled;    /* per micropolygon (global mp id) 1 = culled, or NULL */
 	const float* aov;         /* output variables float[vertex][naov] indexed like Ci, or NULL */
 	int32_t naov;
+	const float* lod;         /* LevelOfDetailBounds float[grid][2] (min, max), or NULL = (0, 1) */
 } OrcGrids;
 
 typedef struct {

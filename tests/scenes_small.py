@@ -281,8 +281,8 @@ def fuzz(seed):
         culled[rng.integers(0, grids.micropolygons, max(1, grids.micropolygons // 10))] = 1
         grids.culled = culled
     sc = custom(fr, grids, seed=seed, dither=fr.q_dither > 0)
-    if dof:
-        mult, _ = sc.frame.dof_terms()
+    if rng.random() < 0.25:
+        sc = S.with_lod(sc, seed=seed)
     return sc
 
 
