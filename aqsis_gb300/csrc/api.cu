@@ -553,8 +553,29 @@ aqh_status aqh_set_samples(aqh_ctx* ctx, const aqh_samples* s) {
 	const size_t np = (size_t)s->npatterns * fp.spp;
 	const size_t npix = (size_t)fp.sw * fp.sh;
 	const size_t ndisp = (size_t)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
-	if (!s->pos_index && (size_t)s->npatterns < npix)
-		return ctx->fail(AQH_EINVAL, "explicit samples need one pattern per pixel of the %dx%d sample region", fp.sw, fp.sh);
+	// every table is read at (pattern of the pixel) * spp: a table without a
+	// per-pixel choice needs one pattern per pixel, and every choice must name
+	// an existing pattern
+	struct Table { const void* data; const uint32_t* index; const char* name; };
+	const Table tables[5] = {{s->pos, s->pos_index, "positions"}, {s->time, s->time_index, "times"},
+	                         {s->dof, s->dof_index, "lens positions"}, {s->shuffle, s->shuffle_index, "lens shuffles"},
+	                         {s->lod, s->lod_index, "detail levels"}};
+	for (const Table& t : tables) {
+		if (!t.data) continue;
+		if (!t.index && (size_t)s->npatterns < npix)
+			return ctx->fail(AQH_EINVAL, "sample %s without pattern choices need one pattern per pixel of the %dx%d "
+			                 "sample region", t.name, fp.sw, fp.sh);
+		if (t.index)
+			for (size_t i = 0; i < npix; ++i)
+				if (t.index[i] >= (uint32_t)s->npatterns)
+					return ctx->fail(AQH_EINVAL, "pattern choice %u for sample %s at pixel %zu; %d patterns",
+					                 t.index[i], t.name, i, s->npatterns);
+	}
+	if (s->shuffle) {
+		for (size_t i = 0; i < np; ++i)
+			if (s->shuffle[i] < 0 || s->shuffle[i] >= fp.spp)
+				return ctx->fail(AQH_EINVAL, "lens shuffle entry %d out of range", s->shuffle[i]);
+	}
 	SamplerDev& m = ctx->smp;
 	std::memset(&m, 0, sizeof m);
 	m.npatterns = s->npatterns;

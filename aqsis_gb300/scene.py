@@ -330,7 +330,9 @@ def with_lod(scene: Scene, seed: int = 0) -> Scene:
     hi = lo + rng.uniform(0.2, 0.6, G)
     b = np.stack([np.where(kind == 0, -1.0, np.where(kind == 1, 0.0, lo)),
                   np.where(kind == 0, 0.0, np.where(kind == 1, 1.0, hi))], -1).astype(np.float32)
-    return Scene(scene.frame, dataclasses.replace(scene.grids, lod=b), dataclasses.replace(scene.samples, lod=lod))
+    # detail levels live in a table of the same patterns as the positions
+    smp = dataclasses.replace(scene.samples, lod=lod, lod_index=scene.samples.pos_index)
+    return Scene(scene.frame, dataclasses.replace(scene.grids, lod=b), smp)
 
 
 def opaque_stream(width=1920, height=1080, ngrids=200_000, xs=4, ys=4, seed=0xC1,
