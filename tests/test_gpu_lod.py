@@ -28,3 +28,27 @@ def test_detail_bounds_match_oracle(aqh_lib, oracle, name, batched):
     finally:
         h.close()
     compare(res, oracle.render(sc))
+
+
+def test_sample_tables_are_checked(aqh_lib):
+    """A table without pattern choices needs one pattern per pixel, and
+    choices must name existing patterns: both are refused on the host
+    before anything reads them."""
+    import dataclasses
+    import numpy as np
+    from aqsis_gb300.aqh import AqhError
+    sc = SS.opaque_small(seed=76, scale=0.02)
+    smp = sc.samples
+    assert smp.pos_index is not None and smp.npatterns < sc.frame.sample_region[2] * sc.frame.sample_region[3]
+    n = np.asarray(smp.pos).reshape(-1, 2).shape[0]
+    h = aqh_lib.Hider(0)
+    try:
+        h.frame_begin(sc.frame)
+        with pytest.raises(AqhError):
+            h.set_samples(dataclasses.replace(smp, lod=np.zeros(n, np.float32), lod_index=None))
+        bad = np.array(smp.pos_index, np.uint32, copy=True)
+        bad[3] = smp.npatterns
+        with pytest.raises(AqhError):
+            h.set_samples(dataclasses.replace(smp, pos_index=bad))
+    finally:
+        h.close()
