@@ -192,6 +192,7 @@ def load(build_if_missing: bool = False):
     L.aqh_set_camera_to_raster.argtypes = [vp, _f32p]
     L.aqh_set_aov_count.argtypes = [vp, C.c_int]
     L.aqh_set_lod_bounds.argtypes = [vp, _f32p, C.c_int]
+    L.aqh_set_csg.argtypes = [vp, _i32p, _i32p, C.c_int, _i32p, C.c_int]
     L.aqh_dspy_geometry_of.argtypes = [vp, C.POINTER(DspyGeometry)]
     L.aqh_dspy_open.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(DspyGeometry), C.POINTER(Display),
                                 C.POINTER(C.c_char_p), C.POINTER(vp)]
@@ -216,7 +217,8 @@ def load(build_if_missing: bool = False):
                  "aqh_read_samples", "aqh_get_stats", "aqh_test_invbilinear", "aqh_set_tuning", "aqh_get_tuning",
                  "aqh_autotune", "aqh_set_camera_to_raster", "aqh_read_display", "aqh_set_aov_count",
                  "aqh_submit_aov_host", "aqh_submit_aov_device", "aqh_read_aov", "aqh_dspy_geometry_of",
-                 "aqh_dspy_open", "aqh_dspy_send", "aqh_dspy_send_image", "aqh_dspy_close", "aqh_set_lod_bounds"):
+                 "aqh_dspy_open", "aqh_dspy_send", "aqh_dspy_send_image", "aqh_dspy_close", "aqh_set_lod_bounds",
+                 "aqh_set_csg"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -335,6 +337,16 @@ class Hider:
         b = np.ascontiguousarray(bounds, np.float32).reshape(-1, 2)
         self._check(self.L.aqh_set_lod_bounds(self.ctx, _p(b, _f32p), b.shape[0]), "aqh_set_lod_bounds")
 
+    def set_csg(self, node_type, node_parent, grid_node):
+        """The frame's CSG trees and each grid's primitive node (aqh_set_csg)."""
+        t = np.ascontiguousarray(node_type, np.int32).ravel()
+        par = np.ascontiguousarray(node_parent, np.int32).ravel()
+        gn = np.ascontiguousarray(grid_node, np.int32).ravel()
+        if t.shape != par.shape:
+            raise ValueError("node_type and node_parent differ in length")
+        self._check(self.L.aqh_set_csg(self.ctx, _p(t, _i32p), _p(par, _i32p), t.shape[0], _p(gn, _i32p),
+                                       gn.shape[0]), "aqh_set_csg")
+
     def set_aov_count(self, n: int):
         """Output variables per vertex for this frame (aqh_set_aov_count), before any grid."""
         self._check(self.L.aqh_set_aov_count(self.ctx, int(n)), "aqh_set_aov_count")
@@ -380,6 +392,8 @@ class Hider:
             mpbase += cu * cv
         if getattr(g, "lod", None) is not None:
             self.set_lod_bounds(g.lod)
+        if getattr(g, "csg_node", None) is not None:
+            self.set_csg(g.csg_type, g.csg_parent, g.csg_node)
 
     def submit_grids_host(self, g, packed3: bool = False):
         """Submit a whole packed scene.Grids in one aqh_submit_grids_host call
@@ -419,6 +433,8 @@ class Hider:
             keep.append(av)
         if getattr(g, "lod", None) is not None:
             self.set_lod_bounds(g.lod)
+        if getattr(g, "csg_node", None) is not None:
+            self.set_csg(g.csg_type, g.csg_parent, g.csg_node)
         self._packed_keep = keep
 
     def submit_grids_device(self, ngrids, d_cu, d_cv, d_nkeys, d_flags, d_pbase, d_cbase, d_tbase, d_times,

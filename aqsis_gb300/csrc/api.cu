@@ -341,6 +341,10 @@ struct aqh_ctx {
 	std::vector<float> h_lod;
 	bool lod_set = false;
 	DevBuf d_lod;
+	// CSG: the tree and each grid's node, host arrays laid out for CsgDev
+	int csg_n = 0;
+	std::vector<int32_t> csg_grid_node, csg_type, csg_parent, csg_child, csg_nch, csg_pfirst, csg_pcount, csg_post;
+	DevBuf d_csg, d_csg_overflow;
 
 	// host-submitted packed arrays (caller-owned, uploaded at render)
 	bool host_packed = false;
@@ -533,6 +537,7 @@ aqh_status aqh_frame_begin(aqh_ctx* ctx, const aqh_frame_desc* d) {
 	ctx->h_aov.clear();
 	ctx->h_lod.clear();
 	ctx->lod_set = false;
+	ctx->csg_n = 0;
 	ctx->hp_aov = nullptr;
 	ctx->hp_naov_vertices = 0;
 	ctx->dev_aov = nullptr;
@@ -1039,7 +1044,7 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	FragPool& pool = P.pool;
 	pool = FragPool{};
 	fp.frag_only = 0;
-	if (ctx->any_transparent || !fp.cullable || fp.midpoint_store) {
+	if (ctx->any_transparent || !fp.cullable || fp.midpoint_store || ctx->csg_n > 0) {
 		if (ctx->frag_capacity == 0) ctx->frag_capacity = std::max<int64_t>(1 << 20, (int64_t)P.nsamp * 2);
 		AQH_TRY(ctx->d_frag.ensure(ctx->frag_capacity * sizeof(float4)), "alloc fragments");
 		AQH_TRY(ctx->d_next.ensure(ctx->frag_capacity * sizeof(int32_t)), "alloc fragments");
@@ -1069,6 +1074,46 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	P.g = g;
 	AQH_TRY(ctx->d_idgrid.ensure(sizeof(int32_t) * (size_t)((P.nmps + 255) / 256 + 1)), "alloc id table");
 	P.g.id_grid = ctx->d_idgrid.as<int32_t>();
+	P.g.csg = CsgDev{};
+	if (ctx->csg_n > 0) {
+		// one buffer: grid nodes (G, -1 past the given ones), then the node tables
+		const int N = ctx->csg_n;
+		std::vector<int32_t> buf;
+		buf.reserve((size_t)G + 7 * N + ctx->csg_post.size());
+		for (int i = 0; i < G; ++i) buf.push_back(i < (int)ctx->csg_grid_node.size() ? ctx->csg_grid_node[i] : -1);
+		const size_t o_type = buf.size();
+		buf.insert(buf.end(), ctx->csg_type.begin(), ctx->csg_type.end());
+		const size_t o_parent = buf.size();
+		buf.insert(buf.end(), ctx->csg_parent.begin(), ctx->csg_parent.end());
+		const size_t o_child = buf.size();
+		buf.insert(buf.end(), ctx->csg_child.begin(), ctx->csg_child.end());
+		const size_t o_nch = buf.size();
+		buf.insert(buf.end(), ctx->csg_nch.begin(), ctx->csg_nch.end());
+		const size_t o_pf = buf.size();
+		buf.insert(buf.end(), ctx->csg_pfirst.begin(), ctx->csg_pfirst.end());
+		const size_t o_pc = buf.size();
+		buf.insert(buf.end(), ctx->csg_pcount.begin(), ctx->csg_pcount.end());
+		const size_t o_post = buf.size();
+		buf.insert(buf.end(), ctx->csg_post.begin(), ctx->csg_post.end());
+		buf.push_back(0);
+		AQH_TRY(ctx->d_csg.ensure(buf.size() * 4), "alloc CSG tree");
+		AQH_TRY(cudaMemcpyAsync(ctx->d_csg.p, buf.data(), buf.size() * 4, cudaMemcpyHostToDevice, s), "upload CSG tree");
+		AQH_TRY(ctx->d_csg_overflow.ensure(16), "alloc");
+		AQH_TRY(cudaMemsetAsync(ctx->d_csg_overflow.p, 0, 4, s), "memset");
+		AQH_TRY(cudaStreamSynchronize(s), "upload CSG tree");
+		const int32_t* b = ctx->d_csg.as<int32_t>();
+		CsgDev& c = P.g.csg;
+		c.nnodes = N;
+		c.grid_node = b;
+		c.type = b + o_type;
+		c.parent = b + o_parent;
+		c.child_index = b + o_child;
+		c.nchildren = b + o_nch;
+		c.post_first = b + o_pf;
+		c.post_count = b + o_pc;
+		c.post = b + o_post;
+		c.overflow = ctx->d_csg_overflow.as<int32_t>();
+	}
 	P.g.lod = nullptr;
 	if (ctx->lod_set && G > 0) {
 		// grids past the given bounds keep the attribute default (0, 1)
@@ -1196,6 +1241,7 @@ static aqh_status render_plain(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 			AQH_TRY(cudaMemsetAsync(P.pool.count, 0, 8, s), "memset");
 			AQH_TRY(cudaMemsetAsync(P.pool.overflow, 0, 4, s), "memset");
 		}
+		if (P.g.csg.nnodes > 0) AQH_TRY(cudaMemsetAsync(P.g.csg.overflow, 0, 4, s), "memset");
 		cudaEventRecord(ctx->ev[1], s);
 		if (P.mbdof) {
 			if (ctx->cioi_pending) AQH_TRY(cudaStreamWaitEvent(s, ctx->ev_cioi, 0), "wait for colours");
@@ -1222,6 +1268,14 @@ static aqh_status render_plain(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 		P.pool.next = ctx->d_next.as<int32_t>();
 		P.pool.capacity = ctx->frag_capacity;
 		ctx->graph_valid = false;
+	}
+	if (P.g.csg.nnodes > 0) {
+		int32_t co = 0;
+		AQH_TRY(cudaMemcpyAsync(&co, P.g.csg.overflow, 4, cudaMemcpyDeviceToHost, s), "readback");
+		AQH_TRY(cudaStreamSynchronize(s), "sample");
+		if (co)
+			return ctx->fail(AQH_ELIMIT, "CSG: a sample holds more than %d fragments, or a NaN depth, or the tree "
+			                 "needed more than 64 resolve rounds", 24);
 	}
 	cudaEventRecord(ctx->ev[2], s);
 	// the frame's r g b a display is quantized in the filter pass when it fits 8 bits
@@ -1312,8 +1366,9 @@ aqh_status aqh_render(aqh_ctx* ctx, int sync) {
 	ctx->stats.micropolygons = P.nmps;
 	ctx->stats.samples = (int64_t)P.nsamp;
 	ctx->stats.grids = P.g.ngrids;
-	if (ctx->mode == AQH_MODE_BATCHED) return render_batched(ctx, P, sync != 0);
-	return render_plain(ctx, P, sync != 0);
+	// CSG frames take the plain path, which reads the resolve's overflow flag
+	if (ctx->mode == AQH_MODE_BATCHED && P.g.csg.nnodes == 0) return render_batched(ctx, P, sync != 0);
+	return render_plain(ctx, P, sync != 0 || P.g.csg.nnodes > 0);
 }
 
 aqh_status aqh_synchronize(aqh_ctx* ctx) {
@@ -1359,6 +1414,63 @@ aqh_status aqh_dspy_geometry_of(aqh_ctx* ctx, aqh_dspy_geometry* g) {
 	g->full_height = ctx->desc.height;
 	g->bucket_x = ctx->desc.bucket_x > 0 ? ctx->desc.bucket_x : 16;
 	g->bucket_y = ctx->desc.bucket_y > 0 ? ctx->desc.bucket_y : 16;
+	return AQH_OK;
+}
+
+aqh_status aqh_set_csg(aqh_ctx* ctx, const int32_t* node_type, const int32_t* node_parent, int nnodes,
+                       const int32_t* grid_node, int ngrids) {
+	if (!ctx || nnodes < 0 || ngrids < 0 || (nnodes > 0 && (!node_type || !node_parent)) || (ngrids > 0 && !grid_node))
+		return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	ctx->csg_n = 0;
+	if (nnodes == 0) return AQH_OK;
+	std::vector<int32_t> nch(nnodes, 0), child(nnodes, 0);
+	for (int i = 0; i < nnodes; ++i) {
+		if (node_type[i] < 0 || node_type[i] > 3) return ctx->fail(AQH_EINVAL, "CSG node %d: bad type %d", i, node_type[i]);
+		const int p = node_parent[i];
+		if (p < -1 || p >= nnodes) return ctx->fail(AQH_EINVAL, "CSG node %d: bad parent %d", i, p);
+		if (p >= 0) {
+			if (node_type[p] == 0) return ctx->fail(AQH_EINVAL, "CSG node %d: a primitive cannot have children", p);
+			child[i] = nch[p]++;
+			if (nch[p] > 32) return ctx->fail(AQH_ELIMIT, "CSG node %d: more than 32 children", p);
+		}
+		// no cycles: the walk up ends within nnodes steps
+		int up = p, steps = 0;
+		while (up >= 0 && steps <= nnodes) { up = node_parent[up]; ++steps; }
+		if (up >= 0) return ctx->fail(AQH_EINVAL, "CSG node %d: its parents form a cycle", i);
+	}
+	for (int i = 0; i < ngrids; ++i)
+		if (grid_node[i] < -1 || grid_node[i] >= nnodes) return ctx->fail(AQH_EINVAL, "grid %d: bad CSG node", i);
+	// per node, the non-primitive nodes of its subtree with children first
+	// (children in index order, as CqCSGTreeNode::ProcessSampleList recurses)
+	std::vector<std::vector<int>> kids(nnodes);
+	for (int i = 0; i < nnodes; ++i)
+		if (node_parent[i] >= 0) kids[node_parent[i]].push_back(i);
+	std::vector<int32_t> pfirst(nnodes), pcount(nnodes), post;
+	for (int n = 0; n < nnodes; ++n) {
+		pfirst[n] = (int32_t)post.size();
+		std::vector<std::pair<int, size_t>> stack{{n, 0}};
+		while (!stack.empty()) {
+			auto& top = stack.back();
+			if (top.second < kids[top.first].size()) {
+				const int c = kids[top.first][top.second++];
+				if (node_type[c] != 0) stack.push_back({c, 0});
+			} else {
+				if (node_type[top.first] != 0) post.push_back(top.first);
+				stack.pop_back();
+			}
+		}
+		pcount[n] = (int32_t)post.size() - pfirst[n];
+	}
+	ctx->csg_type.assign(node_type, node_type + nnodes);
+	ctx->csg_parent.assign(node_parent, node_parent + nnodes);
+	ctx->csg_child = child;
+	ctx->csg_nch = nch;
+	ctx->csg_pfirst = pfirst;
+	ctx->csg_pcount = pcount;
+	ctx->csg_post = post;
+	ctx->csg_grid_node.assign(grid_node, grid_node + ngrids);
+	ctx->csg_n = nnodes;
 	return AQH_OK;
 }
 

@@ -56,6 +56,21 @@ struct FrameParams {
 	int filter_ctas;                         // filter CTAs per SM (0: by the samples' L2 footprint)
 };
 
+// CSG trees (RiSolidBegin / RiSolidEnd) in device memory.  Node types:
+// 0 primitive, 1 union, 2 intersection, 3 difference.
+struct CsgDev {
+	int nnodes;                  // 0: no CSG in the frame
+	const int32_t* grid_node;    // per grid: its primitive node, -1 none
+	const int32_t* type;         // per node
+	const int32_t* parent;       // per node, -1 for a root
+	const int32_t* child_index;  // per node: its place among its parent's children
+	const int32_t* nchildren;    // per node
+	const int32_t* post_first;   // per node: the non-primitive nodes of its subtree, children
+	const int32_t* post_count;   //   before parents, at post[post_first .. + post_count)
+	const int32_t* post;
+	int32_t* overflow;           // set when a sample's CSG list exceeds what Combine holds
+};
+
 // Grid stream in device memory (aqh_submit_grids_device layout).
 struct GridsDev {
 	int ngrids;
@@ -77,6 +92,7 @@ struct GridsDev {
 	int naov;
 	int colour3;             // Ci / Oi hold packed three-float entries (float[3 n]) rather than float4
 	const float2* lod;       // LevelOfDetailBounds (min, max) per grid, or null: (0, 1) for every grid
+	CsgDev csg;
 };
 
 // Sample pattern caches (aqh_samples) in device memory.

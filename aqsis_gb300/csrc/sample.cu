@@ -54,9 +54,10 @@ struct RecS {
 	int bits;                      // 1 linear, 2 occluding store
 };  // 43 words: an odd stride spreads neighbouring records over the banks
 
-// RecS::bits; the grid index sits above bit 4
-constexpr int kRecLinear = 1, kRecOccluding = 2, kRecTriangular = 4, kRecLod = 8;
-constexpr int kRecGridShift = 4;
+// RecS::bits; the grid index sits above bit 5.  kRecCsg: a CSG solid's
+// micropolygon, never occlusion-cullable.
+constexpr int kRecLinear = 1, kRecOccluding = 2, kRecTriangular = 4, kRecLod = 8, kRecCsg = 16;
+constexpr int kRecGridShift = 5;
 
 // The triangle split line of the record's grid (key 0: static micropolygons).
 __device__ __forceinline__ bool rec_keeps(const BinBuffers& bb, int bits, float x, float y) {
@@ -150,6 +151,7 @@ __device__ __forceinline__ void build_record(const FrameParams& fp, const GridsD
 	if (opaque || (gflags & 4)) bits |= kRecOccluding;
 	if (gflags & 16) bits |= kRecTriangular;
 	if (lod_active(fp, g, gi)) bits |= kRecLod;
+	if (csg_grid(g, gi)) bits = (bits & ~kRecOccluding) | kRecCsg;
 	bits |= gi << kRecGridShift;
 	rec.bits = bits;
 }
@@ -183,8 +185,9 @@ __device__ __forceinline__ void resolve_sample(const FrameParams& fp, const Grid
 	bool valid = w >= 0;
 	int src = w;
 	if (TRANSP && head >= 0) {
-		nf = combine_fragments(fp, g, pool, head, w >= 0, oz, occl, occl_flags, w, src);
-		valid = true;
+		bool emptied = false;
+		nf = combine_fragments(fp, g, pool, head, w >= 0, oz, occl, occl_flags, w, src, emptied);
+		valid = !emptied;
 	}
 	if (nf == 0 && valid) {
 		// imagepixel.cpp:303-330: opaque matte hits become transparent black;
@@ -226,7 +229,7 @@ __device__ __forceinline__ bool stage_candidates(const FrameParams& fp, const Gr
 				gid = bb.st_list[li];
 				const int4 rc = bb.grid_rect[gid];
 				f = rc.x < rc.y && rc.x < tpx1 && rc.y > tpx0 && rc.z < tpy1 && rc.w > tpy0;
-				if (f && cullable) {
+				if (f && cullable && !csg_grid(g, gid)) {
 					// whole grid behind every sample of the 4x4-pixel blocks it overlaps
 					const int bx0 = (max(rc.x, tpx0) - tpx0) >> 2, bx1 = (min(rc.y, tpx1) - 1 - tpx0) >> 2;
 					const int by0 = (max(rc.z, tpy0) - tpy0) >> 2, by1 = (min(rc.w, tpy1) - 1 - tpy0) >> 2;
@@ -322,7 +325,7 @@ __device__ __forceinline__ bool stage_candidates(const FrameParams& fp, const Gr
 			const int sX = max((int)floorf(bminx), tpx0), eX = min(lceil_f(bmaxx), tpx1);
 			const int sY = max((int)floorf(bminy), tpy0), eY = min(lceil_f(bmaxy), tpy1);
 			active = !culled && !cropped && sX < eX && sY < eY;
-			if (active && cullable) {
+			if (active && cullable && !csg_grid(g, gid)) {
 				// early-z for every pixel it visits: behind all their samples' occluding depths
 				float mx = -FLT_MAX;
 				for (int yy = sY; yy < eY; ++yy)
@@ -456,7 +459,8 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 					const int b = __ffs(bits) - 1;
 					bits &= bits - 1u;
 					const RecS& r = sm.rec[wd * 32 + b];
-					if (cullable && r.bminz > gmax) continue;  // hidden from all 32 samples
+					const bool rcull = cullable && !(r.bits & kRecCsg);  // CSG: never occlusion-culled
+					if (rcull && r.bminz > gmax) continue;  // hidden from all 32 samples
 					bool ok = valid && px >= r.px0 && px < r.px1 && py >= r.py0 && py < r.py1;
 					if (ok) {
 						const int m_lo = (px == r.px0) ? r.im : 0;
@@ -467,7 +471,7 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 					}
 					// CqBound::Contains2D (bound.h:144-151) and early-z (bucketprocessor.cpp:1179)
 					ok = ok && !((x < r.bminx || x > r.bmaxx) || (y < r.bminy || y > r.bmaxy));
-					ok = ok && !(cullable && r.bminz > oz);
+					ok = ok && !(rcull && r.bminz > oz);
 					ok = ok && !((r.bits & kRecLod) && lod_rejects(fp, g, smp, r.bits >> kRecGridShift, px, py,
 					                                               sn * fp.xs + smm));
 					ok = ok && edges_inside(r.ym, r.xm, r.ex, r.ey, x, y);
@@ -478,8 +482,8 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 						             (r.bits & kRecLinear) != 0, x, y, u, v);
 						const float D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
 						// StoreSample (bucketprocessor.cpp:1471-1569) for a hit the split line keeps
-						if (rec_keeps(bb, r.bits, x, y) && !(cullable && oz <= D)) {
-							if ((r.bits & kRecOccluding) && cullable) {
+						if (rec_keeps(bb, r.bits, x, y) && !(rcull && oz <= D)) {
+							if ((r.bits & kRecOccluding) && rcull) {
 								if (TRANSP && fp.midpoint_store) {
 									// midpoint filter with a z display (bucketprocessor.cpp:1502-1530):
 									// occlZ follows the second-nearest opaque depth, the hit the nearest
@@ -1098,14 +1102,14 @@ sample_frag_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sa
 				const float x = (float)px + o.x, y = (float)py + o.y;
 				// Contains2D, early-z against occlZ = FLT_MAX, fContains, StoreSample's test
 				hit = !((x < r.bminx || x > r.bmaxx) || (y < r.bminy || y > r.bmaxy)) &&
-				      !(cullable && r.bminz > FLT_MAX) &&
+				      !(cullable && !(r.bits & kRecCsg) && r.bminz > FLT_MAX) &&
 				      !((r.bits & kRecLod) && lod_rejects(fp, g, smp, r.bits >> kRecGridShift, px, py, si)) &&
 				      edges_inside(r.ym, r.xm, r.ex, r.ey, x, y);
 				if (hit) {
 					inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y, (r.bits & kRecLinear) != 0, x,
 					             y, u, v);
 					D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
-					hit = rec_keeps(bb, r.bits, x, y) && !(cullable && FLT_MAX <= D);
+					hit = rec_keeps(bb, r.bits, x, y) && !(cullable && !(r.bits & kRecCsg) && FLT_MAX <= D);
 					id = r.id;
 				}
 			}

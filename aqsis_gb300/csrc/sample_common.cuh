@@ -29,6 +29,72 @@ __device__ __forceinline__ bool lod_rejects(const FrameParams& fp, const GridsDe
 	return b.x > level || level >= b.y;
 }
 
+// Does grid gi belong to a CSG solid?  Such micropolygons are never
+// occlusion-cullable (bucketprocessor.cpp:1074-1080).
+__device__ __forceinline__ bool csg_grid(const GridsDev& g, int gi) {
+	return g.csg.nnodes > 0 && __ldg(g.csg.grid_node + gi) >= 0;
+}
+
+// CqCSGNode*::EvaluateState (csgtree.cpp:280-351) over the child in/out bits.
+__device__ __forceinline__ bool csg_eval(int type, uint32_t st, int nch) {
+	if (type == 1) return st != 0u;
+	if (type == 2) return st == (nch >= 32 ? 0xffffffffu : ((1u << nch) - 1u));
+	if (type == 3) return nch >= 1 && (st & 1u) && !(st & ~1u);
+	return false;
+}
+
+// The CSG resolve of Combine (imagepixel.cpp:170-190; csgtree.cpp:144-258)
+// over a depth-sorted entry list: while an entry still names a node, the
+// tree holding the first such entry is processed from its top, node by node
+// with children first; at each node the child states start false, every
+// entry of a child toggles its state, entries that leave the node's state
+// unchanged are dropped and the rest are promoted to the node (to none at
+// the top).  A primitive at the top just releases its entries.  Returns
+// false if the trees are not processed within the bound (flagged).
+template <class E>
+__device__ inline bool csg_resolve(const CsgDev& c, E* ent, int* node, int& n) {
+	for (int round = 0; round < 64; ++round) {
+		int start = -1;
+		for (int i = 0; i < n && start < 0; ++i) start = node[i];
+		if (start < 0) return true;
+		int top = start;
+		for (int up = 0; up < c.nnodes && __ldg(c.parent + top) >= 0; ++up) top = __ldg(c.parent + top);
+		if (__ldg(c.type + top) == 0) {
+			for (int i = 0; i < n; ++i)
+				if (node[i] == top) node[i] = -1;
+			continue;
+		}
+		const int pf = __ldg(c.post_first + top), pc = __ldg(c.post_count + top);
+		for (int q = 0; q < pc; ++q) {
+			const int nd = __ldg(c.post + pf + q);
+			const int ty = __ldg(c.type + nd), nch = __ldg(c.nchildren + nd);
+			const int promote = __ldg(c.parent + nd) >= 0 ? nd : -1;
+			uint32_t st = 0u;
+			bool cur = csg_eval(ty, st, nch);
+			int w = 0;
+			for (int i = 0; i < n; ++i) {
+				const int e = node[i];
+				if (e < 0 || __ldg(c.parent + e) != nd) {
+					ent[w] = ent[i];
+					node[w] = e;
+					++w;
+					continue;
+				}
+				st ^= 1u << __ldg(c.child_index + e);
+				const bool nw = csg_eval(ty, st, nch);
+				if (nw == cur) continue;  // no change: the entry goes
+				cur = nw;
+				ent[w] = ent[i];
+				node[w] = promote;
+				++w;
+			}
+			n = w;
+		}
+	}
+	if (c.overflow) atomicOr(c.overflow, 1);
+	return false;
+}
+
 // Entry i of a colour array (Ci or Oi): float4, or three packed floats when
 // the grids arrived in the three-float host layout.
 __device__ __forceinline__ float4 ld_colour(const GridsDev& g, const float4* p, long long i) {
@@ -247,18 +313,22 @@ constexpr int kCombineLocal = 24;  // lists up to this long are sorted in local 
 // occluding hit).
 __device__ inline int combine_fragments(const FrameParams& fp, const GridsDev& g, const FragPool& pool, int head,
                                         bool has_occl, float occlZ, float occl[7], int& occl_flags, int occl_id,
-                                        int& top_id) {
+                                        int& top_id, bool& emptied) {
 	int n = 0;
 	bool nan = occl[6] != occl[6];
+	bool any_csg = false;
 	for (int f = head; f >= 0; f = pool.next[f]) {
 		++n;
-		const float d = pool.frag[f].x;
-		nan |= d != d;
+		const float4 fr = pool.frag[f];
+		nan |= fr.x != fr.x;
+		if (g.csg.nnodes > 0) any_csg = any_csg || csg_grid(g, grid_of(g, __float_as_int(fr.y)));
 	}
-	const int ntot = n + (has_occl ? 1 : 0);
+	int ntot = n + (has_occl ? 1 : 0);
+	emptied = false;
 	// short lists: the entries sorted once (insertion sort, ascending key);
 	// long ones (or NaN depths) are walked in order by selection
 	const bool local = ntot <= kCombineLocal && !nan;
+	if (any_csg && !local && g.csg.overflow) atomicOr(g.csg.overflow, 1);  // CSG needs the sorted list held
 	FragKey ent[kCombineLocal];
 	if (local) {
 		int m = 0, seq = n - 1;
@@ -275,6 +345,18 @@ __device__ inline int combine_fragments(const FrameParams& fp, const GridsDev& g
 			insert(fr.x, __float_as_int(fr.y), seq, f);
 		}
 		if (has_occl) insert(occl[6], 0x7fffffff, n, -1);
+		if (any_csg) {
+			// CSG resolve of the sorted list (imagepixel.cpp:170-190); a list it
+			// empties leaves the sample as it was (imagepixel.cpp:249)
+			int node[kCombineLocal];
+			for (int k = 0; k < ntot; ++k)
+				node[k] = ent[k].idx < 0 ? -1 : __ldg(g.csg.grid_node + grid_of(g, ent[k].id));
+			csg_resolve(g.csg, ent, node, ntot);
+			if (ntot == 0) {
+				emptied = true;
+				return n;
+			}
+		}
 	}
 	float sc[3] = {0, 0, 0}, so[3] = {0, 0, 0};
 	float opaque0 = occlZ, opaque1 = FLT_MAX, maxOpaque = FLT_MAX;

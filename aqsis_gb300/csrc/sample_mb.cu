@@ -266,8 +266,11 @@ __device__ __forceinline__ void build_mb_record(const FrameParams& fp, const Gri
 			opaque = opaque && (o.x >= 1.0f && o.y >= 1.0f && o.z >= 1.0f);
 		}
 	}
-	// bits: 2 occluding, 4 triangular, 8 level-of-detail test
-	rr.bits = ((opaque || (gflags & 4)) ? 2 : 0) | ((gflags & 16) ? 4 : 0) | (lod_active(fp, g, gi) ? 8 : 0);
+	// bits: 2 occluding, 4 triangular, 8 level-of-detail test, 16 CSG (never
+	// occlusion-cullable, never occluding)
+	const bool csg = csg_grid(g, gi);
+	rr.bits = ((!csg && (opaque || (gflags & 4))) ? 2 : 0) | ((gflags & 16) ? 4 : 0) |
+	          (lod_active(fp, g, gi) ? 8 : 0) | (csg ? 16 : 0);
 	rr.id = (int)(__ldg(g.mpbase + gi) + m);
 	rr.grid = gi;
 }
@@ -325,8 +328,9 @@ __device__ __forceinline__ void mb_resolve(const FrameParams& fp, const GridsDev
 	bool valid = w >= 0;
 	int src = w;
 	if (TRANSP && head >= 0) {
-		nf = combine_fragments(fp, g, pool, head, w >= 0, ozv, occl, occl_flags, w, src);
-		valid = true;
+		bool emptied = false;
+		nf = combine_fragments(fp, g, pool, head, w >= 0, ozv, occl, occl_flags, w, src, emptied);
+		valid = !emptied;
 	}
 	if (nf == 0 && valid) {
 		if (occl_flags & 1)
@@ -628,7 +632,8 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 					const int b = __ffs(bits) - 1;
 					bits &= bits - 1u;
 					const MbRec& r = sm.rec[wd * 32 + b];
-					if (cullable && r.bmn[2] > gmax) continue;  // behind all 32 samples for the whole shutter
+					const bool rcull = cullable && !(r.bits & 16);  // CSG: never occlusion-culled
+					if (rcull && r.bmn[2] > gmax) continue;  // behind all 32 samples for the whole shutter
 					const bool moving = r.nkeys > 1;
 					bool stored = false;
 					if (valid) {
@@ -694,12 +699,12 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 							    py >= lceil_f(TB.mxy))
 								continue;
 							if ((x < TB.mnx || x > TB.mxx) || (y < TB.mny || y > TB.mxy)) continue;
-							if (cullable && B.mnz > oz) continue;
+							if (rcull && B.mnz > oz) continue;
 							if ((r.bits & 8) && lod_rejects(fp, g, smp, r.grid, px, py, j)) continue;
 							float D, u, v;
 							if (!mb_sample(fp, r, moving, usingDof, x, y, stime, sdx, sdy, D, u, v, bb.tri)) continue;
-							if (cullable && oz <= D) continue;
-							if ((r.bits & 2) && cullable) {
+							if (rcull && oz <= D) continue;
+							if ((r.bits & 2) && rcull) {
 								if (TRANSP && fp.midpoint_store) {
 									// midpoint filter with a z display (bucketprocessor.cpp:1502-1530)
 									const long long hx =

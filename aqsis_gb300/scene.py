@@ -118,6 +118,9 @@ class Grids:
     culled: Optional[np.ndarray] = None  # uint8[total micropolygons]
     aov: Optional[np.ndarray] = None     # float32[NC, naov] output variables per vertex, indexed like Ci
     lod: Optional[np.ndarray] = None     # float32[G, 2] LevelOfDetailBounds (min, max) per grid
+    csg_node: Optional[np.ndarray] = None    # int32[G] primitive CSG node of each grid, -1 = none
+    csg_type: Optional[np.ndarray] = None    # int32[N] CSG node types (GRID_CSG_*)
+    csg_parent: Optional[np.ndarray] = None  # int32[N] parent node, -1 = a root
 
     @property
     def ngrids(self) -> int:
@@ -335,6 +338,40 @@ def with_lod(scene: Scene, seed: int = 0) -> Scene:
     return Scene(scene.frame, dataclasses.replace(scene.grids, lod=b), smp)
 
 
+CSG_PRIMITIVE, CSG_UNION, CSG_INTERSECTION, CSG_DIFFERENCE = 0, 1, 2, 3
+
+
+def with_csg(scene: Scene, seed: int = 0, ntrees: int = 2, frac: float = 0.6) -> Scene:
+    """The scene with seeded CSG trees: `ntrees` solids, each an operation
+    node over primitives and (sometimes) a nested operation; about `frac` of
+    the grids are primitives of a randomly chosen solid, each grid its own
+    primitive node.  The grids of a solid are made two-sided and visible
+    from both sides by the caller's scene (their culling state is kept)."""
+    rng = np.random.default_rng(seed)
+    G = scene.grids.ngrids
+    types, parents = [], []
+    ops = []  # operation nodes that take primitives
+    for _ in range(ntrees):
+        root = len(types)
+        types.append(int(rng.integers(1, 4)))
+        parents.append(-1)
+        ops.append(root)
+        if rng.random() < 0.5:
+            sub = len(types)
+            types.append(int(rng.integers(1, 4)))
+            parents.append(root)
+            ops.append(sub)
+    node = np.full(G, -1, np.int32)
+    for gi in range(G):
+        if rng.random() < frac:
+            node[gi] = len(types)
+            types.append(CSG_PRIMITIVE)
+            parents.append(int(ops[rng.integers(0, len(ops))]))
+    g = dataclasses.replace(scene.grids, csg_node=node, csg_type=np.array(types, np.int32),
+                            csg_parent=np.array(parents, np.int32))
+    return Scene(scene.frame, g, scene.samples)
+
+
 def opaque_stream(width=1920, height=1080, ngrids=200_000, xs=4, ys=4, seed=0xC1,
                   npatterns=250, explicit_samples=False, filt=("gaussian", 2.0, 2.0)) -> Scene:
     """Opaque synthetic stream: 16x16-quad raster grids, Oi = 1, PixelSamples xs ys."""
@@ -492,7 +529,7 @@ def to_camera_space(scene: Scene, m=None, every: int = 1, **camera_kw) -> Scene:
 # Scene files
 
 _GRID_KEYS = ("cu", "cv", "nkeys", "flags", "pbase", "cbase", "tbase", "times", "P", "Ci", "Oi", "culled", "aov",
-              "lod")
+              "lod", "csg_node", "csg_type", "csg_parent")
 _SAMPLE_KEYS = ("pos", "time", "dof", "shuffle", "lod", "pos_index", "dof_index", "time_index",
                 "shuffle_index", "lod_index", "dither")
 

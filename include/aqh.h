@@ -334,6 +334,24 @@ aqh_status aqh_read_samples(aqh_ctx* ctx, int32_t* winner, float* occlz, int32_t
  * 1182-1190, 1404-1412, 1439-1447).  Reset by aqh_frame_begin. */
 aqh_status aqh_set_lod_bounds(aqh_ctx* ctx, const float* bounds, int ngrids);
 
+/* ---- constructive solid geometry ------------------------------------------------- */
+/* The frame's CSG trees (RiSolidBegin / RiSolidEnd; CqCSGTreeNode,
+ * libs/core/csgtree.h:64-260) and each grid's primitive node.  node_type[n]
+ * is AQH_CSG_*; node_parent[n] is its parent node or -1 for a root; the
+ * children of a node are the nodes naming it as parent, in index order (at
+ * most 32).  grid_node[i] is the primitive node of grid i in submission order,
+ * -1 for a grid outside any solid; grids beyond `ngrids` are outside.  At each
+ * sample the depth-sorted hit list passes through the tree of every solid it
+ * holds (CqImagePixel::Combine, imagepixel.cpp:166-188; ProcessSampleList /
+ * EvaluateState, csgtree.cpp:166-350): a hit survives where it changes its
+ * tree's inside/outside state; a list left empty leaves the sample unwritten.
+ * CSG grids are never depth-culled.  A sample with a CSG hit and more than 24
+ * hits, or a NaN depth, fails the render with AQH_ELIMIT.  nnodes = 0 clears
+ * the trees.  Reset by aqh_frame_begin. */
+enum { AQH_CSG_PRIMITIVE = 0, AQH_CSG_UNION = 1, AQH_CSG_INTERSECTION = 2, AQH_CSG_DIFFERENCE = 3 };
+aqh_status aqh_set_csg(aqh_ctx* ctx, const int32_t* node_type, const int32_t* node_parent, int nnodes,
+                       const int32_t* grid_node, int ngrids);
+
 /* ---- arbitrary output variables ----------------------------------------------- */
 /* Extra float channels per vertex: the shader outputs a display asks for
  * (CqRenderer's output data map).  Each stored hit carries its

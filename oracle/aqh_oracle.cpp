@@ -211,6 +211,7 @@ struct MP {
 	// attributes.cpp:127); the test runs when the minimum is >= 0
 	float lodMin, lodMax;
 	bool lodTest() const { return lodMin >= 0.0f; }
+	int csgNode;  // the grid's CSG primitive node, -1 if none
 	bool lodRejects(float level) const { return lodMin > level || level >= lodMax; }
 };
 
@@ -300,6 +301,7 @@ struct Frag {
 	int mp;
 	float data[7];
 	int flags;
+	int csg;  // SqImageSample::csgNode: the CSG node the entry belongs to (-1: none)
 };
 struct Sample {
 	V2 position, dofOffset;
@@ -378,6 +380,7 @@ static void storeSample(Frame& fr, const MP& mp, Sample& sd, float D, V2 uv) {
 	} else {
 		sd.data.push_back(Frag());
 		sd.data.back().mp = mp.id;
+		sd.data.back().csg = mp.csgNode;
 		sd.data.back().flags = 0;
 		hitData = sd.data.back().data;
 		hitFlags = &sd.data.back().flags;
@@ -780,13 +783,81 @@ static void renderMBOrDof(Frame& fr, MP& mp, bool isMoving, bool usingDof, const
 	}
 }
 
-// imagepixel.cpp:144-332 (CSG not modelled)
-static void combine(const OrcFrame* f, Sample& sd) {
+// CSG resolve of one sample's depth-sorted entries (csgtree.cpp:144-351):
+// CqCSGTreeNode::ProcessSampleList, depth first over non-primitive children,
+// then this node: child in/out states start false (the reference's "camera
+// inside" test can never fire), every entry of a child toggles that child's
+// state; entries that do not change this node's state are removed, the
+// others are promoted to this node (to no node at the top of the tree).
+struct CsgTree {
+	const OrcGrids* g;
+	bool evaluate(int node, const std::vector<char>& st) const {
+		const int t = g->csg_type[node];
+		if (t == ORC_CSG_UNION) {
+			for (char c : st) if (c) return true;
+			return false;
+		}
+		if (t == ORC_CSG_INTERSECTION) {
+			for (char c : st) if (!c) return false;
+			return true;
+		}
+		if (t == ORC_CSG_DIFFERENCE) {
+			if (st.empty() || !st[0]) return false;
+			for (size_t i = 1; i < st.size(); ++i) if (st[i]) return false;
+			return true;
+		}
+		return false;
+	}
+	std::vector<int> children(int node) const {
+		std::vector<int> c;
+		for (int i = 0; i < g->csg_nnodes; ++i) if (g->csg_parent[i] == node) c.push_back(i);
+		return c;
+	}
+	void process(int node, std::vector<Frag>& data) const {
+		const std::vector<int> ch = children(node);
+		if (g->csg_type[node] == ORC_CSG_PRIMITIVE) {
+			// CqCSGNodePrimitive::ProcessSampleList (a primitive at the top)
+			for (Frag& e : data) if (e.csg == node) e.csg = -1;
+			return;
+		}
+		for (int c : ch) if (g->csg_type[c] != ORC_CSG_PRIMITIVE) process(c, data);
+		std::vector<char> st(ch.size(), 0);
+		bool cur = evaluate(node, st);
+		for (size_t i = 0; i < data.size();) {
+			int ci = -1;
+			for (size_t k = 0; k < ch.size(); ++k) if (data[i].csg == ch[k]) ci = (int)k;
+			if (ci < 0) { ++i; continue; }
+			st[ci] = !st[ci];
+			const bool nw = evaluate(node, st);
+			if (nw == cur) {
+				data.erase(data.begin() + i);
+			} else {
+				cur = nw;
+				data[i].csg = g->csg_parent[node] >= 0 ? node : -1;
+				++i;
+			}
+		}
+	}
+	void resolve(std::vector<Frag>& data) const {
+		for (;;) {
+			int start = -1;
+			for (const Frag& e : data) if (e.csg >= 0) { start = e.csg; break; }
+			if (start < 0) return;
+			int top = start;
+			while (g->csg_parent[top] >= 0) top = g->csg_parent[top];
+			process(top, data);
+		}
+	}
+};
+
+// CqImagePixel::Combine (imagepixel.cpp:144-332)
+static void combine(const OrcFrame* f, Sample& sd, const OrcGrids* g) {
 	const float zt[3] = {f->zthreshold[0], f->zthreshold[1], f->zthreshold[2]};
 	if (!sd.data.empty()) {
 		if (sd.occlValid) {
 			Frag o;
 			o.mp = sd.occlMp;
+			o.csg = -1;  // occluding hits never come from CSG grids (not cullable)
 			o.flags = sd.occlFlags;
 			std::memcpy(o.data, sd.occl, sizeof(o.data));
 			sd.data.push_back(o);
@@ -796,6 +867,12 @@ static void combine(const OrcFrame* f, Sample& sd) {
 		// which is stable, so this matches the reference for such lists).
 		std::stable_sort(sd.data.begin(), sd.data.end(),
 		                 [](const Frag& a, const Frag& b) { return a.data[6] < b.data[6]; });
+		// CSG (imagepixel.cpp:170-190); a list it empties leaves the sample as
+		// it was (imagepixel.cpp:249: nothing is written back)
+		if (g->csg_node && g->csg_nnodes > 0) {
+			CsgTree{g}.resolve(sd.data);
+			if (sd.data.empty()) return;
+		}
 		float sc[3] = {0, 0, 0}, so[3] = {0, 0, 0};
 		float opaqueDepths[2] = {sd.occlZ, FLT_MAX};
 		float maxOpaqueDepth = FLT_MAX;
@@ -1101,7 +1178,10 @@ extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples
 				mp.lodMin = g->lod ? g->lod[2 * gi] : 0.0f;
 				mp.lodMax = g->lod ? g->lod[2 * gi + 1] : 1.0f;
 				mp.matteFlag = flags & (ORC_GRID_MATTE | ORC_GRID_MATTEALPHA);
-				mp.isCullable = cullable;
+				// a micropolygon of a CSG solid is never occlusion-cullable
+				// (bucketprocessor.cpp:1074-1080)
+				mp.csgNode = (g->csg_node && g->csg_nnodes > 0) ? g->csg_node[gi] : -1;
+				mp.isCullable = cullable && mp.csgNode < 0;
 				const int vidx[4] = {index, index + 1, index + cu + 1, index + cu + 2};
 				const int ncol = mp.smooth ? 4 : 1;
 				for (int i = 0; i < ncol; ++i) {
@@ -1130,7 +1210,7 @@ extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples
 		if (out->nfrag) out->nfrag[i] = (int32_t)sd.data.size();
 	}
 	// CombineElements (bucketprocessor.cpp:365-375)
-	for (size_t i = 0; i < nsamp; ++i) combine(f, fr.samples[i]);
+	for (size_t i = 0; i < nsamp; ++i) combine(f, fr.samples[i], g);
 	for (size_t i = 0; i < nsamp; ++i) {
 		const Sample& sd = fr.samples[i];
 		if (out->valid) out->valid[i] = sd.occlValid ? 1 : 0;

@@ -75,7 +75,16 @@ typedef struct {
 	const float* aov;         /* output variables float[vertex][naov] indexed like Ci, or NULL */
 	int32_t naov;
 	const float* lod;         /* LevelOfDetailBounds float[grid][2] (min, max), or NULL = (0, 1) */
+	/* CSG (RiSolidBegin / RiSolidEnd): the primitive node of each grid (-1: none)
+	 * and the tree: per node its type (ORC_CSG_*) and parent (-1: a root); the
+	 * children of a node are the nodes naming it as parent, in index order */
+	const int32_t* csg_node;
+	int32_t csg_nnodes;
+	const int32_t* csg_type;
+	const int32_t* csg_parent;
 } OrcGrids;
+
+enum { ORC_CSG_PRIMITIVE = 0, ORC_CSG_UNION = 1, ORC_CSG_INTERSECTION = 2, ORC_CSG_DIFFERENCE = 3 };
 
 typedef struct {
 	int32_t x0, y0, w, h;     /* sample region in pixels: [x0,x0+w) x [y0,y0+h) */

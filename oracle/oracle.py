@@ -42,7 +42,8 @@ class OrcGrids(C.Structure):
     _fields_ = [("ngrids", C.c_int32), ("cu", _i32p), ("cv", _i32p), ("nkeys", _i32p),
                 ("pbase", _i64p), ("cbase", _i64p), ("tbase", _i64p), ("times", _f32p),
                 ("P", _f32p), ("Ci", _f32p), ("Oi", _f32p), ("flags", _i32p), ("culled", _u8p),
-                ("aov", _f32p), ("naov", C.c_int32), ("lod", _f32p)]
+                ("aov", _f32p), ("naov", C.c_int32), ("lod", _f32p),
+                ("csg_node", _i32p), ("csg_nnodes", C.c_int32), ("csg_type", _i32p), ("csg_parent", _i32p)]
 
 
 class OrcSamples(C.Structure):
@@ -199,6 +200,15 @@ def render(scene, qchannels=(0, 1, 2, 6), want_samples: bool = True) -> dict:
                   _p(arr(g.Oi, np.float32), _f32p), _p(arr(g.flags, np.int32), _i32p),
                   _p(arr(g.culled, np.uint8), _u8p), _p(arr(getattr(g, "aov", None), np.float32), _f32p),
                   naov, _p(arr(getattr(g, "lod", None), np.float32), _f32p))
+    if getattr(g, "csg_node", None) is not None:
+        # grids past the given node list are outside any solid
+        cn = np.full(g.ngrids, -1, np.int32)
+        given = np.asarray(g.csg_node, np.int32).ravel()[:g.ngrids]
+        cn[:given.shape[0]] = given
+        og.csg_node = _p(arr(cn, np.int32), _i32p)
+        og.csg_nnodes = int(np.asarray(g.csg_type).shape[0])
+        og.csg_type = _p(arr(g.csg_type, np.int32), _i32p)
+        og.csg_parent = _p(arr(g.csg_parent, np.int32), _i32p)
     os_ = OrcSamples(x0, y0, w, h, s.npatterns, _p(arr(s.pos, np.float32), _f32p),
                      _p(arr(s.time, np.float32), _f32p), _p(arr(s.dof, np.float32), _f32p),
                      _p(arr(s.shuffle, np.int32), _i32p), _p(arr(s.lod, np.float32), _f32p),
