@@ -26,3 +26,27 @@ def test_random_frame_batched(aqh_lib, oracle, seed):
     finally:
         h.close()
     compare(res, oracle.render(sc))
+
+
+@pytest.mark.parametrize("seed", SEEDS[:150])
+def test_random_frame_with_solids(aqh_lib, oracle, seed):
+    """Random frames with random CSG trees over their grids.  The device
+    refuses (AQH_ELIMIT) a sample holding a CSG hit among more than 24 hits
+    or a NaN depth; the oracle's hit counts must then show such a sample."""
+    import numpy as np
+    from aqsis_gb300 import scene as S
+    from aqsis_gb300.aqh import AqhError
+    sc = S.with_csg(SS.fuzz(seed), seed=seed, ntrees=1 + seed % 3)
+    ref = oracle.render(sc)
+    h = aqh_lib.Hider(0)
+    try:
+        h.set_mode(seed % 2 == 1)
+        try:
+            res = h.render_scene(sc)
+        except AqhError:
+            ntot = ref["nfrag"] + (ref["winner"] >= 0)
+            assert ntot.max() > 24 or np.isnan(ref["occlz"]).any() or np.isnan(sc.grids.P).any()
+            return
+    finally:
+        h.close()
+    compare(res, ref)
