@@ -193,6 +193,7 @@ def load(build_if_missing: bool = False):
     L.aqh_set_aov_count.argtypes = [vp, C.c_int]
     L.aqh_set_lod_bounds.argtypes = [vp, _f32p, C.c_int]
     L.aqh_set_csg.argtypes = [vp, _i32p, _i32p, C.c_int, _i32p, C.c_int]
+    L.aqh_set_trim.argtypes = [vp, _i32p, C.c_int, _f32p, C.c_size_t, _f32p, C.c_int, _i32p, C.c_int, _i32p, C.c_int]
     L.aqh_dspy_geometry_of.argtypes = [vp, C.POINTER(DspyGeometry)]
     L.aqh_dspy_open.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(DspyGeometry), C.POINTER(Display),
                                 C.POINTER(C.c_char_p), C.POINTER(vp)]
@@ -218,7 +219,7 @@ def load(build_if_missing: bool = False):
                  "aqh_autotune", "aqh_set_camera_to_raster", "aqh_read_display", "aqh_set_aov_count",
                  "aqh_submit_aov_host", "aqh_submit_aov_device", "aqh_read_aov", "aqh_dspy_geometry_of",
                  "aqh_dspy_open", "aqh_dspy_send", "aqh_dspy_send_image", "aqh_dspy_close", "aqh_set_lod_bounds",
-                 "aqh_set_csg"):
+                 "aqh_set_csg", "aqh_set_trim"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -347,6 +348,18 @@ class Hider:
         self._check(self.L.aqh_set_csg(self.ctx, _p(t, _i32p), _p(par, _i32p), t.shape[0], _p(gn, _i32p),
                                        gn.shape[0]), "aqh_set_csg")
 
+    def set_trim(self, grid_set, uv, points, loop_first, set_first):
+        """Trim curves (aqh_set_trim): each grid's trim set, per-vertex (u, v)
+        indexed like Ci, and the sets as loops of points."""
+        gs = np.ascontiguousarray(grid_set, np.int32).ravel()
+        uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 2)
+        lf = np.ascontiguousarray(loop_first, np.int32).ravel()
+        sf = np.ascontiguousarray(set_first, np.int32).ravel()
+        self._check(self.L.aqh_set_trim(self.ctx, _p(gs, _i32p), gs.shape[0], _p(uv, _f32p), uv.shape[0],
+                                        _p(pts, _f32p), pts.shape[0], _p(lf, _i32p), lf.shape[0] - 1,
+                                        _p(sf, _i32p), sf.shape[0] - 1), "aqh_set_trim")
+
     def set_aov_count(self, n: int):
         """Output variables per vertex for this frame (aqh_set_aov_count), before any grid."""
         self._check(self.L.aqh_set_aov_count(self.ctx, int(n)), "aqh_set_aov_count")
@@ -394,6 +407,8 @@ class Hider:
             self.set_lod_bounds(g.lod)
         if getattr(g, "csg_node", None) is not None:
             self.set_csg(g.csg_type, g.csg_parent, g.csg_node)
+        if getattr(g, "trim_set", None) is not None:
+            self.set_trim(g.trim_set, g.trim_uv, g.trim_points, g.trim_loop_first, g.trim_set_first)
 
     def submit_grids_host(self, g, packed3: bool = False):
         """Submit a whole packed scene.Grids in one aqh_submit_grids_host call
@@ -435,6 +450,8 @@ class Hider:
             self.set_lod_bounds(g.lod)
         if getattr(g, "csg_node", None) is not None:
             self.set_csg(g.csg_type, g.csg_parent, g.csg_node)
+        if getattr(g, "trim_set", None) is not None:
+            self.set_trim(g.trim_set, g.trim_uv, g.trim_points, g.trim_loop_first, g.trim_set_first)
         self._packed_keep = keep
 
     def submit_grids_device(self, ngrids, d_cu, d_cv, d_nkeys, d_flags, d_pbase, d_cbase, d_tbase, d_times,

@@ -345,6 +345,11 @@ struct aqh_ctx {
 	int csg_n = 0;
 	std::vector<int32_t> csg_grid_node, csg_type, csg_parent, csg_child, csg_nch, csg_pfirst, csg_pcount, csg_post;
 	DevBuf d_csg, d_csg_overflow;
+	// trim curves: host copies of the sets, the grids' sets and the uv array
+	int trim_nsets = 0;
+	std::vector<int32_t> trim_grid_set, trim_loop_first, trim_set_first;
+	std::vector<float> trim_pts, trim_uv;
+	DevBuf d_trim_i, d_trim_f, d_trim_mark, d_trim_cull, d_trim_err;
 
 	// host-submitted packed arrays (caller-owned, uploaded at render)
 	bool host_packed = false;
@@ -538,6 +543,7 @@ aqh_status aqh_frame_begin(aqh_ctx* ctx, const aqh_frame_desc* d) {
 	ctx->h_lod.clear();
 	ctx->lod_set = false;
 	ctx->csg_n = 0;
+	ctx->trim_nsets = 0;
 	ctx->hp_aov = nullptr;
 	ctx->hp_naov_vertices = 0;
 	ctx->dev_aov = nullptr;
@@ -990,6 +996,8 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 		        "upload slice times");
 	}
 	const int G = g.ngrids;
+	// the sampling records keep the grid index above six flag bits
+	if (G > (1 << 25)) return ctx->fail(AQH_ELIMIT, "%d grids in one frame; at most 2^25", G);
 	P.nsamp = (size_t)fp.sw * fp.sh * fp.spp;
 	P.nst = fp.nstx * fp.nsty;
 	BinBuffers& bb = P.bb;
@@ -1133,6 +1141,55 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 			return ctx->fail(AQH_EINVAL, "output variables are set but aqh_submit_aov_device was not called");
 		P.g.aov = ctx->dev_aov;
 		P.g.naov = ctx->dev_aov ? ctx->naov : 0;
+	}
+	P.g.trim = TrimDev{};
+	if (ctx->trim_nsets > 0 && G > 0) {
+		// ints: grid sets (G, -1 past the given ones), loop starts, set starts;
+		// floats: loop points, then uv
+		std::vector<int32_t> bi;
+		bi.reserve((size_t)G + ctx->trim_loop_first.size() + ctx->trim_set_first.size());
+		for (int i = 0; i < G; ++i) bi.push_back(i < (int)ctx->trim_grid_set.size() ? ctx->trim_grid_set[i] : -1);
+		const size_t o_lf = bi.size();
+		bi.insert(bi.end(), ctx->trim_loop_first.begin(), ctx->trim_loop_first.end());
+		const size_t o_sf = bi.size();
+		bi.insert(bi.end(), ctx->trim_set_first.begin(), ctx->trim_set_first.end());
+		const size_t npf = ctx->trim_pts.size();
+		AQH_TRY(ctx->d_trim_i.ensure(bi.size() * 4), "alloc trim sets");
+		AQH_TRY(ctx->d_trim_f.ensure((npf + ctx->trim_uv.size() + 2) * 4), "alloc trim sets");
+		AQH_TRY(cudaMemcpyAsync(ctx->d_trim_i.p, bi.data(), bi.size() * 4, cudaMemcpyHostToDevice, s), "upload trim sets");
+		float* df = ctx->d_trim_f.as<float>();
+		if (npf) AQH_TRY(cudaMemcpyAsync(df, ctx->trim_pts.data(), npf * 4, cudaMemcpyHostToDevice, s), "upload trim sets");
+		if (!ctx->trim_uv.empty())
+			AQH_TRY(cudaMemcpyAsync(df + npf, ctx->trim_uv.data(), ctx->trim_uv.size() * 4, cudaMemcpyHostToDevice, s),
+			        "upload trim uv");
+		const size_t nm = (size_t)std::max<int64_t>(P.nmps, 1);
+		AQH_TRY(ctx->d_trim_mark.ensure(nm), "alloc trim marks");
+		AQH_TRY(ctx->d_trim_cull.ensure(nm), "alloc trim marks");
+		AQH_TRY(ctx->d_trim_err.ensure(16), "alloc");
+		AQH_TRY(cudaMemsetAsync(ctx->d_trim_mark.p, 0, nm, s), "memset");
+		AQH_TRY(cudaMemsetAsync(ctx->d_trim_err.p, 0, 4, s), "memset");
+		// the frame's culled mask plus the micropolygons trimmed out
+		if (P.g.culled && P.nmps > 0)
+			AQH_TRY(cudaMemcpyAsync(ctx->d_trim_cull.p, P.g.culled, (size_t)P.nmps, cudaMemcpyDeviceToDevice, s), "copy");
+		else
+			AQH_TRY(cudaMemsetAsync(ctx->d_trim_cull.p, 0, nm, s), "memset");
+		const int32_t* b = ctx->d_trim_i.as<int32_t>();
+		TrimDev& t = P.g.trim;
+		t.nsets = ctx->trim_nsets;
+		t.grid_set = b;
+		t.loop_first = b + o_lf;
+		t.set_first = b + o_sf;
+		t.pts = reinterpret_cast<const float2*>(df);
+		t.uv = reinterpret_cast<const float2*>(df + npf);
+		t.mark = ctx->d_trim_mark.as<uint8_t>();
+		launch_trim_mark(P.g, (long long)(ctx->trim_uv.size() / 2), ctx->d_trim_mark.as<uint8_t>(),
+		                 ctx->d_trim_cull.as<uint8_t>(), ctx->d_trim_err.as<int32_t>(), s);
+		AQH_TRY(cudaGetLastError(), "trim kernel launch");
+		int32_t err = 0;
+		AQH_TRY(cudaMemcpyAsync(&err, ctx->d_trim_err.p, 4, cudaMemcpyDeviceToHost, s), "readback");
+		AQH_TRY(cudaStreamSynchronize(s), "trim curves");
+		if (err) return ctx->fail(AQH_EINVAL, "trim curves: a trimmable grid's vertices run past the uv array");
+		P.g.culled = ctx->d_trim_cull.as<uint8_t>();
 	}
 	if (P.g.naov > 0) {
 		AQH_TRY(ctx->d_aovsrc.ensure(nstore * sizeof(int32_t)), "alloc output variable sources");
@@ -1366,8 +1423,10 @@ aqh_status aqh_render(aqh_ctx* ctx, int sync) {
 	ctx->stats.micropolygons = P.nmps;
 	ctx->stats.samples = (int64_t)P.nsamp;
 	ctx->stats.grids = P.g.ngrids;
-	// CSG frames take the plain path, which reads the resolve's overflow flag
-	if (ctx->mode == AQH_MODE_BATCHED && P.g.csg.nnodes == 0) return render_batched(ctx, P, sync != 0);
+	// CSG frames take the plain path, which reads the resolve's overflow flag;
+	// so do frames with trim curves (their micropolygon marks are per frame)
+	if (ctx->mode == AQH_MODE_BATCHED && P.g.csg.nnodes == 0 && P.g.trim.nsets == 0)
+		return render_batched(ctx, P, sync != 0);
 	return render_plain(ctx, P, sync != 0 || P.g.csg.nnodes > 0);
 }
 
@@ -1471,6 +1530,34 @@ aqh_status aqh_set_csg(aqh_ctx* ctx, const int32_t* node_type, const int32_t* no
 	ctx->csg_post = post;
 	ctx->csg_grid_node.assign(grid_node, grid_node + ngrids);
 	ctx->csg_n = nnodes;
+	return AQH_OK;
+}
+
+aqh_status aqh_set_trim(aqh_ctx* ctx, const int32_t* grid_set, int ngrids, const float* uv, size_t nuv,
+                        const float* points, int npoints, const int32_t* loop_first, int nloops,
+                        const int32_t* set_first, int nsets) {
+	if (!ctx || ngrids < 0 || npoints < 0 || nloops < 0 || nsets < 0) return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	ctx->trim_nsets = 0;
+	if (nsets == 0) return AQH_OK;
+	if ((ngrids > 0 && !grid_set) || (nuv > 0 && !uv) || (npoints > 0 && !points) || !loop_first || !set_first)
+		return ctx->fail(AQH_EINVAL, "trim curves: missing array");
+	if (loop_first[0] < 0 || loop_first[nloops] > npoints)
+		return ctx->fail(AQH_EINVAL, "trim curves: loop starts outside the point array");
+	for (int l = 0; l < nloops; ++l)
+		if (loop_first[l + 1] < loop_first[l]) return ctx->fail(AQH_EINVAL, "trim curves: loop starts decrease");
+	if (set_first[0] < 0 || set_first[nsets] > nloops)
+		return ctx->fail(AQH_EINVAL, "trim curves: set starts outside the loop array");
+	for (int k = 0; k < nsets; ++k)
+		if (set_first[k + 1] < set_first[k]) return ctx->fail(AQH_EINVAL, "trim curves: set starts decrease");
+	for (int i = 0; i < ngrids; ++i)
+		if (grid_set[i] < -1 || grid_set[i] >= nsets) return ctx->fail(AQH_EINVAL, "grid %d: bad trim set %d", i, grid_set[i]);
+	ctx->trim_grid_set.assign(grid_set, grid_set + ngrids);
+	ctx->trim_uv.assign(uv, uv + 2 * nuv);
+	ctx->trim_pts.assign(points, points + 2 * (size_t)npoints);
+	ctx->trim_loop_first.assign(loop_first, loop_first + nloops + 1);
+	ctx->trim_set_first.assign(set_first, set_first + nsets + 1);
+	ctx->trim_nsets = nsets;
 	return AQH_OK;
 }
 

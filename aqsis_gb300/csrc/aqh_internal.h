@@ -72,6 +72,18 @@ struct CsgDev {
 };
 
 // Grid stream in device memory (aqh_submit_grids_device layout).
+// Trim curves of NURBS grids (CqTrimLoopArray, trimcurve.h:110-160):
+// prepared loops as point lists, grouped in sets; each grid names a set or -1.
+struct TrimDev {
+	int nsets;                  // 0: nothing is trimmed this frame
+	const int32_t* grid_set;    // per grid: its set, -1 = not trimmable
+	const float2* uv;           // surface (u, v) per vertex, indexed like Ci
+	const float2* pts;          // loop points
+	const int32_t* loop_first;  // [nloops + 1]
+	const int32_t* set_first;   // [nsets + 1]
+	const uint8_t* mark;        // per micropolygon: 1 = trimmed (tested at each hit)
+};
+
 struct GridsDev {
 	int ngrids;
 	const int32_t* cu;
@@ -93,6 +105,7 @@ struct GridsDev {
 	int colour3;             // Ci / Oi hold packed three-float entries (float[3 n]) rather than float4
 	const float2* lod;       // LevelOfDetailBounds (min, max) per grid, or null: (0, 1) for every grid
 	CsgDev csg;
+	TrimDev trim;
 };
 
 // Sample pattern caches (aqh_samples) in device memory.
@@ -195,6 +208,10 @@ void launch_grid_rects(const FrameParams& fp, const GridsDev& g, const BinBuffer
 void launch_id_grid(const GridsDev& g, int64_t nmps, int32_t* table, cudaStream_t s);
 // Split's camera-to-raster projection of AQH_GRID_CAMERA grids, in place in
 // P (the grids' point array, g.P made writable) and clearing the flag.
+// Split's trimming of every micropolygon of a trimmable grid: trimmed out
+// ones are set in `culled`, ones to test at each hit in `mark`; a grid whose
+// vertices run past `nuv` uv entries sets *err and is skipped.
+void launch_trim_mark(const GridsDev& g, long long nuv, uint8_t* mark, uint8_t* culled, int32_t* err, cudaStream_t s);
 void launch_project_grids(const GridsDev& g, float4* P, int32_t* flags, const CamMatrix& m, cudaStream_t s);
 void launch_st_count(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);
 void launch_scan_i32(const int32_t* in, int32_t* out, int n, int32_t* scratch, cudaStream_t s);

@@ -289,6 +289,51 @@ void launch_project_grids(const GridsDev& g, float4* P, int32_t* flags, const Ca
 	project_grids_kernel<<<g.ngrids, 256, 0, s>>>(g, P, flags, m);
 }
 
+// CqMicroPolyGrid::Split / CqMotionMicroPolyGrid::Split trimming
+// (micropolygon.cpp:754-835, 1056-1130), one block per grid: the corners'
+// surface parameters (index, index+1, index+cu+2, index+cu+1) are classified
+// against the grid's trim set, inverted for the "outside" sense; all four
+// trimmed with no edge crossing a loop drops the micropolygon, any trimmed
+// marks it for the per-hit test.
+__global__ void trim_mark_kernel(GridsDev g, long long nuv, uint8_t* mark, uint8_t* culled, int32_t* err) {
+	const int gi = blockIdx.x;
+	const int set = __ldg(g.trim.grid_set + gi);
+	if (set < 0) return;
+	const int cu = __ldg(g.cu + gi), cv = __ldg(g.cv + gi);
+	const long long cb = __ldg(g.cbase + gi);
+	if (cb < 0 || cb + (long long)(cu + 1) * (cv + 1) > nuv) {
+		if (threadIdx.x == 0) atomicOr(err, 1);
+		return;
+	}
+	const bool outside = (__ldg(g.flags + gi) & 64) != 0;
+	const int l0 = __ldg(g.trim.set_first + set), l1 = __ldg(g.trim.set_first + set + 1);
+	const long long mb = __ldg(g.mpbase + gi);
+	const int nm = cu * cv;
+	for (int m = threadIdx.x; m < nm; m += blockDim.x) {
+		if (culled[mb + m]) continue;
+		const long long c = cb + (long long)(m / cu) * (cu + 1) + (m % cu);
+		const float2 A = __ldg(g.trim.uv + c), B = __ldg(g.trim.uv + c + 1);
+		const float2 C = __ldg(g.trim.uv + c + cu + 2), D = __ldg(g.trim.uv + c + cu + 1);
+		const bool tA = trim_point(g.trim.pts, g.trim.loop_first, l0, l1, A.x, A.y) != outside;
+		const bool tB = trim_point(g.trim.pts, g.trim.loop_first, l0, l1, B.x, B.y) != outside;
+		const bool tC = trim_point(g.trim.pts, g.trim.loop_first, l0, l1, C.x, C.y) != outside;
+		const bool tD = trim_point(g.trim.pts, g.trim.loop_first, l0, l1, D.x, D.y) != outside;
+		if (tA && tB && tC && tD && !trim_line(g.trim.pts, g.trim.loop_first, l0, l1, A, B) &&
+		    !trim_line(g.trim.pts, g.trim.loop_first, l0, l1, B, C) &&
+		    !trim_line(g.trim.pts, g.trim.loop_first, l0, l1, C, D) &&
+		    !trim_line(g.trim.pts, g.trim.loop_first, l0, l1, D, A)) {
+			culled[mb + m] = 1;
+			continue;
+		}
+		if (tA || tB || tC || tD) mark[mb + m] = 1;
+	}
+}
+
+void launch_trim_mark(const GridsDev& g, long long nuv, uint8_t* mark, uint8_t* culled, int32_t* err, cudaStream_t s) {
+	if (g.ngrids == 0) return;
+	trim_mark_kernel<<<g.ngrids, 128, 0, s>>>(g, nuv, mark, culled, err);
+}
+
 void launch_id_grid(const GridsDev& g, int64_t nmps, int32_t* table, cudaStream_t s) {
 	if (g.ngrids == 0) return;
 	id_grid_kernel<<<(g.ngrids + 255) / 256, 256, 0, s>>>(g, nmps, table);

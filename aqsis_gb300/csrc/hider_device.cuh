@@ -203,6 +203,69 @@ __device__ __forceinline__ float2 project_to_circle(float x, float y) {
 	return make_float2(adj * x, adj * y);
 }
 
+// CqTrimLoopArray::TrimPoint (trimcurve.cpp:145-169, 223-237) over the loops
+// [l0, l1): per loop the even-odd count of its edges crossing the point's
+// row on the left; no loops trims nothing, else a point inside an even
+// number of loops is trimmed.
+__device__ __forceinline__ bool trim_point(const float2* pts, const int32_t* loop_first, int l0, int l1, float x,
+                                           float y) {
+	if (l1 == l0) return false;
+	int crosses = 0;
+	for (int l = l0; l < l1; ++l) {
+		const int p0 = __ldg(loop_first + l), n = __ldg(loop_first + l + 1) - p0;
+		bool odd = false;
+		float2 b = n > 0 ? __ldg(pts + p0 + n - 1) : make_float2(0.0f, 0.0f);
+		for (int i = 0; i < n; ++i) {
+			const float2 a = __ldg(pts + p0 + i);
+			if (((a.y < y) && (b.y >= y)) || ((b.y < y) && (a.y >= y))) {
+				if (a.x + (y - a.y) / (b.y - a.y) * (b.x - a.x) < x) odd = !odd;
+			}
+			b = a;
+		}
+		crosses += odd ? 1 : 0;
+	}
+	return !(crosses & 1);
+}
+
+// CqTrimLoopArray::LineIntersects (trimcurve.cpp:172-198, 240-253).
+__device__ __forceinline__ bool trim_line(const float2* pts, const int32_t* loop_first, int l0, int l1, float2 v1,
+                                          float2 v2) {
+	const float x1 = v1.x, y1 = v1.y, x2 = v2.x, y2 = v2.y;
+	for (int l = l0; l < l1; ++l) {
+		const int p0 = __ldg(loop_first + l), n = __ldg(loop_first + l + 1) - p0;
+		float2 q4 = n > 0 ? __ldg(pts + p0 + n - 1) : make_float2(0.0f, 0.0f);
+		for (int i = 0; i < n; ++i) {
+			const float2 q3 = __ldg(pts + p0 + i);
+			const float x3 = q3.x, y3 = q3.y, x4 = q4.x, y4 = q4.y;
+			q4 = q3;
+			const float d = (x2 - x1) * (y4 - y3) - (y2 - y1) * (x4 - x3);
+			if (d == 0.0f) continue;
+			const float r = ((y1 - y3) * (x4 - x3) - (x1 - x3) * (y4 - y3)) / d;
+			const float s = ((y1 - y3) * (x2 - x1) - (x1 - x3) * (y2 - y1)) / d;
+			if ((r >= 0.0f) && (s >= 0.0f) && (r <= 1.0f) && (s <= 1.0f)) return true;
+		}
+	}
+	return false;
+}
+
+// BilinearEvaluate (bilinear.h:189-224) of two-component corners.
+__device__ __forceinline__ float2 bilinear_evaluate(float2 A, float2 B, float2 C, float2 D, float s, float t) {
+	float2 AB, CD;
+	if (s <= 0.0f) {
+		AB = A;
+		CD = C;
+	} else if (s >= 1.0f) {
+		AB = B;
+		CD = D;
+	} else {
+		AB = make_float2((B.x - A.x) * s + A.x, (B.y - A.y) * s + A.y);
+		CD = make_float2((D.x - C.x) * s + C.x, (D.y - C.y) * s + C.y);
+	}
+	if (t <= 0.0f) return AB;
+	if (t >= 1.0f) return CD;
+	return make_float2((CD.x - AB.x) * t + AB.x, (CD.y - AB.y) * t + AB.y);
+}
+
 // The triangle split line test of CqMicroPolygon::Sample and
 // CqMicroPolygonMotion::Sample (micropolygon.cpp:1630-1654, 1885-1907): line
 // (A.x, A.y, B.x, B.y); a hit at (hx, hy) on or behind it misses.

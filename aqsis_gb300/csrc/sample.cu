@@ -54,13 +54,17 @@ struct RecS {
 	int bits;                      // 1 linear, 2 occluding store
 };  // 43 words: an odd stride spreads neighbouring records over the banks
 
-// RecS::bits; the grid index sits above bit 5.  kRecCsg: a CSG solid's
-// micropolygon, never occlusion-cullable.
-constexpr int kRecLinear = 1, kRecOccluding = 2, kRecTriangular = 4, kRecLod = 8, kRecCsg = 16;
-constexpr int kRecGridShift = 5;
+// RecS::bits; the grid index sits from bit 6 up.  kRecCsg: a CSG solid's
+// micropolygon, never occlusion-cullable; kRecTrim: marked trimmed.
+constexpr int kRecLinear = 1, kRecOccluding = 2, kRecTriangular = 4, kRecLod = 8, kRecCsg = 16, kRecTrim = 32;
+constexpr int kRecGridShift = 6;
 
-// The triangle split line of the record's grid (key 0: static micropolygons).
-__device__ __forceinline__ bool rec_keeps(const BinBuffers& bb, int bits, float x, float y) {
+// The tests after fContains that can still reject a static hit at (x, y),
+// (u, v): the trim curves of a micropolygon marked trimmed, then the split
+// line of a triangular grid (key 0).
+__device__ __forceinline__ bool rec_keeps(const GridsDev& g, const BinBuffers& bb, int bits, int id, float x, float y,
+                                          float u, float v) {
+	if ((bits & kRecTrim) && trim_rejects(g, id, bits >> kRecGridShift, u, v)) return false;
 	return !(bits & kRecTriangular) || triangle_keeps(__ldg(bb.tri + (size_t)(bits >> kRecGridShift) * kMaxKeys), x, y);
 }
 
@@ -152,6 +156,7 @@ __device__ __forceinline__ void build_record(const FrameParams& fp, const GridsD
 	if (gflags & 16) bits |= kRecTriangular;
 	if (lod_active(fp, g, gi)) bits |= kRecLod;
 	if (csg_grid(g, gi)) bits = (bits & ~kRecOccluding) | kRecCsg;
+	if (g.trim.nsets > 0 && __ldg(g.trim.mark + rec.id)) bits |= kRecTrim;
 	bits |= gi << kRecGridShift;
 	rec.bits = bits;
 }
@@ -482,7 +487,7 @@ sample_static_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 						             (r.bits & kRecLinear) != 0, x, y, u, v);
 						const float D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
 						// StoreSample (bucketprocessor.cpp:1471-1569) for a hit the split line keeps
-						if (rec_keeps(bb, r.bits, x, y) && !(rcull && oz <= D)) {
+						if (rec_keeps(g, bb, r.bits, r.id, x, y, u, v) && !(rcull && oz <= D)) {
 							if ((r.bits & kRecOccluding) && rcull) {
 								if (TRANSP && fp.midpoint_store) {
 									// midpoint filter with a z display (bucketprocessor.cpp:1502-1530):
@@ -783,7 +788,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 			inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y, (r.bits & kRecLinear) != 0, x, y, u,
 			             v);
 			const float D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
-			if (!rec_keeps(bb, r.bits, x, y)) continue;
+			if (!rec_keeps(g, bb, r.bits, r.id, x, y, u, v)) continue;
 			if (!(D >= r.bminz) || D == 0.0f) {
 				atomicOr(&sm.flag[s >> 5], 1u << (s & 31));
 			} else {
@@ -836,7 +841,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 								D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
 								bz = r.bminz;
 								id = r.id;
-								hit = rec_keeps(bb, r.bits, x, y);
+								hit = rec_keeps(g, bb, r.bits, r.id, x, y, u, v);
 							}
 						}
 						uint32_t hb = __ballot_sync(0xffffffffu, hit);
@@ -1109,7 +1114,7 @@ sample_frag_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sa
 					inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y, (r.bits & kRecLinear) != 0, x,
 					             y, u, v);
 					D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
-					hit = rec_keeps(bb, r.bits, x, y) && !(cullable && !(r.bits & kRecCsg) && FLT_MAX <= D);
+					hit = rec_keeps(g, bb, r.bits, r.id, x, y, u, v) && !(cullable && !(r.bits & kRecCsg) && FLT_MAX <= D);
 					id = r.id;
 				}
 			}

@@ -95,6 +95,23 @@ __device__ inline bool csg_resolve(const CsgDev& c, E* ent, int* node, int& n) {
 	return false;
 }
 
+// The trim test of CqMicroPolygon::Sample (micropolygon.cpp:1592-1627) for a
+// hit at (u, v) on micropolygon `id` of grid gi, marked trimmed: the surface
+// parameters there inside the grid's trim set reject the hit, with the
+// "inside" sense only.
+__device__ __forceinline__ bool trim_rejects(const GridsDev& g, int id, int gi, float u, float v) {
+	if (g.flags && (__ldg(g.flags + gi) & 64)) return false;  // "outside": no test at the hit
+	const int cu = __ldg(g.cu + gi);
+	const int m = id - (int)__ldg(g.mpbase + gi);
+	const long long c = __ldg(g.cbase + gi) + (long long)(m / cu) * (cu + 1) + (m % cu);
+	const float2 A = __ldg(g.trim.uv + c), B = __ldg(g.trim.uv + c + 1);
+	const float2 C = __ldg(g.trim.uv + c + cu + 1), D = __ldg(g.trim.uv + c + cu + 2);
+	const float2 r = bilinear_evaluate(A, B, C, D, u, v);
+	const int set = __ldg(g.trim.grid_set + gi);
+	return trim_point(g.trim.pts, g.trim.loop_first, __ldg(g.trim.set_first + set), __ldg(g.trim.set_first + set + 1),
+	                  r.x, r.y);
+}
+
 // Entry i of a colour array (Ci or Oi): float4, or three packed floats when
 // the grids arrived in the three-float host layout.
 __device__ __forceinline__ float4 ld_colour(const GridsDev& g, const float4* p, long long i) {

@@ -62,9 +62,11 @@ __device__ __forceinline__ bool dof_in_bound(const Bnd& b, float cminx, float cm
 
 // Hit test of one sample against one micropolygon: CqMicroPolygon::Sample
 // (static, with DoF) or CqMicroPolygonMotion::Sample.  On a hit returns depth
-// and (u,v).
+// and (u,v).  With `gt`, a static micropolygon marked trimmed also takes the
+// trim test (the motion form has none, micropolygon.cpp:1876-1882).
 __device__ bool mb_sample(const FrameParams& fp, const MbRec& r, bool moving, bool dof, float px, float py,
-                          float time, float dx, float dy, float& D, float& u, float& v, const float4* tri = nullptr) {
+                          float time, float dx, float dy, float& D, float& u, float& v, const float4* tri = nullptr,
+                          const GridsDev* gt = nullptr) {
 	V3f pts[4];
 	if (!moving) {
 		// dof only (the static no-DoF case never reaches this kernel)
@@ -135,6 +137,7 @@ __device__ bool mb_sample(const FrameParams& fp, const MbRec& r, bool moving, bo
 	if (!edges_inside(h.ym, h.xm, h.ex, h.ey, px, py)) return false;
 	inv_bilinear(h.ax, h.ay, h.e_x, h.e_y, h.f_x, h.f_y, h.g_x, h.g_y, h.linear, px, py, u, v);
 	D = bilerp1(h.z[0], h.z[1], h.z[2], h.z[3], u, v);
+	if (gt && !moving && (r.bits & 32) && trim_rejects(*gt, r.id, r.grid, u, v)) return false;
 	if (tri && (r.bits & 4)) {
 		// triangle split line at the sample time (TriangleSplitPoints,
 		// micropolygon.cpp:895-900, over CqMotionSpec::GetMotionObjectInterpolated,
@@ -267,11 +270,12 @@ __device__ __forceinline__ void build_mb_record(const FrameParams& fp, const Gri
 		}
 	}
 	// bits: 2 occluding, 4 triangular, 8 level-of-detail test, 16 CSG (never
-	// occlusion-cullable, never occluding)
+	// occlusion-cullable, never occluding), 32 marked trimmed
 	const bool csg = csg_grid(g, gi);
-	rr.bits = ((!csg && (opaque || (gflags & 4))) ? 2 : 0) | ((gflags & 16) ? 4 : 0) |
-	          (lod_active(fp, g, gi) ? 8 : 0) | (csg ? 16 : 0);
 	rr.id = (int)(__ldg(g.mpbase + gi) + m);
+	rr.bits = ((!csg && (opaque || (gflags & 4))) ? 2 : 0) | ((gflags & 16) ? 4 : 0) |
+	          (lod_active(fp, g, gi) ? 8 : 0) | (csg ? 16 : 0) |
+	          ((g.trim.nsets > 0 && __ldg(g.trim.mark + rr.id)) ? 32 : 0);
 	rr.grid = gi;
 }
 
@@ -702,7 +706,7 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 							if (rcull && B.mnz > oz) continue;
 							if ((r.bits & 8) && lod_rejects(fp, g, smp, r.grid, px, py, j)) continue;
 							float D, u, v;
-							if (!mb_sample(fp, r, moving, usingDof, x, y, stime, sdx, sdy, D, u, v, bb.tri)) continue;
+							if (!mb_sample(fp, r, moving, usingDof, x, y, stime, sdx, sdy, D, u, v, bb.tri, &g)) continue;
 							if (rcull && oz <= D) continue;
 							if ((r.bits & 2) && rcull) {
 								if (TRANSP && fp.midpoint_store) {
@@ -966,7 +970,7 @@ struct SmemP {
 __device__ __forceinline__ bool mb_slice_test(const FrameParams& fp, const MbRec& r, const Bnd& B, bool moving,
                                               float time0, float time1, const float* dofb_k, int px, int py,
                                               float x, float y, float stime, float sdx, float sdy, float oz,
-                                              float& D, const float4* tri) {
+                                              float& D, const float4* tri, const GridsDev* gt) {
 	if (moving && (stime < time0 || stime > time1)) return false;
 	const Bnd TB = fp.use_dof ? stratum_bound(fp, B, dofb_k) : B;
 	if (px < (int)floorf(TB.mnx) || px >= lceil_f(TB.mxx) || py < (int)floorf(TB.mny) || py >= lceil_f(TB.mxy))
@@ -974,7 +978,7 @@ __device__ __forceinline__ bool mb_slice_test(const FrameParams& fp, const MbRec
 	if ((x < TB.mnx || x > TB.mxx) || (y < TB.mny || y > TB.mxy)) return false;
 	if (B.mnz > oz) return false;
 	float u, v;
-	return mb_sample(fp, r, moving, fp.use_dof != 0, x, y, stime, sdx, sdy, D, u, v, tri);
+	return mb_sample(fp, r, moving, fp.use_dof != 0, x, y, stime, sdx, sdy, D, u, v, tri, gt);
 }
 
 __global__ void __launch_bounds__(kThreadsM, 1)
@@ -1161,7 +1165,7 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 					float D, u, v;
 					if (!((r.bits & 8) && lod_rejects(fp, g, smp, r.grid, px, py, j)) &&
 					    mb_sample(fp, r, r.nkeys > 1, usingDof, (float)px + o.x, (float)py + o.y, sm.stime[s], d.x, d.y,
-					              D, u, v, bb.tri)) {
+					              D, u, v, bb.tri, &g)) {
 						if (!(D >= wz[lane]) || D == 0.0f)
 							atomicOr(&sm.flag[s >> 5], 1u << (s & 31));
 						else
@@ -1347,7 +1351,7 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 						if (j < j0 || j >= j1) continue;
 						if ((r.bits & 8) && lod_rejects(fp, g, smp, r.grid, px, py, j)) continue;
 						float D;
-						if (!mb_slice_test(fp, r, B, moving, time0, time1, dk, px, py, x, y, stime, d.x, d.y, oz, D, bb.tri))
+						if (!mb_slice_test(fp, r, B, moving, time0, time1, dk, px, py, x, y, stime, d.x, d.y, oz, D, bb.tri, &g))
 							continue;
 						if (!(oz <= D)) {
 							oz = D;

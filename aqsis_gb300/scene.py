@@ -30,6 +30,7 @@ import numpy as np
 FILTERS = {"box": 0, "triangle": 1, "gaussian": 2, "catmull-rom": 3, "sinc": 4,
            "disk": 5, "bessel": 6, "mitchell": 7}
 GRID_SMOOTH, GRID_MATTE, GRID_MATTEALPHA, GRID_OPAQUE, GRID_TRIANGULAR, GRID_CAMERA = 1, 2, 4, 8, 16, 32
+GRID_TRIM_OUTSIDE = 64
 FLT_MAX = float(np.finfo(np.float32).max)
 
 
@@ -121,6 +122,11 @@ class Grids:
     csg_node: Optional[np.ndarray] = None    # int32[G] primitive CSG node of each grid, -1 = none
     csg_type: Optional[np.ndarray] = None    # int32[N] CSG node types (GRID_CSG_*)
     csg_parent: Optional[np.ndarray] = None  # int32[N] parent node, -1 = a root
+    trim_set: Optional[np.ndarray] = None    # int32[G] trim set of each grid, -1 = not trimmable
+    trim_uv: Optional[np.ndarray] = None     # float32[NC, 2] surface (u, v) per vertex, indexed like Ci
+    trim_points: Optional[np.ndarray] = None      # float32[NPTS, 2] prepared trim-curve points
+    trim_loop_first: Optional[np.ndarray] = None  # int32[NLOOPS + 1] first point of each loop
+    trim_set_first: Optional[np.ndarray] = None   # int32[NSETS + 1] first loop of each set
 
     @property
     def ngrids(self) -> int:
@@ -372,6 +378,52 @@ def with_csg(scene: Scene, seed: int = 0, ntrees: int = 2, frac: float = 0.6) ->
     return Scene(scene.frame, g, scene.samples)
 
 
+def trim_sets(loops_per_set, seed=0):
+    """Seeded trim sets: each set a list of closed polylines (circles of 8-40
+    points at random centres and radii in the unit square, some with a
+    second loop inside as a hole).  Returns (points, loop_first, set_first)."""
+    rng = np.random.default_rng(seed)
+    pts, loop_first, set_first = [], [0], [0]
+    for nl in loops_per_set:
+        for _ in range(nl):
+            n = int(rng.integers(8, 41))
+            c = rng.uniform(0.2, 0.8, 2)
+            r = rng.uniform(0.1, 0.45)
+            a = np.sort(rng.uniform(0, 2 * np.pi, n))
+            pts.append(np.stack([c[0] + r * np.cos(a), c[1] + r * np.sin(a)], -1))
+            loop_first.append(loop_first[-1] + n)
+        set_first.append(set_first[-1] + nl)
+    P = np.concatenate(pts).astype(np.float32) if pts else np.zeros((0, 2), np.float32)
+    return P, np.array(loop_first, np.int32), np.array(set_first, np.int32)
+
+
+def with_trim(scene: Scene, seed: int = 0, frac: float = 0.7) -> Scene:
+    """The scene with seeded trim curves: each grid's vertices get the
+    surface parameters (iu / cu, iv / cv); about `frac` of the grids are
+    trimmable, using one of four sets (no loops, one loop, two loops, three
+    loops), a quarter of them with the "outside" sense."""
+    rng = np.random.default_rng(seed)
+    g = scene.grids
+    G = g.ngrids
+    pts, lf, sf = trim_sets([0, 1, 2, 3], seed=seed + 1)
+    uv = np.zeros((len(g.Ci), 2), np.float32)
+    for gi in range(G):
+        cu, cv = int(g.cu[gi]), int(g.cv[gi])
+        U, V = np.meshgrid(np.arange(cu + 1) / max(cu, 1), np.arange(cv + 1) / max(cv, 1))
+        # a random affine map of the unit square keeps every set in play
+        o = rng.uniform(-0.3, 0.3, 2)
+        sc = rng.uniform(0.8, 1.5)
+        cb = int(g.cbase[gi])
+        uv[cb:cb + (cu + 1) * (cv + 1), 0] = (o[0] + sc * U).ravel()
+        uv[cb:cb + (cu + 1) * (cv + 1), 1] = (o[1] + sc * V).ravel()
+    tset = np.where(rng.random(G) < frac, rng.integers(0, 4, G), -1).astype(np.int32)
+    flags = np.array(g.flags, np.int32, copy=True)
+    flags[(tset >= 0) & (rng.random(G) < 0.25)] |= GRID_TRIM_OUTSIDE
+    g2 = dataclasses.replace(g, flags=flags, trim_set=tset, trim_uv=uv, trim_points=pts, trim_loop_first=lf,
+                             trim_set_first=sf)
+    return Scene(scene.frame, g2, scene.samples)
+
+
 def opaque_stream(width=1920, height=1080, ngrids=200_000, xs=4, ys=4, seed=0xC1,
                   npatterns=250, explicit_samples=False, filt=("gaussian", 2.0, 2.0)) -> Scene:
     """Opaque synthetic stream: 16x16-quad raster grids, Oi = 1, PixelSamples xs ys."""
@@ -529,7 +581,8 @@ def to_camera_space(scene: Scene, m=None, every: int = 1, **camera_kw) -> Scene:
 # Scene files
 
 _GRID_KEYS = ("cu", "cv", "nkeys", "flags", "pbase", "cbase", "tbase", "times", "P", "Ci", "Oi", "culled", "aov",
-              "lod", "csg_node", "csg_type", "csg_parent")
+              "lod", "csg_node", "csg_type", "csg_parent", "trim_set", "trim_uv", "trim_points", "trim_loop_first",
+              "trim_set_first")
 _SAMPLE_KEYS = ("pos", "time", "dof", "shuffle", "lod", "pos_index", "dof_index", "time_index",
                 "shuffle_index", "lod_index", "dither")
 

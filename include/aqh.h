@@ -67,8 +67,9 @@ enum {
 	AQH_GRID_OPAQUE = 8,      /* caller guarantees Oi >= 1 on every vertex (skips reading Oi while sampling) */
 	AQH_GRID_TRIANGULAR = 16, /* CqMicroPolyGridBase::fTriangular (micropolygon.h:139-147): hits on or behind
 	                             the line through corners cu and cv*(cu+1) miss (micropolygon.cpp:1630-1654) */
-	AQH_GRID_CAMERA = 32      /* P holds camera-space points: projected on the device with the frame's
+	AQH_GRID_CAMERA = 32,     /* P holds camera-space points: projected on the device with the frame's
 	                             camera-to-raster matrix (aqh_set_camera_to_raster) */
+	AQH_GRID_TRIM_OUTSIDE = 64 /* "trimcurve" "sense" "outside" (micropolygon.cpp:754-759) */
 };
 
 typedef struct aqh_ctx aqh_ctx;
@@ -351,6 +352,27 @@ aqh_status aqh_set_lod_bounds(aqh_ctx* ctx, const float* bounds, int ngrids);
 enum { AQH_CSG_PRIMITIVE = 0, AQH_CSG_UNION = 1, AQH_CSG_INTERSECTION = 2, AQH_CSG_DIFFERENCE = 3 };
 aqh_status aqh_set_csg(aqh_ctx* ctx, const int32_t* node_type, const int32_t* node_parent, int nnodes,
                        const int32_t* grid_node, int ngrids);
+
+/* ---- trim curves ----------------------------------------------------------------- */
+/* Trim curves of NURBS grids (CqTrimLoopArray, trimcurve.h:110-160).  A set
+ * is a list of loops, a loop a closed polyline of prepared curve points
+ * (CqTrimLoop::Prepare's m_aCurvePoints, trimcurve.cpp:110-133):
+ * points float[npoints][2]; loop l runs over points [loop_first[l],
+ * loop_first[l+1]); set k over loops [set_first[k], set_first[k+1]).
+ * grid_set[i] is the set of grid i in submission order, -1 for a grid that
+ * cannot be trimmed (grids beyond `ngrids` cannot); uv float[nuv][2] holds
+ * the surface (u, v) of every vertex, indexed like Ci.  As Split does
+ * (micropolygon.cpp:754-835, 1056-1130), a micropolygon whose four corners
+ * are all trimmed (in the grid's sense, AQH_GRID_TRIM_OUTSIDE inverting) and
+ * whose edges cross no loop is dropped, one with any corner trimmed is
+ * tested at each static hit (micropolygon.cpp:1592-1627: the "inside" sense
+ * rejects a hit whose bilinear (u, v) is trimmed; moving micropolygons take
+ * no test).  The arrays are copied; nsets = 0 turns trimming off.  A grid
+ * whose vertices run past `nuv` fails aqh_render with AQH_EINVAL.  Reset by
+ * aqh_frame_begin. */
+aqh_status aqh_set_trim(aqh_ctx* ctx, const int32_t* grid_set, int ngrids, const float* uv, size_t nuv,
+                        const float* points, int npoints, const int32_t* loop_first, int nloops,
+                        const int32_t* set_first, int nsets);
 
 /* ---- arbitrary output variables ----------------------------------------------- */
 /* Extra float channels per vertex: the shader outputs a display asks for

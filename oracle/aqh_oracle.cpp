@@ -168,6 +168,7 @@ static const int Degeneracy_Mask = 0x8000000;  // micropolygon.h:791
 // Frame-level context (the parts of CqRenderer / SqOptionCache the hider reads).
 struct Ctx {
 	const OrcFrame* f;
+	const OrcGrids* g;
 	int xs, ys, spp;
 	int shiftX, shiftY;
 	// renderer.h:401-406
@@ -212,6 +213,9 @@ struct MP {
 	float lodMin, lodMax;
 	bool lodTest() const { return lodMin >= 0.0f; }
 	int csgNode;  // the grid's CSG primitive node, -1 if none
+	int trimSet;  // the grid's trim set when the micropolygon is marked trimmed (MarkTrimmed), else -1
+	bool trimOutside;
+	V2 trimUV[4];  // u v at index, index+1, index+cu+1, index+cu+2
 	bool lodRejects(float level) const { return lodMin > level || level >= lodMax; }
 };
 
@@ -451,9 +455,75 @@ static bool triangleSplitKeeps(const Ctx& ctx, const MP& mp, const Sample& sampl
 	return !(v <= 0);
 }
 
-// micropolygon.cpp:1561-1660 (static micropolygon; trimming not modelled).
+// CqTrimLoop::TrimPoint (trimcurve.cpp:145-169): crossings of the loop's
+// edges on the left of the point, by the even-odd rule.
+static bool trimLoopPoint(const float* pts, int first, int size, V2 v) {
+	const float x = v.x, y = v.y;
+	bool odd = false;
+	for (int i = 0, j = size - 1; i < size; j = i++) {
+		const float ax = pts[2 * (first + i)], ay = pts[2 * (first + i) + 1];
+		const float bx = pts[2 * (first + j)], by = pts[2 * (first + j) + 1];
+		if (((ay < y) && (by >= y)) || ((by < y) && (ay >= y))) {
+			if (ax + (y - ay) / (by - ay) * (bx - ax) < x) odd = !odd;
+		}
+	}
+	return odd;
+}
+
+// CqTrimLoopArray::TrimPoint (trimcurve.cpp:223-237): no loops trims nothing;
+// else a point inside an even number of loops is trimmed.
+static bool trimPoint(const OrcGrids* g, int set, V2 v) {
+	const int l0 = g->trim_set_first[set], l1 = g->trim_set_first[set + 1];
+	if (l1 == l0) return false;
+	int crosses = 0;
+	for (int l = l0; l < l1; ++l) {
+		const int p0 = g->trim_loop_first[l];
+		crosses += trimLoopPoint(g->trim_points, p0, g->trim_loop_first[l + 1] - p0, v) ? 1 : 0;
+	}
+	return !(crosses & 1);
+}
+
+// CqTrimLoop::LineIntersects / CqTrimLoopArray::LineIntersects
+// (trimcurve.cpp:172-198, 240-253).
+static bool trimLine(const OrcGrids* g, int set, V2 v1, V2 v2) {
+	const float x1 = v1.x, y1 = v1.y, x2 = v2.x, y2 = v2.y;
+	for (int l = g->trim_set_first[set]; l < g->trim_set_first[set + 1]; ++l) {
+		const int p0 = g->trim_loop_first[l], size = g->trim_loop_first[l + 1] - p0;
+		const float* P = g->trim_points;
+		for (int i = 0, j = size - 1; i < size; j = i++) {
+			const float x3 = P[2 * (p0 + i)], y3 = P[2 * (p0 + i) + 1];
+			const float x4 = P[2 * (p0 + j)], y4 = P[2 * (p0 + j) + 1];
+			const float d = (x2 - x1) * (y4 - y3) - (y2 - y1) * (x4 - x3);
+			if (d == 0.0f) continue;
+			const float r = ((y1 - y3) * (x4 - x3) - (x1 - x3) * (y4 - y3)) / d;
+			const float s = ((y1 - y3) * (x2 - x1) - (x1 - x3) * (y2 - y1)) / d;
+			if ((r >= 0.0f) && (s >= 0.0f) && (r <= 1.0f) && (s <= 1.0f)) return true;
+		}
+	}
+	return false;
+}
+
+// BilinearEvaluate (bilinear.h:189-224) of CqVector2D corners.
+static V2 bilinearEvaluate(V2 A, V2 B, V2 C, V2 D, float s, float t) {
+	V2 AB, CD;
+	if (s <= 0.0) {
+		AB = A;
+		CD = C;
+	} else if (s >= 1.0) {
+		AB = B;
+		CD = D;
+	} else {
+		AB = V2((B.x - A.x) * s + A.x, (B.y - A.y) * s + A.y);
+		CD = V2((D.x - C.x) * s + C.x, (D.y - C.y) * s + C.y);
+	}
+	if (t <= 0.0) return AB;
+	if (t >= 1.0) return CD;
+	return V2((CD.x - AB.x) * t + AB.x, (CD.y - AB.y) * t + AB.y);
+}
+
+// micropolygon.cpp:1561-1660 (static micropolygon).
 static bool sampleStatic(const Ctx& ctx, const MP& mp, HitTestCache& cache, const Sample& sample, float& D, V2& uv,
-                         bool usingDof) {
+                         bool usingDof, const OrcGrids* g) {
 	V2 vecSample = sample.position;
 	if (usingDof) {
 		if (!dofSampleInBound(mp.bound, cache, sample)) return false;
@@ -468,6 +538,12 @@ static bool sampleStatic(const Ctx& ctx, const MP& mp, HitTestCache& cache, cons
 		cachePointInPolyTest(mp, cache, points);
 	}
 	if (!fContains(cache, vecSample, D, uv)) return false;
+	// trimmed micropolygons (micropolygon.cpp:1592-1627): only the "inside"
+	// sense rejects here
+	if (mp.trimSet >= 0) {
+		const V2 vR = bilinearEvaluate(mp.trimUV[0], mp.trimUV[1], mp.trimUV[2], mp.trimUV[3], uv.x, uv.y);
+		if (trimPoint(g, mp.trimSet, vR) && !mp.trimOutside) return false;
+	}
 	return !mp.triangular || triangleSplitKeeps(ctx, mp, sample, D, sample.time, usingDof);
 }
 
@@ -604,7 +680,7 @@ static void renderStatic(Frame& fr, MP& mp) {
 					fr.splBoundHits++;
 					float D;
 					V2 uv;
-					if (sampleStatic(ctx, mp, cache, sd, D, uv, false)) storeSample(fr, mp, sd, D, uv);
+					if (sampleStatic(ctx, mp, cache, sd, D, uv, false, ctx.g)) storeSample(fr, mp, sd, D, uv);
 				}
 				index_start += iXSamples;
 			}
@@ -774,7 +850,7 @@ static void renderMBOrDof(Frame& fr, MP& mp, bool isMoving, bool usingDof, const
 						float D;
 						V2 uv;
 						bool hit = isMoving ? sampleMotion(ctx, mp, cache, sd, D, uv, time, usingDof)
-						                    : sampleStatic(ctx, mp, cache, sd, D, uv, usingDof);
+						                    : sampleStatic(ctx, mp, cache, sd, D, uv, usingDof, ctx.g);
 						if (hit) storeSample(fr, mp, sd, D, uv);
 					} while (!usingDof && index < indexT1);
 				}
@@ -1051,6 +1127,7 @@ extern "C" void orc_bilerp2(const float* q, const float* uv, int n, float* P) {
 extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples* s, const float* ftab, OrcOut* out) {
 	Frame fr;
 	fr.ctx.f = f;
+	fr.ctx.g = g;
 	fr.ctx.xs = f->xsamples;
 	fr.ctx.ys = f->ysamples;
 	fr.ctx.spp = f->xsamples * f->ysamples;
@@ -1127,6 +1204,34 @@ extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples
 			for (int iu = 0; iu < cu; iu++, mpid++) {
 				if (g->culled && g->culled[mpid]) continue;
 				const int index = iv * (cu + 1) + iu;
+				// trimming in Split (micropolygon.cpp:754-835, 1056-1130)
+				mp.trimSet = -1;
+				if (g->trim_set && g->trim_set[gi] >= 0) {
+					const int set = g->trim_set[gi];
+					const long long c = cb + index;
+					auto uvAt = [&](long long k) { return V2(g->trim_uv[2 * k], g->trim_uv[2 * k + 1]); };
+					const V2 vecA = uvAt(c), vecB = uvAt(c + 1), vecC = uvAt(c + cu + 2), vecD = uvAt(c + cu + 1);
+					const bool outside = (flags & ORC_GRID_TRIM_OUTSIDE) != 0;
+					bool tA = trimPoint(g, set, vecA), tB = trimPoint(g, set, vecB);
+					bool tC = trimPoint(g, set, vecC), tD = trimPoint(g, set, vecD);
+					if (outside) {
+						tA = !tA;
+						tB = !tB;
+						tC = !tC;
+						tD = !tD;
+					}
+					if (tA && tB && tC && tD && !trimLine(g, set, vecA, vecB) && !trimLine(g, set, vecB, vecC) &&
+					    !trimLine(g, set, vecC, vecD) && !trimLine(g, set, vecD, vecA))
+						continue;  // trimmed out: never added
+					if (tA || tB || tC || tD) {
+						mp.trimSet = set;
+						mp.trimOutside = outside;
+						mp.trimUV[0] = vecA;
+						mp.trimUV[1] = vecB;
+						mp.trimUV[2] = vecD;  // index + cu + 1
+						mp.trimUV[3] = vecC;  // index + cu + 2
+					}
+				}
 				mp.id = mpid;
 				mp.grid = gi;
 				mp.index = index;

@@ -36,7 +36,8 @@ enum {
 	ORC_GRID_MATTE = 2,       /* SqImageSample::Flag_Matte */
 	ORC_GRID_MATTEALPHA = 4,  /* SqImageSample::Flag_MatteAlpha */
 	ORC_GRID_TRIANGULAR = 16, /* CqMicroPolyGridBase::fTriangular: split line through corners cu, cv*(cu+1) */
-	ORC_GRID_CAMERA = 32      /* P in camera space: orc_project_points first (orc_render itself ignores it) */
+	ORC_GRID_CAMERA = 32,     /* P in camera space: orc_project_points first (orc_render itself ignores it) */
+	ORC_GRID_TRIM_OUTSIDE = 64 /* "trimcurve" "sense" "outside" */
 };
 
 typedef struct {
@@ -82,6 +83,14 @@ typedef struct {
 	int32_t csg_nnodes;
 	const int32_t* csg_type;
 	const int32_t* csg_parent;
+	/* trim curves (NURBS surfaces, CqTrimLoopArray, trimcurve.h:110-160): the
+	 * trim set of each grid (-1: not trimmable) and the sets as loops of
+	 * prepared curve points; uv float[vertex][2] indexed like Ci */
+	const int32_t* trim_set;
+	const float* trim_uv;
+	const float* trim_points;      /* float[point][2] */
+	const int32_t* trim_loop_first; /* [nloops + 1] first point of each loop */
+	const int32_t* trim_set_first;  /* [nsets + 1] first loop of each set */
 } OrcGrids;
 
 enum { ORC_CSG_PRIMITIVE = 0, ORC_CSG_UNION = 1, ORC_CSG_INTERSECTION = 2, ORC_CSG_DIFFERENCE = 3 };

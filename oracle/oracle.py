@@ -43,7 +43,9 @@ class OrcGrids(C.Structure):
                 ("pbase", _i64p), ("cbase", _i64p), ("tbase", _i64p), ("times", _f32p),
                 ("P", _f32p), ("Ci", _f32p), ("Oi", _f32p), ("flags", _i32p), ("culled", _u8p),
                 ("aov", _f32p), ("naov", C.c_int32), ("lod", _f32p),
-                ("csg_node", _i32p), ("csg_nnodes", C.c_int32), ("csg_type", _i32p), ("csg_parent", _i32p)]
+                ("csg_node", _i32p), ("csg_nnodes", C.c_int32), ("csg_type", _i32p), ("csg_parent", _i32p),
+                ("trim_set", _i32p), ("trim_uv", _f32p), ("trim_points", _f32p), ("trim_loop_first", _i32p),
+                ("trim_set_first", _i32p)]
 
 
 class OrcSamples(C.Structure):
@@ -209,6 +211,15 @@ def render(scene, qchannels=(0, 1, 2, 6), want_samples: bool = True) -> dict:
         og.csg_nnodes = int(np.asarray(g.csg_type).shape[0])
         og.csg_type = _p(arr(g.csg_type, np.int32), _i32p)
         og.csg_parent = _p(arr(g.csg_parent, np.int32), _i32p)
+    if getattr(g, "trim_set", None) is not None:
+        ts = np.full(g.ngrids, -1, np.int32)
+        given = np.asarray(g.trim_set, np.int32).ravel()[:g.ngrids]
+        ts[:given.shape[0]] = given
+        og.trim_set = _p(arr(ts, np.int32), _i32p)
+        og.trim_uv = _p(arr(g.trim_uv, np.float32), _f32p)
+        og.trim_points = _p(arr(np.asarray(g.trim_points, np.float32).reshape(-1, 2), np.float32), _f32p)
+        og.trim_loop_first = _p(arr(g.trim_loop_first, np.int32), _i32p)
+        og.trim_set_first = _p(arr(g.trim_set_first, np.int32), _i32p)
     os_ = OrcSamples(x0, y0, w, h, s.npatterns, _p(arr(s.pos, np.float32), _f32p),
                      _p(arr(s.time, np.float32), _f32p), _p(arr(s.dof, np.float32), _f32p),
                      _p(arr(s.shuffle, np.int32), _i32p), _p(arr(s.lod, np.float32), _f32p),
