@@ -50,3 +50,17 @@ def test_random_frame_with_solids(aqh_lib, oracle, seed):
     finally:
         h.close()
     compare(res, ref)
+
+
+@pytest.mark.parametrize("seed", SEEDS[:150])
+def test_random_frame_with_trims(aqh_lib, oracle, seed):
+    """Random frames with random trim sets over their grids."""
+    from aqsis_gb300 import scene as S
+    sc = S.with_trim(SS.fuzz(seed), seed=seed, frac=0.4 + 0.6 * (seed % 5) / 4)
+    h = aqh_lib.Hider(0)
+    try:
+        h.set_mode(seed % 2 == 1)
+        res = h.render_scene(sc)
+    finally:
+        h.close()
+    compare(res, oracle.render(sc))
