@@ -193,6 +193,7 @@ def load(build_if_missing: bool = False):
     L.aqh_set_aov_count.argtypes = [vp, C.c_int]
     L.aqh_set_lod_bounds.argtypes = [vp, _f32p, C.c_int]
     L.aqh_set_csg.argtypes = [vp, _i32p, _i32p, C.c_int, _i32p, C.c_int]
+    L.aqh_set_host_copy.argtypes = [vp, C.c_int]
     L.aqh_set_trim.argtypes = [vp, _i32p, C.c_int, _f32p, C.c_size_t, _f32p, C.c_int, _i32p, C.c_int, _i32p, C.c_int]
     L.aqh_dspy_geometry_of.argtypes = [vp, C.POINTER(DspyGeometry)]
     L.aqh_dspy_open.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(DspyGeometry), C.POINTER(Display),
@@ -219,7 +220,7 @@ def load(build_if_missing: bool = False):
                  "aqh_autotune", "aqh_set_camera_to_raster", "aqh_read_display", "aqh_set_aov_count",
                  "aqh_submit_aov_host", "aqh_submit_aov_device", "aqh_read_aov", "aqh_dspy_geometry_of",
                  "aqh_dspy_open", "aqh_dspy_send", "aqh_dspy_send_image", "aqh_dspy_close", "aqh_set_lod_bounds",
-                 "aqh_set_csg", "aqh_set_trim"):
+                 "aqh_set_csg", "aqh_set_trim", "aqh_set_host_copy"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -485,6 +486,10 @@ class Hider:
 
     def set_stream(self, stream_handle: int):
         self._check(self.L.aqh_set_stream(self.ctx, stream_handle or None), "aqh_set_stream")
+
+    def set_host_copy(self, engines: bool):
+        """Three-float P by the copy engines (True) or read by a kernel (aqh_set_host_copy)."""
+        self._check(self.L.aqh_set_host_copy(self.ctx, 1 if engines else 0), "aqh_set_host_copy")
 
     def render(self, sync: bool = True):
         self._check(self.L.aqh_render(self.ctx, 1 if sync else 0), "aqh_render")

@@ -327,6 +327,7 @@ struct aqh_ctx {
 	bool any_transparent = false;
 	// Split's projection: grids flagged AQH_GRID_CAMERA and the frame's matrix
 	bool any_camera = false;
+	int host_copy = AQH_HOST_COPY_AUTO;
 	bool camera_set = false;
 	aqh::CamMatrix camera{};
 	// output variables: count, per-vertex values staged for host grids, the
@@ -858,8 +859,9 @@ static aqh_status upload_packed_grids(aqh_ctx* ctx) {
 		// over this link, and no second pass), else copied up and widened
 		AQH_TRY(ctx->d_P.ensure(std::max<size_t>(hp.nP, 1) * 16), "upload P");
 		cudaPointerAttributes pa{};
-		const bool mapped = hp.nP && cudaPointerGetAttributes(&pa, hp.P) == cudaSuccess &&
-		                    pa.type == cudaMemoryTypeHost && pa.devicePointer;
+		const bool mapped = ctx->host_copy == AQH_HOST_COPY_AUTO && hp.nP &&
+		                    cudaPointerGetAttributes(&pa, hp.P) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+		                    pa.devicePointer;
 		cudaGetLastError();
 		if (mapped) {
 			launch_widen3(static_cast<const float*>(pa.devicePointer), ctx->d_P.as<float4>(), hp.nP, ctx->stream);
@@ -1558,6 +1560,13 @@ aqh_status aqh_set_trim(aqh_ctx* ctx, const int32_t* grid_set, int ngrids, const
 	ctx->trim_loop_first.assign(loop_first, loop_first + nloops + 1);
 	ctx->trim_set_first.assign(set_first, set_first + nsets + 1);
 	ctx->trim_nsets = nsets;
+	return AQH_OK;
+}
+
+aqh_status aqh_set_host_copy(aqh_ctx* ctx, int mode) {
+	if (!ctx) return AQH_EINVAL;
+	if (mode != AQH_HOST_COPY_AUTO && mode != AQH_HOST_COPY_ENGINES) return ctx->fail(AQH_EINVAL, "bad host copy mode %d", mode);
+	ctx->host_copy = mode;
 	return AQH_OK;
 }
 

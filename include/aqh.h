@@ -222,6 +222,13 @@ aqh_status aqh_submit_grids_host3(aqh_ctx* ctx, int ngrids,
                                   const int32_t* tbase, const float* times, size_t ntimes,
                                   const float* P, size_t nP, const float* Ci, const float* Oi, size_t nC,
                                   const uint8_t* culled, int64_t total_micropolygons);
+/* How aqh_render moves three-float P from page-locked host memory:
+ * AQH_HOST_COPY_AUTO (default) widens it with a kernel that reads the host
+ * array directly (fastest for one frame at a time); AQH_HOST_COPY_ENGINES
+ * copies it with the copy engines and widens it on the device, so the
+ * transfer overlaps another context's frame in flight. */
+enum { AQH_HOST_COPY_AUTO = 0, AQH_HOST_COPY_ENGINES = 1 };
+aqh_status aqh_set_host_copy(aqh_ctx* ctx, int mode);
 /* Page-locked host memory for grid arrays. */
 void* aqh_host_alloc(size_t bytes);
 void aqh_host_free(void* p);

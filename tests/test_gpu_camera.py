@@ -108,8 +108,9 @@ def test_three_float_host_grids(aqh_lib, oracle, name):
     ref = oracle.render(sc)
     h = aqh_lib.Hider(0)
     try:
-        for batched in (False, True):
+        for batched, engines in ((False, False), (True, False), (True, True)):
             h.set_mode(batched)
+            h.set_host_copy(engines)
             h.frame_begin(sc.frame)
             h.set_samples(sc.samples)
             h.submit_grids_host(sc.grids, packed3=True)
