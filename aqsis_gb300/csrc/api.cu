@@ -853,6 +853,33 @@ static aqh_status upload_packed_grids(aqh_ctx* ctx) {
 	AQH_TRY(up(ctx->d_mpbase, ctx->h_mpbase.data(), G * 8), "upload grids");
 	AQH_TRY(up(ctx->d_times, hp.times, std::max<size_t>(hp.ntimes, 1) * 4), "upload grids");
 	const bool packed3 = hp.comps == 3;
+	// Ci/Oi go up on the copy stream, after everything already queued on the
+	// main stream (the previous frame may still read the old colours); with
+	// the copy engines moving P as well they start at once, beside P, so a
+	// widening kernel that waits for another context's frame to leave the
+	// SMs does not hold them back; otherwise after P's widening kernel, which
+	// reads the host array over the same link
+	DevBuf& dCi = packed3 ? ctx->d_C3 : ctx->d_Ci;
+	DevBuf& dOi = packed3 ? ctx->d_O3 : ctx->d_Oi;
+	const size_t csz = packed3 ? 12 : 16;
+	AQH_TRY(dCi.ensure(std::max<size_t>(hp.nC, 1) * csz), "upload Ci");
+	AQH_TRY(dOi.ensure(std::max<size_t>(hp.nC, 1) * csz), "upload Oi");
+	auto colours_up = [&]() -> aqh_status {
+		AQH_TRY(cudaEventRecord(ctx->ev_before_up, ctx->stream), "upload Ci");
+		AQH_TRY(cudaStreamWaitEvent(ctx->cstream, ctx->ev_before_up, 0), "upload Ci");
+		if (hp.Ci && hp.nC)
+			AQH_TRY(cudaMemcpyAsync(dCi.p, hp.Ci, hp.nC * csz, cudaMemcpyHostToDevice, ctx->cstream), "upload Ci");
+		if (hp.Oi && hp.nC)
+			AQH_TRY(cudaMemcpyAsync(dOi.p, hp.Oi, hp.nC * csz, cudaMemcpyHostToDevice, ctx->cstream), "upload Oi");
+		AQH_TRY(cudaEventRecord(ctx->ev_cioi, ctx->cstream), "upload Ci");
+		ctx->cioi_pending = true;
+		return AQH_OK;
+	};
+	const bool colours_first = ctx->host_copy == AQH_HOST_COPY_ENGINES;
+	if (colours_first) {
+		const aqh_status st = colours_up();
+		if (st != AQH_OK) return st;
+	}
 	if (packed3) {
 		// three-float P: widened to float4 by a kernel that reads the host
 		// array itself when it is page-locked (as fast as the copy engines
@@ -872,22 +899,11 @@ static aqh_status upload_packed_grids(aqh_ctx* ctx) {
 	} else {
 		AQH_TRY(up(ctx->d_P, hp.P, hp.nP * 16), "upload P");
 	}
-	// Ci/Oi on the copy stream, after everything already queued on the main
-	// stream (the previous frame may still read the old colours); three-float
-	// colours stay packed on the device (GridsDev::colour3)
-	DevBuf& dCi = packed3 ? ctx->d_C3 : ctx->d_Ci;
-	DevBuf& dOi = packed3 ? ctx->d_O3 : ctx->d_Oi;
-	const size_t csz = packed3 ? 12 : 16;
-	AQH_TRY(dCi.ensure(std::max<size_t>(hp.nC, 1) * csz), "upload Ci");
-	AQH_TRY(dOi.ensure(std::max<size_t>(hp.nC, 1) * csz), "upload Oi");
-	AQH_TRY(cudaEventRecord(ctx->ev_before_up, ctx->stream), "upload Ci");
-	AQH_TRY(cudaStreamWaitEvent(ctx->cstream, ctx->ev_before_up, 0), "upload Ci");
-	if (hp.Ci && hp.nC)
-		AQH_TRY(cudaMemcpyAsync(dCi.p, hp.Ci, hp.nC * csz, cudaMemcpyHostToDevice, ctx->cstream), "upload Ci");
-	if (hp.Oi && hp.nC)
-		AQH_TRY(cudaMemcpyAsync(dOi.p, hp.Oi, hp.nC * csz, cudaMemcpyHostToDevice, ctx->cstream), "upload Oi");
-	AQH_TRY(cudaEventRecord(ctx->ev_cioi, ctx->cstream), "upload Ci");
-	ctx->cioi_pending = true;
+	// three-float colours stay packed on the device (GridsDev::colour3)
+	if (!colours_first) {
+		const aqh_status st = colours_up();
+		if (st != AQH_OK) return st;
+	}
 	if (hp.culled) AQH_TRY(up(ctx->d_culled, hp.culled, (size_t)ctx->h_mps), "upload culled");
 	GridsDev& g = ctx->dg;
 	g.ngrids = G;
