@@ -397,32 +397,34 @@ def run_gpu(args):
     barrier()
     single_ms = max_over_ranks(f0.elapsed_time(f1) / e2e_steps, dist, dev)
     h2.close()
-    # two frames in flight: two contexts on two streams, the copy engines
-    # bringing one frame's arrays up while the other frame samples; every
-    # frame still uploads its own inputs and reads back its own image
-    s2 = torch.cuda.Stream(dev)
-    pair = [host_hider(stream, True), host_hider(s2, True)]
-    for hh in pair:
+    # several frames in flight: one context per frame on its own stream, the
+    # copy engines bringing later frames' arrays up while one frame samples;
+    # every frame still uploads its own inputs and reads back its own image
+    k = max(1, args.e2e_inflight)
+    streams = [stream] + [torch.cuda.Stream(dev) for _ in range(k - 1)]
+    pool = [host_hider(s, True) for s in streams]
+    for hh in pool:
         for _ in range(max(1, args.warmup)):
             hh.render(sync=True)
             out = hh.read_quantized(qch)
-    n2 = 2 * e2e_steps
+    n2 = k * e2e_steps
     barrier()
     torch.cuda.synchronize(dev)
     f0.record(stream)
     for i in range(n2):
-        hh = pair[i % 2]
-        if i >= 2:
-            out = hh.read_quantized(qch)  # frame i-2, before this context renders again
+        hh = pool[i % k]
+        if i >= k:
+            out = hh.read_quantized(qch)  # frame i-k, before this context renders again
         hh.render(sync=False)
-    for hh in (pair[n2 % 2], pair[(n2 + 1) % 2]):
-        out = hh.read_quantized(qch)
-    stream.wait_stream(s2)
+    for i in range(n2 - k, n2):
+        out = pool[i % k].read_quantized(qch)
+    for s in streams[1:]:
+        stream.wait_stream(s)
     f1.record(stream)
     torch.cuda.synchronize(dev)
     barrier()
     e2e_ms_max = max_over_ranks(f0.elapsed_time(f1) / n2, dist, dev)
-    for hh in pair:
+    for hh in pool:
         hh.close()
     e2e_value = replica_throughput(mps, world, e2e_ms_max)
     h2d = sum(int(p.numel() * p.element_size()) for p in pin.values())
@@ -468,7 +470,7 @@ def run_gpu(args):
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_ms_max,
                     "path": "aqh_submit_grids_host3 (P, Ci, Oi as float3) + aqh_render + aqh_read_quantized_u8; "
-                            "two contexts, two frames in flight, copy-engine uploads",
+                            "%d contexts, %d frames in flight, copy-engine uploads" % (k, k),
                     "one_in_flight": {"value": replica_throughput(mps, world, single_ms), "ms_per_step": single_ms}}}
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
@@ -619,6 +621,8 @@ def main():
     ap.add_argument("--cpu-scale", type=float, default=0.4)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--e2e-inflight", type=int, default=3,
+                    help="frames in flight in the end-to-end leg (one context each)")
     ap.add_argument("--workload", default="opaque", choices=["opaque", "transparent", "mbdof", "spheres", "served"])
     ap.add_argument("--jobs", type=int, default=256)
     ap.add_argument("--distinct", type=int, default=32)
