@@ -184,6 +184,9 @@ aqh_status aqh_server_create(const aqh_server_opts* o, aqh_server** out) {
 			return st;
 		}
 		aqh_set_mode(c, o->mode);
+		// several jobs are in flight: host arrays move on the copy engines,
+		// colours beside P, while another slot's frame holds the SMs
+		aqh_set_host_copy(c, AQH_HOST_COPY_ENGINES);
 		sv->ctx.push_back(c);
 	}
 	aqh_server* raw = sv.release();
