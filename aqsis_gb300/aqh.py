@@ -194,6 +194,7 @@ def load(build_if_missing: bool = False):
     L.aqh_set_lod_bounds.argtypes = [vp, _f32p, C.c_int]
     L.aqh_set_csg.argtypes = [vp, _i32p, _i32p, C.c_int, _i32p, C.c_int]
     L.aqh_set_host_copy.argtypes = [vp, C.c_int]
+    L.aqh_set_cull_normals.argtypes = [vp, _f32p, _f32p, C.c_size_t]
     L.aqh_set_trim.argtypes = [vp, _i32p, C.c_int, _f32p, C.c_size_t, _f32p, C.c_int, _i32p, C.c_int, _i32p, C.c_int]
     L.aqh_dspy_geometry_of.argtypes = [vp, C.POINTER(DspyGeometry)]
     L.aqh_dspy_open.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(DspyGeometry), C.POINTER(Display),
@@ -220,7 +221,8 @@ def load(build_if_missing: bool = False):
                  "aqh_autotune", "aqh_set_camera_to_raster", "aqh_read_display", "aqh_set_aov_count",
                  "aqh_submit_aov_host", "aqh_submit_aov_device", "aqh_read_aov", "aqh_dspy_geometry_of",
                  "aqh_dspy_open", "aqh_dspy_send", "aqh_dspy_send_image", "aqh_dspy_close", "aqh_set_lod_bounds",
-                 "aqh_set_csg", "aqh_set_trim", "aqh_set_host_copy"):
+                 "aqh_set_csg", "aqh_set_trim", "aqh_set_host_copy",
+                 "aqh_set_cull_normals"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -410,6 +412,8 @@ class Hider:
             self.set_csg(g.csg_type, g.csg_parent, g.csg_node)
         if getattr(g, "trim_set", None) is not None:
             self.set_trim(g.trim_set, g.trim_uv, g.trim_points, g.trim_loop_first, g.trim_set_first)
+        if getattr(g, "cull_Ng", None) is not None or (np.asarray(g.flags) & 256).any():
+            self.set_cull_normals(getattr(g, "cull_Ng", None), getattr(g, "cull_N", None))
 
     def submit_grids_host(self, g, packed3: bool = False):
         """Submit a whole packed scene.Grids in one aqh_submit_grids_host call
@@ -453,6 +457,8 @@ class Hider:
             self.set_csg(g.csg_type, g.csg_parent, g.csg_node)
         if getattr(g, "trim_set", None) is not None:
             self.set_trim(g.trim_set, g.trim_uv, g.trim_points, g.trim_loop_first, g.trim_set_first)
+        if getattr(g, "cull_Ng", None) is not None or (np.asarray(g.flags) & 256).any():
+            self.set_cull_normals(getattr(g, "cull_Ng", None), getattr(g, "cull_N", None))
         self._packed_keep = keep
 
     def submit_grids_device(self, ngrids, d_cu, d_cv, d_nkeys, d_flags, d_pbase, d_cbase, d_tbase, d_times,
@@ -486,6 +492,14 @@ class Hider:
 
     def set_stream(self, stream_handle: int):
         self._check(self.L.aqh_set_stream(self.ctx, stream_handle or None), "aqh_set_stream")
+
+    def set_cull_normals(self, Ng, N=None):
+        """Shade / Split culling for the frame (aqh_set_cull_normals): camera-space
+        Ng and N (or None) per P entry."""
+        ng = None if Ng is None else np.ascontiguousarray(Ng, np.float32).reshape(-1, 3)
+        n = None if N is None else np.ascontiguousarray(N, np.float32).reshape(-1, 3)
+        cnt = 0 if ng is None else ng.shape[0]
+        self._check(self.L.aqh_set_cull_normals(self.ctx, _p(ng, _f32p), _p(n, _f32p), cnt), "aqh_set_cull_normals")
 
     def set_host_copy(self, engines: bool):
         """Three-float P by the copy engines (True) or read by a kernel (aqh_set_host_copy)."""

@@ -348,6 +348,9 @@ struct aqh_ctx {
 	DevBuf d_csg, d_csg_overflow;
 	// trim curves: host copies of the sets, the grids' sets and the uv array
 	int trim_nsets = 0;
+	bool cull_on = false;
+	std::vector<float> cull_Ng, cull_N;
+	DevBuf d_cull_n;
 	std::vector<int32_t> trim_grid_set, trim_loop_first, trim_set_first;
 	std::vector<float> trim_pts, trim_uv;
 	DevBuf d_trim_i, d_trim_f, d_trim_mark, d_trim_cull, d_trim_err;
@@ -545,6 +548,7 @@ aqh_status aqh_frame_begin(aqh_ctx* ctx, const aqh_frame_desc* d) {
 	ctx->lod_set = false;
 	ctx->csg_n = 0;
 	ctx->trim_nsets = 0;
+	ctx->cull_on = false;
 	ctx->hp_aov = nullptr;
 	ctx->hp_naov_vertices = 0;
 	ctx->dev_aov = nullptr;
@@ -1161,6 +1165,31 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 		P.g.naov = ctx->dev_aov ? ctx->naov : 0;
 	}
 	P.g.trim = TrimDev{};
+	if ((ctx->trim_nsets > 0 || ctx->cull_on) && G > 0) {
+		// the frame's own culled mask: the caller's (or none) plus what Shade /
+		// Split culling and trimming drop
+		const size_t nm = (size_t)std::max<int64_t>(P.nmps, 1);
+		AQH_TRY(ctx->d_trim_cull.ensure(nm), "alloc culled mask");
+		AQH_TRY(ctx->d_trim_err.ensure(16), "alloc");
+		AQH_TRY(cudaMemsetAsync(ctx->d_trim_err.p, 0, 4, s), "memset");
+		if (P.g.culled && P.nmps > 0)
+			AQH_TRY(cudaMemcpyAsync(ctx->d_trim_cull.p, P.g.culled, (size_t)P.nmps, cudaMemcpyDeviceToDevice, s), "copy");
+		else
+			AQH_TRY(cudaMemsetAsync(ctx->d_trim_cull.p, 0, nm, s), "memset");
+	}
+	if (ctx->cull_on && G > 0) {
+		const size_t n3 = ctx->cull_Ng.size();
+		AQH_TRY(ctx->d_cull_n.ensure((n3 + ctx->cull_N.size() + 4) * 4), "alloc normals");
+		float* dn = ctx->d_cull_n.as<float>();
+		if (n3) AQH_TRY(cudaMemcpyAsync(dn, ctx->cull_Ng.data(), n3 * 4, cudaMemcpyHostToDevice, s), "upload Ng");
+		if (!ctx->cull_N.empty())
+			AQH_TRY(cudaMemcpyAsync(dn + n3, ctx->cull_N.data(), ctx->cull_N.size() * 4, cudaMemcpyHostToDevice, s),
+			        "upload N");
+		const int zblack = fp.zthr[0] == 0.0f && fp.zthr[1] == 0.0f && fp.zthr[2] == 0.0f;
+		launch_cull_grids(P.g, n3 ? dn : nullptr, ctx->cull_N.empty() ? nullptr : dn + n3, (long long)(n3 / 3), zblack,
+		                  ctx->d_trim_cull.as<uint8_t>(), ctx->d_trim_err.as<int32_t>(), s);
+		AQH_TRY(cudaGetLastError(), "cull kernel launch");
+	}
 	if (ctx->trim_nsets > 0 && G > 0) {
 		// ints: grid sets (G, -1 past the given ones), loop starts, set starts;
 		// floats: loop points, then uv
@@ -1182,15 +1211,7 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 			        "upload trim uv");
 		const size_t nm = (size_t)std::max<int64_t>(P.nmps, 1);
 		AQH_TRY(ctx->d_trim_mark.ensure(nm), "alloc trim marks");
-		AQH_TRY(ctx->d_trim_cull.ensure(nm), "alloc trim marks");
-		AQH_TRY(ctx->d_trim_err.ensure(16), "alloc");
 		AQH_TRY(cudaMemsetAsync(ctx->d_trim_mark.p, 0, nm, s), "memset");
-		AQH_TRY(cudaMemsetAsync(ctx->d_trim_err.p, 0, 4, s), "memset");
-		// the frame's culled mask plus the micropolygons trimmed out
-		if (P.g.culled && P.nmps > 0)
-			AQH_TRY(cudaMemcpyAsync(ctx->d_trim_cull.p, P.g.culled, (size_t)P.nmps, cudaMemcpyDeviceToDevice, s), "copy");
-		else
-			AQH_TRY(cudaMemsetAsync(ctx->d_trim_cull.p, 0, nm, s), "memset");
 		const int32_t* b = ctx->d_trim_i.as<int32_t>();
 		TrimDev& t = P.g.trim;
 		t.nsets = ctx->trim_nsets;
@@ -1203,10 +1224,14 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 		launch_trim_mark(P.g, (long long)(ctx->trim_uv.size() / 2), ctx->d_trim_mark.as<uint8_t>(),
 		                 ctx->d_trim_cull.as<uint8_t>(), ctx->d_trim_err.as<int32_t>(), s);
 		AQH_TRY(cudaGetLastError(), "trim kernel launch");
+	}
+	if ((ctx->trim_nsets > 0 || ctx->cull_on) && G > 0) {
 		int32_t err = 0;
 		AQH_TRY(cudaMemcpyAsync(&err, ctx->d_trim_err.p, 4, cudaMemcpyDeviceToHost, s), "readback");
-		AQH_TRY(cudaStreamSynchronize(s), "trim curves");
-		if (err) return ctx->fail(AQH_EINVAL, "trim curves: a trimmable grid's vertices run past the uv array");
+		AQH_TRY(cudaStreamSynchronize(s), "culling");
+		if (err)
+			return ctx->fail(AQH_EINVAL, "culling: a grid's vertices run past the uv array (trim curves) or the "
+			                 "normal arrays (back faces), or back-face culling without Ng");
 		P.g.culled = ctx->d_trim_cull.as<uint8_t>();
 	}
 	if (P.g.naov > 0) {
@@ -1443,7 +1468,7 @@ aqh_status aqh_render(aqh_ctx* ctx, int sync) {
 	ctx->stats.grids = P.g.ngrids;
 	// CSG frames take the plain path, which reads the resolve's overflow flag;
 	// so do frames with trim curves (their micropolygon marks are per frame)
-	if (ctx->mode == AQH_MODE_BATCHED && P.g.csg.nnodes == 0 && P.g.trim.nsets == 0)
+	if (ctx->mode == AQH_MODE_BATCHED && P.g.csg.nnodes == 0 && P.g.trim.nsets == 0 && !ctx->cull_on)
 		return render_batched(ctx, P, sync != 0);
 	return render_plain(ctx, P, sync != 0 || P.g.csg.nnodes > 0);
 }
@@ -1576,6 +1601,16 @@ aqh_status aqh_set_trim(aqh_ctx* ctx, const int32_t* grid_set, int ngrids, const
 	ctx->trim_loop_first.assign(loop_first, loop_first + nloops + 1);
 	ctx->trim_set_first.assign(set_first, set_first + nsets + 1);
 	ctx->trim_nsets = nsets;
+	return AQH_OK;
+}
+
+aqh_status aqh_set_cull_normals(aqh_ctx* ctx, const float* Ng, const float* N, size_t n) {
+	if (!ctx) return AQH_EINVAL;
+	if (!ctx->frame_open) return ctx->fail(AQH_EINVAL, "no frame");
+	if (!Ng && N) return ctx->fail(AQH_EINVAL, "N without Ng");
+	ctx->cull_Ng.assign(Ng ? Ng : nullptr, Ng ? Ng + 3 * n : nullptr);
+	ctx->cull_N.assign(N ? N : nullptr, N ? N + 3 * n : nullptr);
+	ctx->cull_on = true;
 	return AQH_OK;
 }
 

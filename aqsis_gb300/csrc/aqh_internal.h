@@ -211,6 +211,10 @@ void launch_id_grid(const GridsDev& g, int64_t nmps, int32_t* table, cudaStream_
 // Split's trimming of every micropolygon of a trimmable grid: trimmed out
 // ones are set in `culled`, ones to test at each hit in `mark`; a grid whose
 // vertices run past `nuv` uv entries sets *err and is skipped.
+// Shade / Split culling of the flagged grids, before projection: sets
+// `culled` per micropolygon; a grid that cannot be culled as asked sets *err.
+void launch_cull_grids(const GridsDev& g, const float* Ng, const float* N, long long nng, int zthr_black,
+                       uint8_t* culled, int32_t* err, cudaStream_t s);
 void launch_trim_mark(const GridsDev& g, long long nuv, uint8_t* mark, uint8_t* culled, int32_t* err, cudaStream_t s);
 void launch_project_grids(const GridsDev& g, float4* P, int32_t* flags, const CamMatrix& m, cudaStream_t s);
 void launch_st_count(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cudaStream_t s);

@@ -289,6 +289,76 @@ void launch_project_grids(const GridsDev& g, float4* P, int32_t* flags, const Ca
 	project_grids_kernel<<<g.ngrids, 256, 0, s>>>(g, P, flags, m);
 }
 
+// CqBasicVec3 dot product (vector3d.h:602-606) and the back-face test of one
+// vertex (micropolygon.cpp:451-459, 1013-1017).
+__device__ __forceinline__ bool back_facing(float4 p, const float* ng, const float* n) {
+	const float gx = __ldg(ng), gy = __ldg(ng + 1), gz = __ldg(ng + 2);
+	float s = 1.0f;
+	if (n) s = ((__ldg(n) * gx + __ldg(n + 1) * gy) + __ldg(n + 2) * gz < 0.0f) ? -1.0f : 1.0f;
+	return ((s * gx) * p.x + (s * gy) * p.y) + (s * gz) * p.z >= 0.0f;
+}
+
+// CqMicroPolyGrid::Shade's and CqMotionMicroPolyGrid::Split's culling, one
+// block per flagged grid, on camera-space P before projection.
+__global__ void cull_grids_kernel(GridsDev g, const float* Ng, const float* N, long long nng, int zthr_black,
+                                  uint8_t* culled, int32_t* err) {
+	__shared__ int last_visible;
+	const int gi = blockIdx.x;
+	const int flags = __ldg(g.flags + gi);
+	if (!(flags & (AQH_GRID_CULL_BACKFACING | AQH_GRID_CULL_TRANSPARENT))) return;
+	const int cu = __ldg(g.cu + gi), cv = __ldg(g.cv + gi), nk = __ldg(g.nkeys + gi);
+	const int nv = (cu + 1) * (cv + 1);
+	const long long pb = __ldg(g.pbase + gi), cb = __ldg(g.cbase + gi), mb = __ldg(g.mpbase + gi);
+	// the back-face test needs camera-space P: a grid already projected (a
+	// device-resident grid after its first frame) keeps the result of none
+	const bool bf = (flags & AQH_GRID_CULL_BACKFACING) && (flags & AQH_GRID_CAMERA);
+	if (bf && (!Ng || pb < 0 || pb + (long long)nk * nv > nng)) {
+		if (threadIdx.x == 0) atomicOr(err, 1);
+		return;
+	}
+	// the trailing run of black Oi starts after the last vertex that is not black
+	const bool tr = nk == 1 && (flags & AQH_GRID_CULL_TRANSPARENT) && g.Oi && !zthr_black;
+	if (threadIdx.x == 0) last_visible = -1;
+	__syncthreads();
+	if (tr) {
+		int mx = -1;
+		for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+			float r, gg, b;
+			if (g.colour3) {
+				const float* o = reinterpret_cast<const float*>(g.Oi) + 3 * (cb + i);
+				r = __ldg(o); gg = __ldg(o + 1); b = __ldg(o + 2);
+			} else {
+				const float4 o = __ldg(g.Oi + cb + i);
+				r = o.x; gg = o.y; b = o.z;
+			}
+			if (!(r == 0.0f && gg == 0.0f && b == 0.0f)) mx = i;
+		}
+		atomicMax(&last_visible, mx);
+	}
+	__syncthreads();
+	const int run_start = tr ? last_visible + 1 : nv;
+	for (int m = threadIdx.x; m < cu * cv; m += blockDim.x) {
+		const int ia = (m / cu) * (cu + 1) + (m % cu);
+		bool c = false;
+		if (bf) {
+			int facing_away = 0;
+			for (int k = 0; k < nk; ++k) {
+				const long long e = pb + (long long)k * nv + ia;
+				facing_away += back_facing(__ldg(g.P + e), Ng + 3 * e, N ? N + 3 * e : nullptr) ? 1 : 0;
+			}
+			c = facing_away == nk;
+		}
+		c = c || ia >= run_start;
+		if (c) culled[mb + m] = 1;
+	}
+}
+
+void launch_cull_grids(const GridsDev& g, const float* Ng, const float* N, long long nng, int zthr_black,
+                       uint8_t* culled, int32_t* err, cudaStream_t s) {
+	if (g.ngrids == 0) return;
+	cull_grids_kernel<<<g.ngrids, 256, 0, s>>>(g, Ng, N, nng, zthr_black, culled, err);
+}
+
 // CqMicroPolyGrid::Split / CqMotionMicroPolyGrid::Split trimming
 // (micropolygon.cpp:754-835, 1056-1130), one block per grid: the corners'
 // surface parameters (index, index+1, index+cu+2, index+cu+1) are classified

@@ -31,6 +31,7 @@ FILTERS = {"box": 0, "triangle": 1, "gaussian": 2, "catmull-rom": 3, "sinc": 4,
            "disk": 5, "bessel": 6, "mitchell": 7}
 GRID_SMOOTH, GRID_MATTE, GRID_MATTEALPHA, GRID_OPAQUE, GRID_TRIANGULAR, GRID_CAMERA = 1, 2, 4, 8, 16, 32
 GRID_TRIM_OUTSIDE = 64
+GRID_CULL_BACKFACING, GRID_CULL_TRANSPARENT = 128, 256
 FLT_MAX = float(np.finfo(np.float32).max)
 
 
@@ -127,6 +128,8 @@ class Grids:
     trim_points: Optional[np.ndarray] = None      # float32[NPTS, 2] prepared trim-curve points
     trim_loop_first: Optional[np.ndarray] = None  # int32[NLOOPS + 1] first point of each loop
     trim_set_first: Optional[np.ndarray] = None   # int32[NSETS + 1] first loop of each set
+    cull_Ng: Optional[np.ndarray] = None  # float32[NP, 3] camera-space geometric normal per P entry (every key)
+    cull_N: Optional[np.ndarray] = None   # float32[NP, 3] shading normal per P entry, or None
 
     @property
     def ngrids(self) -> int:
@@ -424,6 +427,33 @@ def with_trim(scene: Scene, seed: int = 0, frac: float = 0.7) -> Scene:
     return Scene(scene.frame, g2, scene.samples)
 
 
+def with_culling(scene: Scene, seed: int = 0) -> Scene:
+    """The scene with seeded Shade / Split culling on its camera-space grids:
+    a geometric normal per P entry (random directions, so about half the
+    vertices face away), shading normals on some grids (flipping Ng where
+    they disagree), GRID_CULL_BACKFACING on about 60% of the camera grids
+    and GRID_CULL_TRANSPARENT with a trailing run of black Oi on about half."""
+    rng = np.random.default_rng(seed)
+    g = scene.grids
+    Ng = rng.normal(size=(len(g.P), 3)).astype(np.float32)
+    N = rng.normal(size=(len(g.P), 3)).astype(np.float32)
+    flags = np.array(g.flags, np.int32, copy=True)
+    Oi = np.array(g.Oi, np.float32, copy=True)
+    cam = (flags & GRID_CAMERA) != 0
+    flags[cam & (rng.random(g.ngrids) < 0.6)] |= GRID_CULL_BACKFACING
+    tr = cam & (rng.random(g.ngrids) < 0.5)
+    flags[tr] |= GRID_CULL_TRANSPARENT
+    for i in np.nonzero(tr)[0]:
+        nv = (int(g.cu[i]) + 1) * (int(g.cv[i]) + 1)
+        run = int(rng.integers(0, nv + 1))
+        cb = int(g.cbase[i])
+        Oi[cb + nv - run:cb + nv, :3] = 0.0
+        flags[i] &= ~GRID_OPAQUE
+    use_n = rng.random() < 0.5
+    g2 = dataclasses.replace(g, flags=flags, Oi=Oi, cull_Ng=Ng, cull_N=N if use_n else None)
+    return Scene(scene.frame, g2, scene.samples)
+
+
 def opaque_stream(width=1920, height=1080, ngrids=200_000, xs=4, ys=4, seed=0xC1,
                   npatterns=250, explicit_samples=False, filt=("gaussian", 2.0, 2.0)) -> Scene:
     """Opaque synthetic stream: 16x16-quad raster grids, Oi = 1, PixelSamples xs ys."""
@@ -582,7 +612,7 @@ def to_camera_space(scene: Scene, m=None, every: int = 1, **camera_kw) -> Scene:
 
 _GRID_KEYS = ("cu", "cv", "nkeys", "flags", "pbase", "cbase", "tbase", "times", "P", "Ci", "Oi", "culled", "aov",
               "lod", "csg_node", "csg_type", "csg_parent", "trim_set", "trim_uv", "trim_points", "trim_loop_first",
-              "trim_set_first")
+              "trim_set_first", "cull_Ng", "cull_N")
 _SAMPLE_KEYS = ("pos", "time", "dof", "shuffle", "lod", "pos_index", "dof_index", "time_index",
                 "shuffle_index", "lod_index", "dither")
 

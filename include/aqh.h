@@ -69,7 +69,11 @@ enum {
 	                             the line through corners cu and cv*(cu+1) miss (micropolygon.cpp:1630-1654) */
 	AQH_GRID_CAMERA = 32,     /* P holds camera-space points: projected on the device with the frame's
 	                             camera-to-raster matrix (aqh_set_camera_to_raster) */
-	AQH_GRID_TRIM_OUTSIDE = 64 /* "trimcurve" "sense" "outside" (micropolygon.cpp:754-759) */
+	AQH_GRID_TRIM_OUTSIDE = 64, /* "trimcurve" "sense" "outside" (micropolygon.cpp:754-759) */
+	AQH_GRID_CULL_BACKFACING = 128, /* Sides 1, outside any solid, "cull" "backfacing" 1: back-facing
+	                                   micropolygons are culled (camera-space grids, aqh_set_cull_normals) */
+	AQH_GRID_CULL_TRANSPARENT = 256 /* the surface shader uses Oi: a static grid's trailing run of vertices
+	                                   with black Oi is culled (micropolygon.cpp:486-506) */
 };
 
 typedef struct aqh_ctx aqh_ctx;
@@ -359,6 +363,23 @@ aqh_status aqh_set_lod_bounds(aqh_ctx* ctx, const float* bounds, int ngrids);
 enum { AQH_CSG_PRIMITIVE = 0, AQH_CSG_UNION = 1, AQH_CSG_INTERSECTION = 2, AQH_CSG_DIFFERENCE = 3 };
 aqh_status aqh_set_csg(aqh_ctx* ctx, const int32_t* node_type, const int32_t* node_parent, int nnodes,
                        const int32_t* grid_node, int ngrids);
+
+/* ---- culling ------------------------------------------------------------------------ */
+/* The culling of CqMicroPolyGrid::Shade and CqMotionMicroPolyGrid::Split done
+ * on the device before projection (micropolygon.cpp:431-506, 957-1020,
+ * 1075-1080), for grids flagged AQH_GRID_CULL_*: Ng (and N, which may be
+ * NULL) are camera-space float[n][3] indexed like P, every key.  A static
+ * grid culls the micropolygons whose first vertex faces away (P . Ng >= 0,
+ * Ng flipped to N's side) and, with AQH_GRID_CULL_TRANSPARENT unless
+ * zthreshold is black, those whose first vertex lies in the trailing run of
+ * vertices with black Oi; a moving grid culls a micropolygon whose first
+ * vertex faces away at every key.  Calling this turns the culling on for the
+ * frame (Ng may be NULL when no grid asks for back faces); the arrays are
+ * copied.  The back-face test applies to AQH_GRID_CAMERA grids only (P still
+ * in camera space; a device-resident grid is projected in place by its first
+ * frame).  A flagged camera grid whose P entries run past `n`, or with no
+ * Ng, fails aqh_render with AQH_EINVAL.  Reset by aqh_frame_begin. */
+aqh_status aqh_set_cull_normals(aqh_ctx* ctx, const float* Ng, const float* N, size_t n);
 
 /* ---- trim curves ----------------------------------------------------------------- */
 /* Trim curves of NURBS grids (CqTrimLoopArray, trimcurve.h:110-160).  A set

@@ -503,6 +503,18 @@ static bool trimLine(const OrcGrids* g, int set, V2 v1, V2 v2) {
 	return false;
 }
 
+// CqBasicVec3 dot product (vector3d.h:602-606)
+static float dot3(const float* a, const float* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// The back-face test of one vertex (micropolygon.cpp:451-459, 1013-1017):
+// Ng flipped to N's side when N is given, facing away from the eye (P . Ng >= 0).
+static bool backFacing(const float* P4, const float* Ng3, const float* N3) {
+	float s = 1.0f;
+	if (N3) s = (dot3(N3, Ng3) < 0.0f) ? -1.0f : 1.0f;
+	const float sn[3] = {s * Ng3[0], s * Ng3[1], s * Ng3[2]};
+	return dot3(sn, P4) >= 0;
+}
+
 // BilinearEvaluate (bilinear.h:189-224) of CqVector2D corners.
 static V2 bilinearEvaluate(V2 A, V2 B, V2 C, V2 D, float s, float t) {
 	V2 AB, CD;
@@ -1583,4 +1595,34 @@ extern "C" void orc_project_points(const float* m, const float* Pin, int64_t n, 
 		Pout[4 * i + 2] = z;
 		Pout[4 * i + 3] = w;
 	}
+}
+
+extern "C" void orc_cull_grid(int cu, int cv, int nkeys, int flags, const float* P, const float* Ng, const float* N,
+                              const float* Oi, int zthreshold_black, uint8_t* culled) {
+	const int gs = (cu + 1) * (cv + 1);
+	std::vector<int> count(gs, 0);
+	std::vector<char> cullV(gs, 0);
+	const bool bf = (flags & ORC_GRID_CULL_BACKFACING) && Ng;
+	if (nkeys <= 1) {
+		// CqMicroPolyGrid::Shade: back faces, then the trailing run of black Oi
+		if (bf)
+			for (int i = gs - 1; i >= 0; i--)
+				if (backFacing(P + 4 * i, Ng + 3 * i, N ? N + 3 * i : nullptr)) cullV[i] = 1;
+		if ((flags & ORC_GRID_CULL_TRANSPARENT) && Oi && !zthreshold_black)
+			for (int i = gs - 1; i >= 0; i--) {
+				if (Oi[4 * i] == 0.0f && Oi[4 * i + 1] == 0.0f && Oi[4 * i + 2] == 0.0f) cullV[i] = 1;
+				else break;
+			}
+	} else if (bf) {
+		// CqMotionMicroPolyGrid::Split: culled where every key faces away
+		for (int k = 0; k < nkeys; ++k)
+			for (int i = gs - 1; i >= 0; i--) {
+				const long long e = (long long)k * gs + i;
+				if (backFacing(P + 4 * e, Ng + 3 * e, N ? N + 3 * e : nullptr)) count[i]++;
+			}
+		for (int i = 0; i < gs; ++i) cullV[i] = count[i] == nkeys;
+	}
+	for (int iv = 0; iv < cv; ++iv)
+		for (int iu = 0; iu < cu; ++iu)
+			if (cullV[iv * (cu + 1) + iu]) culled[iv * cu + iu] = 1;
 }

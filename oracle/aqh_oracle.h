@@ -37,7 +37,9 @@ enum {
 	ORC_GRID_MATTEALPHA = 4,  /* SqImageSample::Flag_MatteAlpha */
 	ORC_GRID_TRIANGULAR = 16, /* CqMicroPolyGridBase::fTriangular: split line through corners cu, cv*(cu+1) */
 	ORC_GRID_CAMERA = 32,     /* P in camera space: orc_project_points first (orc_render itself ignores it) */
-	ORC_GRID_TRIM_OUTSIDE = 64 /* "trimcurve" "sense" "outside" */
+	ORC_GRID_TRIM_OUTSIDE = 64, /* "trimcurve" "sense" "outside" */
+	ORC_GRID_CULL_BACKFACING = 128, /* Sides 1, outside any solid, "cull" "backfacing" 1 */
+	ORC_GRID_CULL_TRANSPARENT = 256 /* the surface shader uses Oi */
 };
 
 typedef struct {
@@ -159,6 +161,14 @@ void orc_multijitter_tables(int xs, int ys, float* pos, float* t1d, int32_t* shu
  * 735-745, 1023-1032; CqMatrix::operator*(CqVector3D), matrix.h:717-750):
  * raster x, y and the camera-space z.  m: CqMatrix elements m[row*4 + col]. */
 void orc_project_points(const float* m, const float* Pin, int64_t n, float* Pout);
+
+/* The culling of CqMicroPolyGrid::Shade (micropolygon.cpp:431-506) and
+ * CqMotionMicroPolyGrid::Split (micropolygon.cpp:957-1020, 1075-1080) for
+ * one grid in camera space: P float4 and Ng / N (N may be NULL) float3 per
+ * P entry, every key; Oi float4 per vertex or NULL.  Sets culled[mp] for
+ * the grid's cu*cv micropolygons (never clears). */
+void orc_cull_grid(int cu, int cv, int nkeys, int flags, const float* P, const float* Ng, const float* N,
+                   const float* Oi, int zthreshold_black, uint8_t* culled);
 
 /* The rounding helpers of libs/math/math.h:46-70 as the oracle uses them
  * (lfloor/lceil of a float, lround of a double). */

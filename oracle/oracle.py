@@ -99,6 +99,7 @@ def lib():
         L.orc_lceil.argtypes = [C.c_float]
         L.orc_lceil.restype = C.c_long
         L.orc_project_points.argtypes = [_f32p, _f32p, C.c_int64, _f32p]
+        L.orc_cull_grid.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, _u8p]
         L.orc_lround.argtypes = [C.c_double]
         L.orc_lround.restype = C.c_long
         _lib = L
@@ -164,6 +165,27 @@ def projected_grids(scene):
     if m is None or not (np.asarray(g.flags) & GRID_CAMERA).any():
         return g
     P = np.array(g.P, np.float32, copy=True)
+    flags = np.asarray(g.flags)
+    if getattr(g, "cull_Ng", None) is not None or (flags & 256).any():
+        # Shade / Split culling in camera space, before the projection
+        L = lib()
+        culled = (np.zeros(g.micropolygons, np.uint8) if g.culled is None
+                  else np.array(g.culled, np.uint8, copy=True))
+        Ng = None if getattr(g, "cull_Ng", None) is None else np.ascontiguousarray(g.cull_Ng, np.float32)
+        N = None if getattr(g, "cull_N", None) is None else np.ascontiguousarray(g.cull_N, np.float32)
+        Oi = None if g.Oi is None else np.ascontiguousarray(g.Oi, np.float32)
+        zblack = int(all(float(z) == 0.0 for z in scene.frame.zthreshold))
+        mpb = 0
+        for i in range(g.ngrids):
+            cu, cv, nk, f = int(g.cu[i]), int(g.cv[i]), int(g.nkeys[i]), int(flags[i])
+            if (f & GRID_CAMERA) and (f & (128 | 256)):
+                b, cb = int(g.pbase[i]), int(g.cbase[i])
+                out = culled[mpb:mpb + cu * cv]
+                L.orc_cull_grid(cu, cv, nk, f, _p(P[b:], _f32p), None if Ng is None else _p(Ng[b:], _f32p),
+                                None if N is None else _p(N[b:], _f32p), None if Oi is None else _p(Oi[cb:], _f32p),
+                                zblack, out.ctypes.data_as(_u8p))
+            mpb += cu * cv
+        g = dataclasses.replace(g, culled=culled)
     for i in np.nonzero(np.asarray(g.flags) & GRID_CAMERA)[0]:
         nv = (int(g.cu[i]) + 1) * (int(g.cv[i]) + 1) * int(g.nkeys[i])
         b = int(g.pbase[i])
