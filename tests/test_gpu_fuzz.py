@@ -64,3 +64,30 @@ def test_random_frame_with_trims(aqh_lib, oracle, seed):
     finally:
         h.close()
     compare(res, oracle.render(sc))
+
+
+def _positive_depth_seeds(n):
+    """Random frames whose depths are all positive (camera space needs them)."""
+    import numpy as np
+    out = []
+    for s in range(1000):
+        if len(out) == n:
+            break
+        if not (np.asarray(SS.fuzz(s).grids.P)[:, 2] <= 0).any():
+            out.append(s)
+    return out
+
+
+@pytest.mark.parametrize("seed", _positive_depth_seeds(60))
+def test_random_frame_with_culling(aqh_lib, oracle, seed):
+    """Random frames turned to camera space (every other grid) with random
+    normals and trailing black opacity culled on the device."""
+    from aqsis_gb300 import scene as S
+    sc = S.with_culling(S.to_camera_space(SS.fuzz(seed), every=2), seed=seed)
+    h = aqh_lib.Hider(0)
+    try:
+        h.set_mode(seed % 2 == 1)
+        res = h.render_scene(sc)
+    finally:
+        h.close()
+    compare(res, oracle.render(sc), exact_pixels=False)
