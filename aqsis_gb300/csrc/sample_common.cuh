@@ -327,10 +327,11 @@ constexpr int kCombineLocal = 24;  // lists up to this long are sorted in local 
 // (imagepixel.cpp:155-301).  Returns the fragment count; writes the collapsed
 // sample into occl / occl_flags, and into top_id the micropolygon of the
 // front entry, whose output variables the sample keeps (occl_id for the
-// occluding hit).
-__device__ inline int combine_fragments(const FrameParams& fp, const GridsDev& g, const FragPool& pool, int head,
-                                        bool has_occl, float occlZ, float occl[7], int& occl_flags, int occl_id,
-                                        int& top_id, bool& emptied) {
+// occluding hit).  CSG: the frame has CSG trees (compiled out otherwise).
+template <bool CSG>
+__device__ __forceinline__ int combine_fragments_t(const FrameParams& fp, const GridsDev& g, const FragPool& pool,
+                                                   int head, bool has_occl, float occlZ, float occl[7],
+                                                   int& occl_flags, int occl_id, int& top_id, bool& emptied) {
 	int n = 0;
 	bool nan = occl[6] != occl[6];
 	bool any_csg = false;
@@ -338,14 +339,14 @@ __device__ inline int combine_fragments(const FrameParams& fp, const GridsDev& g
 		++n;
 		const float4 fr = pool.frag[f];
 		nan |= fr.x != fr.x;
-		if (g.csg.nnodes > 0) any_csg = any_csg || csg_grid(g, grid_of(g, __float_as_int(fr.y)));
+		if (CSG) any_csg = any_csg || csg_grid(g, grid_of(g, __float_as_int(fr.y)));
 	}
 	int ntot = n + (has_occl ? 1 : 0);
 	emptied = false;
 	// short lists: the entries sorted once (insertion sort, ascending key);
 	// long ones (or NaN depths) are walked in order by selection
 	const bool local = ntot <= kCombineLocal && !nan;
-	if (any_csg && !local && g.csg.overflow) atomicOr(g.csg.overflow, 1);  // CSG needs the sorted list held
+	if (CSG && any_csg && !local && g.csg.overflow) atomicOr(g.csg.overflow, 1);  // CSG needs the sorted list held
 	FragKey ent[kCombineLocal];
 	if (local) {
 		int m = 0, seq = n - 1;
@@ -362,7 +363,7 @@ __device__ inline int combine_fragments(const FrameParams& fp, const GridsDev& g
 			insert(fr.x, __float_as_int(fr.y), seq, f);
 		}
 		if (has_occl) insert(occl[6], 0x7fffffff, n, -1);
-		if (any_csg) {
+		if (CSG && any_csg) {
 			// CSG resolve of the sorted list (imagepixel.cpp:170-190); a list it
 			// empties leaves the sample as it was (imagepixel.cpp:249)
 			int node[kCombineLocal];
@@ -458,6 +459,14 @@ __device__ inline int combine_fragments(const FrameParams& fp, const GridsDev& g
 	occl[6] = depth;
 	occl_flags = top_flags;
 	return n;
+}
+
+__device__ inline int combine_fragments(const FrameParams& fp, const GridsDev& g, const FragPool& pool, int head,
+                                        bool has_occl, float occlZ, float occl[7], int& occl_flags, int occl_id,
+                                        int& top_id, bool& emptied) {
+	if (g.csg.nnodes > 0)
+		return combine_fragments_t<true>(fp, g, pool, head, has_occl, occlZ, occl, occl_flags, occl_id, top_id, emptied);
+	return combine_fragments_t<false>(fp, g, pool, head, has_occl, occlZ, occl, occl_flags, occl_id, top_id, emptied);
 }
 
 
