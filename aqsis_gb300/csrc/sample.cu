@@ -217,7 +217,9 @@ __device__ __forceinline__ void resolve_sample(const FrameParams& fp, const Grid
 // whole grids behind every sample of the 4x4-pixel blocks they overlap are
 // skipped.  Survivors are compacted with block scans, so the staged order is
 // the insertion order.
-template <int kSlots, class Smem>
+// MAY_CSG: the calling kernel can see CSG grids (the opaque kernel never
+// does: frames with solids always render with fragments).
+template <int kSlots, bool MAY_CSG = true, class Smem>
 __device__ __forceinline__ bool stage_candidates(const FrameParams& fp, const GridsDev& g, const BinBuffers& bb,
                                                  Smem& sm, int tpx0, int tpy0, int tpx1, int tpy1, int lend, int& lp,
                                                  int& r0, int& qtotal, int& npend) {
@@ -234,7 +236,7 @@ __device__ __forceinline__ bool stage_candidates(const FrameParams& fp, const Gr
 				gid = bb.st_list[li];
 				const int4 rc = bb.grid_rect[gid];
 				f = rc.x < rc.y && rc.x < tpx1 && rc.y > tpx0 && rc.z < tpy1 && rc.w > tpy0;
-				if (f && cullable && !csg_grid(g, gid)) {
+				if (f && cullable && !(MAY_CSG && csg_grid(g, gid))) {
 					// whole grid behind every sample of the 4x4-pixel blocks it overlaps
 					const int bx0 = (max(rc.x, tpx0) - tpx0) >> 2, bx1 = (min(rc.y, tpx1) - 1 - tpx0) >> 2;
 					const int by0 = (max(rc.z, tpy0) - tpy0) >> 2, by1 = (min(rc.w, tpy1) - 1 - tpy0) >> 2;
@@ -330,7 +332,7 @@ __device__ __forceinline__ bool stage_candidates(const FrameParams& fp, const Gr
 			const int sX = max((int)floorf(bminx), tpx0), eX = min(lceil_f(bmaxx), tpx1);
 			const int sY = max((int)floorf(bminy), tpy0), eY = min(lceil_f(bmaxy), tpy1);
 			active = !culled && !cropped && sX < eX && sY < eY;
-			if (active && cullable && !csg_grid(g, gid)) {
+			if (active && cullable && !(MAY_CSG && csg_grid(g, gid))) {
 				// early-z for every pixel it visits: behind all their samples' occluding depths
 				float mx = -FLT_MAX;
 				for (int yy = sY; yy < eY; ++yy)
@@ -703,7 +705,7 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 	int lp = lbeg, r0 = 0, qtotal = 0, npend = 0;
 	for (;;) {
 		const bool exhausted =
-		    stage_candidates<kSlotsO>(fp, g, bb, sm, tpx0, tpy0, tpx1, tpy1, lend, lp, r0, qtotal, npend);
+		    stage_candidates<kSlotsO, false>(fp, g, bb, sm, tpx0, tpy0, tpx1, tpy1, lend, lp, r0, qtotal, npend);
 		if (npend == 0) break;
 
 		// ---- records, and the (candidate, sample) tests RenderMPG_Static makes ----
