@@ -423,9 +423,13 @@ def run_gpu(args):
     f1.record(stream)
     torch.cuda.synchronize(dev)
     barrier()
-    e2e_ms_max = max_over_ranks(f0.elapsed_time(f1) / n2, dist, dev)
+    multi_ms = max_over_ranks(f0.elapsed_time(f1) / n2, dist, dev)
     for hh in pool:
         hh.close()
+    # the faster of the two ways of driving the same API, both measured here
+    # (frames in flight lose on hosts whose copy engines share the link badly)
+    pipelined = multi_ms <= single_ms
+    e2e_ms_max = multi_ms if pipelined else single_ms
     e2e_value = replica_throughput(mps, world, e2e_ms_max)
     h2d = sum(int(p.numel() * p.element_size()) for p in pin.values())
     d2h = int(out.nbytes)
@@ -469,9 +473,12 @@ def run_gpu(args):
             "roofline": roof, "clocks": clk, "gpu_launches": launches_per_step * args.steps,
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_ms_max,
-                    "path": "aqh_submit_grids_host3 (P, Ci, Oi as float3) + aqh_render + aqh_read_quantized_u8; "
-                            "%d contexts, %d frames in flight, copy-engine uploads" % (k, k),
-                    "one_in_flight": {"value": replica_throughput(mps, world, single_ms), "ms_per_step": single_ms}}}
+                    "path": "aqh_submit_grids_host3 (P, Ci, Oi as float3) + aqh_render + aqh_read_quantized_u8; " +
+                            ("%d contexts, %d frames in flight, copy-engine uploads" % (k, k) if pipelined
+                             else "one frame at a time (faster than %d in flight on this host)" % k),
+                    "one_in_flight": {"value": replica_throughput(mps, world, single_ms), "ms_per_step": single_ms},
+                    "in_flight": {"frames": k, "value": replica_throughput(mps, world, multi_ms),
+                                  "ms_per_step": multi_ms}}}
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
     print(json.dumps(line), flush=True)
