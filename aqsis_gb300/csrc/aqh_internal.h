@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -232,8 +233,13 @@ void launch_sample_tiles_q(const FrameParams& fp, const GridsDev& g, const Sampl
                            SampleStore st, FragPool pool, int* queue, const int* order, int nctas, cudaStream_t s,
                            cudaEvent_t colours_ready = nullptr, unsigned wait_flags = 0);
 int sample_static_ctas_per_sm(bool transp);
+// Kernel attributes (dynamic shared memory above 48 KB) apply to the current
+// device's context: both set them once per device.
 void configure_sample_kernels();
 void configure_sample_mb_kernels();
+// True the first time it is called for the current device with this `mask`
+// (one static bitmask per caller); false afterwards or without a device.
+bool first_use_on_device(std::mutex& mu, uint64_t& mask);
 // `slice_times`: for every slice count d in 1..max(4, spp), the d accumulated
 // slice end times of CqMicroPolygonMotion::BuildBoundList, at offset d*(d-1)/2.
 void launch_sample_mb(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,

@@ -14,6 +14,17 @@
 // call should come before any stream capture.  All calls share the arrays and
 // each call overwrites what it uses; calls whose work overlaps on the GPU
 // (different streams, or different host threads) race on them.
+//
+// Every call copies its small host tables into the arrays and then waits for
+// `stream` (cudaStreamSynchronize) before it returns, because those copies
+// read host memory that the call owns only until it returns.
+//
+// All checks run on the host before anything is queued: pattern choices must
+// name existing patterns, each grid's vertices must lie inside the caller's
+// P (nP vertices) and Ci/Oi (nC vertices) arrays, and flags this form does not
+// carry out (camera space, culling, trim curves) are refused, not ignored.
+// Null Ci or Oi is allowed and means what it means on the context path:
+// white colour, full opacity.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -119,12 +130,14 @@ using namespace aqh;
 extern "C" aqh_status aqh_render_noalloc(const aqh_frame_desc* desc, const float* pos, int npatterns,
                                          const uint32_t* pos_index, int ngrids, const int32_t* cu,
                                          const int32_t* cv, const int32_t* flags, const int64_t* pbase,
-                                         const int64_t* cbase, const float* d_P, const float* d_Ci,
-                                         const float* d_Oi, float* d_channels, void* stream, char* err,
-                                         size_t err_len) {
+                                         const int64_t* cbase, const float* d_P, size_t nP, const float* d_Ci,
+                                         const float* d_Oi, size_t nC, float* d_channels,
+                                         size_t channels_floats, void* stream, char* err, size_t err_len) {
 	if (!desc || !pos || npatterns <= 0 || ngrids < 0 || (ngrids > 0 && (!cu || !cv || !flags || !pbase || !cbase)) ||
 	    !d_P || !d_channels)
 		return na_fail(err, err_len, AQH_EINVAL, "aqh_render_noalloc: null argument");
+	if ((d_Ci || d_Oi) && nC == 0)
+		return na_fail(err, err_len, AQH_EINVAL, "aqh_render_noalloc: colours given with nC == 0");
 	FrameParams fp{};
 	std::vector<float> ftab;
 	std::string msg;
@@ -132,6 +145,11 @@ extern "C" aqh_status aqh_render_noalloc(const aqh_frame_desc* desc, const float
 	if (st != AQH_OK) return na_fail(err, err_len, st, msg.c_str());
 	char buf[256];
 	const long long npix_disp = (long long)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
+	if ((unsigned long long)npix_disp * AQH_NCHANNELS > channels_floats) {
+		snprintf(buf, sizeof buf, "aqh_render_noalloc: the output holds %zu floats; %lld needed", channels_floats,
+		         npix_disp * AQH_NCHANNELS);
+		return na_fail(err, err_len, AQH_EINVAL, buf);
+	}
 	const long long npix = (long long)fp.sw * fp.sh;
 	const long long nsamp = npix * fp.spp;
 	if (fp.use_dof) return na_fail(err, err_len, AQH_ELIMIT, "aqh_render_noalloc: depth of field is not supported");
@@ -144,7 +162,6 @@ extern "C" aqh_status aqh_render_noalloc(const aqh_frame_desc* desc, const float
 		         fp.sw, fp.sh, fp.spp, kNaMaxRegionPixels, kNaMaxSamples);
 		return na_fail(err, err_len, AQH_ELIMIT, buf);
 	}
-	(void)npix_disp;
 	if ((long long)npatterns * fp.spp > kNaMaxPatternEntries) {
 		snprintf(buf, sizeof buf, "aqh_render_noalloc: %d patterns x %d samples exceeds %d pattern samples", npatterns,
 		         fp.spp, kNaMaxPatternEntries);
@@ -152,6 +169,16 @@ extern "C" aqh_status aqh_render_noalloc(const aqh_frame_desc* desc, const float
 	}
 	if (!pos_index && npatterns < npix)
 		return na_fail(err, err_len, AQH_EINVAL, "aqh_render_noalloc: explicit samples need one pattern per pixel");
+	// every choice must name an existing pattern: the samplers index the
+	// pattern array with it and do not check it again
+	if (pos_index) {
+		for (long long i = 0; i < npix; ++i)
+			if (pos_index[i] >= (uint32_t)npatterns) {
+				snprintf(buf, sizeof buf, "aqh_render_noalloc: pattern choice %u at pixel %lld; %d patterns",
+				         pos_index[i], i, npatterns);
+				return na_fail(err, err_len, AQH_EINVAL, buf);
+			}
+	}
 	if (ngrids > kNaMaxGrids) {
 		snprintf(buf, sizeof buf, "aqh_render_noalloc: %d grids exceeds the limit of %d", ngrids, kNaMaxGrids);
 		return na_fail(err, err_len, AQH_ELIMIT, buf);
@@ -163,13 +190,27 @@ extern "C" aqh_status aqh_render_noalloc(const aqh_frame_desc* desc, const float
 	std::vector<int64_t> mpb(ngrids);
 	int64_t acc = 0;
 	for (int i = 0; i < ngrids; ++i) {
-		if (cu[i] <= 0 || cv[i] <= 0) return na_fail(err, err_len, AQH_EINVAL, "aqh_render_noalloc: empty grid");
+		if (cu[i] <= 0 || cv[i] <= 0 || cu[i] > 65535 || cv[i] > 65535)
+			return na_fail(err, err_len, AQH_EINVAL, "aqh_render_noalloc: empty or oversized grid");
 		if (!(flags[i] & AQH_GRID_OPAQUE))
 			return na_fail(err, err_len, AQH_ELIMIT,
 			               "aqh_render_noalloc: every grid must be opaque (AQH_GRID_OPAQUE); transparency needs "
 			               "the fragment pool of the context path");
 		if (flags[i] & AQH_GRID_TRIANGULAR)
 			return na_fail(err, err_len, AQH_ELIMIT, "aqh_render_noalloc: triangular grids are not supported");
+		if (flags[i] & ~(AQH_GRID_SMOOTH | AQH_GRID_MATTE | AQH_GRID_MATTEALPHA | AQH_GRID_OPAQUE)) {
+			snprintf(buf, sizeof buf,
+			         "aqh_render_noalloc: grid %d has flags 0x%x; camera-space grids, culling and trim curves "
+			         "are not supported (raster-space grids with AQH_GRID_SMOOTH, _MATTE, _MATTEALPHA, _OPAQUE only)",
+			         i, (unsigned)flags[i]);
+			return na_fail(err, err_len, AQH_ELIMIT, buf);
+		}
+		const int64_t nv = (int64_t)(cu[i] + 1) * (cv[i] + 1);
+		if (pbase[i] < 0 || (uint64_t)(pbase[i] + nv) > (uint64_t)nP ||
+		    ((d_Ci || d_Oi) && (cbase[i] < 0 || (uint64_t)(cbase[i] + nv) > (uint64_t)nC))) {
+			snprintf(buf, sizeof buf, "aqh_render_noalloc: grid %d: vertices out of range (nP %zu, nC %zu)", i, nP, nC);
+			return na_fail(err, err_len, AQH_EINVAL, buf);
+		}
 		mpb[i] = acc;
 		acc += (int64_t)cu[i] * cv[i];
 	}

@@ -1242,9 +1242,19 @@ void launch_sample_tiles_q(const FrameParams& fp, const GridsDev& g, const Sampl
 
 // Shared-memory limits of the sampling kernels; safe to call repeatedly, and
 // done before any graph capture (context creation calls it).
+bool first_use_on_device(std::mutex& mu, uint64_t& mask) {
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+	std::lock_guard<std::mutex> lock(mu);
+	if (mask >> dev & 1) return false;
+	mask |= uint64_t(1) << dev;
+	return true;
+}
+
 void configure_sample_kernels() {
-	static bool configured = false;
-	if (configured) return;
+	static std::mutex mu;
+	static uint64_t configured = 0;
+	if (!first_use_on_device(mu, configured)) return;
 	const int smem_transp = (int)(sizeof(SmemS) + sizeof(int32_t) * kTileSampMax);
 	cudaFuncSetAttribute(sample_opaque_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemO));
 	cudaFuncSetAttribute(sample_static_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_transp);
@@ -1253,7 +1263,6 @@ void configure_sample_kernels() {
 	cudaFuncSetAttribute(sample_frag_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemF));
 	cudaFuncSetAttribute(sample_frag_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemF));
 	configure_sample_mb_kernels();
-	configured = true;
 }
 
 int sample_static_ctas_per_sm(bool transp) {

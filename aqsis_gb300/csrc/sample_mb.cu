@@ -1407,11 +1407,11 @@ void launch_sample_mb(const FrameParams& fp, const GridsDev& g, const SamplerDev
 }
 
 void configure_sample_mb_kernels() {
-	static bool configured = false;
-	if (configured) return;
+	static std::mutex mu;
+	static uint64_t configured = 0;
+	if (!first_use_on_device(mu, configured)) return;
 	cudaFuncSetAttribute(sample_mbp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemP));
 	cudaFuncSetAttribute(sample_mb_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sample_mb_smem(true));
-	configured = true;
 }
 
 }  // namespace aqh

@@ -571,15 +571,27 @@ size_t aqh_job_footprint(const aqh_job* job);
  * (crop width x crop height x AQH_NCHANNELS) floats; all intermediate data
  * lives in fixed device arrays of about 19 MB that every GPU loading this
  * library holds until the process exits.  Limits: AQH_NOALLOC_MAX_GRIDS
- * grids, AQH_NOALLOC_MAX_REGION_PIXELS pixels and AQH_NOALLOC_MAX_SAMPLES
- * samples in the sample region (at most 16 super-tiles of 128x128 pixels),
- * AQH_NOALLOC_MAX_PATTERN_SAMPLES pattern entries; no motion blur, no depth of field, every grid AQH_GRID_OPAQUE;
- * larger inputs return AQH_ELIMIT with a message in `err`.
+ * grids of at most 65535 x 65535 micropolygons, AQH_NOALLOC_MAX_REGION_PIXELS
+ * pixels and AQH_NOALLOC_MAX_SAMPLES samples in the sample region (at most
+ * 16 super-tiles of 128x128 pixels), AQH_NOALLOC_MAX_PATTERN_SAMPLES pattern
+ * entries; no motion blur, no depth of field; every grid AQH_GRID_OPAQUE in
+ * raster space, with no flags but AQH_GRID_SMOOTH, _MATTE, _MATTEALPHA and
+ * _OPAQUE (camera-space grids, culling and trim curves need the context
+ * path).  Larger or unsupported inputs return AQH_ELIMIT, bad ones AQH_EINVAL,
+ * with a message in `err`; every check runs on the host before anything is
+ * queued.
+ * Sizes: `nP` is the number of float4 vertices in d_P, `nC` that of d_Ci and
+ * d_Oi; pbase[i] + (cu[i]+1)*(cv[i]+1) must not exceed nP, nor cbase[i] + the
+ * same count nC.  d_Ci or d_Oi may be NULL (white colour, full opacity, as on
+ * the context path).  `channels_floats` is the size of d_channels in floats.
+ * `pos`/`pos_index` follow aqh_samples (host arrays): every pattern choice
+ * must be below `npatterns`.
  * The first call on a device looks up the arrays' device addresses with that
- * device current, so make it before any stream capture.  Calls share the
- * arrays: calls whose work overlaps on the GPU (other streams, other threads)
- * race.  `pos`/`pos_index` follow aqh_samples (host arrays); the work is
- * queued on `stream` (a cudaStream_t, NULL = default stream). */
+ * device current, so make it before any stream capture.  Each call queues its
+ * work on `stream` (a cudaStream_t, NULL = default stream) and waits for that
+ * stream once, after copying its small host tables into the arrays, before
+ * queueing the kernels.  Calls share the arrays: calls whose work overlaps on
+ * the GPU (other streams, other threads) race. */
 #define AQH_NOALLOC_MAX_GRIDS 65536
 #define AQH_NOALLOC_MAX_REGION_PIXELS 36864
 #define AQH_NOALLOC_MAX_SAMPLES 300000
@@ -587,8 +599,9 @@ size_t aqh_job_footprint(const aqh_job* job);
 aqh_status aqh_render_noalloc(const aqh_frame_desc* desc, const float* pos, int npatterns,
                               const uint32_t* pos_index, int ngrids, const int32_t* cu, const int32_t* cv,
                               const int32_t* flags, const int64_t* pbase, const int64_t* cbase,
-                              const float* d_P, const float* d_Ci, const float* d_Oi,
-                              float* d_channels, void* stream, char* err, size_t err_len);
+                              const float* d_P, size_t nP, const float* d_Ci, const float* d_Oi, size_t nC,
+                              float* d_channels, size_t channels_floats, void* stream, char* err,
+                              size_t err_len);
 
 /* ---- weight table and test hooks ----------------------------------------- */
 /* Host-side filter weight table [(2*sy+1)*(2*sx+1)][spp] evaluated at sub-pixel
