@@ -1021,6 +1021,82 @@ static void combine(const OrcFrame* f, Sample& sd, const OrcGrids* g) {
 	}
 }
 
+
+// Float64 twin of combine() (CqImagePixel::Combine, imagepixel.cpp:144-332):
+// the same entries, the same stable (depth, insertion) order and CSG resolve,
+// composited back to front in double.  Called before combine(), which sorts
+// and overwrites the sample in place.  Never feeds the float path.
+struct Occl64 {
+	bool valid;
+	double d[7];
+};
+static void combine64(const OrcFrame* f, const Sample& sd, const OrcGrids* g, Occl64& o) {
+	const double zt[3] = {f->zthreshold[0], f->zthreshold[1], f->zthreshold[2]};
+	o.valid = sd.occlValid;
+	for (int k = 0; k < 7; ++k) o.d[k] = sd.occl[k];
+	if (!sd.data.empty()) {
+		std::vector<Frag> data = sd.data;
+		if (sd.occlValid) {
+			Frag e;
+			e.mp = sd.occlMp;
+			e.csg = -1;
+			e.flags = sd.occlFlags;
+			std::memcpy(e.data, sd.occl, sizeof(e.data));
+			data.push_back(e);
+		}
+		std::stable_sort(data.begin(), data.end(), [](const Frag& a, const Frag& b) { return a.data[6] < b.data[6]; });
+		if (g->csg_node && g->csg_nnodes > 0) {
+			CsgTree{g}.resolve(data);
+			if (data.empty()) return;
+		}
+		double sc[3] = {0, 0, 0}, so[3] = {0, 0, 0};
+		double opaqueDepths[2] = {sd.occlZ, FLT_MAX};
+		double maxOpaqueDepth = FLT_MAX;
+		for (auto it = data.rbegin(); it != data.rend(); ++it) {
+			double d[7];
+			for (int k = 0; k < 7; ++k) d[k] = it->data[k];
+			if (it->flags & 1) {
+				double nc[3], no[3];
+				for (int k = 0; k < 3; ++k) nc[k] = (1 - d[3 + k]) * sc[k];
+				for (int k = 0; k < 3; ++k) no[k] = (1 - d[k]) * so[k];
+				for (int k = 0; k < 3; ++k) { sc[k] = nc[k]; so[k] = no[k]; }
+			} else {
+				for (int k = 0; k < 3; ++k) {
+					const double op = d[3 + k];
+					const double cl = op < 0.0 ? 0.0 : (op > 1.0 ? 1.0 : op);
+					sc[k] = sc[k] * (1.0 - cl) + d[k];
+				}
+				for (int k = 0; k < 3; ++k) so[k] = (1.0 - so[k]) * d[3 + k] + so[k];
+			}
+			if (d[3] >= zt[0] && d[4] >= zt[1] && d[5] >= zt[2]) {
+				opaqueDepths[1] = opaqueDepths[0];
+				opaqueDepths[0] = d[6];
+				if (!(maxOpaqueDepth < FLT_MAX)) maxOpaqueDepth = d[6];
+			}
+		}
+		for (int k = 0; k < 7; ++k) o.d[k] = data.front().data[k];
+		for (int k = 0; k < 3; ++k) { o.d[k] = sc[k]; o.d[3 + k] = so[k]; }
+		o.valid = true;
+		if (f->depth_filter == ORC_DEPTH_MIDPOINT) {
+			o.d[6] = data.size() > 1 ? (opaqueDepths[0] + opaqueDepths[1]) * 0.5 : FLT_MAX;
+		} else if (f->depth_filter == ORC_DEPTH_MAX) {
+			o.d[6] = maxOpaqueDepth;
+		} else if (f->depth_filter == ORC_DEPTH_AVERAGE) {
+			double tot = 0.0;
+			int cnt = 0;
+			for (auto& e : data)
+				if (e.data[3] >= zt[0] || e.data[4] >= zt[1] || e.data[5] >= zt[2]) { tot += e.data[6]; cnt++; }
+			o.d[6] = tot / cnt;
+		} else {
+			o.d[6] = opaqueDepths[0];
+		}
+	} else if (sd.occlValid) {
+		if (sd.occlFlags & 1)
+			for (int k = 0; k < 6; ++k) o.d[k] = 0;
+		if (f->depth_filter == ORC_DEPTH_MIDPOINT) o.d[6] = 0.5 * ((double)sd.occl[6] + (double)sd.occlZ);
+	}
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -1326,8 +1402,16 @@ extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples
 		if (out->occlz) out->occlz[i] = sd.occlZ;
 		if (out->nfrag) out->nfrag[i] = (int32_t)sd.data.size();
 	}
+	// the float64 twin reads each sample before combine() rewrites it
+	const bool want64 = out->sdata64 || out->channels64;
+	std::vector<Occl64> occl64(want64 ? nsamp : 0);
+	if (want64)
+		for (size_t i = 0; i < nsamp; ++i) combine64(f, fr.samples[i], g, occl64[i]);
 	// CombineElements (bucketprocessor.cpp:365-375)
 	for (size_t i = 0; i < nsamp; ++i) combine(f, fr.samples[i], g);
+	if (out->sdata64)
+		for (size_t i = 0; i < nsamp; ++i)
+			for (int k = 0; k < 7; ++k) out->sdata64[7 * i + k] = occl64[i].valid ? occl64[i].d[k] : 0.0;
 	for (size_t i = 0; i < nsamp; ++i) {
 		const Sample& sd = fr.samples[i];
 		if (out->valid) out->valid[i] = sd.occlValid ? 1 : 0;
@@ -1426,6 +1510,56 @@ extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples
 		}
 	}
 	if (out->channels) std::memcpy(out->channels, chan.data(), chan.size() * sizeof(float));
+	// Float64 twin of the filter and exposure above: the same window test on
+	// the same float sample positions (membership is a selection, not
+	// arithmetic), the table weights as exact inputs, sums and the
+	// normalisation in double.
+	if (out->channels64) {
+		for (int y = f->crop_ymin; y < f->crop_ymax; y++) {
+			const float ycent = y + 0.5f;
+			for (int x = f->crop_xmin; x < f->crop_xmax; x++) {
+				const float xcent = x + 0.5f;
+				double gTot = 0.0, acc[7] = {0, 0, 0, 0, 0, 0, 0};
+				int cnt = 0;
+				for (int fy = -ymax; fy <= ymax; fy++)
+					for (int fx = -xmax; fx <= xmax; fx++) {
+						const int index = ((fy + ymax) * (2 * xmax + 1) + fx + xmax) * numSubPixels;
+						for (int si = 0; si < numSubPixels; ++si) {
+							const Sample& sd = fr.at(x + fx, y + fy, si);
+							const V2 vecS = sd.position - V2(xcent, ycent);
+							if (vecS.x >= -xfwo2 && vecS.y >= -yfwo2 && vecS.x <= xfwo2 && vecS.y <= yfwo2) {
+								const double gw = ftab[index + si];
+								gTot += gw;
+								const size_t sidx = (size_t)(&sd - fr.samples.data());
+								if (occl64[sidx].valid) {
+									for (int k = 0; k < 7; ++k) acc[k] += occl64[sidx].d[k] * gw;
+									cnt++;
+								}
+							}
+						}
+					}
+				double* c = out->channels64 + ((size_t)(y - f->crop_ymin) * dw + (x - f->crop_xmin)) * 9;
+				double coverage = 0.0;
+				if (cnt == 0) {
+					for (int k = 0; k < 9; ++k) c[k] = 0.0;
+					c[7] = FLT_MAX;
+				} else {
+					const double inv = 1.0 / gTot;
+					for (int k = 0; k < 6; ++k) c[k] = acc[k] * inv;
+					c[7] = acc[6] * inv;
+					coverage = cnt >= numSubPixels ? 1.0 : (double)cnt / numSubPixels;
+				}
+				c[6] = (c[3] + c[4] + c[5]) / 3.0 * coverage;
+				c[8] = coverage;
+				if (!(f->gain == 1.0f && f->gamma == 1.0f)) {
+					for (int k = 0; k < 3; ++k) {
+						if (f->gain != 1.0f) c[k] *= f->gain;
+						if (f->gamma != 1.0f) c[k] = std::pow(c[k], 1.0 / f->gamma);
+					}
+				}
+			}
+		}
+	}
 	// FormatBucketForDisplay quantize (ddmanager.cpp:1022-1119)
 	if (out->quantized && out->qchannels) {
 		for (size_t p = 0; p < (size_t)dw * dh; ++p) {

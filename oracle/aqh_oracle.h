@@ -132,6 +132,14 @@ typedef struct {
 	int64_t spl_count, spl_bound_hits, spl_hits;
 	/* per display pixel: the filtered output variables (naov floats), or NULL */
 	float* aov_channels;
+	/* Float64 twin (NULL = not computed): Combine's composite and FilterBucket /
+	 * ExposeBucket re-evaluated in double from the same per-sample entries
+	 * (the float hit data StoreSample wrote, taken as exact inputs) and the
+	 * same filter table.  Per sample 7 doubles after Combine (as sdata; a
+	 * sample without a valid entry is all zero), per display pixel 9 doubles
+	 * (as channels).  Used to state the float path's rounding error. */
+	double* sdata64;
+	double* channels64;
 } OrcOut;
 
 /* Weight table [(2*shiftY+1)*(2*shiftX+1)][spp] (bucketprocessor.cpp:811-856). */

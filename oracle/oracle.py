@@ -61,7 +61,7 @@ class OrcOut(C.Structure):
                 ("sdata", _f32p), ("channels", _f32p), ("quantized", _f64p),
                 ("qchannels", _i32p), ("nqchannels", C.c_int32),
                 ("spl_count", C.c_int64), ("spl_bound_hits", C.c_int64), ("spl_hits", C.c_int64),
-                ("aov_channels", _f32p)]
+                ("aov_channels", _f32p), ("sdata64", _f64p), ("channels64", _f64p)]
 
 
 def build(quiet: bool = True) -> str:
@@ -193,10 +193,15 @@ def projected_grids(scene):
     return dataclasses.replace(g, P=P, flags=np.asarray(g.flags) & ~GRID_CAMERA)
 
 
-def render(scene, qchannels=(0, 1, 2, 6), want_samples: bool = True) -> dict:
-    """Run the oracle on a Scene (aqsis_gb300.scene).  Returns numpy arrays."""
+def render(scene, qchannels=(0, 1, 2, 6), want_samples: bool = True, want_fp64: bool = False,
+           grids=None) -> dict:
+    """Run the oracle on a Scene (aqsis_gb300.scene).  Returns numpy arrays.
+    `want_fp64` adds the float64 twin of Combine and the filter
+    ("sdata64" with `want_samples`, "channels64").  `grids` replaces the
+    scene's grids after projection (callers that project once)."""
     from aqsis_gb300.scene import FILTERS
-    fr, g, s = scene.frame, projected_grids(scene), scene.samples
+    fr, s = scene.frame, scene.samples
+    g = projected_grids(scene) if grids is None else grids
     naov = 0 if getattr(g, "aov", None) is None else int(np.asarray(g.aov).reshape(len(g.Ci), -1).shape[1])
     cx0, cx1, cy0, cy1 = fr.crop_window
     x0, y0, w, h = fr.sample_region
@@ -263,11 +268,117 @@ def render(scene, qchannels=(0, 1, 2, 6), want_samples: bool = True) -> dict:
     res["quantized"] = np.zeros((dh, dw, len(qc)), np.float64)
     if naov:
         res["aov"] = np.zeros((dh, dw, naov), np.float32)
+    if want_fp64:
+        res["channels64"] = np.zeros((dh, dw, 9), np.float64)
+        if want_samples:
+            res["sdata64"] = np.zeros((ns, 7), np.float64)
     oo = OrcOut(_p(res.get("winner"), _i32p), _p(res.get("occlz"), _f32p), _p(res.get("nfrag"), _i32p),
                 _p(res.get("valid"), _u8p), _p(res.get("sdata"), _f32p), _p(res["channels"], _f32p),
-                _p(res["quantized"], _f64p), _p(qc, _i32p), len(qc), 0, 0, 0, _p(res.get("aov"), _f32p))
+                _p(res["quantized"], _f64p), _p(qc, _i32p), len(qc), 0, 0, 0, _p(res.get("aov"), _f32p),
+                _p(res.get("sdata64"), _f64p), _p(res.get("channels64"), _f64p))
     rc = lib().orc_render(C.byref(of), C.byref(og), C.byref(os_), _p(ftab, _f32p), C.byref(oo))
     if rc != 0:
         raise RuntimeError("oracle render failed: %d" % rc)
     res["spl_count"], res["spl_bound_hits"], res["spl_hits"] = oo.spl_count, oo.spl_bound_hits, oo.spl_hits
     return res
+
+
+def strip_scene(scene, y0: int, y1: int):
+    """The scene restricted to display rows [y0, y1) of its crop window: the
+    same grids, a crop window of those rows, and the sample choices of the
+    rows of the full sample region that the strip's sample region covers, so
+    that every sample of the strip is the one the whole frame has there."""
+    import dataclasses
+    fr = scene.frame
+    cx0, cx1, cy0, cy1 = fr.crop_window
+    assert cy0 <= y0 < y1 <= cy1
+    X0, Y0, W, H = fr.sample_region
+    f2 = dataclasses.replace(fr, crop=(cx0, cx1, y0, y1))
+    x0, sy0, w, h = f2.sample_region
+    r0 = sy0 - Y0
+    s = scene.samples
+
+    def rows(idx):
+        full = np.arange(W * H, dtype=np.uint32) if idx is None else np.asarray(idx, np.uint32)
+        return np.ascontiguousarray(full.reshape(H, W)[r0:r0 + h].ravel())
+
+    kw = {"pos_index": rows(s.pos_index)}
+    for k in ("time_index", "dof_index", "shuffle_index", "lod_index"):
+        src = getattr(s, k)
+        if src is not None or getattr(s, k.replace("_index", "")) is not None:
+            kw[k] = rows(src)
+    if s.dither is not None:
+        dw = cx1 - cx0
+        kw["dither"] = np.ascontiguousarray(np.asarray(s.dither).reshape(cy1 - cy0, dw)[y0 - cy0:y1 - cy0].ravel())
+    return type(scene)(f2, scene.grids, dataclasses.replace(s, **kw))
+
+
+def render_strips(scene, nthreads: int = 0, qchannels=(0, 1, 2, 6), want_fp64: bool = False,
+                  nstrips: int = 0) -> dict:
+    """The oracle over a whole frame in horizontal strips, one host thread per
+    strip (the oracle keeps no global state, and ctypes drops the GIL while
+    it runs).  Channels, quantized values and the float64 twin's channels,
+    stitched in display order."""
+    from concurrent.futures import ThreadPoolExecutor
+    fr = scene.frame
+    cx0, cx1, cy0, cy1 = fr.crop_window
+    n = nthreads or os.cpu_count() or 1
+    k = max(1, min(nstrips or 4 * n, cy1 - cy0))
+    g = projected_grids(scene)
+    edges = [cy0 + (cy1 - cy0) * i // k for i in range(k + 1)]
+    parts = [(edges[i], edges[i + 1]) for i in range(k) if edges[i + 1] > edges[i]]
+    ybounds = _grid_ybounds(g) if not fr.use_dof else None
+
+    def one(b):
+        gs = g
+        if ybounds is not None:
+            # grids whose raster y range (every key) reaches the strip's
+            # AddMPG window, in their original order: the others are culled
+            # by the oracle anyway, and a subset in the same order keeps
+            # every sample's sequence of candidates
+            m = (ybounds[1] >= b[0] - fr.yfilter / 2.0 - 2.0) & (ybounds[0] <= b[1] + fr.yfilter / 2.0 + 2.0)
+            gs = _grid_subset(g, np.nonzero(m)[0])
+        return render(strip_scene(scene, *b), qchannels, want_samples=False, want_fp64=want_fp64, grids=gs)
+
+    with ThreadPoolExecutor(max_workers=n) as ex:
+        outs = list(ex.map(one, parts))
+    res = {key: np.concatenate([o[key] for o in outs], axis=0)
+           for key in ("channels", "quantized") + (("channels64",) if want_fp64 else ())}
+    return res
+
+
+def _grid_ybounds(g):
+    """Per grid (min, max) raster y over every key, or None when the grids
+    are not packed back to back in P (then no strip culling is done) or
+    carry per-grid extras that a subset would have to renumber."""
+    for k in ("aov", "lod", "csg_node", "trim_set", "culled"):
+        if getattr(g, k, None) is not None:
+            return None
+    nv = (g.cu.astype(np.int64) + 1) * (g.cv.astype(np.int64) + 1) * g.nkeys.astype(np.int64)
+    pb = np.asarray(g.pbase, np.int64)
+    if g.ngrids == 0 or pb[0] != 0 or not np.array_equal(pb[1:], np.cumsum(nv)[:-1]):
+        return None
+    y = np.ascontiguousarray(np.asarray(g.P)[:int(nv.sum()), 1])
+    return np.minimum.reduceat(y, pb), np.maximum.reduceat(y, pb)
+
+
+def _grid_subset(g, idx):
+    import dataclasses
+    return dataclasses.replace(g, cu=g.cu[idx], cv=g.cv[idx], nkeys=g.nkeys[idx], flags=g.flags[idx],
+                               pbase=g.pbase[idx], cbase=g.cbase[idx], tbase=g.tbase[idx])
+
+
+def fp64_error(dev, ref64, finite_only: bool = True) -> dict:
+    """Largest absolute and relative difference of float results `dev` from
+    the float64 twin `ref64` (relative over entries with |ref64| >= 1e-6).
+    Entries where the twin is not finite, or at FLT_MAX (an empty pixel's
+    depth), are left out."""
+    a = np.asarray(dev, np.float64)
+    b = np.asarray(ref64, np.float64)
+    m = np.isfinite(b) & (np.abs(b) < 3.0e38) if finite_only else np.ones(b.shape, bool)
+    if not m.any():
+        return {"max_abs": 0.0, "max_rel": 0.0, "entries": 0}
+    d = np.abs(a[m] - b[m])
+    big = np.abs(b[m]) >= 1e-6
+    rel = float((d[big] / np.abs(b[m][big])).max()) if big.any() else 0.0
+    return {"max_abs": float(d.max()), "max_rel": rel, "entries": int(m.sum())}

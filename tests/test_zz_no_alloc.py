@@ -55,7 +55,10 @@ def test_noalloc_rejects_oversized_frames(aqh_lib):
     sc = S.scaled(S.opaque_stream, 0.2, seed=92)  # 384x216 display: beyond the sample-region limit
     dev = torch.device("cuda", 0)
     t = torch.zeros(16, device=dev)
-    rc, msg = call_noalloc(aqh_lib.load(), sc, t.data_ptr(), 4, t.data_ptr(), t.data_ptr(), 4, t.data_ptr(), 16, 0)
+    # a full-size output, so that only the sample-region limit can refuse the call
+    out = torch.zeros(sc.frame.width * sc.frame.height * 9, device=dev)
+    rc, msg = call_noalloc(aqh_lib.load(), sc, t.data_ptr(), 4, t.data_ptr(), t.data_ptr(), 4, out.data_ptr(),
+                           out.numel(), 0)
     assert rc == 7 and "exceeds" in msg, (rc, msg)
 
 
