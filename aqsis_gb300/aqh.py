@@ -615,7 +615,8 @@ class JobInfo(C.Structure):
 
 
 class ServerOpts(C.Structure):
-    _fields_ = [("device", C.c_int), ("hbm_budget", C.c_size_t), ("slots", C.c_int), ("mode", C.c_int)]
+    _fields_ = [("device", C.c_int), ("hbm_budget", C.c_size_t), ("slots", C.c_int), ("mode", C.c_int),
+                ("admission", C.c_int)]
 
 
 class ServerInfo(C.Structure):
@@ -690,11 +691,13 @@ def make_job(scene: Scene, keep: list, want_channels: bool = False):
 class Server:
     """aqh_server: jobs admitted by HBM footprint onto `slots` resident contexts."""
 
-    def __init__(self, device: int = 0, budget: int = 0, slots: int = 4, batched: bool = True):
+    def __init__(self, device: int = 0, budget: int = 0, slots: int = 4, batched: bool = True,
+                 admission: str = "arrival"):
         self.L = load()
         _bind_server(self.L)
         self.sv = C.c_void_p()
-        rc = self.L.aqh_server_create(C.byref(ServerOpts(device, budget, slots, 1 if batched else 0)),
+        adm = {"arrival": 0, "fifo": 0, "smallest": 1}[admission]
+        rc = self.L.aqh_server_create(C.byref(ServerOpts(device, budget, slots, 1 if batched else 0, adm)),
                                       C.byref(self.sv))
         if rc != AQH_OK:
             raise AqhError(rc, "aqh_server_create")

@@ -8,7 +8,9 @@
 // order when a slot is free and their estimated HBM footprint fits in what
 // the admitted jobs leave of the budget; an admitted job runs on its slot's
 // stream while other slots' jobs run on theirs, so work from different
-// requests overlaps on the device.  A job that could never fit is rejected
+// requests overlaps on the device.  With AQH_ADMIT_SMALLEST the smallest
+// fitting job is admitted first (a job that has waited more than
+// AQH_ADMIT_MAX_WAIT_MS goes first in arrival order).  A job that could never fit is rejected
 // at submission.
 #include <cuda_runtime.h>
 
@@ -137,11 +139,24 @@ static void worker_main(aqh_server* sv, int slot) {
 			std::unique_lock<std::mutex> lock(sv->mu);
 			for (;;) {
 				if (sv->stop) return;
-				// admission: the oldest pending job, if its footprint fits now
+				// admission: the oldest pending job if its footprint fits now; with
+				// AQH_ADMIT_SMALLEST the smallest fitting one, unless the oldest has
+				// waited past the limit
 				if (!sv->pending.empty()) {
-					Job* head = sv->pending.front();
+					auto pick = sv->pending.begin();
+					const bool aged =
+						(sv->now() - (*pick)->t_submit) * 1e3 > AQH_ADMIT_MAX_WAIT_MS;
+					if (sv->opts.admission == AQH_ADMIT_SMALLEST && !aged) {
+						auto best = sv->pending.end();
+						for (auto it = sv->pending.begin(); it != sv->pending.end(); ++it)
+							if ((*it)->footprint + sv->in_use <= sv->opts.hbm_budget &&
+							    (best == sv->pending.end() || (*it)->footprint < (*best)->footprint))
+								best = it;
+						if (best != sv->pending.end()) pick = best;
+					}
+					Job* head = *pick;
 					if (head->footprint + sv->in_use <= sv->opts.hbm_budget) {
-						sv->pending.pop_front();
+						sv->pending.erase(pick);
 						job = head;
 						job->state = 1;
 						job->slot = slot;
@@ -166,6 +181,7 @@ extern "C" {
 
 aqh_status aqh_server_create(const aqh_server_opts* o, aqh_server** out) {
 	if (!o || !out || o->slots <= 0 || o->slots > 64) return AQH_EINVAL;
+	if (o->admission != AQH_ADMIT_ARRIVAL && o->admission != AQH_ADMIT_SMALLEST) return AQH_EINVAL;
 	*out = nullptr;
 	std::unique_ptr<aqh_server> sv(new aqh_server());
 	sv->opts = *o;

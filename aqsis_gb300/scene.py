@@ -512,17 +512,19 @@ def scaled(scene_fn, scale: float, **kw) -> Scene:
 SERVED_RESOLUTIONS = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
 
 
-def served_job(rng: np.random.Generator, seed: int, max_mps: float = 8e6) -> Scene:
+def served_job(rng: np.random.Generator, seed: int, max_mps: float = 8e6, kind: Optional[str] = None) -> Scene:
     """One request of the served mixed stream: resolution from the five sizes,
     PixelSamples n n with n in {2, 4, 8}, micropolygons log-uniform in
     [50k, 8M] (16x16-quad grids), 20% motion blur + depth of field (two keys,
     displacement U[0,20] px), 30% transparency (Oi ~ U[0.1,0.9]^3, centre
-    window), the rest opaque; filters as the stream's base configurations."""
+    window), the rest opaque; filters as the stream's base configurations.
+    `kind` ("mb", "transparent", "opaque") fixes the request's kind."""
     w, h = SERVED_RESOLUTIONS[int(rng.integers(0, len(SERVED_RESOLUTIONS)))]
     n = int(rng.choice([2, 4, 8]))
     mps = float(np.exp(rng.uniform(np.log(5e4), np.log(max_mps))))
     ngrids = max(1, int(mps / 256))
-    kind = rng.choice(["mb", "transparent", "opaque"], p=[0.2, 0.3, 0.5])
+    k = rng.choice(["mb", "transparent", "opaque"], p=[0.2, 0.3, 0.5])
+    kind = k if kind is None else kind
     sub = np.random.default_rng(seed)
     if kind == "mb":
         fr = Frame(width=w, height=h, xsamples=n, ysamples=n, filter="box", xfilter=1.0, yfilter=1.0,
@@ -540,6 +542,18 @@ def served_job(rng: np.random.Generator, seed: int, max_mps: float = 8e6) -> Sce
     sc = Scene(fr, g, make_samples(fr, sub, 250))
     sc.kind = str(kind)
     return sc
+
+
+def served_stream(njobs: int, seed: int = 0xC4, max_mps: float = 8e6) -> list:
+    """`njobs` distinct requests of the served mixed stream with the kinds in
+    the configured proportions exactly (20% motion blur + depth of field, 30%
+    transparency, the rest opaque; rounded), in a seeded random order."""
+    rng = np.random.default_rng(seed)
+    nmb = int(round(0.2 * njobs))
+    ntr = int(round(0.3 * njobs))
+    kinds = ["mb"] * nmb + ["transparent"] * ntr + ["opaque"] * (njobs - nmb - ntr)
+    rng.shuffle(kinds)
+    return [served_job(rng, 1000 + i, max_mps=max_mps, kind=kinds[i]) for i in range(njobs)]
 
 
 # ---------------------------------------------------------------------------

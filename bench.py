@@ -196,57 +196,217 @@ def cpu_baseline(args) -> dict:
                       % (sc.frame.width, sc.frame.height, sc.grids.ngrids, mps, dt)}
 
 
-def _strip_worker(payload):
-    """One horizontal strip of the frame through the oracle (crop window)."""
-    scale, y0, y1 = payload
-    from aqsis_gb300 import scene as S
-    from oracle import oracle as O
-    sc = S.scaled(S.opaque_stream, scale, seed=0xC1)
-    sc.frame.crop = (0, sc.frame.width, y0, y1)
-    from aqsis_gb300.scene import make_samples
-    sc.samples = make_samples(sc.frame, np.random.default_rng(7), 250)
-    t0 = time.perf_counter()
-    O.render(sc, want_samples=False)
-    return time.perf_counter() - t0
+def _close_or_same(a, b, rel=1e-5, abs_=1e-6):
+    """Within 1e-5 relative / 1e-6 absolute, or the same non-finite value."""
+    with np.errstate(invalid="ignore", over="ignore"):
+        d = np.abs(a.astype(np.float64) - b.astype(np.float64))
+        ok = (d <= rel * np.abs(b)) | (d <= abs_)
+    return ok | (np.isnan(a) & np.isnan(b)) | (np.isinf(a) & (a == b))
 
 
-def run_reference(args):
-    rank, world, _ = dist_env()
-    if rank != 0:
-        return 0
-    import multiprocessing as mp
-    from aqsis_gb300 import scene as S
+def frame_parity(sc, dev_channels, dev_q, qch, e2e_q=None) -> dict:
+    """The timed frame against the oracle (a restatement of the reference
+    hider) run over the same frame in image strips on every host core, with
+    the oracle's float64 twin of compositing and filtering for the error
+    figure.  Bars: channels within 1e-5 relative (1e-6 absolute), 8-bit
+    values within 1 LSB."""
     from oracle import oracle as O
     O.build()
     cores = os.cpu_count() or 1
-    sc = S.scaled(S.opaque_stream, args.cpu_scale, seed=0xC1)
-    h = sc.frame.height
-    nstrip = cores
-    bounds = [(args.cpu_scale, h * k // nstrip, h * (k + 1) // nstrip) for k in range(nstrip)]
-    bounds = [b for b in bounds if b[2] > b[1]]
-    ctx = mp.get_context("spawn")
-    times = []
-    with ctx.Pool(len(bounds)) as pool:
-        for step in range(args.warmup + args.steps):
-            t0 = time.perf_counter()
-            pool.map(_strip_worker, bounds)
-            dt = time.perf_counter() - t0
-            if step >= args.warmup:
-                times.append(dt)
-    ms = 1e3 * float(np.mean(times))
+    t0 = time.perf_counter()
+    ref = O.render_strips(sc, nthreads=cores, qchannels=qch, want_fp64=True)
+    dt = time.perf_counter() - t0
+    ok = _close_or_same(dev_channels, ref["channels"])
+    q = np.abs(dev_q.astype(np.int64) - ref["quantized"].astype(np.int64))
+    bit = bool(np.array_equal(dev_channels.view(np.uint32), ref["channels"].view(np.uint32)))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        fin = np.isfinite(ref["channels"]) & (np.abs(ref["channels"]) > 1e-6)
+        rel = np.abs(dev_channels.astype(np.float64) - ref["channels"]) / np.abs(ref["channels"])
+    colour = [0, 1, 2, 3, 4, 5, 6, 8]
+    out = {"frame": "the timed frame, %dx%d" % (sc.frame.width, sc.frame.height),
+           "oracle": "restatement of the reference hider in %d image strips on %d host threads, %.1f s"
+                     % (max(1, min(4 * cores, sc.frame.height)), cores, dt),
+           "channels": {"entries": int(ok.size), "outside_bar": int((~ok).sum()), "bit_exact": bit,
+                        "max_rel": float(rel[fin].max()) if fin.any() else 0.0},
+           "u8_max_lsb": int(q.max()) if q.size else 0,
+           "fp64": {"channels": O.fp64_error(dev_channels[..., colour], ref["channels64"][..., colour]),
+                    "depth": O.fp64_error(dev_channels[..., 7], ref["channels64"][..., 7])},
+           "pass": bool(ok.all() and (q.max() if q.size else 0) <= 1)}
+    if e2e_q is not None:
+        qe = np.abs(e2e_q.astype(np.int64) - ref["quantized"].astype(np.int64))
+        out["e2e_u8_max_lsb"] = int(qe.max()) if qe.size else 0
+        out["pass"] = out["pass"] and out["e2e_u8_max_lsb"] <= 1
+    return out
+
+
+def run_reference(args):
+    """The reference's CPU hider timed on this machine's host cores: the oracle
+    restatement (the reference does not build here) over the same 1080p
+    frame, in image strips on one host thread per core (the oracle releases
+    the GIL; each strip takes the grids whose bounds reach it, as the
+    reference's bucket lists do).  The scene is generated before timing."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    sc = make_scene(argparse.Namespace(workload=args.workload if args.workload != "served" else "opaque",
+                                       scale=1.0))
     mps = sc.grids.micropolygons
+    times = []
+    for step in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        O.render_strips(sc, nthreads=cores, qchannels=(0, 1, 2, 6))
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+    ms = 1e3 * float(np.mean(times))
     value = mps / (ms / 1e3)
+    # the same code on one thread and on every core over a slice of the frame
+    from aqsis_gb300 import scene as S
+    sl = S.scaled(S.opaque_stream, args.cpu_scale, seed=0xC1)
+    t0 = time.perf_counter()
+    O.render_strips(sl, nthreads=1, nstrips=1)
+    one = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.render_strips(sl, nthreads=cores)
+    allc = time.perf_counter() - t0
+    cfg = dict(CONFIG, **WORKLOADS.get(args.workload, WORKLOADS["opaque"])[2])
+    cfg["grids"], cfg["micropolygons"] = sc.grids.ngrids, mps
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": dict(CONFIG, cpu_sample_scale=args.cpu_scale),
-            "cpu_baseline": {"value": value, "unit": METRIC, "cores": len(bounds), "kind": "port",
-                             "sample": "%dx%d slice of the stream (%d micropolygons, same density) split into "
-                                       "%d image strips, one process per host core; includes per-process "
-                                       "scene generation" % (sc.frame.width, sc.frame.height, mps, len(bounds))},
+            "config": cfg,
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+                             "sample": "the whole %dx%d frame (%d micropolygons) per step, %d image strips on %d "
+                                       "host threads; scene generated before timing"
+                                       % (sc.frame.width, sc.frame.height, mps, max(1, min(4 * cores, sc.frame.height)),
+                                          cores)},
+            "thread_scaling": {"slice": "%dx%d, %d micropolygons" % (sl.frame.width, sl.frame.height,
+                                                                     sl.grids.micropolygons),
+                               "one_thread_s": one, "all_threads_s": allc, "threads": cores,
+                               "speedup": one / allc},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def resident_leg(sc, local, dev, stream, steps, warmup, autotune, barrier=lambda: None, clocks=None,
+                 qch=(0, 1, 2, 6)) -> dict:
+    """The device-resident leg: grids uploaded once, then `steps` frames
+    timed with CUDA events on the hider's stream (batched form, after the
+    autotuner picks the launch shape when `autotune`), plus the plain form
+    (one launch per stage).  Returns timings and the last batched frame's
+    channels and 8-bit values, read back after the timed region."""
+    import torch
+    from aqsis_gb300 import aqh, scene as S
+    fr, g, smp = sc.frame, sc.grids, sc.samples
+    t = {k: torch.from_numpy(np.ascontiguousarray(getattr(g, k))).to(dev)
+         for k in ("cu", "cv", "nkeys", "flags", "pbase", "cbase", "tbase", "times", "P", "Ci", "Oi")}
+    h = aqh.Hider(local)
+    h.set_stream(stream.cuda_stream)
+    h.frame_begin(fr)
+    h.set_samples(smp)
+    h.submit_grids_device(g.ngrids, t["cu"].data_ptr(), t["cv"].data_ptr(), t["nkeys"].data_ptr(),
+                          t["flags"].data_ptr(), t["pbase"].data_ptr(), t["cbase"].data_ptr(), t["tbase"].data_ptr(),
+                          t["times"].data_ptr(), t["P"].data_ptr(), t["Ci"].data_ptr(), t["Oi"].data_ptr(),
+                          g.micropolygons)
+    # camera-space grids are projected in place (as Split overwrites P):
+    # restore them before every frame, outside the timed region
+    cam = bool((np.asarray(g.flags) & S.GRID_CAMERA).any())
+    cam_src = (t["P"].clone(), t["flags"].clone()) if cam else None
+    # inputs that fit in L2 are evicted between timed frames by writing a buffer twice its size
+    flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device=dev) if g.nbytes_algorithmic() < 2 * L2_BYTES \
+        else None
+
+    def prep():
+        with torch.cuda.stream(stream):
+            if cam_src is not None:
+                t["P"].copy_(cam_src[0])
+                t["flags"].copy_(cam_src[1])
+            if flush is not None:
+                flush.zero_()
+
+    def timed_frames(batched: bool, n: int, w: int):
+        h.set_mode(batched)
+        for _ in range(w):
+            prep()
+            h.render(sync=True)
+        barrier()
+        torch.cuda.synchronize(dev)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        stage = {"bin": [], "sample": [], "filter": []}
+        for i in range(n):
+            prep()
+            ev[i][0].record(stream)
+            h.render(sync=True)
+            ev[i][1].record(stream)
+            st = h.stats()
+            stage["bin"].append(st["ms_bin"])
+            stage["sample"].append(st["ms_sample"])
+            stage["filter"].append(st["ms_filter"])
+        torch.cuda.synchronize(dev)
+        barrier()
+        lat = [a.elapsed_time(b) for a, b in ev]
+        return float(np.mean(lat)), lat, {k: float(np.mean(v)) for k, v in stage.items()}
+
+    plain_ms, plain_lat, plain_stage = timed_frames(False, max(2, steps // 2), 1)
+    h.set_mode(True)
+    prep()
+    tuning = h.autotune(repeats=3) if autotune else dict(h.get_tuning(), ms=None)
+    if clocks is not None:
+        clocks.start()
+    ms, lat, stage = timed_frames(True, steps, warmup)
+    clk = clocks.stop() if clocks is not None else None
+    res = {"ms": ms, "lat": lat, "stage": stage, "plain_ms": plain_ms, "plain_lat": plain_lat,
+           "plain_stage": plain_stage, "tuning": tuning, "clocks": clk,
+           "channels": h.read_channels(), "quantized": h.read_quantized(qch), "stats": h.stats()}
+    h.close()
+    del t
+    torch.cuda.empty_cache()
+    return res
+
+
+def sub_workload(name, local, dev, stream, steps, warmup) -> dict:
+    """A bounded run of one more configuration in the default bench: its
+    full-size frame, device resident, timed like the headline (default launch
+    shape), with parity against the oracle: the whole frame for the
+    transparent stream and the sphere scene, the 0.1 slice (192x108) for the
+    motion blur + depth of field stream, whose full frame the oracle needs
+    minutes for."""
+    ns = argparse.Namespace(workload=name, scale=1.0)
+    t0 = time.perf_counter()
+    sc = make_scene(ns)
+    gen = time.perf_counter() - t0
+    fr, g = sc.frame, sc.grids
+    r = resident_leg(sc, local, dev, stream, steps, warmup, autotune=False)
+    mps = g.micropolygons
+    out = {"config": dict(WORKLOADS[name][2], grids=g.ngrids, micropolygons=mps),
+           "ms_per_step": r["ms"], "micropolygons_per_s": mps / (r["ms"] / 1e3),
+           "samples_per_s": fr.width * fr.height * fr.spp / (r["ms"] / 1e3),
+           "stage_ms": r["stage"], "plain_ms_per_step": r["plain_ms"],
+           "frame_latency_ms": {"p50": float(np.percentile(r["lat"], 50)), "p99": float(np.percentile(r["lat"], 99))},
+           "kernel": KERNELS[name], "steps": steps, "warmup": warmup, "generation_s": gen,
+           "roofline": {"achieved": g.nbytes_algorithmic() / (r["stage"]["sample"] / 1e3) / 1e9, "unit": "GB/s",
+                        "frac": g.nbytes_algorithmic() / (r["stage"]["sample"] / 1e3) / 1e9 / peaks()["hbm_gbs"],
+                        "algorithmic_bytes": g.nbytes_algorithmic()}}
+    if name == "mbdof":
+        from aqsis_gb300 import aqh, scene as S
+        sl = S.scaled(S.motion_dof_stream, 0.1, seed=0xC3)
+        h = aqh.Hider(local)
+        h.set_mode(True)
+        h.frame_begin(sl.frame)
+        h.set_samples(sl.samples)
+        h.submit_grids_host(sl.grids)
+        h.render(sync=True)
+        ch, q = h.read_channels(), h.read_quantized((0, 1, 2, 6))
+        h.close()
+        out["parity"] = frame_parity(sl, ch, q, (0, 1, 2, 6))
+        out["parity"]["frame"] = "the 192x108 slice of the stream (1,000 grids), batched form"
+    else:
+        out["parity"] = frame_parity(sc, r["channels"], r["quantized"], (0, 1, 2, 6))
+    return out
 
 
 def run_gpu(args):
@@ -271,79 +431,17 @@ def run_gpu(args):
 
     # ---- device-resident leg ----
     dev = torch.device("cuda", local)
-    t = {k: torch.from_numpy(np.ascontiguousarray(getattr(g, k))).to(dev)
-         for k in ("cu", "cv", "nkeys", "flags", "pbase", "cbase", "tbase", "times", "P", "Ci", "Oi")}
     stream = torch.cuda.Stream(dev)  # the hider's work and the timing events share this stream
-    h = aqh.Hider(local)
-    h.set_stream(stream.cuda_stream)
-    h.frame_begin(fr)
-    h.set_samples(smp)
-    h.submit_grids_device(G, t["cu"].data_ptr(), t["cv"].data_ptr(), t["nkeys"].data_ptr(), t["flags"].data_ptr(),
-                          t["pbase"].data_ptr(), t["cbase"].data_ptr(), t["tbase"].data_ptr(), t["times"].data_ptr(),
-                          t["P"].data_ptr(), t["Ci"].data_ptr(), t["Oi"].data_ptr(), mps)
     qch = np.array([0, 1, 2, 6], np.int32)
-    from aqsis_gb300 import scene as S
-    # camera-space grids are projected in place (as Split overwrites P):
-    # restore them before every frame, outside the timed region
-    cam = bool((np.asarray(g.flags) & S.GRID_CAMERA).any())
-    cam_src = (t["P"].clone(), t["flags"].clone()) if cam else None
-    # inputs that fit in L2 are evicted between timed frames by writing a buffer twice its size
-    flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device=dev) if g.nbytes_algorithmic() < 2 * L2_BYTES \
-        else None
-
-    def prep():
-        with torch.cuda.stream(stream):
-            if cam_src is not None:
-                t["P"].copy_(cam_src[0])
-                t["flags"].copy_(cam_src[1])
-            if flush is not None:
-                flush.zero_()
-
-    def timed_frames(batched: bool, steps: int, warmup: int):
-        """Device time of `steps` frames (CUDA events on the hider's stream
-        around each frame; restores and L2 flushes between frames are not
-        timed) and per-frame latencies; plain = one launch per stage with host
-        round trips."""
-        h.set_mode(batched)
-        for _ in range(warmup):
-            prep()
-            h.render(sync=True)
-        barrier()
-        torch.cuda.synchronize(dev)
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        stage = {"bin": [], "sample": [], "filter": []}
-        for i in range(steps):
-            prep()
-            ev[i][0].record(stream)
-            h.render(sync=True)
-            ev[i][1].record(stream)
-            st = h.stats()
-            stage["bin"].append(st["ms_bin"])
-            stage["sample"].append(st["ms_sample"])
-            stage["filter"].append(st["ms_filter"])
-        torch.cuda.synchronize(dev)
-        barrier()
-        lat = [a.elapsed_time(b) for a, b in ev]
-        return float(np.mean(lat)), lat, stage
-
-    plain_ms, plain_lat, _ = timed_frames(False, max(2, args.steps // 2), 1)
-    # launch shape picked by the autotuner on this frame (batched form), before
-    # the timed region; no tuning changes a pixel
-    h.set_mode(True)
-    prep()
-    tuning = h.autotune(repeats=3) if not args.no_autotune else dict(h.get_tuning(), ms=None)
     clocks = ClockSampler(local)
-    clocks.start()
-    ms, lat, stage = timed_frames(True, args.steps, args.warmup)
-    clk = clocks.stop()
-    sample_ms, bin_ms, filt_ms = stage["sample"], stage["bin"], stage["filter"]
+    r = resident_leg(sc, local, dev, stream, args.steps, args.warmup, not args.no_autotune, barrier, clocks,
+                     tuple(int(c) for c in qch))
+    ms, lat, tuning, clk = r["ms"], r["lat"], r["tuning"], r["clocks"]
+    plain_ms, plain_lat = r["plain_ms"], r["plain_lat"]
     ms_max = max_over_ranks(ms, dist, dev)
     value = replica_throughput(mps, world, ms_max)
     launches_per_step = LAUNCHES[args.workload]
-    img = h.read_quantized(qch)  # exercise the readback of the resident frame
-    h.close()
-    del t
-    torch.cuda.empty_cache()
+    dev_channels, dev_q = r["channels"], r["quantized"]
 
     # ---- end-to-end leg: host arrays through the C-ABI ----
     import ctypes as C
@@ -378,7 +476,7 @@ def run_gpu(args):
             raise RuntimeError("aqh_submit_grids_host3: " + L.aqh_last_error(hh.ctx).decode())
         return hh
 
-    e2e_steps = max(1, min(args.steps, 5))
+    e2e_steps = max(20, args.steps)
     out = np.zeros((fr.height, fr.width, 4), np.uint8)
     # one frame in flight: upload, render and read back per call
     h2 = host_hider(stream, False)
@@ -445,7 +543,7 @@ def run_gpu(args):
     # (profiles/sample_opaque_kernel_opaque_stream_scale035.md); None where no
     # capture of that kernel exists
     traffic = TRAFFIC_PER_MP[args.workload] * mps if TRAFFIC_PER_MP.get(args.workload) else None
-    ms_sample = float(np.mean(sample_ms))
+    ms_sample = r["stage"]["sample"]
     achieved = alg_bytes / (ms_sample / 1e3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
@@ -463,7 +561,7 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": cfg,
             "samples_per_s": fr.width * fr.height * fr.spp * world / (ms_max / 1e3),
-            "stage_ms": {"bin": float(np.mean(bin_ms)), "sample": ms_sample, "filter": float(np.mean(filt_ms))},
+            "stage_ms": r["stage"],
             "mode": "batched (persistent tile queue, one CUDA graph per frame)",
             "tuning": tuning,
             "frame_latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
@@ -481,44 +579,60 @@ def run_gpu(args):
                                   "ms_per_step": multi_ms}}}
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args)
+    if not args.no_parity:
+        line["parity"] = frame_parity(sc, dev_channels, dev_q, tuple(int(c) for c in qch), e2e_q=out)
+    if args.workload == "opaque" and not args.no_extra:
+        del pin
+        torch.cuda.empty_cache()
+        line["workloads"] = {}
+        for name in ("transparent", "mbdof", "spheres"):
+            steps = 5 if name == "mbdof" else 10
+            line["workloads"][name] = sub_workload(name, local, dev, stream, steps, 3)
+            torch.cuda.empty_cache()
+        line["served"] = served_measure(argparse.Namespace(jobs=args.served_jobs, gap_ms=args.gap_ms,
+                                                           slots=args.slots, max_mps=args.max_mps,
+                                                           slot_mode=args.slot_mode, seed=0xC4,
+                                                           admission=args.admission))
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
     return 0
 
 
-def run_served(args):
-    """The served mixed request stream: `args.jobs` requests (drawn from
-    `args.distinct` generated scenes, cycled), Poisson arrivals with a mean gap
-    of `args.gap_ms`.  Plain = one frame at a time on one context in plain mode
-    (one launch per stage); served = the batched server (continuous admission
-    onto resident slots, persistent kernels, CUDA graphs).  Reports p50/p99
-    latency (arrival -> image on the host) under the Poisson schedule and
-    frames/s with every request queued at once (saturated)."""
+def served_measure(args) -> dict:
+    """The served mixed request stream: `args.jobs` distinct requests with
+    the configured kinds in proportion (20% motion blur + depth of field, 30%
+    transparency, the rest opaque), Poisson arrivals with a mean gap of
+    `args.gap_ms`.  Plain = one frame at a time on one context in plain mode
+    (one launch per stage); served = the batched server (continuous
+    admission onto resident slots, persistent kernels, CUDA graphs).  Both
+    submit packed host grids in one call and read back RGBA8.  Reports p50 /
+    p99 latency (arrival -> image on the host) under the Poisson schedule and
+    frames/s with every request queued at once (saturated), plus the plain
+    path's device time per kind."""
     import torch
     from aqsis_gb300 import aqh, scene as S
     aqh.load(build_if_missing=True)
-    rng = np.random.default_rng(0xC4)
     t0 = time.perf_counter()
-    scenes = [S.served_job(rng, 1000 + i, max_mps=args.max_mps) for i in range(args.distinct)]
+    scenes = S.served_stream(args.jobs, seed=args.seed, max_mps=args.max_mps)
     gen_s = time.perf_counter() - t0
     # page-locked copies of every input array (the requests' host buffers)
     for sc in scenes:
         g = sc.grids
         for k in ("P", "Ci", "Oi"):
             setattr(g, k, torch.from_numpy(getattr(g, k)).pin_memory().numpy())
-    order = [i % args.distinct for i in range(args.jobs)]
+    rng = np.random.default_rng(args.seed + 1)
     gaps = rng.exponential(args.gap_ms / 1e3, args.jobs)
     arrivals = np.cumsum(gaps) - gaps[0]
-    mps_total = sum(scenes[i].grids.micropolygons for i in order)
+    mps_total = sum(sc.grids.micropolygons for sc in scenes)
 
-    # warm both paths on every distinct scene (context buffers, graphs, JIT)
     h = aqh.Hider(0)
     h.set_mode(False)
-    sv = aqh.Server(0, slots=args.slots, batched=args.slot_mode == "batched")
+    sv = aqh.Server(0, slots=args.slots, batched=args.slot_mode == "batched",
+                    admission=getattr(args, "admission", "smallest"))
     qch = (0, 1, 2, 6)
-
     plain_phases = []
+    plain_device = []
 
     def plain_frame(sc):
         """One request the way a served job runs it (packed host grids in one
@@ -532,88 +646,91 @@ def run_served(args):
         t2 = time.perf_counter()
         out = h.read_quantized(qch)
         plain_phases.append((t1 - t0, t2 - t1, time.perf_counter() - t2))
+        plain_device.append((sc.kind, h.stats()["ms_total"]))
         return out
 
+    # warm both paths on every request once (context buffers grown, graphs
+    # captured), as on a server that has been up for a while
     for sc in scenes:
         plain_frame(sc)
-    # every slot meets the requests' sizes before the timed runs (buffers grown,
-    # graphs captured), as on a server that has been up for a while
-    for _ in range(2):
-        ids = [sv.submit(sc) for sc in scenes]
-        for jid in ids:
-            sv.wait(jid)
-            sv.release(jid)
+    ids = [sv.submit(sc) for sc in scenes]
+    for jid in ids:
+        sv.wait(jid)
+        sv.release(jid)
 
     def plain_run(poisson: bool):
         lat = []
         start = time.perf_counter()
-        for k, i in enumerate(order):
+        for k, sc in enumerate(scenes):
             arr = arrivals[k] if poisson else 0.0
             now = time.perf_counter() - start
             if poisson and now < arr:
                 time.sleep(arr - now)
-            plain_frame(scenes[i])
+            plain_frame(sc)
             lat.append(time.perf_counter() - start - arr)
         return time.perf_counter() - start, lat
 
     def served_run(poisson: bool):
         ids = []
         start = time.perf_counter()
-        for k, i in enumerate(order):
+        for k, sc in enumerate(scenes):
             if poisson:
                 now = time.perf_counter() - start
                 if now < arrivals[k]:
                     time.sleep(arrivals[k] - now)
-            ids.append((sv.submit(scenes[i]), arrivals[k] if poisson else 0.0))
-        lat, service, device, phases = [], [], [], []
-        for jid, arr in ids:
+            ids.append(sv.submit(sc))
+        lat, device = [], []
+        for jid in ids:
             rc, info = sv.wait(jid)
             if rc != 0:
                 raise RuntimeError("served job failed: " + sv.error(jid))
             # the server's own clock: submission (= arrival) to completion
             lat.append(info.t_done - info.t_submit)
-            service.append(info.t_done - info.t_admit)
-            device.append(info.ms_device / 1e3)
-            phases.append((info.ms_prepare, info.ms_render, info.ms_read))
+            device.append(info.ms_device)
             sv.release(jid)
-        ph = np.mean(np.array(phases), axis=0)
-        served_run.breakdown = {"mean_service_ms": 1e3 * float(np.mean(service)),
-                                "mean_device_ms": 1e3 * float(np.mean(device)),
-                                "mean_prepare_ms": float(ph[0]), "mean_render_ms": float(ph[1]),
-                                "mean_read_ms": float(ph[2])}
         return time.perf_counter() - start, lat
 
-    del plain_phases[:]
+    del plain_phases[:], plain_device[:]
     plain_sat, _ = plain_run(False)
     pph = 1e3 * np.mean(np.array(plain_phases), axis=0)
+    busy = {}
+    for kind, msd in plain_device:
+        busy[kind] = busy.get(kind, 0.0) + msd
     served_sat, _ = served_run(False)
     plain_p, plain_lat = plain_run(True)
     served_p, served_lat = served_run(True)
     st = sv.stats()
     sv.close()
     h.close()
-    kinds = {k: sum(1 for i in order if scenes[i].kind == k) for k in ("opaque", "transparent", "mb")}
-    line = {"metric": "frames/s", "value": args.jobs / served_sat, "unit": "frames/s", "n_gpus": 1,
-            "steps": args.jobs, "warmup": args.distinct, "ms_per_step": 1e3 * served_sat / args.jobs,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "workload": "served_mixed_stream",
-            "config": {"workload": "served_mixed_stream", "jobs": args.jobs, "distinct_scenes": args.distinct,
-                       "mean_gap_ms": args.gap_ms, "slots": args.slots, "slot_mode": args.slot_mode, "kinds": kinds,
-                       "max_micropolygons": args.max_mps, "generation_s": gen_s},
+    kinds = {k: sum(1 for sc in scenes if sc.kind == k) for k in ("opaque", "transparent", "mb")}
+    return {"config": {"workload": "served_mixed_stream", "jobs": args.jobs, "distinct_requests": args.jobs,
+                       "mean_gap_ms": args.gap_ms, "slots": args.slots, "slot_mode": args.slot_mode,
+                       "admission": getattr(args, "admission", "smallest"), "kinds": kinds,
+                       "micropolygons": mps_total, "max_micropolygons": args.max_mps, "generation_s": gen_s},
             "served": {"frames_per_s_saturated": args.jobs / served_sat,
                        "micropolygons_per_s_saturated": mps_total / served_sat,
                        "latency_ms_poisson": {"p50": 1e3 * float(np.percentile(served_lat, 50)),
                                               "p99": 1e3 * float(np.percentile(served_lat, 99))},
                        "peak_jobs_in_flight": st["peak_running"], "peak_hbm_bytes": st["peak_in_use"],
-                       "graphs_built": st["graphs_built"], "rerenders": st["rerenders"],
-                       "poisson_run": served_run.breakdown},
-            "plain": {"saturated_run": {"mean_prepare_ms": float(pph[0]), "mean_render_ms": float(pph[1]),
-                                        "mean_read_ms": float(pph[2])},
-                      "frames_per_s_saturated": args.jobs / plain_sat,
+                       "graphs_built": st["graphs_built"], "rerenders": st["rerenders"]},
+            "plain": {"frames_per_s_saturated": args.jobs / plain_sat,
                       "micropolygons_per_s_saturated": mps_total / plain_sat,
                       "latency_ms_poisson": {"p50": 1e3 * float(np.percentile(plain_lat, 50)),
-                                             "p99": 1e3 * float(np.percentile(plain_lat, 99))}},
+                                             "p99": 1e3 * float(np.percentile(plain_lat, 99))},
+                      "mean_host_ms": {"prepare": float(pph[0]), "render": float(pph[1]), "read": float(pph[2])},
+                      "device_busy_ms_by_kind": busy},
             "speedup_saturated": plain_sat / served_sat}
+
+
+def run_served(args):
+    """`--workload served`: the served stream alone, as its own JSON line."""
+    args.seed = 0xC4
+    r = served_measure(args)
+    line = {"metric": "frames/s", "value": r["served"]["frames_per_s_saturated"], "unit": "frames/s", "n_gpus": 1,
+            "steps": args.jobs, "warmup": args.jobs, "ms_per_step": 1e3 / r["served"]["frames_per_s_saturated"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "workload": "served_mixed_stream"}
+    line.update(r)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -631,8 +748,13 @@ def main():
     ap.add_argument("--e2e-inflight", type=int, default=3,
                     help="frames in flight in the end-to-end leg (one context each)")
     ap.add_argument("--workload", default="opaque", choices=["opaque", "transparent", "mbdof", "spheres", "served"])
-    ap.add_argument("--jobs", type=int, default=256)
-    ap.add_argument("--distinct", type=int, default=32)
+    ap.add_argument("--jobs", type=int, default=256, help="requests of --workload served (all distinct)")
+    ap.add_argument("--served-jobs", type=int, default=64, help="requests of the default run's served leg")
+    ap.add_argument("--admission", default="smallest", choices=["fifo", "smallest"],
+                    help="served admission order among requests that fit")
+    ap.add_argument("--no-parity", action="store_true", help="skip the check of the timed frame against the oracle")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="default run: skip the other workloads and the served leg")
     ap.add_argument("--gap-ms", type=float, default=20.0)
     ap.add_argument("--slots", type=int, default=2)
     ap.add_argument("--max-mps", type=float, default=8e6)

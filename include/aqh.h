@@ -496,8 +496,8 @@ aqh_status aqh_get_stats(aqh_ctx* ctx, aqh_frame_stats* st);
 /* ---- serving --------------------------------------------------------------- */
 /* No counterpart in the reference, which renders one frame per process.  A
  * server keeps `slots` contexts resident on one GPU, each with its own
- * stream and device buffers reused from job to job; jobs are admitted in
- * arrival order when a slot is free and their estimated HBM footprint fits
+ * stream and device buffers reused from job to job; jobs are admitted (in
+ * the order `admission` names) when a slot is free and their estimated HBM footprint fits
  * in the budget the running jobs leave, and jobs on different slots run
  * concurrently on the device.  A job that can never fit is rejected at
  * submission (AQH_EREJECTED). */
@@ -507,7 +507,16 @@ typedef struct {
 	size_t hbm_budget;   /* bytes the admitted jobs may hold together; 0 = 80% of free memory */
 	int slots;           /* jobs in flight at once (1..64) */
 	int mode;            /* AQH_MODE_BATCHED or AQH_MODE_PLAIN for every slot */
+	int admission;       /* AQH_ADMIT_ARRIVAL (0) or AQH_ADMIT_SMALLEST */
 } aqh_server_opts;
+/* Admission order among pending jobs whose footprint fits: arrival order, or
+ * the smallest footprint first (shorter jobs finish sooner, which lowers the
+ * median latency of a mixed stream); under AQH_ADMIT_SMALLEST a job pending
+ * for more than AQH_ADMIT_MAX_WAIT_MS goes first, in arrival order, so large
+ * jobs are not starved. */
+#define AQH_ADMIT_ARRIVAL 0
+#define AQH_ADMIT_SMALLEST 1
+#define AQH_ADMIT_MAX_WAIT_MS 1000
 /* One render request.  Every pointer is host memory that must stay valid
  * until the job completes; grids use the aqh_submit_grids_host layout. */
 typedef struct {

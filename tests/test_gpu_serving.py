@@ -29,11 +29,12 @@ def alone(aqh_lib, sc):
         h.close()
 
 
-@pytest.mark.parametrize("batched", [True, False], ids=["batched", "plain-slots"])
-def test_results_same_alone_and_in_the_mix(aqh_lib, batched):
+@pytest.mark.parametrize("batched,admission", [(True, "arrival"), (False, "arrival"), (True, "smallest")],
+                         ids=["batched", "plain-slots", "batched-smallest-first"])
+def test_results_same_alone_and_in_the_mix(aqh_lib, batched, admission):
     scenes = mixed_scenes()
     refs = [alone(aqh_lib, sc) for sc in scenes]
-    sv = aqh_lib.Server(0, slots=4, batched=batched)
+    sv = aqh_lib.Server(0, slots=4, batched=batched, admission=admission)
     try:
         ids = [sv.submit(sc, want_channels=True) for sc in scenes]
         for jid, (ref8, refc) in zip(ids, refs):
@@ -100,3 +101,38 @@ def test_cancel_and_timeout(aqh_lib):
             assert rc == AQH_OK, sv.error(jid)
     finally:
         sv.close()
+
+
+def test_smallest_first_admits_small_jobs_ahead(aqh_lib):
+    """With one slot and AQH_ADMIT_SMALLEST, small jobs queued behind a large
+    pending one are admitted before it (within the aging limit)."""
+    from aqsis_gb300 import scene as S
+    busy = S.scaled(S.opaque_stream, 0.5, seed=231)
+    large = S.scaled(S.opaque_stream, 0.4, seed=232)
+    smalls = [SS.opaque_small(seed=233 + i) for i in range(3)]
+    sv = aqh_lib.Server(0, slots=1, admission="smallest")
+    try:
+        first = sv.submit(busy)           # occupies the slot
+        big = sv.submit(large)
+        little = [sv.submit(sc) for sc in smalls]
+        infos = {}
+        for jid in [first, big] + little:
+            rc, info = sv.wait(jid)
+            assert rc == AQH_OK, sv.error(jid)
+            infos[jid] = info
+        # every small job was admitted no later than the large one, unless the
+        # large one aged past the limit while the first job ran
+        waited = (infos[big].t_admit - infos[big].t_submit) * 1e3
+        if waited < 1000:
+            assert all(infos[j].t_admit <= infos[big].t_admit for j in little)
+    finally:
+        sv.close()
+
+
+def test_bad_admission_order_is_refused(aqh_lib):
+    import ctypes as C
+    L = aqh_lib.load()
+    aqh_lib._bind_server(L)
+    sv = C.c_void_p()
+    rc = L.aqh_server_create(C.byref(aqh_lib.ServerOpts(0, 0, 1, 1, 7)), C.byref(sv))
+    assert rc == 1 and not sv.value
