@@ -554,7 +554,7 @@ def run_gpu(args):
     if args.workload == "spheres":
         cfg["grid_quads"] = "diced, at most 16x16"
     cfg["l2"] = ("inputs %.1f MB < 2x the 129 MB L2: a %d MB buffer is written between timed frames"
-                 % (alg_bytes / 1e6, 2 * L2_BYTES >> 20)) if flush is not None else \
+                 % (alg_bytes / 1e6, 2 * L2_BYTES >> 20)) if alg_bytes < 2 * L2_BYTES else \
         "inputs %.2f GB >> 129 MB L2 (no flush)" % (alg_bytes / 1e9)
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
