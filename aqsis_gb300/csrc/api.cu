@@ -1001,7 +1001,15 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	if (ctx->dev_grids) motion = ctx->dev_motion;
 	fp.any_motion = motion ? 1 : 0;
 	P.mbdof = fp.use_dof || fp.any_motion;
-	set_tiling(fp, ctx->tune.tile_pixels, ctx->tune.supertile_pixels);
+	// opaque motion blur / depth of field frames sample smaller tiles (two
+	// CTAs share an SM); frames that keep fragments use the default size
+	const bool frags = ctx->any_transparent || !fp.cullable || fp.midpoint_store || ctx->csg_n > 0;
+	int tile_pixels = ctx->tune.tile_pixels;
+	if (P.mbdof && !frags) {
+		const int cap = sample_mb_opaque_tile_pixels(fp.spp);
+		tile_pixels = tile_pixels > 0 ? std::min(tile_pixels, cap) : cap;
+	}
+	set_tiling(fp, tile_pixels, ctx->tune.supertile_pixels);
 	fp.filter_ctas = ctx->tune.filter_ctas_per_sm;
 	fp.use_lod = (ctx->smp.lod != nullptr || ctx->lod_set) ? 1 : 0;
 	if (P.mbdof) {

@@ -246,6 +246,8 @@ void launch_sample_mb(const FrameParams& fp, const GridsDev& g, const SamplerDev
                       SampleStore st, FragPool pool, const float4* dof_bounds, const float* slice_times,
                       cudaStream_t s);
 void slice_times_h(float open, float close, int spp, std::vector<float>& out);
+// Largest sampling tile (pixels) of opaque motion blur / depth of field frames.
+int sample_mb_opaque_tile_pixels(int spp);
 void static_tiling(FrameParams& fp, int tile_pixels);
 // Frame options resolved from an aqh_frame_desc (plus the host filter table).
 aqh_status resolve_frame(const aqh_frame_desc& d, FrameParams& fp, std::vector<float>& ftab, std::string& err);

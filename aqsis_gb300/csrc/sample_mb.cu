@@ -6,16 +6,16 @@
 // CqMicroPolygon::Sample (1561-1592) and CqMicroPolygon::dofSampleInBound
 // (1531-1550).
 //
-// Same structure as the static kernel (sample.cu): the tile's micropolygons
-// are staged into shared-memory records in insertion order and a warp walks
-// 32 samples' candidates, one sample per lane.  For a moving micropolygon the
-// reference tests a sample once per time slice whose window holds the
-// sample's time (and, without depth of field, whose sample-index range holds
-// the sample); each lane finds those slices directly -- by binary search in a
-// per-frame table of the reference's accumulated slice times -- and builds
-// that slice's bound directly, in slice order.  With depth of field each
+// The tile's micropolygons are staged into shared-memory records in insertion
+// order.  For a moving micropolygon the reference tests a sample once per
+// time slice whose window holds the sample's time (and, without depth of
+// field, whose sample-index range holds the sample); with depth of field each
 // sample belongs to one lens stratum, whose shifted bound decides whether the
-// reference visits it.
+// reference visits it.  Frames with transparency (sample_mb_kernel) walk each
+// sample's candidates in insertion order, one sample per lane, finding the
+// slices by binary search in a per-frame table of the reference's accumulated
+// slice times; opaque frames (sample_mbq_kernel) test (slice, sample) pairs in
+// parallel and fold the hits (see the section on opaque frames).
 #include "aqh_internal.h"
 #include "hider_device.cuh"
 #include "sample_common.cuh"
@@ -445,7 +445,7 @@ __device__ Bnd sub_bound(const MbRec& r, const float* T, int b) {
 // grown by the largest circle of confusion in their depth range -- meets the
 // tile and passes AddMPG's crop cull.  Returns true when the list is
 // exhausted.
-template <int kSlots, class Smem>
+template <int kSlots, class Smem, int kThreads = kThreadsM>
 __device__ __forceinline__ bool stage_mb(const FrameParams& fp, const GridsDev& g, const BinBuffers& bb, Smem& sm,
                                          int tpx0, int tpy0, int tpx1, int tpy1, int lend, int& lp, int& r0,
                                          int& qtotal, int& npend) {
@@ -478,7 +478,7 @@ __device__ __forceinline__ bool stage_mb(const FrameParams& fp, const GridsDev& 
 			__syncthreads();
 			qtotal = sm.qcum[sm.qn];
 			r0 = 0;
-			lp += kThreadsM;
+			lp += kThreads;
 			continue;
 		}
 		const int p = r0 + t;
@@ -527,12 +527,12 @@ __device__ __forceinline__ bool stage_mb(const FrameParams& fp, const GridsDev& 
 		int total;
 		const int rank = block_excl_scan(sm.warp_tot, active, total);
 		const int navail = kSlots - npend;
-		if (t == 0) sm.first_reject = kThreadsM;
+		if (t == 0) sm.first_reject = kThreads;
 		__syncthreads();
 		if (active && rank == navail) sm.first_reject = t;
 		if (active && rank < navail) sm.pend[npend + rank] = make_int2(gid, m);
 		__syncthreads();
-		const int consumed = (total > navail) ? sm.first_reject : min(kThreadsM, qtotal - r0);
+		const int consumed = (total > navail) ? sm.first_reject : min(kThreads, qtotal - r0);
 		npend += min(total, navail);
 		r0 += consumed;
 	}
@@ -793,15 +793,16 @@ sample_mb_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Samp
 // min.z > occlZ and keeps a hit only if D < occlZ, so for every hit with D
 // at or above its slice bound's min.z the winner is the least (D, insertion
 // order) whatever the order of visits.  Work items are (micropolygon, time
-// slice) pairs; each walks the pixels and samples RenderMPG_MBOrDof would
-// visit for that slice (the sample-index window without depth of field; with
-// depth of field every sample of the pixels covered by some lens stratum's
-// shifted bound, then the sample's own stratum) and folds hits into a 64-bit
-// shared-memory atomicMin.  Hits below their slice's min.z, NaN or zero
-// depths flag the sample for an in-order replay from the round's start.
-constexpr int kSlotsP = 128;
-constexpr int kSurvivors = 512;
-
+// slice) pairs; each covers the pixels RenderMPG_MBOrDof would visit for
+// that slice (with depth of field, the pixels some lens stratum's shifted
+// bound covers) times a window of samples that is the same for each of its
+// pixels, so that a flat index over all items' (pixel, sample) slots maps to
+// its slot with two multiplications.  Each warp takes a contiguous share of
+// the slots; a slot's cheap tests (time window, the sample's own stratum
+// bound, pixel range, position, early-z against the round's start state)
+// queue it for the full hit test, 32 at a time, whose hits fold into a
+// 64-bit shared-memory atomicMin.  Hits below their slice's min.z, NaN or
+// zero depths flag the sample for an in-order replay from the round's start.
 __device__ __forceinline__ unsigned long long depth_key_m(float z, int w) {
 	const uint32_t u = __float_as_uint(z);
 	const uint32_t o = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
@@ -934,36 +935,62 @@ __device__ __forceinline__ float2 lens_offset(const SamplerDev& smp, int dp, int
 	return project_to_circle(-1.0f + 2.0f * d.x, -1.0f + 2.0f * d.y);
 }
 
-struct SmemP {
-	unsigned long long key[kTileSampM];   // occluding hit of each tile sample (depth_key_m)
-	unsigned long long prev[kTileSampM];  // ... at the start of the round
-	MbRec rec[kSlotsP];
-	float stime[kTileSampM];              // time of each tile sample
-	float dofb[AQH_MAX_SPP_DEV][4];
-	int2 pend[kSlotsP];
-	int pref[kSlotsP + 1];                // running count of (candidate, slice) items
-	int qgrid[kThreadsM];
-	int qcum[kThreadsM + 1];
-	int patidx[kTilePixM];
-	int dofidx[kTilePixM];                // lens pattern of each tile pixel
-	int warp_tot[32];
-	int first_reject;
-	int qn;
-	float dext[4];                        // min dofb[.][0], min [.][1], max [.][2], max [.][3]
-	float tsort[kTileSampM];              // each pixel's sample times, ascending (NaN last)
-	uint8_t tord[kTileSampM];             // ... and the sample index of each
-	int tval[kTilePixM];                  // non-NaN times per pixel
-	int wpre[kWarpsM][32];                // per-warp running counts of pixel windows
-	uint32_t surv[kSurvivors];            // kept (candidate, slice) items: slot | slice << 8
-	int ipref[kSurvivors];                // running pixel count of the kept items
-	MbItem items[kSurvivors];             // ... and their bounds, windows and pixel ranges
-	int nsurv;
-	uint32_t wq[kWarpsM][64];             // per-warp queue of (candidate, sample) tests
-	float wz[kWarpsM][64];                // ... with their slice bound's min z
-	uint32_t flag[kTileSampM / 32];
-	uint32_t sticky[kTileSampM / 32];
-	uint8_t kinv[kTileSampM];             // lens stratum of each tile sample
+// Tiles of the opaque kernel hold at most kTileSampQ samples so that two
+// 256-thread CTAs fit on an SM (shared memory below half of 228 KB).
+constexpr int kThreadsQ = 256;
+constexpr int kWarpsQ = kThreadsQ / 32;
+constexpr int kSlotsQ = 64;      // candidates staged per round
+constexpr int kItemsQ = 256;     // kept (candidate, slice) items per pass (one per thread)
+constexpr int kTileSampQ = 2048;
+constexpr int kTilePixQ = 256;
+constexpr int kBinsQ = 64;       // time bins of a pixel at most
+constexpr int kBinTabQ = kTileSampQ + kTilePixQ;  // (bins + 1) entries per pixel, over the tile
+
+// One kept (candidate, slice) item of a pass.  Its sample slots are the
+// product of its pixel rectangle and a window of `width` samples that is the
+// same for every pixel: an index window [wbase, wbase + width) (no depth of
+// field: RenderMPG_MBOrDof's sample-index range; a static micropolygon under
+// depth of field: every sample), or, for a moving micropolygon under depth of
+// field, the samples of each pixel whose time bin lies in [q0, q1] -- `wtime`
+// slots, the most any pixel of the rectangle has there -- followed by the
+// pixel's samples without a time (NaN), which every slice tests.
+struct ItemQ {
+	Bnd B;
+	float time0, time1, maxCocX, maxCocY;
+	int sX, sY, rw, npix, width, wtime, wbase;
+	int info;  // staged slot | 1 << 8 moving | 1 << 9 time window | q1 << 10
+	unsigned long long mnpix, mrw;  // ceil(2^32 / npix), ceil(2^32 / rw): exact quotients of slot indices
 };
+
+struct SmemQ {
+	unsigned long long key[kTileSampQ];   // occluding hit of each tile sample (depth_key_m)
+	unsigned long long prev[kTileSampQ];  // ... at the start of the round
+	float stime[kTileSampQ];              // time of each tile sample
+	uint8_t kinv[kTileSampQ];             // lens stratum of each tile sample
+	uint8_t tord[kTileSampQ];             // each pixel's samples by time bin (NaN times last)
+	uint16_t tstart[kBinTabQ];            // per pixel: first tord position of each time bin, then the end
+	int16_t tval[kTilePixQ];              // samples with a time per pixel
+	int patidx[kTilePixQ];
+	int dofidx[kTilePixQ];                // lens pattern of each tile pixel
+	float dofb[AQH_MAX_SPP_DEV][4];
+	MbRec rec[kSlotsQ];
+	int2 pend[kSlotsQ];
+	int pref[kSlotsQ + 1];                // running count of (candidate, slice) items
+	ItemQ items[kItemsQ];
+	int ipref[kItemsQ + 1];               // running count of the kept items' sample slots
+	int qgrid[kThreadsQ];
+	int qcum[kThreadsQ + 1];
+	uint32_t wq[kWarpsQ][64];             // per-warp queue of (candidate, sample) tests
+	float wz[kWarpsQ][64];                // ... with their slice bound's min z
+	uint32_t flag[kTileSampQ / 32];
+	uint32_t sticky[kTileSampQ / 32];
+	int warp_tot[32];
+	int first_reject, qn, nsurv, any_nan;
+	float dext[4];                        // min dofb[.][0], min [.][1], max [.][2], max [.][3]
+};
+
+// two CTAs per SM: 228 KB of shared memory less 1 KB reserved per CTA
+static_assert(sizeof(SmemQ) <= (228 * 1024 - 2 * 1024) / 2, "two opaque motion CTAs must fit on an SM");
 
 // One (slice, sample) test as RenderMPG_MBOrDof makes it, given occlZ:
 // returns true with D when the sample is hit and not skipped by early-z.
@@ -981,11 +1008,19 @@ __device__ __forceinline__ bool mb_slice_test(const FrameParams& fp, const MbRec
 	return mb_sample(fp, r, moving, fp.use_dof != 0, x, y, stime, sdx, sdy, D, u, v, tri, gt);
 }
 
-__global__ void __launch_bounds__(kThreadsM, 1)
-sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, SampleStore st,
+__device__ __forceinline__ unsigned long long quot_magic(int d) {
+	return (0x100000000ull + (unsigned long long)d - 1ull) / (unsigned long long)d;
+}
+// r / d for 0 <= r, r * d < 2^32, with m = quot_magic(d)
+__device__ __forceinline__ int quot(int r, unsigned long long m) {
+	return (int)(((unsigned long long)(unsigned)r * m) >> 32);
+}
+
+__global__ void __launch_bounds__(kThreadsQ, 2)
+sample_mbq_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, SampleStore st,
                   const float4* dof_bounds, const float* slice_times) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	SmemP& sm = *reinterpret_cast<SmemP*>(smem_raw);
+	SmemQ& sm = *reinterpret_cast<SmemQ*>(smem_raw);
 	const int tile = blockIdx.x;
 	const int tx = tile % fp.ntx, ty = tile / fp.ntx;
 	const int tpx0 = fp.sx0 + tx * fp.tile_w, tpy0 = fp.sy0 + ty * fp.tile_h;
@@ -999,28 +1034,38 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 	const bool usingDof = fp.use_dof != 0;
 	const Shutter sh = shutter_of(fp);
 	const unsigned long long kinit = depth_key_m(FLT_MAX, -1);
+	// time bins: only moving micropolygons under depth of field use time
+	// windows; the bin of a time is monotone in the time, so a slice's window
+	// [time0, time1] holds no sample outside bins [bin(time0), bin(time1)]
+	const int Q = (usingDof && fp.any_motion && sh.close > sh.open) ? min(spp, kBinsQ) : 1;
+	const float qscale = (Q > 1) ? (float)Q / (sh.close - sh.open) : 0.0f;
+	auto tbin = [&](float tm) -> int {
+		const float f = (tm - sh.open) * qscale;
+		return (Q == 1 || !(f > 0.0f)) ? 0 : (f >= (float)(Q - 1) ? Q - 1 : (int)f);
+	};
 
-	for (int i = t; i < spp; i += kThreadsM) {
+	for (int i = t; i < spp; i += kThreadsQ) {
 		const float4 b = dof_bounds[i];
 		sm.dofb[i][0] = b.x; sm.dofb[i][1] = b.y; sm.dofb[i][2] = b.z; sm.dofb[i][3] = b.w;
 	}
-	for (int i = t; i < tsamp; i += kThreadsM) {
+	for (int i = t; i < tsamp; i += kThreadsQ) {
 		sm.key[i] = kinit;
 		sm.prev[i] = kinit;
 		sm.kinv[i] = (uint8_t)(i % spp);
 	}
-	for (int i = t; i < kTileSampM / 32; i += kThreadsM) {
+	for (int i = t; i < kTileSampQ / 32; i += kThreadsQ) {
 		sm.flag[i] = 0u;
 		sm.sticky[i] = 0u;
 	}
 	if (t == 0) {
 		sm.qn = 0;
 		sm.qcum[0] = 0;
+		sm.any_nan = 0;
 	}
 	__syncthreads();
 	// pattern of each pixel and the lens stratum of each sample (the shuffle
 	// table inverted: the stratum of sample j is the q with shuffle[q] == j)
-	for (int pl = t; pl < tpix; pl += kThreadsM) {
+	for (int pl = t; pl < tpix; pl += kThreadsQ) {
 		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 		int pat = 0;
 		if (px < tpx1 && py < tpy1) {
@@ -1058,9 +1103,8 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 			sm.dext[3] = a3;
 		}
 	}
-	__syncthreads();
-	// time and lens offset of each sample
-	for (int s = t; s < tsamp; s += kThreadsM) {
+	// time of each sample and the lens pattern of each pixel
+	for (int s = t; s < tsamp; s += kThreadsQ) {
 		const int pl = s / spp, j = s - pl * spp;
 		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 		float tm = 0.0f;
@@ -1074,41 +1118,46 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 		sm.stime[s] = tm;
 	}
 	__syncthreads();
-	// each pixel's samples in time order, so a time slice's samples form a
-	// window (insertion sort, ties by index; NaN times go last)
-	for (int pl = t; pl < tpix; pl += kThreadsM) {
-		float* ts = sm.tsort + pl * spp;
-		uint8_t* ord = sm.tord + pl * spp;
+	// each pixel's samples grouped by time bin (a counting sort; NaN times
+	// go last): tstart[pl*(Q+1) + q] is the first position of bin q
+	for (int pl = t; pl < tpix; pl += kThreadsQ) {
+		uint16_t* row = sm.tstart + pl * (Q + 1);
 		const float* tm = sm.stime + pl * spp;
+		uint8_t* ord = sm.tord + pl * spp;
+		for (int q = 0; q <= Q; ++q) row[q] = 0;
 		int nv = 0;
 		for (int j = 0; j < spp; ++j) {
 			const float v = tm[j];
 			if (v != v) continue;
-			int k = nv++;
-			while (k > 0 && ts[k - 1] > v) {
-				ts[k] = ts[k - 1];
-				ord[k] = ord[k - 1];
-				--k;
-			}
-			ts[k] = v;
-			ord[k] = (uint8_t)j;
+			row[tbin(v) + 1]++;
+			++nv;
 		}
+		for (int q = 1; q <= Q; ++q) row[q] = (uint16_t)(row[q] + row[q - 1]);
+		// scatter with row[q] as the cursor of bin q - 1 ... then shift back
+		for (int j = 0; j < spp; ++j) {
+			const float v = tm[j];
+			if (v != v) continue;
+			const int q = tbin(v);
+			ord[row[q]] = (uint8_t)j;
+			row[q] = (uint16_t)(row[q] + 1);
+		}
+		for (int q = Q; q > 0; --q) row[q] = row[q - 1];
+		row[0] = 0;
 		int k = nv;
 		for (int j = 0; j < spp; ++j)
-			if (tm[j] != tm[j]) {
-				ts[k] = tm[j];
-				ord[k] = (uint8_t)j;
-				++k;
-			}
-		sm.tval[pl] = nv;
+			if (tm[j] != tm[j]) ord[k++] = (uint8_t)j;
+		sm.tval[pl] = (int16_t)nv;
+		if (nv < spp) sm.any_nan = 1;
 	}
 	__syncthreads();
+	const bool any_nan = sm.any_nan != 0;
 
 	const int lbeg = bb.st_offset[st_idx * bb.nranges];
 	const int lend = (int)min((long long)bb.st_offset[(st_idx + 1) * bb.nranges], (long long)bb.list_capacity);
 	int lp = lbeg, r0 = 0, qtotal = 0, npend = 0;
 	for (;;) {
-		const bool exhausted = stage_mb<kSlotsP>(fp, g, bb, sm, tpx0, tpy0, tpx1, tpy1, lend, lp, r0, qtotal, npend);
+		const bool exhausted =
+			stage_mb<kSlotsQ, SmemQ, kThreadsQ>(fp, g, bb, sm, tpx0, tpy0, tpx1, tpy1, lend, lp, r0, qtotal, npend);
 		if (npend == 0) break;
 
 		// ---- records and (candidate, slice) items ----
@@ -1124,31 +1173,69 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 		if (t < npend) sm.pref[t] = pre;
 		__syncthreads();
 
-		// ---- parallel pass over (candidate, slice) items ----
-		// Most items of a moving micropolygon lie outside the tile, so threads
-		// first keep the items whose pixel rectangle meets it (chunks of at
-		// most kSurvivors items); then a warp takes each kept item: lanes run
-		// the cheap tests of its (pixel, sample) pairs, pairs that pass queue
-		// up per warp, and every 32 of them take the full hit test together,
-		// one per lane.
-		for (int base = 0; base < total; base += kSurvivors) {
+		for (int base = 0; base < total; base += kItemsQ) {
+			// ---- keep the items whose pixel rectangle meets the tile ----
 			if (t == 0) sm.nsurv = 0;
 			__syncthreads();
-			for (int p = base + t; p < min(total, base + kSurvivors); p += kThreadsM) {
+			for (int p = base + t; p < min(total, base + kItemsQ); p += kThreadsQ) {
 				int lo = 0, hi = npend - 1;
 				while (lo < hi) {
 					const int mid = (lo + hi + 1) >> 1;
 					if (sm.pref[mid] <= p) lo = mid; else hi = mid - 1;
 				}
+				const MbRec& r = sm.rec[lo];
 				MbItem it;
-				if (mb_item(fp, sh, sm.rec[lo], slice_times, p - sm.pref[lo], sm.dext, tpx0, tpy0, tpx1, tpy1, it)) {
-					const int at = atomicAdd(&sm.nsurv, 1);
-					sm.surv[at] = (uint32_t)lo | ((uint32_t)(p - sm.pref[lo]) << 8);
-					sm.items[at] = it;
+				if (!mb_item(fp, sh, r, slice_times, p - sm.pref[lo], sm.dext, tpx0, tpy0, tpx1, tpy1, it)) continue;
+				const bool moving = r.nkeys > 1;
+				const int rw = it.eX - it.sX, npix = rw * (it.eY - it.sY);
+				int width, wtime, wbase, info = lo | (moving ? 1 << 8 : 0);
+				if (moving && usingDof) {
+					const int q0 = tbin(it.time0), q1 = tbin(it.time1);
+					int wt = 0, wn = 0;
+					for (int py = it.sY; py < it.eY; ++py)
+						for (int px = it.sX; px < it.eX; ++px) {
+							const int pl = (py - tpy0) * fp.tile_w + (px - tpx0);
+							const uint16_t* row = sm.tstart + pl * (Q + 1);
+							wt = max(wt, (int)row[q1 + 1] - (int)row[q0]);
+							if (any_nan) wn = max(wn, spp - (int)sm.tval[pl]);
+						}
+					wtime = wt;
+					width = wt + wn;
+					wbase = q0;
+					info |= (1 << 9) | (q1 << 10);
+				} else {
+					wbase = it.j0;
+					width = wtime = it.j1 - it.j0;
 				}
+				if (width <= 0) continue;
+				const int at = atomicAdd(&sm.nsurv, 1);
+				ItemQ& q = sm.items[at];
+				q.B = it.B;
+				q.time0 = it.time0;
+				q.time1 = it.time1;
+				q.maxCocX = it.maxCocX;
+				q.maxCocY = it.maxCocY;
+				q.sX = it.sX;
+				q.sY = it.sY;
+				q.rw = rw;
+				q.npix = npix;
+				q.width = width;
+				q.wtime = wtime;
+				q.wbase = wbase;
+				q.info = info;
+				q.mnpix = quot_magic(npix);
+				q.mrw = quot_magic(rw);
 			}
 			__syncthreads();
 			const int nsurv = sm.nsurv;
+			const int nslots_t = (t < nsurv) ? sm.items[t].npix * sm.items[t].width : 0;
+			int nslots;
+			const int ipre = block_excl_sum(sm.warp_tot, nslots_t, nslots);
+			if (t < nsurv) sm.ipref[t] = ipre;
+			if (t == 0) sm.ipref[nsurv] = nslots;
+			__syncthreads();
+
+			// ---- sample slots: each warp a contiguous share, 32 at a time ----
 			uint32_t* wq = sm.wq[warp];
 			float* wz = sm.wz[warp];
 			int qn = 0;
@@ -1174,99 +1261,45 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 				}
 				__syncwarp();
 			};
-			// pixel counts of the kept items and their running sum: warps take
-			// 32 (item, pixel) slots at a time, several items per warp
-			int npx_t = 0;
-			if (t < nsurv) {
-				const MbItem& it = sm.items[t];
-				npx_t = (it.eX - it.sX) * (it.eY - it.sY);
-			}
-			int totpx;
-			const int ipre = block_excl_sum(sm.warp_tot, npx_t, totpx);
-			if (t < nsurv) sm.ipref[t] = ipre;
-			__syncthreads();
-			for (int g0 = warp * 32; g0 < totpx; g0 += kThreadsM) {
-				// this lane's (item, pixel) and its run of samples: with motion and
-				// depth of field the samples whose time lies in the slice's window
-				// (each pixel's time order; NaN times always included), else the
-				// slice's sample-index window
-				const int gs = g0 + lane;
-				int k = 0, wpl = 0, wa = 0, wn = 0, wnv = 0, cnt = 0, win = 0;
-				if (gs < totpx) {
-					int lo = 0, hi = nsurv - 1;
-					while (lo < hi) {
-						const int mid = (lo + hi + 1) >> 1;
-						if (sm.ipref[mid] <= gs) lo = mid; else hi = mid - 1;
-					}
-					k = lo;
-					const MbItem& it = sm.items[k];
-					const int li = gs - sm.ipref[k], w = it.eX - it.sX;
-					const int px = it.sX + li % w, py = it.sY + li / w;
-					wpl = (py - tpy0) * fp.tile_w + (px - tpx0);
-					win = (sm.rec[sm.surv[k] & 0xffu].nkeys > 1 && usingDof) ? 1 : 0;
-					if (win) {
-						const float* ts = sm.tsort + wpl * spp;
-						wnv = sm.tval[wpl];
-						int a0 = 0, a1 = wnv;
-						while (a0 < a1) {
-							const int mid = (a0 + a1) >> 1;
-							if (ts[mid] < it.time0) a0 = mid + 1; else a1 = mid;
-						}
-						wa = a0;
-						a1 = wnv;
-						while (a0 < a1) {
-							const int mid = (a0 + a1) >> 1;
-							if (ts[mid] <= it.time1) a0 = mid + 1; else a1 = mid;
-						}
-						wn = a0 - wa;
-						cnt = wn + (spp - wnv);
+			const int g0 = (int)((long long)nslots * warp / kWarpsQ);
+			const int g1 = (int)((long long)nslots * (warp + 1) / kWarpsQ);
+			int cur = advance_item(sm.ipref, nsurv, 0, g0);
+			for (int gb = g0; gb < g1; gb += 32) {
+				const int gs = gb + lane;
+				bool pass = false;
+				int s = 0, c = 0;
+				float bz = 0.0f;
+				int it_l = cur;
+				if (gs < g1) {
+					it_l = advance_item(sm.ipref, nsurv, cur, gs);
+					const ItemQ& it = sm.items[it_l];
+					const int r = gs - sm.ipref[it_l];
+					const int k = quot(r, it.mnpix);
+					const int p = r - k * it.npix;
+					const int oy = quot(p, it.mrw);
+					const int px = it.sX + (p - oy * it.rw), py = it.sY + oy;
+					const int pl = (py - tpy0) * fp.tile_w + (px - tpx0);
+					int j = -1;
+					if (!(it.info & (1 << 9))) {
+						j = it.wbase + k;
+					} else if (k < it.wtime) {
+						const uint16_t* row = sm.tstart + pl * (Q + 1);
+						const int a = row[it.wbase];
+						if (k < (int)row[((it.info >> 10) & 0x7f) + 1] - a) j = sm.tord[pl * spp + a + k];
 					} else {
-						wa = it.j0;
-						wn = it.j1 - it.j0;
-						wnv = spp;
-						cnt = wn;
+						const int kk = k - it.wtime, nv = sm.tval[pl];
+						if (kk < spp - nv) j = sm.tord[pl * spp + nv + kk];
 					}
-				}
-				int inc = cnt;
-#pragma unroll
-				for (int o = 1; o < 32; o <<= 1) {
-					const int v = __shfl_up_sync(0xffffffffu, inc, o);
-					if (lane >= o) inc += v;
-				}
-				sm.wpre[warp][lane] = inc - cnt;
-				const int tot = __shfl_sync(0xffffffffu, inc, 31);
-				__syncwarp();
-				for (int q0 = 0; q0 < tot; q0 += 32) {
-					const int q = q0 + lane;
-					int ol = 0;
-					if (q < tot) {
-						int lo = 0, hi = 31;  // last lane whose run starts at or before q
-						while (lo < hi) {
-							const int mid = (lo + hi + 1) >> 1;
-							if (sm.wpre[warp][mid] <= q) lo = mid; else hi = mid - 1;
-						}
-						ol = lo;
-					}
-					const int ok = __shfl_sync(0xffffffffu, k, ol), opl = __shfl_sync(0xffffffffu, wpl, ol);
-					const int oa = __shfl_sync(0xffffffffu, wa, ol), on = __shfl_sync(0xffffffffu, wn, ol);
-					const int onv = __shfl_sync(0xffffffffu, wnv, ol), owin = __shfl_sync(0xffffffffu, win, ol);
-					bool pass = false;
-					int s = 0, c = 0;
-					float bz = 0.0f;
-					if (q < tot) {
-						const int kk = q - sm.wpre[warp][ol];
-						const int pl = opl;
-						const int j = owin ? sm.tord[pl * spp + ((kk < on) ? oa + kk : onv + (kk - on))] : oa + kk;
-						const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
-						const MbItem& it = sm.items[ok];
-						c = (int)(sm.surv[ok] & 0xffu);
-						const bool moving = sm.rec[c].nkeys > 1;
+					if (j >= 0) {
+						s = pl * spp + j;
+						c = it.info & 0xff;
 						const Bnd& B = it.B;
 						bz = B.mnz;
-						s = pl * spp + j;
 						pass = !(sm.flag[s >> 5] & (1u << (s & 31)));  // else replayed in order below
-						const float stime = sm.stime[s];
-						if (pass && moving) pass = !(stime < it.time0 || stime > it.time1);
+						if (pass && (it.info & (1 << 8))) {
+							const float stime = sm.stime[s];
+							pass = !(stime < it.time0 || stime > it.time1);
+						}
 						if (pass) {
 							Bnd TB = B;
 							if (usingDof) {
@@ -1284,36 +1317,35 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 							       !(B.mnz > key_depth_m(sm.prev[s]));
 						}
 					}
-					const uint32_t bal = __ballot_sync(0xffffffffu, pass);
-					if (pass) {
-						const int at = qn + __popc(bal & ((1u << lane) - 1u));
-						wq[at] = (uint32_t)c | ((uint32_t)s << 8);
-						wz[at] = bz;
-					}
-					qn += __popc(bal);
-					__syncwarp();
-					if (qn >= 32) {
-						drain(32);
-						if (lane < qn - 32) {  // entries [32, qn) move to the front
-							wq[lane] = wq[32 + lane];
-							wz[lane] = wz[32 + lane];
-						}
-						__syncwarp();
-						qn -= 32;
-					}
 				}
-				__syncwarp();  // wpre is rewritten for the next slots
+				cur = __shfl_sync(0xffffffffu, it_l, 31);
+				const uint32_t bal = __ballot_sync(0xffffffffu, pass);
+				if (pass) {
+					const int at = qn + __popc(bal & ((1u << lane) - 1u));
+					wq[at] = (uint32_t)c | ((uint32_t)s << 8);
+					wz[at] = bz;
+				}
+				qn += __popc(bal);
+				__syncwarp();
+				if (qn >= 32) {
+					drain(32);
+					if (lane < qn - 32) {  // entries [32, qn) move to the front
+						wq[lane] = wq[32 + lane];
+						wz[lane] = wz[32 + lane];
+					}
+					__syncwarp();
+					qn -= 32;
+				}
 			}
 			drain(qn);
 			__syncthreads();
 		}
-		__syncthreads();
 		int anyf = 0;
-		for (int i = t; i < nflagw; i += kThreadsM) anyf |= (int)(sm.flag[i] != 0u);
+		for (int i = t; i < nflagw; i += kThreadsQ) anyf |= (int)(sm.flag[i] != 0u);
 
 		// ---- ordered replay of flagged samples, one thread per sample ----
 		if (__syncthreads_or(anyf)) {
-			for (int s = t; s < tsamp; s += kThreadsM) {
+			for (int s = t; s < tsamp; s += kThreadsQ) {
 				if (!(sm.flag[s >> 5] & (1u << (s & 31)))) continue;
 				const int pl = s / spp, j = s - pl * spp;
 				const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
@@ -1342,6 +1374,7 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 						b1 = blo;
 						b0 = b1;
 						while (b0 > 0 && (T[b0] - dt) >= stime) --b0;
+						if (stime != stime) { b0 = 0; b1 = div - 1; }  // a NaN time passes every window test
 					}
 					for (int sb = b0; sb <= b1; ++sb) {
 						Bnd B;
@@ -1364,15 +1397,15 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 			}
 		}
 		__syncthreads();
-		for (int i = t; i < tsamp; i += kThreadsM) sm.prev[i] = sm.key[i];
-		for (int i = t; i < nflagw; i += kThreadsM) sm.flag[i] = sm.sticky[i];
+		for (int i = t; i < tsamp; i += kThreadsQ) sm.prev[i] = sm.key[i];
+		for (int i = t; i < nflagw; i += kThreadsQ) sm.flag[i] = sm.sticky[i];
 		__syncthreads();
 		npend = 0;
 		if (exhausted) break;
 	}
 
 	// ---- resolve (sample-major, see the lane kernel) ----
-	for (int q = t; q < tsamp; q += kThreadsM) {
+	for (int q = t; q < tsamp; q += kThreadsQ) {
 		const int j = q / tpix;
 		const int pl = q - j * tpix;
 		const int s = pl * spp + j;
@@ -1390,6 +1423,8 @@ sample_mbp_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 
 }  // namespace
 
+int sample_mb_opaque_tile_pixels(int spp) { return max(1, min(kTilePixQ, kTileSampQ / max(1, spp))); }
+
 size_t sample_mb_smem(bool transp) {
 	return sizeof(SmemM) + (transp ? sizeof(int32_t) * kTileSampM : 0);
 }
@@ -1403,14 +1438,14 @@ void launch_sample_mb(const FrameParams& fp, const GridsDev& g, const SamplerDev
 		sample_mb_kernel<true><<<ntiles, kThreadsM, sample_mb_smem(true), s>>>(fp, g, sm, b, st, pool, dof_bounds,
 		                                                                      slice_times);
 	else
-		sample_mbp_kernel<<<ntiles, kThreadsM, sizeof(SmemP), s>>>(fp, g, sm, b, st, dof_bounds, slice_times);
+		sample_mbq_kernel<<<ntiles, kThreadsQ, sizeof(SmemQ), s>>>(fp, g, sm, b, st, dof_bounds, slice_times);
 }
 
 void configure_sample_mb_kernels() {
 	static std::mutex mu;
 	static uint64_t configured = 0;
 	if (!first_use_on_device(mu, configured)) return;
-	cudaFuncSetAttribute(sample_mbp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemP));
+	cudaFuncSetAttribute(sample_mbq_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemQ));
 	cudaFuncSetAttribute(sample_mb_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sample_mb_smem(true));
 }
 
