@@ -970,6 +970,7 @@ struct SmemQ {
 	uint8_t tord[kTileSampQ];             // each pixel's samples by time bin (NaN times last)
 	uint16_t tstart[kBinTabQ];            // per pixel: first tord position of each time bin, then the end
 	int16_t tval[kTilePixQ];              // samples with a time per pixel
+	float pxmax[kTilePixQ];               // per pixel: largest occluding depth at the round's start (NaN: +inf)
 	int patidx[kTilePixQ];
 	int dofidx[kTilePixQ];                // lens pattern of each tile pixel
 	float dofb[AQH_MAX_SPP_DEV][4];
@@ -1148,6 +1149,7 @@ sample_mbq_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 			if (tm[j] != tm[j]) ord[k++] = (uint8_t)j;
 		sm.tval[pl] = (int16_t)nv;
 		if (nv < spp) sm.any_nan = 1;
+		sm.pxmax[pl] = FLT_MAX;
 	}
 	__syncthreads();
 	const bool any_nan = sm.any_nan != 0;
@@ -1186,6 +1188,14 @@ sample_mbq_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 				const MbRec& r = sm.rec[lo];
 				MbItem it;
 				if (!mb_item(fp, sh, r, slice_times, p - sm.pref[lo], sm.dext, tpx0, tpy0, tpx1, tpy1, it)) continue;
+				// early-z of the whole item: behind every sample of its pixels at the
+				// round's start, so that every one of its slots would fail the
+				// per-sample test below
+				float zmax = -FLT_MAX;
+				for (int py = it.sY; py < it.eY; ++py)
+					for (int px = it.sX; px < it.eX; ++px)
+						zmax = fmaxf(zmax, sm.pxmax[(py - tpy0) * fp.tile_w + (px - tpx0)]);
+				if (it.B.mnz > zmax) continue;
 				const bool moving = r.nkeys > 1;
 				const int rw = it.eX - it.sX, npix = rw * (it.eY - it.sY);
 				int width, wtime, wbase, info = lo | (moving ? 1 << 8 : 0);
@@ -1280,7 +1290,9 @@ sample_mbq_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 					const int px = it.sX + (p - oy * it.rw), py = it.sY + oy;
 					const int pl = (py - tpy0) * fp.tile_w + (px - tpx0);
 					int j = -1;
-					if (!(it.info & (1 << 9))) {
+					if (it.B.mnz > sm.pxmax[pl]) {
+						// every sample of the pixel is in front of the slice's bound
+					} else if (!(it.info & (1 << 9))) {
 						j = it.wbase + k;
 					} else if (k < it.wtime) {
 						const uint16_t* row = sm.tstart + pl * (Q + 1);
@@ -1399,6 +1411,17 @@ sample_mbq_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 		__syncthreads();
 		for (int i = t; i < tsamp; i += kThreadsQ) sm.prev[i] = sm.key[i];
 		for (int i = t; i < nflagw; i += kThreadsQ) sm.flag[i] = sm.sticky[i];
+		__syncthreads();
+		// largest occluding depth of each pixel (a NaN depth never lets a test be
+		// skipped, so it counts as +inf)
+		for (int pl = t; pl < tpix; pl += kThreadsQ) {
+			float m = -FLT_MAX;
+			for (int j = 0; j < spp; ++j) {
+				const float z = key_depth_m(sm.prev[pl * spp + j]);
+				m = (z != z) ? __int_as_float(0x7f800000) : fmaxf(m, z);
+			}
+			sm.pxmax[pl] = m;
+		}
 		__syncthreads();
 		npend = 0;
 		if (exhausted) break;
