@@ -28,26 +28,38 @@ __device__ __forceinline__ uint32_t pack_range(float mn, float mx, bool bad) {
 	return (uint32_t)(lo & 0xffff) | ((uint32_t)hi << 16);
 }
 
-// Strips: the pixel ranges each micropolygon column and row of a static grid
-// can touch (x over vertex columns iu, iu+1; y over vertex rows iv, iv+1), so
-// the sampler streams only the micropolygons whose column and row both meet
-// its tile -- a superset of those whose bound does.  Lane = vertex column.
-__device__ __forceinline__ void grid_strips(const float4* P, int cu, int cv, int lane, uint32_t* S) {
+// Strips: the pixel ranges each micropolygon column and row of a grid can
+// touch (x over vertex columns iu, iu+1; y over vertex rows iv, iv+1; every
+// motion key), so the sampler streams only the micropolygons whose column and
+// row both meet its tile -- a superset of those whose bound does.  In frames
+// with motion blur or depth of field the ranges grow by `grow` (the grid's
+// largest circle of confusion) and one pixel on each side, which covers the
+// staging rectangles of the motion sampler.  Lane = vertex column.
+__device__ __forceinline__ void grid_strips(const float4* P, int cu, int cv, int nk, float growx, float growy,
+                                            bool margin, int lane, uint32_t* S) {
 	const bool on = lane <= cu;
+	const long long nvk = (long long)(cu + 1) * (cv + 1);
 	float cmn = FLT_MAX, cmx = -FLT_MAX, pmn = FLT_MAX, pmx = -FLT_MAX;
 	bool cbad = false, pbad = false;
+	const float mg = margin ? 1.0f : 0.0f;
 	for (int j = 0; j <= cv; ++j) {
-		float x = 0.0f, y = 0.0f;
-		if (on) {
-			const float4 p = __ldg(P + j * (cu + 1) + lane);
-			x = p.x;
-			y = p.y;
-			cbad |= (x != x);
-			cmn = fminf(cmn, x);
-			cmx = fmaxf(cmx, x);
+		float ymn = FLT_MAX, ymx = -FLT_MAX;
+		bool ybad = false;
+		for (int k = 0; k < nk; ++k) {
+			if (on) {
+				const float4 p = __ldg(P + k * nvk + j * (cu + 1) + lane);
+				cbad |= (p.x != p.x);
+				cmn = fminf(cmn, p.x);
+				cmx = fmaxf(cmx, p.x);
+				ybad |= (p.y != p.y);
+				ymn = fminf(ymn, p.y);
+				ymx = fmaxf(ymx, p.y);
+			}
 		}
-		float ymn = on ? y : FLT_MAX, ymx = on ? y : -FLT_MAX;
-		bool ybad = on && (y != y);
+		if (margin && on) {
+			ymn = (ymn - growy) - mg;
+			ymx = (ymx + growy) + mg;
+		}
 #pragma unroll
 		for (int o = 16; o > 0; o >>= 1) {
 			ymn = fminf(ymn, __shfl_xor_sync(0xffffffffu, ymn, o));
@@ -58,6 +70,10 @@ __device__ __forceinline__ void grid_strips(const float4* P, int cu, int cv, int
 		pmn = ymn;
 		pmx = ymx;
 		pbad = ybad;
+	}
+	if (margin && on) {
+		cmn = (cmn - growx) - mg;
+		cmx = (cmx + growx) + mg;
 	}
 	const float nmn = __shfl_down_sync(0xffffffffu, cmn, 1), nmx = __shfl_down_sync(0xffffffffu, cmx, 1);
 	const bool nbad = __shfl_down_sync(0xffffffffu, cbad, 1);
@@ -120,8 +136,9 @@ __global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect, float*
 	}
 	if (strips) {
 		uint32_t* S = strips + (long long)warp * 64;
-		const bool has = nk == 1 && cu <= 31 && cv <= 31;
-		if (has) grid_strips(P, cu, cv, lane, S);
+		const bool mbdof = fp.use_dof || fp.any_motion;
+		const bool has = (nk == 1 || mbdof) && nk <= kMaxKeys && cu <= 31 && cv <= 31;
+		if (has) grid_strips(P, cu, cv, nk, mcx, mcy, mbdof, lane, S);
 		if (lane == 0) S[63] = has ? 1u : 0u;
 	}
 	if (lane != 0) return;

@@ -362,6 +362,7 @@ struct SmemM {
 	int2 pend[kSlotsM];
 	int qgrid[kThreadsM];
 	int qcum[kThreadsM + 1];
+	int qsub[kThreadsM];
 	int warp_tot[32];
 	int first_reject;
 	int qn;
@@ -443,26 +444,60 @@ __device__ Bnd sub_bound(const MbRec& r, const float* T, int b) {
 // super-tile's grid list from the cursor (lp, r0, qtotal) and stage, in
 // insertion order, the micropolygons whose bound over the whole shutter --
 // grown by the largest circle of confusion in their depth range -- meets the
-// tile and passes AddMPG's crop cull.  Returns true when the list is
-// exhausted.
+// tile and passes AddMPG's crop cull.  A grid's strips (binning) restrict it
+// to the columns and rows of micropolygons that can reach the tile.  With
+// `blk` (opaque frames: the largest occluding depth of each row's 4-pixel
+// blocks at the round's start), a micropolygon behind every sample its
+// rectangle covers is not staged: each of its slices' bounds has a min z at
+// or above its own min z less a rounding margin (the slice bounds interpolate
+// key bounds; 1e-6 of the largest |z| is several ulps of it), so every one of
+// its tests would fail early-z.  Returns true when the list is exhausted.
 template <int kSlots, class Smem, int kThreads = kThreadsM>
 __device__ __forceinline__ bool stage_mb(const FrameParams& fp, const GridsDev& g, const BinBuffers& bb, Smem& sm,
                                          int tpx0, int tpy0, int tpx1, int tpy1, int lend, int& lp, int& r0,
-                                         int& qtotal, int& npend) {
+                                         int& qtotal, int& npend, const float* blk = nullptr) {
 	const int t = threadIdx.x;
 	const bool usingDof = fp.use_dof != 0;
 	while (npend < kSlots) {
 		if (r0 >= qtotal) {
 			if (lp >= lend) return true;
 			const int li = lp + t;
-			int gid = -1;
+			int gid = -1, nmp = 0, sub = -1;  // sub: first column, first row, width; -1 = whole grid
 			bool f = false;
 			if (li < lend) {
 				gid = bb.st_list[li];
 				const int4 rc = bb.grid_rect[gid];
 				f = rc.x < rc.y && rc.x < tpx1 && rc.y > tpx0 && rc.z < tpy1 && rc.w > tpy0;
 			}
-			const int nmp = f ? __ldg(g.cu + gid) * __ldg(g.cv + gid) : 0;
+			if (f) {
+				const int cu = __ldg(g.cu + gid), cv = __ldg(g.cv + gid);
+				nmp = cu * cv;
+				if (bb.strips && __ldg(bb.strips + (long long)gid * 64 + 63)) {
+					const uint32_t* S = bb.strips + (long long)gid * 64;
+					int iu0 = 64, iu1 = -1, iv0 = 64, iv1 = -1;
+					for (int k = 0; k < cu; ++k) {
+						const uint32_t w = __ldg(S + k);
+						if ((int)(int16_t)(w & 0xffffu) < tpx1 && (int)(int16_t)(w >> 16) > tpx0) {
+							iu0 = min(iu0, k);
+							iu1 = k;
+						}
+					}
+					for (int k = 0; k < cv; ++k) {
+						const uint32_t w = __ldg(S + 32 + k);
+						if ((int)(int16_t)(w & 0xffffu) < tpy1 && (int)(int16_t)(w >> 16) > tpy0) {
+							iv0 = min(iv0, k);
+							iv1 = k;
+						}
+					}
+					if (iu1 < 0 || iv1 < 0) {
+						f = false;
+						nmp = 0;
+					} else {
+						nmp = (iu1 - iu0 + 1) * (iv1 - iv0 + 1);
+						sub = iu0 | (iv0 << 8) | ((iu1 - iu0 + 1) << 16);
+					}
+				}
+			}
 			int total, sum;
 			const int pos = block_excl_scan(sm.warp_tot, f, total);
 			__syncthreads();
@@ -470,6 +505,7 @@ __device__ __forceinline__ bool stage_mb(const FrameParams& fp, const GridsDev& 
 			if (f) {
 				sm.qgrid[pos] = gid;
 				sm.qcum[pos] = pre;
+				sm.qsub[pos] = sub;
 			}
 			if (t == 0) {
 				sm.qcum[total] = sum;
@@ -493,6 +529,11 @@ __device__ __forceinline__ bool stage_mb(const FrameParams& fp, const GridsDev& 
 			gid = sm.qgrid[lo];
 			m = p - sm.qcum[lo];
 			const int cu = __ldg(g.cu + gid), nk = __ldg(g.nkeys + gid);
+			const int sub = sm.qsub[lo];
+			if (sub >= 0) {
+				const int w = sub >> 16;
+				m = (((sub >> 8) & 0xff) + m / w) * cu + ((sub & 0xff) + m % w);
+			}
 			const long long nv = (long long)(cu + 1) * (__ldg(g.cv + gid) + 1);
 			const long long pb = __ldg(g.pbase + gid);
 			const int iv = m / cu, iu = m - iv * cu;
@@ -523,6 +564,14 @@ __device__ __forceinline__ bool stage_mb(const FrameParams& fp, const GridsDev& 
 			const int sX = max((int)floorf(mnx - gx) - 1, tpx0), eX = min(lceil_f(mxx + gx) + 1, tpx1);
 			const int sY = max((int)floorf(mny - gy) - 1, tpy0), eY = min(lceil_f(mxy + gy) + 1, tpy1);
 			active = !culled && !cropped && sX < eX && sY < eY;
+			if (active && blk) {
+				float zmax = -FLT_MAX;
+				for (int y = sY; y < eY; ++y)
+					for (int b = (sX - tpx0) >> 2; b <= (eX - 1 - tpx0) >> 2; ++b)
+						zmax = fmaxf(zmax, blk[(y - tpy0) * 4 + b]);
+				const double margin = 1e-6 * (double)fmaxf(fabsf(mnz), fabsf(mxz));
+				if ((double)mnz - margin > (double)zmax) active = false;
+			}
 		}
 		int total;
 		const int rank = block_excl_scan(sm.warp_tot, active, total);
@@ -959,7 +1008,7 @@ struct ItemQ {
 	float time0, time1, maxCocX, maxCocY;
 	int sX, sY, rw, npix, width, wtime, wbase;
 	int info;  // staged slot | 1 << 8 moving | 1 << 9 time window | q1 << 10
-	unsigned long long mnpix, mrw;  // ceil(2^32 / npix), ceil(2^32 / rw): exact quotients of slot indices
+	uint32_t mnpix, mrw;  // ceil(2^32 / npix), ceil(2^32 / rw) (0 for 1): exact quotients of slot indices
 };
 
 struct SmemQ {
@@ -981,6 +1030,8 @@ struct SmemQ {
 	int ipref[kItemsQ + 1];               // running count of the kept items' sample slots
 	int qgrid[kThreadsQ];
 	int qcum[kThreadsQ + 1];
+	int qsub[kThreadsQ];
+	float blk[16 * 4];                    // largest occluding depth of each row's 4-pixel blocks (round start)
 	uint32_t wq[kWarpsQ][64];             // per-warp queue of (candidate, sample) tests
 	float wz[kWarpsQ][64];                // ... with their slice bound's min z
 	uint32_t flag[kTileSampQ / 32];
@@ -1009,13 +1060,12 @@ __device__ __forceinline__ bool mb_slice_test(const FrameParams& fp, const MbRec
 	return mb_sample(fp, r, moving, fp.use_dof != 0, x, y, stime, sdx, sdy, D, u, v, tri, gt);
 }
 
-__device__ __forceinline__ unsigned long long quot_magic(int d) {
-	return (0x100000000ull + (unsigned long long)d - 1ull) / (unsigned long long)d;
+__device__ __forceinline__ uint32_t quot_magic(int d) {
+	return d <= 1 ? 0u : (uint32_t)((0x100000000ull + (unsigned long long)d - 1ull) / (unsigned long long)d);
 }
-// r / d for 0 <= r, r * d < 2^32, with m = quot_magic(d)
-__device__ __forceinline__ int quot(int r, unsigned long long m) {
-	return (int)(((unsigned long long)(unsigned)r * m) >> 32);
-}
+// r / d for 0 <= r, r * d < 2^32, with m = quot_magic(d): floor(r * ceil(2^32 / d) / 2^32)
+// is exact there (the rounding up adds less than r * d / 2^32 / d < 1 / d)
+__device__ __forceinline__ int quot(int r, uint32_t m) { return m == 0u ? r : (int)__umulhi((unsigned)r, m); }
 
 __global__ void __launch_bounds__(kThreadsQ, 2)
 sample_mbq_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, SampleStore st,
@@ -1063,6 +1113,7 @@ sample_mbq_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 		sm.qcum[0] = 0;
 		sm.any_nan = 0;
 	}
+	for (int i = t; i < 16 * 4; i += kThreadsQ) sm.blk[i] = FLT_MAX;
 	__syncthreads();
 	// pattern of each pixel and the lens stratum of each sample (the shuffle
 	// table inverted: the stratum of sample j is the q with shuffle[q] == j)
@@ -1159,7 +1210,8 @@ sample_mbq_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 	int lp = lbeg, r0 = 0, qtotal = 0, npend = 0;
 	for (;;) {
 		const bool exhausted =
-			stage_mb<kSlotsQ, SmemQ, kThreadsQ>(fp, g, bb, sm, tpx0, tpy0, tpx1, tpy1, lend, lp, r0, qtotal, npend);
+			stage_mb<kSlotsQ, SmemQ, kThreadsQ>(fp, g, bb, sm, tpx0, tpy0, tpx1, tpy1, lend, lp, r0, qtotal, npend,
+			                                    sm.blk);
 		if (npend == 0) break;
 
 		// ---- records and (candidate, slice) items ----
@@ -1421,6 +1473,13 @@ sample_mbq_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 				m = (z != z) ? __int_as_float(0x7f800000) : fmaxf(m, z);
 			}
 			sm.pxmax[pl] = m;
+		}
+		__syncthreads();
+		for (int i = t; i < fp.tile_h * 4; i += kThreadsQ) {
+			const int y = i >> 2, x0 = (i & 3) * 4;
+			float m = -FLT_MAX;
+			for (int x = x0; x < min(x0 + 4, fp.tile_w); ++x) m = fmaxf(m, sm.pxmax[y * fp.tile_w + x]);
+			sm.blk[i] = m;
 		}
 		__syncthreads();
 		npend = 0;
