@@ -375,7 +375,7 @@ struct aqh_ctx {
 	// device buffers
 	DevBuf d_cu, d_cv, d_nkeys, d_flags, d_tbase, d_pbase, d_cbase, d_mpbase, d_times, d_culled, d_P, d_Ci, d_Oi;
 	DevBuf d_mpcount;
-	DevBuf d_rect, d_minz, d_strips, d_tri, d_stcount, d_stoffset, d_stlist, d_idgrid;
+	DevBuf d_rect, d_minz, d_strips, d_tri, d_stcount, d_stoffset, d_stlist, d_idgrid, d_mpb;
 	DevBuf d_sa, d_sb, d_win, d_oz, d_nf, d_hz, d_keys, d_wmask;
 	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err, d_occl;
 	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb, d_disp, d_dither_req;
@@ -1046,6 +1046,11 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	bb.tri = ctx->d_tri.as<float4>();
 	bb.st_count = ctx->d_stcount.as<int32_t>();
 	bb.st_offset = ctx->d_stoffset.as<int32_t>();
+	if (P.mbdof && P.nmps > 0) {
+		// each micropolygon's staging bound, computed once instead of in every tile it may reach
+		AQH_TRY(ctx->d_mpb.ensure(sizeof(int4) * (size_t)P.nmps), "alloc staging bounds");
+		bb.mp_bounds = ctx->d_mpb.as<int4>();
+	}
 	const size_t nstore = store_size((long long)fp.sw * fp.sh, fp.spp);
 	AQH_TRY(ctx->d_sa.ensure(nstore * sizeof(float4)), "alloc sample store");
 	AQH_TRY(ctx->d_sb.ensure(nstore * sizeof(float4)), "alloc sample store");
@@ -1273,6 +1278,7 @@ static aqh_status enqueue_frame(aqh_ctx* ctx, RenderPlan& P, bool batched, bool 
 		launch_st_count(fp, P.g, P.bb, s);
 		launch_scan_i32(P.bb.st_count, P.bb.st_offset, P.nst * P.bb.nranges, nullptr, s);
 		launch_st_write(fp, P.g, P.bb, s);
+		if (P.bb.mp_bounds) launch_mb_stage_bounds(fp, P.g, P.bb.mp_bounds, s);
 	} else {
 		AQH_TRY(cudaMemsetAsync(P.bb.st_offset, 0, sizeof(int32_t) * ((size_t)P.nst * P.bb.nranges + 1), s), "memset");
 	}
@@ -1343,7 +1349,8 @@ static aqh_status render_plain(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 	P.bb.st_list = ctx->d_stlist.as<int32_t>();
 	P.bb.list_capacity = ctx->d_stlist.cap / sizeof(int32_t);
 	if (P.g.ngrids > 0) launch_st_write(fp, P.g, P.bb, s);
-	else AQH_TRY(cudaMemsetAsync(P.bb.st_offset, 0, sizeof(int32_t) * ((size_t)P.nst * P.bb.nranges + 1), s), "memset");
+	if (P.g.ngrids > 0 && P.bb.mp_bounds) launch_mb_stage_bounds(fp, P.g, P.bb.mp_bounds, s);
+	if (P.g.ngrids <= 0) AQH_TRY(cudaMemsetAsync(P.bb.st_offset, 0, sizeof(int32_t) * ((size_t)P.nst * P.bb.nranges + 1), s), "memset");
 	for (int attempt = 0; attempt < 4; ++attempt) {
 		if (P.pool.capacity > 0) {
 			AQH_TRY(cudaMemsetAsync(P.pool.count, 0, 8, s), "memset");

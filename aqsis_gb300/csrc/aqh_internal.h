@@ -178,6 +178,7 @@ struct BinBuffers {
 	uint32_t* strips;      // per grid 64 words, or null: [0, 32) the pixel range [lo, hi) of each
 	                       // micropolygon column, [32, 63) of each row (lo | hi << 16, int16 each);
 	                       // word 63 = 1 when present (one motion key, cu and cv at most 31)
+	int4* mp_bounds;       // motion frames, per micropolygon: its staging bound (pack_stage_bound), or null
 	int nranges;
 	int range_size;
 	int64_t list_capacity;
@@ -224,6 +225,8 @@ void launch_st_write(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cu
 // `colours_ready`, when given, is an event the first kernel that reads Ci/Oi
 // waits for (on an opaque frame, the resolve after the sampler), with
 // cudaStreamWaitEvent flags `wait_flags` (cudaEventWaitExternal in a capture).
+// Staging bound of every micropolygon of a motion blur / depth of field frame.
+void launch_mb_stage_bounds(const FrameParams& fp, const GridsDev& g, int4* out, cudaStream_t s);
 void launch_sample_tiles(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, const BinBuffers& b,
                          SampleStore st, FragPool pool, int32_t* err, cudaStream_t s,
                          cudaEvent_t colours_ready = nullptr, unsigned wait_flags = 0);

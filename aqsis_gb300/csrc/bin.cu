@@ -447,4 +447,22 @@ void launch_st_write(const FrameParams& fp, const GridsDev& g, BinBuffers& b, cu
 	                                        b.st_list, (long long)b.list_capacity);
 }
 
+// One warp per grid: the staging bound of each of its micropolygons, read by
+// every motion sampling tile the micropolygon may reach instead of its key
+// vertices.
+__global__ void mb_stage_bounds_kernel(FrameParams fp, GridsDev g, int4* out) {
+	const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const int lane = threadIdx.x & 31;
+	if (warp >= g.ngrids) return;
+	const int n = __ldg(g.cu + warp) * __ldg(g.cv + warp);
+	int4* o = out + __ldg(g.mpbase + warp);
+	for (int m = lane; m < n; m += 32) o[m] = pack_stage_bound(mb_stage_bound(fp, g, warp, m));
+}
+
+void launch_mb_stage_bounds(const FrameParams& fp, const GridsDev& g, int4* out, cudaStream_t s) {
+	if (g.ngrids <= 0) return;
+	const int wpb = kBlock / 32;
+	mb_stage_bounds_kernel<<<(g.ngrids + wpb - 1) / wpb, kBlock, 0, s>>>(fp, g, out);
+}
+
 }  // namespace aqh

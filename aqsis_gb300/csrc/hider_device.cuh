@@ -292,4 +292,77 @@ __device__ __forceinline__ float4 project_point(const float* m, float4 p) {
 	return make_float4(x, y, p.z, p.w);
 }
 
+
+// The motion sampler's staging bound of micropolygon m of grid gi
+// (AddMPG, imagebuffer.cpp:514-539): the bound over every key, grown by the
+// largest circle of confusion of its depth range, as a conservative pixel
+// rectangle [x0, x1) x [y0, y1) with a one-pixel margin over every time slice
+// and lens stratum, and its z range.  `keep` is false when the micropolygon
+// is culled or outside AddMPG's crop cull window.
+struct MbStageBound {
+	int x0, x1, y0, y1;
+	float mnz, mxz;
+	bool keep;
+};
+__device__ __forceinline__ MbStageBound mb_stage_bound(const FrameParams& fp, const GridsDev& g, int gid, int m) {
+	const int cu = __ldg(g.cu + gid), nk = __ldg(g.nkeys + gid);
+	const long long nv = (long long)(cu + 1) * (__ldg(g.cv + gid) + 1);
+	const long long pb = __ldg(g.pbase + gid);
+	const int iv = m / cu, iu = m - iv * cu;
+	const int index = iv * (cu + 1) + iu;
+	float mnx = FLT_MAX, mny = FLT_MAX, mnz = FLT_MAX, mxx = -FLT_MAX, mxy = -FLT_MAX, mxz = -FLT_MAX;
+	for (int k = 0; k < nk; ++k) {
+		const long long kb = pb + k * nv + index;
+		const V3f a = ld3(g.P, kb), b = ld3(g.P, kb + 1), c = ld3(g.P, kb + cu + 1), d = ld3(g.P, kb + cu + 2);
+		mnx = amin(mnx, amin(amin(amin(a.x, b.x), c.x), d.x));
+		mny = amin(mny, amin(amin(amin(a.y, b.y), c.y), d.y));
+		mnz = amin(mnz, amin(amin(amin(a.z, b.z), c.z), d.z));
+		mxx = amax(mxx, amax(amax(amax(a.x, b.x), c.x), d.x));
+		mxy = amax(mxy, amax(amax(amax(a.y, b.y), c.y), d.y));
+		mxz = amax(mxz, amax(amax(amax(a.z, b.z), c.z), d.z));
+	}
+	const bool culled = g.culled && g.culled[__ldg(g.mpbase + gid) + m];
+	float gx = 0.0f, gy = 0.0f;
+	if (fp.use_dof) {
+		const float2 c1 = coc(mnz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+		const float2 c2 = coc(mxz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+		gx = amax(c1.x, c2.x);
+		gy = amax(c1.y, c2.y);
+	}
+	const bool cropped = (mxx + gx) < fp.cull_x0 || (mxy + gy) < fp.cull_y0 || (mnx - gx) > fp.cull_x1 ||
+	                     (mny - gy) > fp.cull_y1;
+	MbStageBound r;
+	r.x0 = (int)floorf(mnx - gx) - 1;
+	r.x1 = lceil_f(mxx + gx) + 1;
+	r.y0 = (int)floorf(mny - gy) - 1;
+	r.y1 = lceil_f(mxy + gy) + 1;
+	r.mnz = mnz;
+	r.mxz = mxz;
+	r.keep = !culled && !cropped;
+	return r;
+}
+
+// The staging bound packed in 16 bytes: the rectangle as int16 pairs
+// (clamped to the int16 range, which keeps every comparison with a tile of a
+// frame below 32768 pixels), the z range as floats; an empty rectangle when
+// the micropolygon is not kept.
+__device__ __forceinline__ int4 pack_stage_bound(const MbStageBound& b) {
+	auto c16 = [](int v) { return v < -32768 ? -32768 : (v > 32767 ? 32767 : v); };
+	int x0 = c16(b.x0), x1 = c16(b.x1), y0 = c16(b.y0), y1 = c16(b.y1);
+	if (!b.keep) { x0 = 32767; x1 = -32768; }
+	return make_int4((x0 & 0xffff) | (x1 << 16), (y0 & 0xffff) | (y1 << 16), __float_as_int(b.mnz),
+	                 __float_as_int(b.mxz));
+}
+__device__ __forceinline__ MbStageBound unpack_stage_bound(int4 q) {
+	MbStageBound b;
+	b.x0 = (int)(int16_t)(q.x & 0xffff);
+	b.x1 = q.x >> 16;
+	b.y0 = (int)(int16_t)(q.y & 0xffff);
+	b.y1 = q.y >> 16;
+	b.mnz = __int_as_float(q.z);
+	b.mxz = __int_as_float(q.w);
+	b.keep = b.x0 < b.x1;
+	return b;
+}
+
 }  // namespace aqh

@@ -534,36 +534,14 @@ __device__ __forceinline__ bool stage_mb(const FrameParams& fp, const GridsDev& 
 				const int w = sub >> 16;
 				m = (((sub >> 8) & 0xff) + m / w) * cu + ((sub & 0xff) + m % w);
 			}
-			const long long nv = (long long)(cu + 1) * (__ldg(g.cv + gid) + 1);
-			const long long pb = __ldg(g.pbase + gid);
-			const int iv = m / cu, iu = m - iv * cu;
-			const int index = iv * (cu + 1) + iu;
-			float mnx = FLT_MAX, mny = FLT_MAX, mnz = FLT_MAX, mxx = -FLT_MAX, mxy = -FLT_MAX, mxz = -FLT_MAX;
-			for (int k = 0; k < nk; ++k) {
-				const long long kb = pb + k * nv + index;
-				const V3f a = ld3(g.P, kb), b = ld3(g.P, kb + 1), c = ld3(g.P, kb + cu + 1), d = ld3(g.P, kb + cu + 2);
-				mnx = amin(mnx, amin(amin(amin(a.x, b.x), c.x), d.x));
-				mny = amin(mny, amin(amin(amin(a.y, b.y), c.y), d.y));
-				mnz = amin(mnz, amin(amin(amin(a.z, b.z), c.z), d.z));
-				mxx = amax(mxx, amax(amax(amax(a.x, b.x), c.x), d.x));
-				mxy = amax(mxy, amax(amax(amax(a.y, b.y), c.y), d.y));
-				mxz = amax(mxz, amax(amax(amax(a.z, b.z), c.z), d.z));
-			}
-			const bool culled = g.culled && g.culled[__ldg(g.mpbase + gid) + m];
-			float gx = 0.0f, gy = 0.0f;
-			if (usingDof) {
-				const float2 c1 = coc(mnz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
-				const float2 c2 = coc(mxz, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
-				gx = amax(c1.x, c2.x);
-				gy = amax(c1.y, c2.y);
-			}
-			// AddMPG (imagebuffer.cpp:514-539): DoF-grown bound against the crop cull window
-			const bool cropped = (mxx + gx) < fp.cull_x0 || (mxy + gy) < fp.cull_y0 || (mnx - gx) > fp.cull_x1 ||
-			                     (mny - gy) > fp.cull_y1;
+			(void)nk;
 			// conservative pixel rectangle over every time slice and lens stratum
-			const int sX = max((int)floorf(mnx - gx) - 1, tpx0), eX = min(lceil_f(mxx + gx) + 1, tpx1);
-			const int sY = max((int)floorf(mny - gy) - 1, tpy0), eY = min(lceil_f(mxy + gy) + 1, tpy1);
-			active = !culled && !cropped && sX < eX && sY < eY;
+			const MbStageBound sb = bb.mp_bounds ? unpack_stage_bound(bb.mp_bounds[__ldg(g.mpbase + gid) + m])
+			                                     : mb_stage_bound(fp, g, gid, m);
+			const float mnz = sb.mnz, mxz = sb.mxz;
+			const int sX = max(sb.x0, tpx0), eX = min(sb.x1, tpx1);
+			const int sY = max(sb.y0, tpy0), eY = min(sb.y1, tpy1);
+			active = sb.keep && sX < eX && sY < eY;
 			if (active && blk) {
 				float zmax = -FLT_MAX;
 				for (int y = sY; y < eY; ++y)

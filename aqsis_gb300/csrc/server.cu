@@ -80,6 +80,9 @@ extern "C" size_t aqh_job_footprint(const aqh_job* j) {
 	b += j->nP * 16 + j->nC * 32 + (size_t)j->ngrids * (5 * 4 + 3 * 8) + j->ntimes * 4;  // grids
 	b += (size_t)j->ngrids * (16 + 4 + 4 * 4) + 65536;                                  // bin
 	if (j->culled) b += (size_t)j->micropolygons;                                        // culled flags
+	bool moving = fp.use_dof != 0;
+	for (int i = 0; i < j->ngrids && !moving; ++i) moving = j->nkeys[i] > 1;
+	if (moving) b += (size_t)j->micropolygons * 16;                                      // staging bounds
 	b += nsamp * (32 + 12);                                                              // sample store (+debug)
 	bool transparent = false;
 	for (int i = 0; i < j->ngrids && !transparent; ++i) transparent = !(j->flags[i] & AQH_GRID_OPAQUE);
