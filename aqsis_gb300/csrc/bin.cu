@@ -35,8 +35,10 @@ __device__ __forceinline__ uint32_t pack_range(float mn, float mx, bool bad) {
 // with motion blur or depth of field the ranges grow by `grow` (the grid's
 // largest circle of confusion) and one pixel on each side, which covers the
 // staging rectangles of the motion sampler.  Lane = vertex column.
+template <int NK>  // NK = 1: one key (its loads pipeline across rows); 0: nk keys
 __device__ __forceinline__ void grid_strips(const float4* P, int cu, int cv, int nk, float growx, float growy,
                                             bool margin, int lane, uint32_t* S) {
+	if (NK == 1) nk = 1;
 	const bool on = lane <= cu;
 	const long long nvk = (long long)(cu + 1) * (cv + 1);
 	float cmn = FLT_MAX, cmx = -FLT_MAX, pmn = FLT_MAX, pmx = -FLT_MAX;
@@ -138,7 +140,10 @@ __global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect, float*
 		uint32_t* S = strips + (long long)warp * 64;
 		const bool mbdof = fp.use_dof || fp.any_motion;
 		const bool has = (nk == 1 || mbdof) && nk <= kMaxKeys && cu <= 31 && cv <= 31;
-		if (has) grid_strips(P, cu, cv, nk, mcx, mcy, mbdof, lane, S);
+		if (has) {
+			if (nk == 1) grid_strips<1>(P, cu, cv, 1, mcx, mcy, mbdof, lane, S);
+			else grid_strips<0>(P, cu, cv, nk, mcx, mcy, mbdof, lane, S);
+		}
 		if (lane == 0) S[63] = has ? 1u : 0u;
 	}
 	if (lane != 0) return;
