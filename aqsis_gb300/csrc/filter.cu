@@ -25,6 +25,10 @@ __device__ __forceinline__ double lround_d(double x) {
 	return (double)(i + 1);
 }
 
+__device__ __forceinline__ void finish_pixel(const FrameParams& fp, const SamplerDev& smp, int spp, float gTot,
+                                             int count, const float acc[7], float* __restrict__ chan,
+                                             uint8_t* __restrict__ q8, int x, int y);
+
 // One display pixel (x, y).  SPP > 0: samples per pixel known at compile
 // time (the sample loop is unrolled by four so its loads issue together); 0:
 // read from fp.
@@ -96,6 +100,16 @@ __device__ __forceinline__ void filter_pixel(const FrameParams& fp, const Sample
 			}
 		}
 	}
+	finish_pixel(fp, smp, spp, gTot, count, acc, chan, q8, x, y);
+}
+
+// The end of FilterBucket for one display pixel from its sums: normalisation
+// by the weight total (1/gTot in double, rounded to float), coverage and
+// alpha; then ExposeBucket, the channel-buffer write and the frame's fused
+// 8-bit r g b a display.
+__device__ __forceinline__ void finish_pixel(const FrameParams& fp, const SamplerDev& smp, int spp, float gTot,
+                                             int count, const float acc[7], float* __restrict__ chan,
+                                             uint8_t* __restrict__ q8, int x, int y) {
 	float c[9];
 	float coverage;
 	if (count == 0) {
@@ -159,6 +173,144 @@ filter_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __res
 		if (x < fp.crop_x1 && y < fp.crop_y1) filter_pixel<SPP>(fp, smp, st, ftab, chan, q8, x, y);
 	}
 }
+
+// ---- 3x3 windows (filter widths in [2, 4), shift 1): a rolling window ----
+//
+// One thread owns a display column and a run of rows.  It reads each row of
+// input pixels once and adds every sample to the three output rows whose
+// windows hold that row: the row below (fy = -1), its own row (fy = 0) and
+// the row above (fy = +1).  Output row y takes its fy = -1 terms from input
+// row y - 1, its fy = 0 terms from row y and its fy = +1 terms from row y + 1;
+// input rows ascend, and within an input row the columns ascend (fx = -1, 0,
+// 1) and then the samples -- the reference's (fy, fx, sy, sx) order, so every
+// sum rounds exactly as in filter_pixel.  Each sample is
+// loaded by three threads (the neighbouring columns, which read it back to
+// back) instead of nine, once per run of rows plus the two rows around it.
+struct FiltSum {
+	float acc[7];
+	float gTot;
+	int count;
+};
+__device__ __forceinline__ void fsum_reset(FiltSum& f) {
+#pragma unroll
+	for (int k = 0; k < 7; ++k) f.acc[k] = 0.0f;
+	f.gTot = 0.0f;
+	f.count = 0;
+}
+__device__ __forceinline__ void fsum_add(FiltSum& f, bool in, float gw, const float4& a, const float4& b) {
+	if (!in) return;
+	f.gTot += gw;
+	if (b.w != 0.0f) {
+		f.acc[0] += a.x * gw;
+		f.acc[1] += a.y * gw;
+		f.acc[2] += a.z * gw;
+		f.acc[3] += b.x * gw;
+		f.acc[4] += b.y * gw;
+		f.acc[5] += b.z * gw;
+		f.acc[6] += a.w * gw;
+		f.count++;
+	}
+}
+
+// Input row r of display column x: its three pixels' samples into the sums
+// of output rows r + 1 (B, window row fy = -1), r (M, fy = 0) and r - 1 (A,
+// fy = +1), each only when that row is the thread's (uB, uM, uA).
+template <int SPP>
+__device__ __forceinline__ void roll_row(const FrameParams& fp, const SamplerDev& smp, const SampleStore& st,
+                                         const float* __restrict__ ftab, int x, int r, FiltSum& B, FiltSum& M,
+                                         FiltSum& A, bool uB, bool uM, bool uA) {
+	const int spp = SPP > 0 ? SPP : fp.spp;
+	const float xcent = x + 0.5f;
+	const float ycB = (r + 1) + 0.5f, ycM = r + 0.5f, ycA = (r - 1) + 0.5f;
+	for (int fx = -1; fx <= 1; ++fx) {
+		const int px = x + fx;
+		const long long pix = (long long)(r - fp.sy0) * fp.sw + (px - fp.sx0);
+		const long long pat = (st.wmask || !smp.pos_index) ? pix : (long long)__ldg(smp.pos_index + pix);
+		const float fpx = (float)px, fpy = (float)r;
+		const int bB = fx + 1, bM = 3 + fx + 1, bA = 6 + fx + 1;  // window bits (fy + 1) * 3 + fx + 1
+		for (int i0 = 0; i0 < spp; i0 += 4) {
+			bool iB[4], iM[4], iA[4];
+			float gB[4], gM[4], gA[4];
+#pragma unroll
+			for (int j = 0; j < 4; ++j) {
+				const int i = i0 + j;
+				const bool ok = (SPP > 0 && SPP % 4 == 0) || i < spp;
+				const int ic = ok ? i : i0;
+				if (st.wmask) {
+					const uint32_t mk = ok ? __ldg(st.wmask + store_index(pix, ic, spp)) : 0u;
+					iB[j] = uB && ((mk >> bB) & 1u);
+					iM[j] = uM && ((mk >> bM) & 1u);
+					iA[j] = uA && ((mk >> bA) & 1u);
+				} else {
+					const float2 o = __ldg(smp.pos + pat * spp + ic);
+					const float vx = (fpx + o.x) - xcent;
+					const bool inx = ok && vx >= -fp.xfwo2 && vx <= fp.xfwo2;
+					const float vB = (fpy + o.y) - ycB, vM = (fpy + o.y) - ycM, vA = (fpy + o.y) - ycA;
+					iB[j] = uB && inx && vB >= -fp.yfwo2 && vB <= fp.yfwo2;
+					iM[j] = uM && inx && vM >= -fp.yfwo2 && vM <= fp.yfwo2;
+					iA[j] = uA && inx && vA >= -fp.yfwo2 && vA <= fp.yfwo2;
+				}
+				gB[j] = ftab[bB * spp + ic];
+				gM[j] = ftab[bM * spp + ic];
+				gA[j] = ftab[bA * spp + ic];
+			}
+			float4 av[4], bv[4];
+#pragma unroll
+			for (int j = 0; j < 4; ++j) {
+				const bool any = iB[j] || iM[j] || iA[j];
+				const long long si = store_index(pix, any ? i0 + j : i0, spp);
+				bv[j] = any ? __ldg(st.b + si) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+				av[j] = any ? __ldg(st.a + si) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+			}
+#pragma unroll
+			for (int j = 0; j < 4; ++j) {
+				fsum_add(B, iB[j], gB[j], av[j], bv[j]);
+				fsum_add(M, iM[j], gM[j], av[j], bv[j]);
+				fsum_add(A, iA[j], gA[j], av[j], bv[j]);
+			}
+		}
+	}
+}
+
+constexpr int kRollThreads = 128;  // display columns per CTA
+constexpr int kRollRows = 8;       // display rows per CTA (8 measured faster than 16)
+
+// Input row q (0 .. R+1) of a run: r = y0 - 1 + q feeds output rows y0 + q
+// (B), y0 + q - 1 (M) and y0 + q - 2 (A); row y0 + q - 2 is then complete.
+#define AQH_ROLL_STEP(QQ, SB, SM, SA)                                                                     \
+	{                                                                                                     \
+		const int q = (QQ);                                                                               \
+		if (q < R + 2) {                                                                                  \
+			if (q < R) fsum_reset(SB);                                                                    \
+			roll_row<SPP>(fp, smp, st, ftab_s, x, y0 - 1 + q, SB, SM, SA, q < R, q >= 1 && q <= R, q >= 2); \
+			if (q >= 2) finish_pixel(fp, smp, spp, SA.gTot, SA.count, SA.acc, chan, q8, x, y0 + q - 2);  \
+		}                                                                                                 \
+	}
+
+template <int SPP>
+__global__ void __launch_bounds__(kRollThreads)
+filter_roll_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* __restrict__ ftab,
+                   float* __restrict__ chan, uint8_t* __restrict__ q8) {
+	__shared__ float ftab_s[9 * AQH_MAX_SPP_DEV];
+	const int spp = SPP > 0 ? SPP : fp.spp;
+	for (int i = threadIdx.x; i < 9 * spp; i += kRollThreads) ftab_s[i] = ftab[i];
+	__syncthreads();
+	const int x = fp.crop_x0 + blockIdx.x * kRollThreads + threadIdx.x;
+	const int y0 = fp.crop_y0 + blockIdx.y * kRollRows;
+	const int R = min(kRollRows, fp.crop_y1 - y0);
+	if (x >= fp.crop_x1 || R <= 0) return;
+	FiltSum S0, S1, S2;
+	fsum_reset(S0);
+	fsum_reset(S1);
+	fsum_reset(S2);
+	// slots rotate with the input row: B = S[q % 3], M = S[(q + 2) % 3], A = S[(q + 1) % 3]
+	for (int q0 = 0; q0 < R + 2; q0 += 3) {
+		AQH_ROLL_STEP(q0, S0, S2, S1)
+		AQH_ROLL_STEP(q0 + 1, S1, S0, S2)
+		AQH_ROLL_STEP(q0 + 2, S2, S1, S0)
+	}
+}
+#undef AQH_ROLL_STEP
 
 // Output variables of one display pixel: FilterBucket's weighted sum over
 // the same window, weights and order as filter_pixel (gTot included), of the
@@ -304,6 +456,20 @@ void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStor
 	// tiles in flight per SM: by default as many as can be resident (the
 	// filter is latency-bound: fewer tiles in flight, whose samples would stay
 	// in L2 between the passes, measured slower)
+	if (fp.shiftX == 1 && fp.shiftY == 1 && fp.spp <= AQH_MAX_SPP_DEV && !st.wmask) {
+		// 3x3 windows: the rolling window reads each sample three times, not
+		// nine (frames with window masks -- at most 16 samples per pixel --
+		// read a word per sample and keep the tile kernel, measured faster)
+		const dim3 rg((w + kRollThreads - 1) / kRollThreads, (h + kRollRows - 1) / kRollRows);
+		switch (fp.spp) {
+		case 4: filter_roll_kernel<4><<<rg, kRollThreads, 0, s>>>(fp, sm, st, ftab, channels, q8); break;
+		case 16: filter_roll_kernel<16><<<rg, kRollThreads, 0, s>>>(fp, sm, st, ftab, channels, q8); break;
+		case 36: filter_roll_kernel<36><<<rg, kRollThreads, 0, s>>>(fp, sm, st, ftab, channels, q8); break;
+		case 64: filter_roll_kernel<64><<<rg, kRollThreads, 0, s>>>(fp, sm, st, ftab, channels, q8); break;
+		default: filter_roll_kernel<0><<<rg, kRollThreads, 0, s>>>(fp, sm, st, ftab, channels, q8); break;
+		}
+		return;
+	}
 	const int per_sm = fp.filter_ctas > 0 ? std::min(fp.filter_ctas, 8) : 8;
 	const int grid = std::max(1, std::min(ntiles, nsm * per_sm));
 	switch (fp.spp) {

@@ -714,6 +714,9 @@ def served_measure(args) -> dict:
                        "peak_jobs_in_flight": st["peak_running"], "peak_hbm_bytes": st["peak_in_use"],
                        "graphs_built": st["graphs_built"], "rerenders": st["rerenders"]},
             "plain": {"frames_per_s_saturated": args.jobs / plain_sat,
+                      # share of the saturated run's wall time the device spent on the frames:
+                      # near 1 means overlapping requests cannot multiply frames/s
+                      "device_busy_fraction": sum(busy.values()) / 1e3 / plain_sat,
                       "micropolygons_per_s_saturated": mps_total / plain_sat,
                       "latency_ms_poisson": {"p50": 1e3 * float(np.percentile(plain_lat, 50)),
                                              "p99": 1e3 * float(np.percentile(plain_lat, 99))},

@@ -516,7 +516,7 @@ typedef struct {
  * jobs are not starved. */
 #define AQH_ADMIT_ARRIVAL 0
 #define AQH_ADMIT_SMALLEST 1
-#define AQH_ADMIT_MAX_WAIT_MS 1000
+#define AQH_ADMIT_MAX_WAIT_MS 250
 /* One render request.  Every pointer is host memory that must stay valid
  * until the job completes; grids use the aqh_submit_grids_host layout. */
 typedef struct {
