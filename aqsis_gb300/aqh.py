@@ -177,6 +177,8 @@ def load(build_if_missing: bool = False):
     L.aqh_frame_desc_defaults.argtypes = [C.POINTER(FrameDesc)]
     L.aqh_frame_desc_defaults.restype = None
     L.aqh_frame_begin.argtypes = [vp, C.POINTER(FrameDesc)]
+    L.aqh_set_imager.argtypes = [vp, C.c_int]
+    L.aqh_apply_imager.argtypes = [vp, _f32p, C.c_size_t]
     L.aqh_set_samples.argtypes = [vp, C.POINTER(Samples)]
     L.aqh_submit_grid.argtypes = [vp, C.POINTER(Grid)]
     L.aqh_submit_grids_device.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int64]
@@ -504,6 +506,15 @@ class Hider:
     def set_host_copy(self, engines: bool):
         """Three-float P by the copy engines (True) or read by a kernel (aqh_set_host_copy)."""
         self._check(self.L.aqh_set_host_copy(self.ctx, 1 if engines else 0), "aqh_set_host_copy")
+
+    def set_imager(self, enabled: bool):
+        """aqh_set_imager: frames stop after the filter until apply_imager."""
+        self._check(self.L.aqh_set_imager(self.ctx, 1 if enabled else 0), "aqh_set_imager")
+
+    def apply_imager(self, ci_oi):
+        """aqh_apply_imager: the imager shader's Ci and Oi, float[pixel][6]."""
+        a = np.ascontiguousarray(ci_oi, np.float32).reshape(-1)
+        self._check(self.L.aqh_apply_imager(self.ctx, _p(a, _f32p), C.c_size_t(a.size)), "aqh_apply_imager")
 
     def render(self, sync: bool = True):
         self._check(self.L.aqh_render(self.ctx, 1 if sync else 0), "aqh_render")

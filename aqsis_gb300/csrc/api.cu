@@ -349,6 +349,9 @@ struct aqh_ctx {
 	// trim curves: host copies of the sets, the grids' sets and the uv array
 	int trim_nsets = 0;
 	bool cull_on = false;
+	bool imager = false;        // aqh_set_imager: frames stop after the filter
+	bool imager_pending = false; // the last frame waits for aqh_apply_imager
+	DevBuf d_imager;
 	std::vector<float> cull_Ng, cull_N;
 	DevBuf d_cull_n;
 	std::vector<int32_t> trim_grid_set, trim_loop_first, trim_set_first;
@@ -990,6 +993,7 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	if (ctx->any_camera && !ctx->camera_set && !ctx->dev_grids)
 		return ctx->fail(AQH_EINVAL, "grids flagged AQH_GRID_CAMERA but no camera-to-raster matrix is set");
 	P.project = ctx->any_camera && ctx->camera_set;
+	P.imager = ctx->imager;
 	P.cam = ctx->camera;
 	P.nmps = ctx->dev_grids ? ctx->dev_mps : ctx->h_mps;
 	bool motion = false;
@@ -1088,7 +1092,9 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	pool = FragPool{};
 	fp.frag_only = 0;
 	if (ctx->any_transparent || !fp.cullable || fp.midpoint_store || ctx->csg_n > 0) {
-		if (ctx->frag_capacity == 0) ctx->frag_capacity = std::max<int64_t>(1 << 20, (int64_t)P.nsamp * 2);
+		// fragment links are int32: the pool indexes at most INT32_MAX fragments
+		if (ctx->frag_capacity == 0)
+			ctx->frag_capacity = std::min<int64_t>(INT32_MAX, std::max<int64_t>(1 << 20, (int64_t)P.nsamp * 2));
 		AQH_TRY(ctx->d_frag.ensure(ctx->frag_capacity * sizeof(float4)), "alloc fragments");
 		AQH_TRY(ctx->d_next.ensure(ctx->frag_capacity * sizeof(int32_t)), "alloc fragments");
 		AQH_TRY(ctx->d_fcount.ensure(16), "alloc");
@@ -1305,9 +1311,14 @@ static aqh_status enqueue_frame(aqh_ctx* ctx, RenderPlan& P, bool batched, bool 
 	if (timing) mark(ctx->ev[2]);
 	// the frame's r g b a display is quantized in the filter pass when it fits 8 bits
 	const bool fuse_q8 = fp.q_one == 0.0f || (fp.q_min >= 0.0f && fp.q_max <= 255.0f);
-	launch_filter(fp, ctx->smp, P.store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(),
-	              fuse_q8 ? ctx->d_q8.as<uint8_t>() : nullptr, s);
-	ctx->q8_default = fuse_q8;
+	// with an imager the channels stay as FilterBucket leaves them (no
+	// exposure, no display) until aqh_apply_imager
+	FrameParams ffp = fp;
+	if (P.imager) ffp.gain = ffp.gamma = 1.0f;
+	launch_filter(ffp, ctx->smp, P.store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(),
+	              (fuse_q8 && !P.imager) ? ctx->d_q8.as<uint8_t>() : nullptr, s);
+	ctx->q8_default = fuse_q8 && !P.imager;
+	ctx->imager_pending = P.imager;
 	if (P.g.naov > 0) launch_filter_aov(fp, ctx->smp, P.store, P.g, ctx->d_ftab.as<float>(), ctx->d_aovchan.as<float>(), s);
 	AQH_TRY(cudaGetLastError(), "filter kernel launch");
 	if (timing) mark(ctx->ev[3]);
@@ -1376,7 +1387,12 @@ static aqh_status render_plain(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 		ctx->stats.fragments = (int64_t)used;
 		if (!ovf) break;
 		// grow the fragment pool to what this frame needed and sample again
-		ctx->frag_capacity = (int64_t)used + (int64_t)used / 4 + 1024;
+		if (used > (unsigned long long)INT32_MAX)
+			return ctx->fail(AQH_ELIMIT,
+			                 "the frame needs %llu transparent fragments; the fragment pool indexes at most %d "
+			                 "(render it in smaller crop windows)",
+			                 used, INT32_MAX);
+		ctx->frag_capacity = std::min<int64_t>(INT32_MAX, (int64_t)used + (int64_t)used / 4 + 1024);
 		AQH_TRY(ctx->d_frag.ensure(ctx->frag_capacity * sizeof(float4)), "alloc fragments");
 		AQH_TRY(ctx->d_next.ensure(ctx->frag_capacity * sizeof(int32_t)), "alloc fragments");
 		P.pool.frag = ctx->d_frag.as<float4>();
@@ -1395,9 +1411,14 @@ static aqh_status render_plain(aqh_ctx* ctx, RenderPlan& P, bool sync) {
 	cudaEventRecord(ctx->ev[2], s);
 	// the frame's r g b a display is quantized in the filter pass when it fits 8 bits
 	const bool fuse_q8 = fp.q_one == 0.0f || (fp.q_min >= 0.0f && fp.q_max <= 255.0f);
-	launch_filter(fp, ctx->smp, P.store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(),
-	              fuse_q8 ? ctx->d_q8.as<uint8_t>() : nullptr, s);
-	ctx->q8_default = fuse_q8;
+	// with an imager the channels stay as FilterBucket leaves them (no
+	// exposure, no display) until aqh_apply_imager
+	FrameParams ffp = fp;
+	if (P.imager) ffp.gain = ffp.gamma = 1.0f;
+	launch_filter(ffp, ctx->smp, P.store, ctx->d_ftab.as<float>(), ctx->d_chan.as<float>(),
+	              (fuse_q8 && !P.imager) ? ctx->d_q8.as<uint8_t>() : nullptr, s);
+	ctx->q8_default = fuse_q8 && !P.imager;
+	ctx->imager_pending = P.imager;
 	if (P.g.naov > 0) launch_filter_aov(fp, ctx->smp, P.store, P.g, ctx->d_ftab.as<float>(), ctx->d_aovchan.as<float>(), s);
 	AQH_TRY(cudaGetLastError(), "filter kernel launch");
 	cudaEventRecord(ctx->ev[3], s);
@@ -1791,6 +1812,31 @@ aqh_status aqh_set_mode(aqh_ctx* ctx, int mode) {
 	cudaSetDevice(ctx->device);
 	AQH_TRY(cudaStreamSynchronize(ctx->stream), "synchronize");
 	ctx->mode = mode;
+	return AQH_OK;
+}
+
+aqh_status aqh_set_imager(aqh_ctx* ctx, int enabled) {
+	if (!ctx) return AQH_EINVAL;
+	ctx->imager = enabled != 0;
+	return AQH_OK;
+}
+
+aqh_status aqh_apply_imager(aqh_ctx* ctx, const float* ci_oi, size_t n_floats) {
+	if (!ctx || !ci_oi) return AQH_EINVAL;
+	if (!ctx->imager_pending) return ctx->fail(AQH_EINVAL, "no frame rendered with an imager is waiting");
+	const FrameParams& fp = ctx->fp;
+	const size_t n = (size_t)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0) * 6;
+	if (n_floats < n) return ctx->fail(AQH_EINVAL, "imager values hold %zu floats, %zu needed", n_floats, n);
+	cudaSetDevice(ctx->device);
+	AQH_TRY(ctx->d_imager.ensure(n * 4), "alloc imager values");
+	AQH_TRY(cudaMemcpyAsync(ctx->d_imager.p, ci_oi, n * 4, cudaMemcpyHostToDevice, ctx->stream), "upload imager");
+	const bool fuse_q8 = fp.q_one == 0.0f || (fp.q_min >= 0.0f && fp.q_max <= 255.0f);
+	launch_imager(fp, ctx->smp, ctx->d_imager.as<float>(), ctx->d_chan.as<float>(),
+	              fuse_q8 ? ctx->d_q8.as<uint8_t>() : nullptr, ctx->stream);
+	AQH_TRY(cudaGetLastError(), "imager launch");
+	AQH_TRY(cudaStreamSynchronize(ctx->stream), "imager");  // the host array may go away on return
+	ctx->q8_default = fuse_q8;
+	ctx->imager_pending = false;
 	return AQH_OK;
 }
 

@@ -203,6 +203,7 @@ struct RenderPlan {
 	int64_t nmps;
 	bool project;  // AQH_GRID_CAMERA grids to project before binning (with cam)
 	CamMatrix cam;
+	bool imager;   // stop after FilterBucket: no exposure or 8-bit display until aqh_apply_imager
 };
 
 // Kernel launchers (implemented in the .cu files).
@@ -264,6 +265,10 @@ void dof_bounds_h(int xs, int ys, std::vector<float4>& out);
 // written in the same pass (the quantize of quantize_u8 with channels 0 1 2 6).
 void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStore& st, const float* ftab,
                    float* channels, uint8_t* q8, cudaStream_t s);
+// The imager's Ci and Oi (float[pixel][6]) into the channels, alpha from
+// that opacity, then exposure and (q8 non-null) the 8-bit r g b a display.
+void launch_imager(const FrameParams& fp, const SamplerDev& sm, const float* ci_oi, float* channels, uint8_t* q8,
+                   cudaStream_t s);
 // Output variables of the crop window, float[pixel][g.naov], filtered like Ci.
 void launch_filter_aov(const FrameParams& fp, const SamplerDev& sm, const SampleStore& st, const GridsDev& g,
                        const float* ftab, float* aov_channels, cudaStream_t s);

@@ -28,6 +28,8 @@ __device__ __forceinline__ double lround_d(double x) {
 __device__ __forceinline__ void finish_pixel(const FrameParams& fp, const SamplerDev& smp, int spp, float gTot,
                                              int count, const float acc[7], float* __restrict__ chan,
                                              uint8_t* __restrict__ q8, int x, int y);
+__device__ __forceinline__ void expose_store(const FrameParams& fp, const SamplerDev& smp, float c[9],
+                                             float* __restrict__ chan, uint8_t* __restrict__ q8, int x, int y);
 
 // One display pixel (x, y).  SPP > 0: samples per pixel known at compile
 // time (the sample loop is unrolled by four so its loads issue together); 0:
@@ -127,6 +129,13 @@ __device__ __forceinline__ void finish_pixel(const FrameParams& fp, const Sample
 	const float a = (c[3] + c[4] + c[5]) / 3.0f;
 	c[6] = a * coverage;
 	c[8] = coverage;
+	expose_store(fp, smp, c, chan, q8, x, y);
+}
+
+// ExposeBucket (bucketprocessor.cpp:766-806) on one display pixel's channels,
+// then the channel-buffer write and the frame's fused 8-bit r g b a display.
+__device__ __forceinline__ void expose_store(const FrameParams& fp, const SamplerDev& smp, float c[9],
+                                             float* __restrict__ chan, uint8_t* __restrict__ q8, int x, int y) {
 	// ExposeBucket: color = (color * gain) ^ (1 / gamma)
 	if (!(fp.gain == 1.0f && fp.gamma == 1.0f)) {
 		const float oneovergamma = 1.0f / fp.gamma;
@@ -380,6 +389,25 @@ filter_aov_kernel(FrameParams fp, SamplerDev smp, SampleStore st, GridsDev g, co
 }
 
 
+// The imager's write-back (bucketprocessor.cpp:712-743): Ci and Oi of each
+// display pixel from the imager shader's output (the shading VM runs on the
+// host), alpha = the mean of that opacity (no coverage factor), then
+// ExposeBucket and the 8-bit display as after the filter.
+__global__ void imager_kernel(FrameParams fp, SamplerDev smp, const float* __restrict__ ci_oi,
+                              float* __restrict__ chan, uint8_t* __restrict__ q8) {
+	const int w = fp.crop_x1 - fp.crop_x0;
+	const long long npix = (long long)w * (fp.crop_y1 - fp.crop_y0);
+	const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (p >= npix) return;
+	float c[9];
+#pragma unroll
+	for (int k = 0; k < 9; ++k) c[k] = chan[p * 9 + k];
+#pragma unroll
+	for (int k = 0; k < 6; ++k) c[k] = ci_oi[p * 6 + k];
+	c[6] = (c[3] + c[4] + c[5]) / 3.0f;
+	expose_store(fp, smp, c, chan, q8, fp.crop_x0 + (int)(p % w), fp.crop_y0 + (int)(p / w));
+}
+
 __global__ void quantize_u8_kernel(FrameParams fp, SamplerDev smp, const float* __restrict__ chan,
                                    const int* __restrict__ chans, int nchan, uint8_t* __restrict__ out) {
 	const long long npix = (long long)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
@@ -479,6 +507,13 @@ void launch_filter(const FrameParams& fp, const SamplerDev& sm, const SampleStor
 	case 64: filter_kernel<64><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels, q8); break;
 	default: filter_kernel<0><<<grid, 256, 0, s>>>(fp, sm, st, ftab, channels, q8); break;
 	}
+}
+
+void launch_imager(const FrameParams& fp, const SamplerDev& sm, const float* ci_oi, float* channels, uint8_t* q8,
+                   cudaStream_t s) {
+	const long long npix = (long long)(fp.crop_x1 - fp.crop_x0) * (fp.crop_y1 - fp.crop_y0);
+	if (npix <= 0) return;
+	imager_kernel<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(fp, sm, ci_oi, channels, q8);
 }
 
 void launch_filter_aov(const FrameParams& fp, const SamplerDev& sm, const SampleStore& st, const GridsDev& g,

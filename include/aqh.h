@@ -569,6 +569,21 @@ aqh_status aqh_server_stats(aqh_server* s, aqh_server_info* info);
 /* Estimated HBM footprint of a job (host arithmetic, no GPU needed); 0 if invalid. */
 size_t aqh_job_footprint(const aqh_job* job);
 
+/* ---- imager shaders --------------------------------------------------------- */
+/* RiImager (bucketprocessor.cpp:712-743): the imager shader runs on the
+ * host's shading VM over the filtered display pixels, after FilterBucket and
+ * before ExposeBucket.  With aqh_set_imager(ctx, 1), aqh_render stops after
+ * the filter: aqh_read_channels / aqh_read_bucket then give the channels
+ * before exposure (the shader's input, as InitialiseColorImager sees them).
+ * The host runs the shader and hands its colour and opacity back with
+ * aqh_apply_imager (float[pixel][6]: Ci r g b, Oi r g b, crop-window pixels in
+ * raster order), which writes them, sets alpha to the mean of that opacity,
+ * and then applies exposure (bucketprocessor.cpp:766-806) and the frame's
+ * 8-bit display.  Reads of the frame before aqh_apply_imager see the
+ * unexposed channels. */
+aqh_status aqh_set_imager(aqh_ctx* ctx, int enabled);
+aqh_status aqh_apply_imager(aqh_ctx* ctx, const float* ci_oi, size_t n_floats);
+
 /* ---- rendering without allocation ---------------------------------------- */
 /* No counterpart in the reference (aqsis renders into memory it allocates
  * per bucket).  For callers that cannot allocate device memory: a host whose

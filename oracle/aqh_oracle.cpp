@@ -1212,6 +1212,58 @@ extern "C" void orc_bilerp2(const float* q, const float* uv, int n, float* P) {
 	}
 }
 
+// ExposeBucket (bucketprocessor.cpp:766-806) over n display pixels' channels.
+static void exposeChannels(const OrcFrame* f, float* chan, size_t n) {
+	if (f->gain == 1.0 && f->gamma == 1.0) return;
+	float oneovergamma = 1.0f / f->gamma;
+	for (size_t p = 0; p < n; ++p) {
+		float* c = &chan[p * 9];
+		if (f->gain != 1.0) { c[0] *= f->gain; c[1] *= f->gain; c[2] *= f->gain; }
+		if (f->gamma != 1.0) {
+			c[0] = std::pow(c[0], oneovergamma);
+			c[1] = std::pow(c[1], oneovergamma);
+			c[2] = std::pow(c[2], oneovergamma);
+		}
+	}
+}
+
+// FormatBucketForDisplay quantize (ddmanager.cpp:1022-1119) of the channels
+// `qch` of n display pixels, one dither value per pixel (or none).
+static void quantizeChannels(const OrcFrame* f, const float* chan, size_t n, const float* dither, const int32_t* qch,
+                             int nq, double* out) {
+	for (size_t p = 0; p < n; ++p) {
+		double sdither = dither ? (double)dither[p] : 0.0;
+		for (int ci = 0; ci < nq; ++ci) {
+			double value = chan[p * 9 + qch[ci]];
+			if (f->q_one != 0) {
+				value = lroundd(f->q_zero + value * (f->q_one - f->q_zero) + (f->q_dither * sdither));
+				value = value < f->q_min ? f->q_min : (value > f->q_max ? f->q_max : value);
+			}
+			out[p * nq + ci] = value;
+		}
+	}
+}
+
+// The imager shader's write-back (bucketprocessor.cpp:712-743) on channels
+// FilterBucket left (before exposure): Ci and Oi from the shader's colour and
+// opacity (ci_oi [pixel][6]), alpha = their mean; then ExposeBucket.
+extern "C" void orc_imager(const OrcFrame* f, float* chan, const float* ci_oi, int64_t n) {
+	for (int64_t p = 0; p < n; ++p) {
+		float* c = &chan[p * 9];
+		const float* im = &ci_oi[p * 6];
+		c[0] = im[0]; c[1] = im[1]; c[2] = im[2];
+		c[3] = im[3]; c[4] = im[4]; c[5] = im[5];
+		const float a = (im[3] + im[4] + im[5]) / 3.0f;
+		c[6] = a;
+	}
+	exposeChannels(f, chan, (size_t)n);
+}
+
+extern "C" void orc_quantize(const OrcFrame* f, const float* chan, int64_t n, const float* dither,
+                             const int32_t* qch, int nq, double* out) {
+	quantizeChannels(f, chan, (size_t)n, dither, qch, nq, out);
+}
+
 extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples* s, const float* ftab, OrcOut* out) {
 	Frame fr;
 	fr.ctx.f = f;
@@ -1496,19 +1548,7 @@ extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples
 			}
 		}
 	}
-	// ExposeBucket (bucketprocessor.cpp:766-806)
-	if (!(f->gain == 1.0 && f->gamma == 1.0)) {
-		float oneovergamma = 1.0f / f->gamma;
-		for (size_t p = 0; p < (size_t)dw * dh; ++p) {
-			float* c = &chan[p * 9];
-			if (f->gain != 1.0) { c[0] *= f->gain; c[1] *= f->gain; c[2] *= f->gain; }
-			if (f->gamma != 1.0) {
-				c[0] = std::pow(c[0], oneovergamma);
-				c[1] = std::pow(c[1], oneovergamma);
-				c[2] = std::pow(c[2], oneovergamma);
-			}
-		}
-	}
+	exposeChannels(f, chan.data(), (size_t)dw * dh);
 	if (out->channels) std::memcpy(out->channels, chan.data(), chan.size() * sizeof(float));
 	// Float64 twin of the filter and exposure above: the same window test on
 	// the same float sample positions (membership is a selection, not
@@ -1560,20 +1600,8 @@ extern "C" int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples
 			}
 		}
 	}
-	// FormatBucketForDisplay quantize (ddmanager.cpp:1022-1119)
-	if (out->quantized && out->qchannels) {
-		for (size_t p = 0; p < (size_t)dw * dh; ++p) {
-			double sdither = s->dither ? (double)s->dither[p] : 0.0;
-			for (int ci = 0; ci < out->nqchannels; ++ci) {
-				double value = chan[p * 9 + out->qchannels[ci]];
-				if (f->q_one != 0) {
-					value = lroundd(f->q_zero + value * (f->q_one - f->q_zero) + (f->q_dither * sdither));
-					value = value < f->q_min ? f->q_min : (value > f->q_max ? f->q_max : value);
-				}
-				out->quantized[p * out->nqchannels + ci] = value;
-			}
-		}
-	}
+	if (out->quantized && out->qchannels)
+		quantizeChannels(f, chan.data(), (size_t)dw * dh, s->dither, out->qchannels, out->nqchannels, out->quantized);
 	out->spl_count = fr.splCount;
 	out->spl_bound_hits = fr.splBoundHits;
 	out->spl_hits = fr.splHits;

@@ -156,6 +156,14 @@ void orc_bilerp2(const float* quad8, const float* uv, int n, float* P);
 int orc_render(const OrcFrame* f, const OrcGrids* g, const OrcSamples* s,
                const float* filter_table, OrcOut* out);
 
+/* The imager shader's write-back (bucketprocessor.cpp:712-743) then
+ * ExposeBucket (766-806), on n display pixels' channels as FilterBucket left
+ * them: Ci, Oi from ci_oi [pixel][6], alpha = the mean of that opacity. */
+void orc_imager(const OrcFrame* f, float* chan, const float* ci_oi, int64_t n);
+/* FormatBucketForDisplay's quantize (ddmanager.cpp:1022-1119) of channels qch. */
+void orc_quantize(const OrcFrame* f, const float* chan, int64_t n, const float* dither, const int32_t* qch, int nq,
+                  double* out);
+
 /* The reference's global MT19937 (libs/math/random.cpp) and its multi-jittered
  * sample tables, for regenerating aqsis' own sample patterns. */
 void orc_mt_seed(uint32_t s);

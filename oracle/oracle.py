@@ -193,6 +193,47 @@ def projected_grids(scene):
     return dataclasses.replace(g, P=P, flags=np.asarray(g.flags) & ~GRID_CAMERA)
 
 
+def frame_struct(fr) -> OrcFrame:
+    """The OrcFrame of a scene.Frame."""
+    cx0, cx1, cy0, cy1 = fr.crop_window
+    mult, inv = fr.dof_terms()
+    return OrcFrame(fr.width, fr.height, cx0, cx1, cy0, cy1, fr.xsamples, fr.ysamples,
+                    fr.xfilter, fr.yfilter, fr.gain, fr.gamma, 0.0, fr.q_one, fr.q_min, fr.q_max,
+                    fr.q_dither, fr.shutter[0], fr.shutter[1], 1 if fr.use_dof else 0, mult, inv,
+                    fr.dof_scale[0], fr.dof_scale[1], fr.depth_filter,
+                    (C.c_float * 3)(*fr.zthreshold), fr.display_z)
+
+
+def imager(frame, chan, ci_oi) -> np.ndarray:
+    """The imager shader's write-back and ExposeBucket (orc_imager) on channels
+    FilterBucket left: returns the new channels."""
+    L = lib()
+    L.orc_imager.argtypes = [C.POINTER(OrcFrame), _f32p, _f32p, C.c_int64]
+    L.orc_imager.restype = None
+    out = np.array(chan, np.float32, copy=True, order="C")
+    im = np.ascontiguousarray(ci_oi, np.float32)
+    n = out.reshape(-1, 9).shape[0]
+    assert im.size == n * 6
+    fs = frame_struct(frame)
+    L.orc_imager(C.byref(fs), _p(out, _f32p), _p(im, _f32p), n)
+    return out
+
+
+def quantize(frame, chan, dither=None, qchannels=(0, 1, 2, 6)) -> np.ndarray:
+    """FormatBucketForDisplay's quantize (orc_quantize) of channels `qchannels`."""
+    L = lib()
+    L.orc_quantize.argtypes = [C.POINTER(OrcFrame), _f32p, C.c_int64, _f32p, _i32p, C.c_int, _f64p]
+    L.orc_quantize.restype = None
+    ch = np.ascontiguousarray(chan, np.float32)
+    n = ch.reshape(-1, 9).shape[0]
+    qc = np.array(qchannels, np.int32)
+    d = None if dither is None else np.ascontiguousarray(dither, np.float32)
+    out = np.zeros(ch.shape[:-1] + (len(qc),), np.float64)
+    fs = frame_struct(frame)
+    L.orc_quantize(C.byref(fs), _p(ch, _f32p), n, _p(d, _f32p), _p(qc, _i32p), len(qc), _p(out, _f64p))
+    return out
+
+
 def render(scene, qchannels=(0, 1, 2, 6), want_samples: bool = True, want_fp64: bool = False,
            grids=None) -> dict:
     """Run the oracle on a Scene (aqsis_gb300.scene).  Returns numpy arrays.
@@ -206,12 +247,7 @@ def render(scene, qchannels=(0, 1, 2, 6), want_samples: bool = True, want_fp64: 
     cx0, cx1, cy0, cy1 = fr.crop_window
     x0, y0, w, h = fr.sample_region
     spp = fr.spp
-    mult, inv = fr.dof_terms()
-    of = OrcFrame(fr.width, fr.height, cx0, cx1, cy0, cy1, fr.xsamples, fr.ysamples,
-                  fr.xfilter, fr.yfilter, fr.gain, fr.gamma, 0.0, fr.q_one, fr.q_min, fr.q_max,
-                  fr.q_dither, fr.shutter[0], fr.shutter[1], 1 if fr.use_dof else 0, mult, inv,
-                  fr.dof_scale[0], fr.dof_scale[1], fr.depth_filter,
-                  (C.c_float * 3)(*fr.zthreshold), fr.display_z)
+    of = frame_struct(fr)
     keep = []
 
     def arr(a, dt):
