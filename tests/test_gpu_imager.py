@@ -59,7 +59,7 @@ def test_imager_write_back(aqh_lib, oracle, batched, transparent):
     raw = dataclasses.replace(sc.frame, gain=1.0, gamma=1.0)
     ref_pre = oracle.render(type(sc)(raw, sc.grids, sc.samples), want_samples=False)["channels"]
     assert close_or_same(pre, ref_pre).all()
-    assert np.array_equal(pre.view(np.uint32), ref_pre.view(np.uint32)) or not transparent
+    assert transparent or np.array_equal(pre.view(np.uint32), ref_pre.view(np.uint32))
     ref_post = oracle.imager(sc.frame, ref_pre, _shader(ref_pre))
     ok = close_or_same(post, ref_post)
     assert ok.all(), "channels differ at %d entries" % int((~ok).sum())
