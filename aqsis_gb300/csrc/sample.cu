@@ -959,6 +959,7 @@ resolve_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, SampleStore st
 // fragment pool in any order: each block iteration reserves its hits' slots
 // with one atomic and links them into per-sample lists in shared memory.
 constexpr int kSlotsF = 256;
+constexpr int kFragRun = 256;  // pool slots a warp reserves at a time
 
 struct SmemF {
 	RecS rec[kSlotsF];
@@ -972,7 +973,6 @@ struct SmemF {
 	int warp_tot[32];
 	int first_reject;
 	int qn;
-	unsigned long long gbase;
 	float pixmax[kTilePixMax];  // stay FLT_MAX: no occluding hits
 	float blkmax[16];
 	int32_t fhead[kTileSampMax];
@@ -988,6 +988,7 @@ sample_frag_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sa
 	__shared__ int next_tile;
 	const int ntiles = fp.ntx * fp.nty;
 	const int cullable = fp.cullable;
+	unsigned long long rnext = 0, rend = 0;  // this warp's reserved pool slots [rnext, rend)
 	for (int job = 0;; ++job) {
 	int tile;
 	if (PERSIST) {
@@ -1064,77 +1065,92 @@ sample_frag_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sa
 		if (t < npend) sm.pref[t] = pre;
 		__syncthreads();
 
-		// block-uniform sweep: each iteration tests kThreadsS pairs and appends
-		// its hits to the pool with one reservation
-		for (int base = 0; base < total; base += kThreadsS) {
-			const int p = base + t;
-			bool hit = false;
-			int s = 0, id = 0;
-			float D = 0.0f, u = 0.0f, v = 0.0f;
-			if (p < total) {
-				int lo = 0, hi = npend - 1;
-				while (lo < hi) {
-					const int mid = (lo + hi + 1) >> 1;
-					if (sm.pref[mid] <= p) lo = mid; else hi = mid - 1;
+		// each warp walks a contiguous run of tests (a lane finds its candidate
+		// a step or two on from where the warp's last lane stopped) and appends
+		// its hits into pool slots it reserved in runs of kFragRun: one global
+		// atomic per run, no block barrier per batch of tests.  Lists are
+		// sorted by (depth, id) in Combine, so their order does not matter;
+		// slots left in a warp's last run stay unused.
+		{
+			const int lane = t & 31;
+			const int chunk = ((total + kThreadsS - 1) / kThreadsS) * 32;
+			const int pw0 = (t >> 5) * chunk, pw1 = min(total, pw0 + chunk);
+			int cur = 0;
+			for (int p0 = pw0; p0 < pw1; p0 += 32) {
+				const int p = p0 + lane;
+				const int lo = advance_item(sm.pref, npend, cur, min(p, pw1 - 1));
+				cur = __shfl_sync(0xffffffffu, lo, 31);
+				bool hit = false;
+				int s = 0, id = 0;
+				float D = 0.0f, u = 0.0f, v = 0.0f;
+				if (p < pw1) {
+					const RecS& r = sm.rec[lo];
+					const int k = p - sm.pref[lo];
+					const int cx0 = sm.rng[lo][0], cy0 = sm.rng[lo][1], totx = sm.rng[lo][2];
+					const uint32_t mtot = (uint32_t)sm.rng[lo][3];
+					const int sX = max(r.px0, tpx0), sY = max(r.py0, tpy0);
+					const int ky = div_small(k, totx, mtot), kx = k - ky * totx;
+					int px, m, py, n;
+					if (kx < cx0) {
+						px = sX;
+						m = ((sX == r.px0) ? r.im : 0) + kx;
+					} else {
+						const int q = kx - cx0;
+						const int qd = div_small(q, xs, mxs);
+						px = sX + 1 + qd;
+						m = q - qd * xs;
+					}
+					if (ky < cy0) {
+						py = sY;
+						n = ((sY == r.py0) ? r.in_ : 0) + ky;
+					} else {
+						const int q = ky - cy0;
+						const int qd = div_small(q, ys, mys);
+						py = sY + 1 + qd;
+						n = q - qd * ys;
+					}
+					const int si = n * xs + m;
+					const int pl = (py - tpy0) * fp.tile_w + (px - tpx0);
+					s = pl * spp + si;
+					const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + si);
+					const float x = (float)px + o.x, y = (float)py + o.y;
+					// Contains2D, early-z against occlZ = FLT_MAX, fContains, StoreSample's test
+					hit = !((x < r.bminx || x > r.bmaxx) || (y < r.bminy || y > r.bmaxy)) &&
+					      !(cullable && !(r.bits & kRecCsg) && r.bminz > FLT_MAX) &&
+					      !((r.bits & kRecLod) && lod_rejects(fp, g, smp, r.bits >> kRecGridShift, px, py, si)) &&
+					      edges_inside(r.ym, r.xm, r.ex, r.ey, x, y);
+					if (hit) {
+						inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y, (r.bits & kRecLinear) != 0,
+						             x, y, u, v);
+						D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
+						hit = rec_keeps(g, bb, r.bits, r.id, x, y, u, v) &&
+						      !(cullable && !(r.bits & kRecCsg) && FLT_MAX <= D);
+						id = r.id;
+					}
 				}
-				const RecS& r = sm.rec[lo];
-				const int k = p - sm.pref[lo];
-				const int cx0 = sm.rng[lo][0], cy0 = sm.rng[lo][1], totx = sm.rng[lo][2];
-				const uint32_t mtot = (uint32_t)sm.rng[lo][3];
-				const int sX = max(r.px0, tpx0), sY = max(r.py0, tpy0);
-				const int ky = div_small(k, totx, mtot), kx = k - ky * totx;
-				int px, m, py, n;
-				if (kx < cx0) {
-					px = sX;
-					m = ((sX == r.px0) ? r.im : 0) + kx;
-				} else {
-					const int q = kx - cx0;
-					const int qd = div_small(q, xs, mxs);
-					px = sX + 1 + qd;
-					m = q - qd * xs;
-				}
-				if (ky < cy0) {
-					py = sY;
-					n = ((sY == r.py0) ? r.in_ : 0) + ky;
-				} else {
-					const int q = ky - cy0;
-					const int qd = div_small(q, ys, mys);
-					py = sY + 1 + qd;
-					n = q - qd * ys;
-				}
-				const int si = n * xs + m;
-				const int pl = (py - tpy0) * fp.tile_w + (px - tpx0);
-				s = pl * spp + si;
-				const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + si);
-				const float x = (float)px + o.x, y = (float)py + o.y;
-				// Contains2D, early-z against occlZ = FLT_MAX, fContains, StoreSample's test
-				hit = !((x < r.bminx || x > r.bmaxx) || (y < r.bminy || y > r.bmaxy)) &&
-				      !(cullable && !(r.bits & kRecCsg) && r.bminz > FLT_MAX) &&
-				      !((r.bits & kRecLod) && lod_rejects(fp, g, smp, r.bits >> kRecGridShift, px, py, si)) &&
-				      edges_inside(r.ym, r.xm, r.ex, r.ey, x, y);
-				if (hit) {
-					inv_bilinear(r.ax, r.ay, r.e_x, r.e_y, r.f_x, r.f_y, r.g_x, r.g_y, (r.bits & kRecLinear) != 0, x,
-					             y, u, v);
-					D = bilerp1(r.z[0], r.z[1], r.z[2], r.z[3], u, v);
-					hit = rec_keeps(g, bb, r.bits, r.id, x, y, u, v) && !(cullable && !(r.bits & kRecCsg) && FLT_MAX <= D);
-					id = r.id;
+				const unsigned bal = __ballot_sync(0xffffffffu, hit);
+				const int nh = __popc(bal);
+				if (nh > 0) {
+					if (rnext + nh > rend) {
+						unsigned long long b = 0;
+						if (lane == 0) b = atomicAdd(pool.count, (unsigned long long)kFragRun);
+						rnext = __shfl_sync(0xffffffffu, b, 0);
+						rend = rnext + kFragRun;
+					}
+					if (hit) {
+						const long long idx = (long long)(rnext + __popc(bal & ((1u << lane) - 1u)));
+						if (idx < pool.capacity) {
+							pool.frag[idx] = make_float4(D, __int_as_float(id), u, v);
+							pool.next[idx] = atomicExch(&sm.fhead[s], (int)idx);
+						} else {
+							atomicOr(pool.overflow, 1);
+						}
+					}
+					rnext += nh;
 				}
 			}
-			int nhits;
-			const int rank = block_excl_scan(sm.warp_tot, hit, nhits);
-			if (t == 0 && nhits) sm.gbase = atomicAdd(pool.count, (unsigned long long)nhits);
-			__syncthreads();
-			if (hit) {
-				const long long idx = (long long)sm.gbase + rank;
-				if (idx < pool.capacity) {
-					pool.frag[idx] = make_float4(D, __int_as_float(id), u, v);
-					pool.next[idx] = atomicExch(&sm.fhead[s], (int)idx);
-				} else {
-					atomicOr(pool.overflow, 1);
-				}
-			}
-			__syncthreads();
 		}
+		__syncthreads();
 		npend = 0;
 		if (exhausted) break;
 	}

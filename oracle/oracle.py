@@ -407,14 +407,19 @@ def _grid_subset(g, idx):
 def fp64_error(dev, ref64, finite_only: bool = True) -> dict:
     """Largest absolute and relative difference of float results `dev` from
     the float64 twin `ref64` (relative over entries with |ref64| >= 1e-6).
-    Entries where the twin is not finite, or at FLT_MAX (an empty pixel's
-    depth), are left out."""
+    Entries where the twin is not finite or at FLT_MAX (an empty pixel's
+    depth) are left out, and so are entries where the float result is not
+    finite while the twin is (the float sum overflowed, as in the reference's
+    own float path, near FLT_MAX depths under negative filter lobes); those
+    are counted as `float_overflow`."""
     a = np.asarray(dev, np.float64)
     b = np.asarray(ref64, np.float64)
-    m = np.isfinite(b) & (np.abs(b) < 3.0e38) if finite_only else np.ones(b.shape, bool)
+    tw = np.isfinite(b) & (np.abs(b) < 3.0e38) if finite_only else np.ones(b.shape, bool)
+    ovf = tw & ~np.isfinite(a)
+    m = tw & np.isfinite(a)
     if not m.any():
-        return {"max_abs": 0.0, "max_rel": 0.0, "entries": 0}
+        return {"max_abs": 0.0, "max_rel": 0.0, "entries": 0, "float_overflow": int(ovf.sum())}
     d = np.abs(a[m] - b[m])
     big = np.abs(b[m]) >= 1e-6
     rel = float((d[big] / np.abs(b[m][big])).max()) if big.any() else 0.0
-    return {"max_abs": float(d.max()), "max_rel": rel, "entries": int(m.sum())}
+    return {"max_abs": float(d.max()), "max_rel": rel, "entries": int(m.sum()), "float_overflow": int(ovf.sum())}
