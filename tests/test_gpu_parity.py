@@ -211,3 +211,20 @@ def test_static_grid_behind_eye_in_motion_frame(hider, oracle, transparent):
     res, ref = run_both(hider, oracle, sc)
     compare(res, ref)
     assert (ref["winner"] >= 0).sum() + (ref["nfrag"] > 0).sum() > 0
+
+
+@pytest.mark.parametrize("xs,ys", [(5, 5), (6, 6), (8, 8)])
+@pytest.mark.parametrize("filt", [("gaussian", 2.0, 2.0), ("catmull-rom", 3.0, 3.0)], ids=["gaussian", "catmull-rom"])
+def test_rolling_filter_windows(hider, oracle, xs, ys, filt):
+    """3x3 windows above 16 samples per pixel take the rolling-window filter:
+    crop windows whose height is not a multiple of its 8-row runs, exposure
+    gain (bit-exact); with a gamma the device's pow may differ from the
+    reference's float pow by an ulp, so that case is held to the tolerance."""
+    sc = SS.edge_cases(seed=81 + xs, xs=xs, ys=ys, filt=filt)
+    sc.frame.crop = (3, sc.frame.width - 4, 2, sc.frame.height - 5)
+    sc.frame.gain = 1.3
+    res, ref = run_both(hider, oracle, sc)
+    compare(res, ref, exact_pixels=True)
+    sc.frame.gamma = 1.8
+    res, ref = run_both(hider, oracle, sc)
+    compare(res, ref)
