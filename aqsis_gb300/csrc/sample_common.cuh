@@ -335,34 +335,53 @@ __device__ __forceinline__ int combine_fragments_t(const FrameParams& fp, const 
 	int n = 0;
 	bool nan = occl[6] != occl[6];
 	bool any_csg = false;
-	for (int f = head; f >= 0; f = pool.next[f]) {
-		++n;
-		const float4 fr = pool.frag[f];
+	// One walk over the list (newest first) counts it, checks for NaN depths
+	// and, while the entries fit, insertion-sorts them by ascending key.  An
+	// entry's sequence number is minus its list position (the occluding hit
+	// 1), so of entries with equal depth and id the newer sorts later, as in
+	// insertion order.  The walk loads the next fragment before sorting in
+	// the current one, so the sort's local-memory traffic overlaps the chase
+	// of the links.
+	FragKey ent[kCombineLocal];
+	int m = 0;
+	auto insert = [&](float d, int id, int sq, int idx) {
+		int k = m++;
+		while (k > 0 && key_less(d, id, sq, ent[k - 1])) {
+			ent[k] = ent[k - 1];
+			--k;
+		}
+		ent[k] = FragKey{d, id, sq, idx};
+	};
+	const int room = kCombineLocal - (has_occl ? 1 : 0);
+	float4 fr = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+	int nx = -1;
+	if (head >= 0) {
+		fr = pool.frag[head];
+		nx = pool.next[head];
+	}
+	for (int f = head; f >= 0;) {
+		float4 frn = fr;
+		int nxn = -1;
+		if (nx >= 0) {
+			frn = pool.frag[nx];
+			nxn = pool.next[nx];
+		}
 		nan |= fr.x != fr.x;
 		if (CSG) any_csg = any_csg || csg_grid(g, grid_of(g, __float_as_int(fr.y)));
+		if (n < room) insert(fr.x, __float_as_int(fr.y), -n, f);
+		++n;
+		f = nx;
+		fr = frn;
+		nx = nxn;
 	}
 	int ntot = n + (has_occl ? 1 : 0);
 	emptied = false;
-	// short lists: the entries sorted once (insertion sort, ascending key);
-	// long ones (or NaN depths) are walked in order by selection
+	// short lists are now sorted; long ones (or NaN depths) are walked in
+	// order by selection
 	const bool local = ntot <= kCombineLocal && !nan;
 	if (CSG && any_csg && !local && g.csg.overflow) atomicOr(g.csg.overflow, 1);  // CSG needs the sorted list held
-	FragKey ent[kCombineLocal];
 	if (local) {
-		int m = 0, seq = n - 1;
-		auto insert = [&](float d, int id, int sq, int idx) {
-			int k = m++;
-			while (k > 0 && key_less(d, id, sq, ent[k - 1])) {
-				ent[k] = ent[k - 1];
-				--k;
-			}
-			ent[k] = FragKey{d, id, sq, idx};
-		};
-		for (int f = head; f >= 0; f = pool.next[f], --seq) {
-			const float4 fr = pool.frag[f];
-			insert(fr.x, __float_as_int(fr.y), seq, f);
-		}
-		if (has_occl) insert(occl[6], 0x7fffffff, n, -1);
+		if (has_occl) insert(occl[6], 0x7fffffff, 1, -1);
 		if (CSG && any_csg) {
 			// CSG resolve of the sorted list (imagepixel.cpp:170-190); a list it
 			// empties leaves the sample as it was (imagepixel.cpp:249)
