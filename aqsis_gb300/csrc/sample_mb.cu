@@ -312,6 +312,84 @@ __device__ __forceinline__ void mb_sample_attrs(const FrameParams& fp, const Sam
 // Final value of one sample: the occluding hit's colour at its (u,v) --
 // the winner's hit test repeated at the sample's time and lens offset -- or
 // the Combine of its fragments; written to the sample store.
+// (u,v) of a hit that mb_sample reported for micropolygon m of grid gi at
+// sample (x, y, time, lens offset dx, dy): the same vertices (the keys around
+// the time, interpolated, shifted by the CoC under depth of field), vertex
+// order and inverse bilinear, built in registers from the grid's arrays
+// rather than from a record.  The bound tests mb_sample makes first passed
+// for this sample and change nothing here.
+__device__ __forceinline__ void mb_hit_uv(const FrameParams& fp, const GridsDev& g, int gi, int m, float x, float y,
+                                          float time, float dx, float dy, float& u, float& v) {
+	const int cu = __ldg(g.cu + gi), cv = __ldg(g.cv + gi);
+	const int nk = __ldg(g.nkeys + gi);
+	const long long nv = (long long)(cu + 1) * (cv + 1);
+	const long long pb = __ldg(g.pbase + gi);
+	const int iv = m / cu, iu = m - iv * cu;
+	const int index = iv * (cu + 1) + iu;
+	const int vi[4] = {index, index + 1, index + cu + 1, index + cu + 2};
+	V3f k0[4];
+#pragma unroll
+	for (int q = 0; q < 4; ++q) k0[q] = ld3(g.P, pb + vi[q]);
+	V3f pts[4];
+	if (nk == 1) {
+		// CacheHitTestValues: each vertex moves by its own CoC times the lens offset
+#pragma unroll
+		for (int q = 0; q < 4; ++q) {
+			float cx = 0.0f, cy = 0.0f;
+			if (fp.use_dof) {
+				const float2 c = coc(k0[q].z, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+				cx = c.x;
+				cy = c.y;
+			}
+			const float ox = cx * dx, oy = cy * dy;
+			pts[q] = V3f{k0[q].x - ox, k0[q].y - oy, k0[q].z - 0.0f};
+		}
+	} else {
+		// the key span of CqMicroPolygonMotion::Sample (micropolygon.cpp:1786-1806)
+		const float* kt = g.times + __ldg(g.tbase + gi);
+		int iIndex = 0;
+		float Fraction = 0.0f;
+		bool Exact = true;
+		if (time > __ldg(kt)) {
+			if (time >= __ldg(kt + nk - 1)) {
+				iIndex = nk - 1;
+			} else {
+				while (time >= __ldg(kt + iIndex + 1)) iIndex += 1;
+				const float t0 = __ldg(kt + iIndex), t1 = __ldg(kt + iIndex + 1);
+				Fraction = (time - t0) / (t1 - t0);
+				Exact = (t0 == time);
+			}
+		}
+		V3f a[4];
+#pragma unroll
+		for (int q = 0; q < 4; ++q) a[q] = ld3(g.P, pb + iIndex * nv + vi[q]);
+		if (Exact) {
+#pragma unroll
+			for (int q = 0; q < 4; ++q) pts[q] = a[q];
+		} else {
+			const float F1 = 1.0f - Fraction;
+#pragma unroll
+			for (int q = 0; q < 4; ++q) {
+				const V3f b = ld3(g.P, pb + (iIndex + 1) * nv + vi[q]);
+				pts[q] = V3f{(F1 * a[q].x) + (Fraction * b.x), (F1 * a[q].y) + (Fraction * b.y),
+				             (F1 * a[q].z) + (Fraction * b.z)};
+			}
+		}
+		if (fp.use_dof) {
+#pragma unroll
+			for (int q = 0; q < 4; ++q) {
+				const float2 c = coc(pts[q].z, fp.dof_mult, fp.dof_inv_fd, fp.dof_scale_x, fp.dof_scale_y);
+				pts[q].x = pts[q].x - c.x * dx;
+				pts[q].y = pts[q].y - c.y * dy;
+				pts[q].z = pts[q].z - 0.0f;
+			}
+		}
+	}
+	HitCoeffs h;
+	hit_setup(pts, vertex_order(k0), h);
+	inv_bilinear(h.ax, h.ay, h.e_x, h.e_y, h.f_x, h.f_y, h.g_x, h.g_y, h.linear, x, y, u, v);
+}
+
 template <bool TRANSP>
 __device__ __forceinline__ void mb_resolve(const FrameParams& fp, const GridsDev& g, const FragPool& pool,
                                            const SampleStore& st, long long sidx, long long aidx, float x, float y,
@@ -321,10 +399,8 @@ __device__ __forceinline__ void mb_resolve(const FrameParams& fp, const GridsDev
 	if (w >= 0) {
 		const int gi = grid_of(g, w);
 		const int m = w - (int)__ldg(g.mpbase + gi);
-		MbRec rr;
-		load_mb_record(fp, g, gi, m, rr);
-		float D, u, v;
-		mb_sample(fp, rr, rr.nkeys > 1, fp.use_dof != 0, x, y, stime, sdx, sdy, D, u, v);
+		float u, v;
+		mb_hit_uv(fp, g, gi, m, x, y, stime, sdx, sdy, u, v);
 		hit_colour(g, gi, m, u, v, occl, occl_flags);
 		occl[6] = (TRANSP && fp.midpoint_store) ? st.hitz[sidx] : ozv;
 	}
