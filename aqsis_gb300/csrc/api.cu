@@ -380,7 +380,7 @@ struct aqh_ctx {
 	DevBuf d_mpcount;
 	DevBuf d_rect, d_minz, d_strips, d_tri, d_stcount, d_stoffset, d_stlist, d_idgrid, d_mpb;
 	DevBuf d_sa, d_sb, d_win, d_oz, d_nf, d_hz, d_keys, d_wmask;
-	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err, d_occl;
+	DevBuf d_frag, d_next, d_fcount, d_foverflow, d_err, d_occl, d_fheads;
 	DevBuf d_ftab, d_chan, d_q8, d_qchan, d_dofb, d_disp, d_dither_req;
 	DevBuf d_q8_req;          // quantized reads with other channel lists
 	DevBuf d_P3, d_C3, d_O3;  // three-float host entries before widening
@@ -1107,6 +1107,13 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 		AQH_TRY(ctx->d_occl.ensure(16), "alloc");
 		pool.occluders = ctx->d_occl.as<int32_t>();
 		fp.frag_only = (!P.mbdof && !fp.midpoint_store) ? 1 : 0;
+		if (fp.frag_only) {
+			// the fragment-only sampler hands its list heads to a separate
+			// Combine kernel, whose sort gets the L1 the sampler's shared memory
+			// leaves too small
+			AQH_TRY(ctx->d_fheads.ensure(P.nsamp * sizeof(int32_t)), "alloc list heads");
+			pool.heads = ctx->d_fheads.as<int32_t>();
+		}
 	}
 	if (pool.capacity == 0 && !P.mbdof && ctx->host_packed) {
 		// colours still on their way from the host: the sampler hands its

@@ -165,6 +165,8 @@ struct FragPool {
 	int64_t capacity;
 	int32_t* overflow;
 	int32_t* occluders;  // nonzero when some micropolygon may be occluding (opaque or matte alpha)
+	int32_t* heads;      // fragment-only frames: each sample's list head, pixel-major ([pixel][sample
+	                     // index]), handed to resolve_frag_kernel; null: the sampler resolves in place
 };
 
 struct BinBuffers {

@@ -1155,19 +1155,45 @@ sample_frag_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sa
 		if (exhausted) break;
 	}
 
-	// ---- resolve: Combine of each sample's fragments ----
+	// ---- resolve: Combine of each sample's fragments (or the list heads
+	// handed to resolve_frag_kernel) ----
 	for (int s = t; s < tsamp; s += kThreadsS) {
 		const int pl = s / spp;
 		const int si = s - pl * spp;
 		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 		if (px >= tpx1 || py >= tpy1) continue;
 		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
+		if (pool.heads) {
+			pool.heads[pix * spp + si] = sm.fhead[s];
+			continue;
+		}
 		const float2 o = __ldg(smp.pos + (long long)sm.patidx[pl] * spp + si);
 		resolve_sample<true>(fp, g, pool, st, pix * spp + si, store_index(pix, si, spp), (float)px + o.x,
 		                     (float)py + o.y, FLT_MAX, -1, sm.fhead[s]);
 		if (st.wmask) st.wmask[store_index(pix, si, spp)] = window_mask(fp, px, py, (float)px + o.x, (float)py + o.y);
 	}
 	}  // tile loop
+}
+
+// Combine of a fragment-only frame's samples from the list heads
+// sample_frag_kernel left: one thread per sample, pixel-major, so a warp
+// walks lists whose fragments the sampler's warps allocated together.  The
+// kernel holds no shared memory, so the sort's local memory stays in L1.
+// Returns at once when the frame has occluders (the ordered kernel resolved).
+__global__ void __launch_bounds__(256)
+resolve_frag_kernel(FrameParams fp, GridsDev g, SamplerDev smp, SampleStore st, FragPool pool) {
+	if (fp.cullable && *pool.occluders) return;
+	const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // pixel * spp + sample index
+	const long long npix = (long long)fp.sw * fp.sh;
+	if (q >= npix * fp.spp) return;
+	const long long pix = q / fp.spp;
+	const int si = (int)(q - pix * fp.spp);
+	const int px = fp.sx0 + (int)(pix % fp.sw), py = fp.sy0 + (int)(pix / fp.sw);
+	const long long pat = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
+	const float2 o = __ldg(smp.pos + pat * fp.spp + si);
+	resolve_sample<true>(fp, g, pool, st, q, store_index(pix, si, fp.spp), (float)px + o.x, (float)py + o.y, FLT_MAX, -1,
+	                     pool.heads[q]);
+	if (st.wmask) st.wmask[store_index(pix, si, fp.spp)] = window_mask(fp, px, py, (float)px + o.x, (float)py + o.y);
 }
 
 // Whether any micropolygon of the frame may be occluding: a grid flagged
@@ -1234,6 +1260,10 @@ void launch_sample_tiles_q(const FrameParams& fp, const GridsDev& g, const Sampl
 		else
 			sample_frag_kernel<false><<<ntiles, kThreadsS, sizeof(SmemF), s>>>(fp, g, sm, b, st, pool, nullptr,
 			                                                                  nullptr);
+		if (pool.heads) {
+			const long long n = (long long)fp.sw * fp.sh * fp.spp;
+			if (n > 0) resolve_frag_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fp, g, sm, st, pool);
+		}
 	}
 	if (queue) {
 		if (transp)
