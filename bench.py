@@ -152,8 +152,10 @@ KERNELS = {"opaque": "sample_opaque_kernel", "transparent": "sample_frag_kernel"
 # kernels one batched frame launches: id table, grid rects, super-tile count,
 # scan, super-tile write (binning); the sampler(s); the filter, which also
 # quantizes the frame's 8-bit display.  The transparent frame launches the
-# occluder scan and both static samplers, of which one returns at once.
-LAUNCHES = {"opaque": 7, "transparent": 9, "mbdof": 7, "spheres": 8}  # spheres: + the projection
+# occluder scan, both static samplers (one returns at once) and the Combine
+# kernel of fragment-only frames (which returns at once when the ordered
+# sampler ran); the motion frame the staging-bounds kernel before its sampler.
+LAUNCHES = {"opaque": 7, "transparent": 10, "mbdof": 8, "spheres": 8}  # spheres: + the projection
 L2_BYTES = 129 << 20
 # measured DRAM bytes per micropolygon of the sampler launch (ncu, 0.35 scale)
 TRAFFIC_PER_MP = {"opaque": (98.411520e6 + 142.133760e6) / 6_272_000}
