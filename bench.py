@@ -147,7 +147,7 @@ WORKLOADS = {
 }
 
 
-KERNELS = {"opaque": "sample_opaque_kernel", "transparent": "sample_frag_kernel", "mbdof": "sample_mbq_kernel",
+KERNELS = {"opaque": "sample_opaque_kernel", "transparent": "sample_frag_kernel + resolve_frag_kernel", "mbdof": "sample_mbq_kernel",
            "spheres": "sample_opaque_kernel"}
 # kernels one batched frame launches: id table, grid rects, super-tile count,
 # scan, super-tile write (binning); the sampler(s); the filter, which also
