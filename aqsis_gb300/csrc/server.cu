@@ -87,6 +87,7 @@ extern "C" size_t aqh_job_footprint(const aqh_job* j) {
 	bool transparent = false;
 	for (int i = 0; i < j->ngrids && !transparent; ++i) transparent = !(j->flags[i] & AQH_GRID_OPAQUE);
 	if (transparent) b += std::max<size_t>(1u << 20, nsamp * 2) * 20;                    // fragment pool
+	if (transparent && !moving) b += nsamp * 4;                                          // list heads (Combine kernel)
 	b += ndisp * (36 + 4);                                                                // channels + rgba
 	const size_t np = (size_t)j->samples.npatterns * fp.spp;
 	b += np * 28 + npix * 4 * 5;                                                          // patterns + choices
