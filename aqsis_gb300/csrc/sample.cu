@@ -297,16 +297,24 @@ __device__ __forceinline__ bool stage_candidates(const FrameParams& fp, const Gr
 			lp += kThreadsS;
 			continue;
 		}
-		// one micropolygon of the stream per thread: is it a candidate of this tile?
+		// one micropolygon of the stream per thread: is it a candidate of this
+		// tile?  Its grid: lane 0 searches for the warp's first position, the
+		// other lanes step on from there.
 		const int p = r0 + t;
-		bool active = false;
-		int gid = 0, m = 0;
-		if (p < qtotal) {
+		int lo0 = 0;
+		if ((t & 31) == 0 && p < qtotal) {
 			int lo = 0, hi = sm.qn - 1;
 			while (lo < hi) {
 				const int mid = (lo + hi + 1) >> 1;
 				if (sm.qcum[mid] <= p) lo = mid; else hi = mid - 1;
 			}
+			lo0 = lo;
+		}
+		lo0 = __shfl_sync(0xffffffffu, lo0, 0);
+		bool active = false;
+		int gid = 0, m = 0;
+		if (p < qtotal) {
+			const int lo = advance_item(sm.qcum, sm.qn, lo0, p);
 			gid = sm.qgrid[lo];
 			m = p - sm.qcum[lo];
 			const int cu = __ldg(g.cu + gid);
@@ -870,29 +878,35 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		__syncthreads();
 
 		// ---- end of round: state and largest occluding depth of the pixels
-		// whose samples changed, flags ----
-		for (int pp = t; pp < tpix; pp += kThreadsS) {
-			if (!(sm.dirty[pp >> 5] & (1u << (pp & 31)))) continue;
+		// whose samples changed (two threads per pixel, even and odd samples;
+		// the maximum does not depend on the order, NaN counting as +inf),
+		// flags ----
+		for (int u0 = 0; u0 < 2 * tpix; u0 += kThreadsS) {
+			const int u = u0 + t, pp = u >> 1, half = u & 1;
+			const bool act = pp < tpix && (sm.dirty[pp >> 5] & (1u << (pp & 31)));
 			float mx = -FLT_MAX;
-			for (int k = 0; k < spp; ++k) {
-				const unsigned long long kk = sm.key[pp * spp + k];
-				sm.prev[pp * spp + k] = kk;
-				mx = max_depth(mx, key_depth(kk));
-			}
-			sm.pixmax[pp] = mx;
+			if (act)
+				for (int k = half; k < spp; k += 2) {
+					const unsigned long long kk = sm.key[pp * spp + k];
+					sm.prev[pp * spp + k] = kk;
+					mx = max_depth(mx, key_depth(kk));
+				}
+			mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+			if (act && half == 0) sm.pixmax[pp] = mx;
 		}
 		for (int i = t; i < nflagw; i += kThreadsS) sm.flag[i] = sm.sticky[i];
 		__syncthreads();
 		if (t < kTilePixMax / 32) sm.dirty[t] = 0u;
-		if (t < 16) {
+		if (t < 16 * 16) {
+			// 4x4-pixel block t / 16, one pixel per thread
+			const int b = t >> 4, j = t & 15;
 			const int nbx = (fp.tile_w + 3) >> 2;
-			const int bx = t % nbx, by = t / nbx;
-			float mx = -FLT_MAX;
-			if (by * 4 < fp.tile_h)
-				for (int yy = by * 4; yy < min(by * 4 + 4, fp.tile_h); ++yy)
-					for (int xx = bx * 4; xx < min(bx * 4 + 4, fp.tile_w); ++xx)
-						mx = max_depth(mx, sm.pixmax[yy * fp.tile_w + xx]);
-			sm.blkmax[t] = mx;
+			const int bx = b % nbx, by = b / nbx;
+			const int yy = by * 4 + (j >> 2), xx = bx * 4 + (j & 3);
+			float mx = (yy < fp.tile_h && xx < fp.tile_w) ? sm.pixmax[yy * fp.tile_w + xx] : -FLT_MAX;
+#pragma unroll
+			for (int o = 1; o < 16; o <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+			if (j == 0) sm.blkmax[b] = mx;
 		}
 		__syncthreads();
 		npend = 0;
