@@ -151,8 +151,8 @@ struct SampleStore {
 	                  // when the sample is inside the filter window of the display pixel at
 	                  // offset (-fx, -fy); null: the filter tests sample positions itself
 	unsigned long long* keys;  // opaque frames: (ordered depth, id + 1) of each sample's occluding
-	                           // hit, sample-major, resolved by a separate kernel; null: the
-	                           // sampler resolves in place
+	                           // hit, pixel-major ([pixel][sample index]), resolved by a separate
+	                           // kernel; null: the sampler resolves in place
 	int32_t* aovsrc;  // micropolygon whose output variables the sample carries after Combine
 	                  // (store layout; -1 none), or null without output variables
 };

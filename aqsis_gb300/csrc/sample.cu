@@ -913,21 +913,25 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 		if (exhausted) break;
 	}
 
-	// ---- resolve: colours of the occluding hits (sample-major within the tile) ----
+	// ---- resolve: colours of the occluding hits ----
 	if (st.keys) {
-		// hand the occluding hits to resolve_opaque_kernel
+		// hand the occluding hits to resolve_opaque_kernel, pixel-major
+		// ([pixel][sample index]) like its threads
 		for (int q = t; q < tsamp; q += kThreadsS) {
-			const int si = q / tpix;
-			const int pl = q - si * tpix;
+			const int pl = q / spp;
+			const int si = q - pl * spp;
 			const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 			if (px >= tpx1 || py >= tpy1) continue;
-			st.keys[store_index((long long)(py - fp.sy0) * fp.sw + (px - fp.sx0), si, spp)] = sm.key[pl * spp + si];
+			st.keys[((long long)(py - fp.sy0) * fp.sw + (px - fp.sx0)) * spp + si] = sm.key[pl * spp + si];
 		}
 		continue;
 	}
+	// pixel-major: the lanes of a pixel's samples mostly resolve the same
+	// winner, whose grid, vertex and colour loads then merge (measured faster
+	// than sample-major order, whose store writes coalesce instead)
 	for (int q = t; q < tsamp; q += kThreadsS) {
-		const int si = q / tpix;
-		const int pl = q - si * tpix;
+		const int pl = q / spp;
+		const int si = q - pl * spp;
 		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 		if (px >= tpx1 || py >= tpy1) continue;
 		const long long pix = (long long)(py - fp.sy0) * fp.sw + (px - fp.sx0);
@@ -941,19 +945,20 @@ sample_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, 
 }
 
 // Colours of the occluding hits of an opaque frame: one thread per sample,
-// sample-major (consecutive threads, consecutive pixels of one sample index).
+// pixel-major (consecutive threads, the samples of one pixel, which mostly
+// share a winner whose loads then merge).
 __global__ void __launch_bounds__(256)
 resolve_opaque_kernel(FrameParams fp, GridsDev g, SamplerDev smp, SampleStore st) {
 	const long long npix = (long long)fp.sw * fp.sh;
-	const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // store index
-	if (q >= (long long)store_size(npix, fp.spp)) return;
-	const int si = (int)((q >> 5) % fp.spp);
-	const long long pix = ((q >> 5) / fp.spp) * 32 + (q & 31);
-	if (pix >= npix) return;
+	const long long q0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // pixel * spp + sample index
+	if (q0 >= npix * fp.spp) return;
+	const long long pix = q0 / fp.spp;
+	const int si = (int)(q0 - pix * fp.spp);
+	const long long q = store_index(pix, si, fp.spp);
 	const int px = fp.sx0 + (int)(pix % fp.sw), py = fp.sy0 + (int)(pix / fp.sw);
 	const long long pat = smp.pos_index ? (long long)__ldg(smp.pos_index + pix) : pix;
 	const float2 o = __ldg(smp.pos + pat * fp.spp + si);
-	const unsigned long long kk = st.keys[q];
+	const unsigned long long kk = st.keys[q0];
 	resolve_sample<false>(fp, g, FragPool{}, st, pix * fp.spp + si, q, (float)px + o.x, (float)py + o.y,
 	                      key_depth(kk), key_winner(kk), -1);
 	if (st.wmask) st.wmask[q] = window_mask(fp, px, py, (float)px + o.x, (float)py + o.y);
@@ -1233,7 +1238,7 @@ __global__ void occluder_scan_kernel(GridsDev g, int32_t* flag) {
 
 void launch_resolve_opaque(const FrameParams& fp, const GridsDev& g, const SamplerDev& sm, SampleStore st,
                            cudaStream_t s) {
-	const long long n = (long long)store_size((long long)fp.sw * fp.sh, fp.spp);
+	const long long n = (long long)fp.sw * fp.sh * fp.spp;
 	if (n > 0) resolve_opaque_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(fp, g, sm, st);
 }
 
