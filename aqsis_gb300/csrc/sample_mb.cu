@@ -1543,10 +1543,11 @@ sample_mbq_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 		if (exhausted) break;
 	}
 
-	// ---- resolve (sample-major, see the lane kernel) ----
+	// ---- resolve, pixel-major (a pixel's samples often share a winner, whose
+	// loads then merge) ----
 	for (int q = t; q < tsamp; q += kThreadsQ) {
-		const int j = q / tpix;
-		const int pl = q - j * tpix;
+		const int j = q % spp;
+		const int pl = q / spp;
 		const int s = pl * spp + j;
 		const int px = tpx0 + pl % fp.tile_w, py = tpy0 + pl / fp.tile_w;
 		if (px >= tpx1 || py >= tpy1) continue;
