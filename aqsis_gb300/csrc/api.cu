@@ -616,6 +616,9 @@ aqh_status aqh_set_samples(aqh_ctx* ctx, const aqh_samples* s) {
 	AQH_TRY(up(ctx->s_ilod, s->lod_index, npix * sizeof(uint32_t)), "upload pattern choices");
 	AQH_TRY(up(ctx->s_dither, s->dither, ndisp * sizeof(float)), "upload dither");
 	m.pos = ctx->s_pos.as<float2>();
+	m.pos_unit = 1;
+	for (size_t i = 0; i < np && m.pos_unit; ++i)
+		m.pos_unit = s->pos[2 * i] >= 0.0f && s->pos[2 * i] <= 1.0f && s->pos[2 * i + 1] >= 0.0f && s->pos[2 * i + 1] <= 1.0f;
 	m.time = s->time ? ctx->s_time.as<float>() : nullptr;
 	m.dof = s->dof ? ctx->s_dof.as<float2>() : nullptr;
 	m.shuffle = s->shuffle ? ctx->s_shuffle.as<int32_t>() : nullptr;

@@ -123,6 +123,7 @@ struct SamplerDev {
 	const uint32_t* shuffle_index;
 	const uint32_t* lod_index;
 	const float* dither;
+	int pos_unit;  // every position offset is a number in [0, 1] (checked on the host)
 };
 
 // Per-sample resolved store (after Combine): R G B depth / OR OG OB flags.

@@ -223,18 +223,21 @@ __device__ __forceinline__ void fsum_add(FiltSum& f, bool in, float gw, const fl
 
 // Input row r of display column x: its three pixels' samples into the sums
 // of output rows r + 1 (B, window row fy = -1), r (M, fy = 0) and r - 1 (A,
-// fy = +1), each only when that row is the thread's (uB, uM, uA).
+// fy = +1), each only when that row is the thread's (uB, uM, uA).  `allin`:
+// every sample of the three pixels is inside all three windows (see
+// filter_roll_kernel), so the window tests are not evaluated.
 template <int SPP>
 __device__ __forceinline__ void roll_row(const FrameParams& fp, const SamplerDev& smp, const SampleStore& st,
                                          const float* __restrict__ ftab, int x, int r, FiltSum& B, FiltSum& M,
-                                         FiltSum& A, bool uB, bool uM, bool uA) {
+                                         FiltSum& A, bool uB, bool uM, bool uA, bool allin) {
 	const int spp = SPP > 0 ? SPP : fp.spp;
 	const float xcent = x + 0.5f;
 	const float ycB = (r + 1) + 0.5f, ycM = r + 0.5f, ycA = (r - 1) + 0.5f;
 	for (int fx = -1; fx <= 1; ++fx) {
 		const int px = x + fx;
 		const long long pix = (long long)(r - fp.sy0) * fp.sw + (px - fp.sx0);
-		const long long pat = (st.wmask || !smp.pos_index) ? pix : (long long)__ldg(smp.pos_index + pix);
+		const long long pat =
+		    (st.wmask || allin || !smp.pos_index) ? pix : (long long)__ldg(smp.pos_index + pix);
 		const float fpx = (float)px, fpy = (float)r;
 		const int bB = fx + 1, bM = 3 + fx + 1, bA = 6 + fx + 1;  // window bits (fy + 1) * 3 + fx + 1
 		for (int i0 = 0; i0 < spp; i0 += 4) {
@@ -250,6 +253,10 @@ __device__ __forceinline__ void roll_row(const FrameParams& fp, const SamplerDev
 					iB[j] = uB && ((mk >> bB) & 1u);
 					iM[j] = uM && ((mk >> bM) & 1u);
 					iA[j] = uA && ((mk >> bA) & 1u);
+				} else if (allin) {
+					iB[j] = uB && ok;
+					iM[j] = uM && ok;
+					iA[j] = uA && ok;
 				} else {
 					const float2 o = __ldg(smp.pos + pat * spp + ic);
 					const float vx = (fpx + o.x) - xcent;
@@ -291,7 +298,7 @@ constexpr int kRollRows = 8;       // display rows per CTA (8 measured faster th
 		const int q = (QQ);                                                                               \
 		if (q < R + 2) {                                                                                  \
 			if (q < R) fsum_reset(SB);                                                                    \
-			roll_row<SPP>(fp, smp, st, ftab_s, x, y0 - 1 + q, SB, SM, SA, q < R, q >= 1 && q <= R, q >= 2); \
+			roll_row<SPP>(fp, smp, st, ftab_s, x, y0 - 1 + q, SB, SM, SA, q < R, q >= 1 && q <= R, q >= 2, allin); \
 			if (q >= 2) finish_pixel(fp, smp, spp, SA.gTot, SA.count, SA.acc, chan, q8, x, y0 + q - 2);  \
 		}                                                                                                 \
 	}
@@ -308,6 +315,14 @@ filter_roll_kernel(FrameParams fp, SamplerDev smp, SampleStore st, const float* 
 	const int y0 = fp.crop_y0 + blockIdx.y * kRollRows;
 	const int R = min(kRollRows, fp.crop_y1 - y0);
 	if (x >= fp.crop_x1 || R <= 0) return;
+	// With every sample offset in [0, 1] and half-widths of at least 1.5,
+	// every sample of the 3x3 neighbourhood passes the window test in float:
+	// for fx = -1, (px + o) >= px rounds to at least x - 1 and x + 0.5 is
+	// exact below 2^22, so v >= -1.5; for fx = +1, px + o <= x + 2, so v <=
+	// 1.5; fx = 0 and the rows alike.  The test then decides nothing.
+	const int lim = 1 << 22;
+	const bool allin = smp.pos_unit && fp.xfwo2 >= 1.5f && fp.yfwo2 >= 1.5f && fp.sx0 > -lim && fp.sy0 > -lim &&
+	                   fp.sx0 + fp.sw < lim && fp.sy0 + fp.sh < lim;
 	FiltSum S0, S1, S2;
 	fsum_reset(S0);
 	fsum_reset(S1);

@@ -228,3 +228,23 @@ def test_rolling_filter_windows(hider, oracle, xs, ys, filt):
     sc.frame.gamma = 1.8
     res, ref = run_both(hider, oracle, sc)
     compare(res, ref)
+
+
+@pytest.mark.parametrize("offsets", ["outside", "edges"])
+def test_rolling_filter_offsets(hider, oracle, offsets):
+    """The rolling-window filter skips the window test only when every sample
+    offset lies in [0, 1] (a 3x3 neighbourhood then lies inside every window
+    of half-width 1.5).  Offsets reaching outside the pixel take the test
+    (`outside`); offsets of exactly 0 and 1 put samples on the window's
+    inclusive edges, -1.5 and +1.5 from the centre (`edges`)."""
+    sc = SS.edge_cases(seed=95, xs=6, ys=6, filt=("catmull-rom", 3.0, 3.0))
+    pos = np.array(sc.samples.pos, dtype=np.float32, copy=True)
+    if offsets == "outside":
+        pos = pos * np.float32(1.3) - np.float32(0.15)
+    else:
+        flat = pos.reshape(-1, 2)
+        flat[0::3] = 0.0
+        flat[1::3] = 1.0
+    sc.samples.pos = pos
+    res, ref = run_both(hider, oracle, sc)
+    compare(res, ref, exact_pixels=True)
