@@ -92,6 +92,8 @@ __global__ void grid_rects_kernel(FrameParams fp, GridsDev g, int4* rect, float*
 	const long long nv = (long long)(cu + 1) * (cv + 1) * nk;
 	const float4* P = g.P + g.pbase[warp];
 	float mnx = FLT_MAX, mny = FLT_MAX, mnz = FLT_MAX, mxx = -FLT_MAX, mxy = -FLT_MAX, mxz = -FLT_MAX;
+	// four loads in flight per lane (the pass is bound by loads in flight)
+#pragma unroll 4
 	for (long long i = lane; i < nv; i += 32) {
 		float4 p = __ldg(P + i);
 		mnx = fminf(mnx, p.x); mxx = fmaxf(mxx, p.x);
