@@ -1659,6 +1659,10 @@ extern "C" float orc_mt_float(void) { return randomFloat(); }
 extern "C" long orc_lfloor(float x) { return lfloor(x); }
 extern "C" long orc_lceil(float x) { return lceil(x); }
 extern "C" long orc_lround(double x) { return lroundd(x); }
+// CqVector2D::Magnitude2 / Magnitude (vector2d.h:132-147) as the oracle uses
+// them (motion divisions, the vertex-order degeneracy test)
+extern "C" float orc_mag2(float x, float y) { return mag2(V2(x, y)); }
+extern "C" float orc_mag(float x, float y) { return mag(V2(x, y)); }
 
 // multijitter.cpp:83-202, multijitter.h:89-101 (the pattern cache; Reseed(19) is
 // left to the caller).

@@ -192,6 +192,10 @@ long orc_lfloor(float x);
 long orc_lceil(float x);
 long orc_lround(double x);
 
+/* CqVector2D::Magnitude2 and Magnitude (libs/math/vector2d.h:132-147). */
+float orc_mag2(float x, float y);
+float orc_mag(float x, float y);
+
 #ifdef __cplusplus
 }
 #endif

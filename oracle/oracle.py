@@ -102,6 +102,10 @@ def lib():
         L.orc_cull_grid.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, _u8p]
         L.orc_lround.argtypes = [C.c_double]
         L.orc_lround.restype = C.c_long
+        L.orc_mag2.argtypes = [C.c_float, C.c_float]
+        L.orc_mag2.restype = C.c_float
+        L.orc_mag.argtypes = [C.c_float, C.c_float]
+        L.orc_mag.restype = C.c_float
         _lib = L
     return _lib
 

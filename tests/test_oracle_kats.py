@@ -35,6 +35,19 @@ def test_lround_reference_cases(oracle, x, want):
     assert oracle.lib().orc_lround(float(np.float32(x))) == want
 
 
+def test_vector2d_magnitudes(oracle):
+    """CqVector2D::Magnitude and Magnitude2 of (0.3, 0.4): the reference's own
+    known answers, checked for exact float equality
+    (libs/math/vector2d_test.cpp:48-60).  0.3f^2 + 0.4f^2 lies exactly halfway
+    between two floats and rounds to the even one, 0.25."""
+    L = oracle.lib()
+    assert L.orc_mag2(0.3, 0.4) == np.float32(0.25)
+    assert L.orc_mag(0.3, 0.4) == np.float32(0.5)
+    # the zero-component branches (vector2d.h:134-137, 143-146)
+    assert L.orc_mag2(0.0, 0.4) == np.float32(0.4) * np.float32(0.4)
+    assert L.orc_mag(-0.3, 0.0) == np.float32(0.3)
+
+
 def test_mt19937_iso_value(oracle):
     L = oracle.lib()
     L.orc_mt_seed(5489)
