@@ -386,6 +386,7 @@ struct aqh_ctx {
 	DevBuf d_P3, d_C3, d_O3;  // three-float host entries before widening
 	bool q8_default = false;  // d_q8 holds the last frame's r g b a display
 	bool dev_motion = false;
+	int dev_max_keys = 0;
 	DevBuf d_queue, d_slices;
 	std::vector<float4> h_dofb;
 	std::vector<float> h_slices;
@@ -557,6 +558,7 @@ aqh_status aqh_frame_begin(aqh_ctx* ctx, const aqh_frame_desc* d) {
 	ctx->dev_aov = nullptr;
 	ctx->dev_grids = false;
 	ctx->dev_motion = false;
+	ctx->dev_max_keys = 0;
 	ctx->host_packed = false;
 	ctx->dev_mps = 0;
 	ctx->samples_set = false;
@@ -721,6 +723,7 @@ __global__ void any_transparent_kernel(int n, const int32_t* flags, const int32_
 	if (i < n && !(flags[i] & AQH_GRID_OPAQUE)) out[0] = 1;
 	if (i < n && nkeys[i] > 1) out[1] = 1;
 	if (i < n && (flags[i] & AQH_GRID_CAMERA)) out[2] = 1;
+	if (i < n) atomicMax(out + 3, nkeys[i]);
 }
 }  // namespace
 
@@ -834,12 +837,13 @@ aqh_status aqh_submit_grids_device(aqh_ctx* ctx, int ngrids, const int32_t* d_cu
 	if (ngrids > 0)
 		any_transparent_kernel<<<(ngrids + 255) / 256, 256, 0, ctx->stream>>>(ngrids, d_flags, d_nkeys,
 		                                                                    ctx->d_err.as<int32_t>() + 8);
-	int32_t anyt[3] = {0, 0, 0};
-	AQH_TRY(cudaMemcpyAsync(anyt, ctx->d_err.as<int32_t>() + 8, 12, cudaMemcpyDeviceToHost, ctx->stream), "readback");
+	int32_t anyt[4] = {0, 0, 0, 0};
+	AQH_TRY(cudaMemcpyAsync(anyt, ctx->d_err.as<int32_t>() + 8, 16, cudaMemcpyDeviceToHost, ctx->stream), "readback");
 	AQH_TRY(cudaStreamSynchronize(ctx->stream), "sync");
 	ctx->any_transparent = anyt[0] != 0;
 	ctx->dev_motion = anyt[1] != 0;
 	ctx->any_camera = anyt[2] != 0;
+	ctx->dev_max_keys = anyt[3];
 	ctx->dev_grids = true;
 	ctx->dev_mps = total_mps;
 	return AQH_OK;
@@ -1000,12 +1004,18 @@ static aqh_status plan_render(aqh_ctx* ctx, RenderPlan& P) {
 	P.cam = ctx->camera;
 	P.nmps = ctx->dev_grids ? ctx->dev_mps : ctx->h_mps;
 	bool motion = false;
+	int max_keys = 0;
 	if (ctx->host_packed) {
-		for (int i = 0; i < ctx->hp.ngrids; ++i) motion = motion || ctx->hp.nkeys[i] > 1;
+		for (int i = 0; i < ctx->hp.ngrids; ++i) max_keys = std::max(max_keys, (int)ctx->hp.nkeys[i]);
 	} else if (!ctx->dev_grids) {
-		for (int k : ctx->h_nkeys) motion = motion || k > 1;
+		for (int k : ctx->h_nkeys) max_keys = std::max(max_keys, k);
 	}
-	if (ctx->dev_grids) motion = ctx->dev_motion;
+	motion = max_keys > 1;
+	if (ctx->dev_grids) {
+		motion = ctx->dev_motion;
+		max_keys = ctx->dev_max_keys;
+	}
+	fp.max_keys = max_keys;
 	fp.any_motion = motion ? 1 : 0;
 	P.mbdof = fp.use_dof || fp.any_motion;
 	// opaque motion blur / depth of field frames sample smaller tiles (two

@@ -51,6 +51,7 @@ struct FrameParams {
 	int st_tiles;                            // tiles per super-tile side
 	int nstx, nsty;
 	int any_motion;
+	int max_keys;  // the most motion keys any grid of the frame has (0: not known)
 	int use_lod;                             // level-of-detail tests can reject samples (sample detail
 	                                         // levels or grid bounds were given)
 	int ftab_n;                              // floats in the filter table

@@ -25,22 +25,29 @@ namespace aqh {
 namespace {
 
 
-struct MbRec {
+// A candidate's record with room for NK motion keys: frames whose grids have
+// at most two keys use two-key records (244 bytes instead of 396), so more
+// candidates fit a round.
+template <int NK>
+struct MbRecT {
+	static constexpr int kKeys = NK;
 	float bmn[3], bmx[3];          // m_Bound (union of the key bounds for moving micropolygons)
-	float key[kMaxKeys][4][3];     // key vertices in natural order: index, index+1, index+cu+1, index+cu+2
-	float kt[kMaxKeys];            // key times
-	float kbmn[kMaxKeys][3], kbmx[kMaxKeys][3];  // per-key bounds
+	float key[NK][4][3];           // key vertices in natural order: index, index+1, index+cu+1, index+cu+2
+	float kt[NK];                  // key times
+	float kbmn[NK][3], kbmx[NK][3];  // per-key bounds
 	float cocm[4][2];              // static DoF: CoC multiplier per vertex
 	float cocmin[2], cocmax[2];    // DoF: min / max CoC multipliers
 	int nkeys, code, id, grid, bits;
 };
+using MbRec = MbRecT<kMaxKeys>;
 
 
 struct Bnd {
 	float mnx, mny, mnz, mxx, mxy, mxz;
 };
 
-__device__ __forceinline__ Bnd key_bound(const MbRec& r, int k) {
+template <class R>
+__device__ __forceinline__ Bnd key_bound(const R& r, int k) {
 	return Bnd{r.kbmn[k][0], r.kbmn[k][1], r.kbmn[k][2], r.kbmx[k][0], r.kbmx[k][1], r.kbmx[k][2]};
 }
 
@@ -64,7 +71,8 @@ __device__ __forceinline__ bool dof_in_bound(const Bnd& b, float cminx, float cm
 // (static, with DoF) or CqMicroPolygonMotion::Sample.  On a hit returns depth
 // and (u,v).  With `gt`, a static micropolygon marked trimmed also takes the
 // trim test (the motion form has none, micropolygon.cpp:1876-1882).
-__device__ bool mb_sample(const FrameParams& fp, const MbRec& r, bool moving, bool dof, float px, float py,
+template <class R>
+__device__ bool mb_sample(const FrameParams& fp, const R& r, bool moving, bool dof, float px, float py,
                           float time, float dx, float dy, float& D, float& u, float& v, const float4* tri = nullptr,
                           const GridsDev* gt = nullptr) {
 	V3f pts[4];
@@ -177,9 +185,12 @@ __device__ bool mb_sample(const FrameParams& fp, const MbRec& r, bool moving, bo
 }
 
 // Load the record of micropolygon m of grid gi from global memory.
-__device__ void load_mb_record(const FrameParams& fp, const GridsDev& g, int gi, int m, MbRec& r) {
+template <class R>
+__device__ void load_mb_record(const FrameParams& fp, const GridsDev& g, int gi, int m, R& r) {
 	const int cu = __ldg(g.cu + gi), cv = __ldg(g.cv + gi);
-	const int nk = __ldg(g.nkeys + gi);
+	// at most the record's keys (the host sends a frame to two-key records
+	// only when no grid has more)
+	const int nk = min(__ldg(g.nkeys + gi), R::kKeys);
 	const long long nv = (long long)(cu + 1) * (cv + 1);
 	const long long pb = __ldg(g.pbase + gi);
 	const int iv = m / cu, iu = m - iv * cu;
@@ -253,7 +264,8 @@ __device__ void load_mb_record(const FrameParams& fp, const GridsDev& g, int gi,
 
 // Record of micropolygon m of grid gi with its occluding flag
 // (SqMpgSampleInfo::isOpaque, micropolygon.cpp:1477-1529) and global id.
-__device__ __forceinline__ void build_mb_record(const FrameParams& fp, const GridsDev& g, int gi, int m, MbRec& rr) {
+template <class R>
+__device__ __forceinline__ void build_mb_record(const FrameParams& fp, const GridsDev& g, int gi, int m, R& rr) {
 	load_mb_record(fp, g, gi, m, rr);
 	const int gflags = __ldg(g.flags + gi);
 	bool opaque = true;
@@ -455,7 +467,8 @@ __device__ __forceinline__ float warp_max_m(float v) {
 
 // Sub-bound count of a moving micropolygon (CqMicroPolygonMotion::BuildBoundList,
 // micropolygon.cpp:1703-1713).
-__device__ __forceinline__ int motion_divisions(const MbRec& r, int timeRanges) {
+template <class R>
+__device__ __forceinline__ int motion_divisions(const R& r, int timeRanges) {
 	const float cx = r.kbmx[0][0] - r.kbmn[0][0], cy = r.kbmx[0][1] - r.kbmn[0][1];
 	// CqVector2D::Magnitude2 (vector2d.h:132-138)
 	const float polyLen2 = (cy == 0.0f) ? cx * cx : ((cx == 0.0f) ? cy * cy : (cx * cx) + (cy * cy));
@@ -471,14 +484,16 @@ __device__ __forceinline__ int motion_divisions(const MbRec& r, int timeRanges) 
 
 // First key index with time >= T (the reference's `endKey` after its while
 // loop at time T, micropolygon.cpp:1724-1725).
-__device__ __forceinline__ int end_key_at(const MbRec& r, float T) {
+template <class R>
+__device__ __forceinline__ int end_key_at(const R& r, float T) {
 	int e = 1;
 	while (T > r.kt[e] && e < r.nkeys - 1) ++e;
 	return e;
 }
 
 // Key bounds interpolated at time T between keys e-1 and e (the `mid` bound).
-__device__ __forceinline__ Bnd mid_at(const MbRec& r, int e, float T) {
+template <class R>
+__device__ __forceinline__ Bnd mid_at(const R& r, int e, float T) {
 	const Bnd end0 = key_bound(r, e - 1), end1 = key_bound(r, e);
 	const float mix = (T - r.kt[e - 1]) / (r.kt[e] - r.kt[e - 1]);
 	Bnd mid = end0;
@@ -496,7 +511,8 @@ __device__ __forceinline__ Bnd mid_at(const MbRec& r, int e, float T) {
 // `mid` (or key 0's bound) grown by this slice's `mid` and the keys the slice
 // passes.  `T` is the per-frame table of the reference's accumulated slice end
 // times for `div` slices.
-__device__ Bnd sub_bound(const MbRec& r, const float* T, int b) {
+template <class R>
+__device__ Bnd sub_bound(const R& r, const float* T, int b) {
 	Bnd bound;
 	int startKey;
 	if (b == 0) {
@@ -939,7 +955,8 @@ __device__ __forceinline__ Shutter shutter_of(const FrameParams& fp) {
 
 // Slice b of micropolygon r: its bound, time window and (without depth of
 // field) sample-index window.  False when the reference skips the slice.
-__device__ __forceinline__ bool mb_slice(const FrameParams& fp, const Shutter& sh, const MbRec& r, const float* T,
+template <class R>
+__device__ __forceinline__ bool mb_slice(const FrameParams& fp, const Shutter& sh, const R& r, const float* T,
                                          int div, float dt, int b, Bnd& B, float& time0, float& time1, int& j0,
                                          int& j1) {
 	const bool moving = r.nkeys > 1;
@@ -1000,7 +1017,8 @@ struct MbItem {
 	int j0, j1, sX, eX, sY, eY;
 };
 
-__device__ __forceinline__ bool mb_item(const FrameParams& fp, const Shutter& sh, const MbRec& r,
+template <class R>
+__device__ __forceinline__ bool mb_item(const FrameParams& fp, const Shutter& sh, const R& r,
                                         const float* slice_times, int b, const float* dext, int tpx0, int tpy0,
                                         int tpx1, int tpy1, MbItem& it) {
 	const bool moving = r.nkeys > 1;
@@ -1068,7 +1086,8 @@ struct ItemQ {
 	uint32_t mnpix, mrw;  // ceil(2^32 / npix), ceil(2^32 / rw) (0 for 1): exact quotients of slot indices
 };
 
-struct SmemQ {
+template <int NK, int SLOTS>
+struct SmemQT {
 	unsigned long long key[kTileSampQ];   // occluding hit of each tile sample (depth_key_m)
 	unsigned long long prev[kTileSampQ];  // ... at the start of the round
 	float stime[kTileSampQ];              // time of each tile sample
@@ -1080,9 +1099,9 @@ struct SmemQ {
 	int patidx[kTilePixQ];
 	int dofidx[kTilePixQ];                // lens pattern of each tile pixel
 	float dofb[AQH_MAX_SPP_DEV][4];
-	MbRec rec[kSlotsQ];
-	int2 pend[kSlotsQ];
-	int pref[kSlotsQ + 1];                // running count of (candidate, slice) items
+	MbRecT<NK> rec[SLOTS];
+	int2 pend[SLOTS];
+	int pref[SLOTS + 1];                  // running count of (candidate, slice) items
 	ItemQ items[kItemsQ];
 	int ipref[kItemsQ + 1];               // running count of the kept items' sample slots
 	int qgrid[kThreadsQ];
@@ -1098,12 +1117,19 @@ struct SmemQ {
 	float dext[4];                        // min dofb[.][0], min [.][1], max [.][2], max [.][3]
 };
 
+// candidates per round: 64 four-key records, or 96 two-key ones in less space
+constexpr int kSlotsQ2 = 96;
+using SmemQ = SmemQT<kMaxKeys, kSlotsQ>;
+using SmemQ2 = SmemQT<2, kSlotsQ2>;
 // two CTAs per SM: 228 KB of shared memory less 1 KB reserved per CTA
 static_assert(sizeof(SmemQ) <= (228 * 1024 - 2 * 1024) / 2, "two opaque motion CTAs must fit on an SM");
+static_assert(sizeof(SmemQ2) <= sizeof(SmemQ), "two-key rounds must fit where four-key ones do");
+static_assert(kSlotsQ2 <= kThreadsQ && kSlotsQ2 < 256, "one record per thread; slots fit 8 bits");
 
 // One (slice, sample) test as RenderMPG_MBOrDof makes it, given occlZ:
 // returns true with D when the sample is hit and not skipped by early-z.
-__device__ __forceinline__ bool mb_slice_test(const FrameParams& fp, const MbRec& r, const Bnd& B, bool moving,
+template <class R>
+__device__ __forceinline__ bool mb_slice_test(const FrameParams& fp, const R& r, const Bnd& B, bool moving,
                                               float time0, float time1, const float* dofb_k, int px, int py,
                                               float x, float y, float stime, float sdx, float sdy, float oz,
                                               float& D, const float4* tri, const GridsDev* gt) {
@@ -1124,9 +1150,12 @@ __device__ __forceinline__ uint32_t quot_magic(int d) {
 // is exact there (the rounding up adds less than r * d / 2^32 / d < 1 / d)
 __device__ __forceinline__ int quot(int r, uint32_t m) { return m == 0u ? r : (int)__umulhi((unsigned)r, m); }
 
+template <int NK, int SLOTS>
 __global__ void __launch_bounds__(kThreadsQ, 2)
 sample_mbq_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, SampleStore st,
                   const float4* dof_bounds, const float* slice_times) {
+	using SmemQ = SmemQT<NK, SLOTS>;
+	using MbRec = MbRecT<NK>;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	SmemQ& sm = *reinterpret_cast<SmemQ*>(smem_raw);
 	const int tile = blockIdx.x;
@@ -1267,7 +1296,7 @@ sample_mbq_kernel(FrameParams fp, GridsDev g, SamplerDev smp, BinBuffers bb, Sam
 	int lp = lbeg, r0 = 0, qtotal = 0, npend = 0;
 	for (;;) {
 		const bool exhausted =
-			stage_mb<kSlotsQ, SmemQ, kThreadsQ>(fp, g, bb, sm, tpx0, tpy0, tpx1, tpy1, lend, lp, r0, qtotal, npend,
+			stage_mb<SLOTS, SmemQ, kThreadsQ>(fp, g, bb, sm, tpx0, tpy0, tpx1, tpy1, lend, lp, r0, qtotal, npend,
 			                                    sm.blk);
 		if (npend == 0) break;
 
@@ -1577,15 +1606,22 @@ void launch_sample_mb(const FrameParams& fp, const GridsDev& g, const SamplerDev
 	if (pool.capacity > 0)
 		sample_mb_kernel<true><<<ntiles, kThreadsM, sample_mb_smem(true), s>>>(fp, g, sm, b, st, pool, dof_bounds,
 		                                                                      slice_times);
+	else if (fp.max_keys >= 1 && fp.max_keys <= 2)
+		sample_mbq_kernel<2, kSlotsQ2><<<ntiles, kThreadsQ, sizeof(SmemQ2), s>>>(fp, g, sm, b, st, dof_bounds,
+		                                                                       slice_times);
 	else
-		sample_mbq_kernel<<<ntiles, kThreadsQ, sizeof(SmemQ), s>>>(fp, g, sm, b, st, dof_bounds, slice_times);
+		sample_mbq_kernel<kMaxKeys, kSlotsQ><<<ntiles, kThreadsQ, sizeof(SmemQ), s>>>(fp, g, sm, b, st, dof_bounds,
+		                                                                             slice_times);
 }
 
 void configure_sample_mb_kernels() {
 	static std::mutex mu;
 	static uint64_t configured = 0;
 	if (!first_use_on_device(mu, configured)) return;
-	cudaFuncSetAttribute(sample_mbq_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemQ));
+	cudaFuncSetAttribute(sample_mbq_kernel<kMaxKeys, kSlotsQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                     (int)sizeof(SmemQ));
+	cudaFuncSetAttribute(sample_mbq_kernel<2, kSlotsQ2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	                     (int)sizeof(SmemQ2));
 	cudaFuncSetAttribute(sample_mb_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sample_mb_smem(true));
 }
 
